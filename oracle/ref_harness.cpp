@@ -1,0 +1,236 @@
+// ref_harness.cpp -- drives the reference's own Transform-PAL, PALcolour,
+// OutputWriter and DropoutCorrector classes, compiled from the reference
+// sources (see oracle/Makefile), on a raw field file. Test infrastructure: it
+// produces the outputs that pin the C restatement in oracle/tpal_oracle.c.
+//
+// The per-frame flow mirrors the reference's decodeSourceFrame /
+// decodeFrameLocked (src/abi/c_api_decoder.cpp:183-527): load a field window
+// with black padding outside the capture (src/decoders/source_field.cpp:68-171),
+// dropout-correct every non-padding window frame that has dropouts
+// (c_api_decoder.cpp:300-321), run PalColour::decodeFrames, then
+// OutputWriter::convert (yuv444p16) or convertToFloat (yuv444ps).
+//
+// Usage (key=value arguments):
+//   mode=decode|chroma|dropout kind=2|3 fmt=p16|ps threshold=0.4
+//   thresholds=<file> in=<fields.u16> nfields=N first=F count=C out=<file>
+//   dropouts=<file> overcorrect=0|1 intra=0|1
+// The field file holds N fields of 1135x313 uint16, first field first.
+// The dropout file holds lines "field_index startx endx fieldLine".
+
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "decoders/palcolour/palcolour.h"
+#include "decoders/palcolour/transform_pal_2d.h"
+#include "decoders/palcolour/transform_pal_3d.h"
+#include "decoders/source_field.h"
+#include "dropout/dropout_corrector.h"
+#include "output/component_frame.h"
+#include "output/output_writer.h"
+
+using chd::metadata::LdDecodeMetaData;
+
+namespace {
+
+// Line-locked 4fsc PAL geometry: the reference's own preset values
+// (src/format/video_standards.cpp:58-70,116-207 and src/metadata/core.cpp:40-50).
+LdDecodeMetaData::VideoParameters palParams()
+{
+    LdDecodeMetaData::VideoParameters vp;
+    vp.system = chd::metadata::PAL;
+    vp.isSubcarrierLocked = false;
+    vp.fieldWidth = 1135;
+    vp.fieldHeight = 313;
+    vp.sampleRate = 4.0 * 625.0 * 25.0 * (1135.0 / 4.0 + 1.0 / 625.0);
+    vp.fSC = 283.75 * 15625.0 + 25.0;
+    vp.colourBurstStart = 98;
+    vp.colourBurstEnd = 138;
+    vp.activeVideoStart = 177;
+    vp.activeVideoEnd = 1125;
+    vp.black16bIre = 256 * 64;
+    vp.white16bIre = 844 * 64;
+    vp.blanking16bIre = 256 * 64;
+    vp.firstActiveFrameLine = 44;
+    vp.lastActiveFrameLine = 619;
+    vp.pictureStart = vp.activeVideoStart;
+    vp.pictureEnd = vp.activeVideoEnd;
+    vp.tileReadStart = vp.activeVideoStart;
+    vp.tileReadEnd = vp.activeVideoEnd;
+    vp.isValid = true;
+    return vp;
+}
+
+std::map<std::string, std::string> parseArgs(int argc, char **argv)
+{
+    std::map<std::string, std::string> m;
+    for (int i = 1; i < argc; i++) {
+        const char *eq = std::strchr(argv[i], '=');
+        if (!eq) continue;
+        m[std::string(argv[i], eq - argv[i])] = std::string(eq + 1);
+    }
+    return m;
+}
+
+struct Capture {
+    std::vector<uint16_t> samples;
+    int nfields = 0;
+    size_t fieldLen = 0;
+    std::vector<chd::metadata::DropOuts> dropouts;  // per field
+};
+
+// Field window for frames [firstFrame - lookBehind, firstFrame + 1 + lookAhead),
+// black padding outside the capture (source_field.cpp:88-170).
+void loadWindow(const Capture &cap, const LdDecodeMetaData::VideoParameters &vp, int frame, int lookBehind,
+                int lookAhead, std::vector<chd::decoders::SourceField> &fields, int &startIndex, int &endIndex)
+{
+    startIndex = 2 * lookBehind;
+    endIndex = startIndex + 2;
+    fields.assign(endIndex + 2 * lookAhead, chd::decoders::SourceField());
+    const int numFrames = cap.nfields / 2;
+    for (size_t i = 0; i < fields.size(); i += 2) {
+        const int f = frame - lookBehind + static_cast<int>(i / 2);
+        const bool pad = f < 0 || f >= numFrames;
+        for (int j = 0; j < 2; j++) {
+            auto &sf = fields[i + j];
+            sf.field.isFirstField = (j == 0);
+            sf.isPadding = pad;
+            const int srcField = pad ? j : 2 * f + j;
+            sf.fieldNumber = srcField + 1;
+            sf.field.dropOuts = cap.dropouts[srcField];
+            if (pad) {
+                sf.data.assign(cap.fieldLen, static_cast<uint16_t>(vp.black16bIre));
+            } else {
+                sf.data.assign(cap.samples.begin() + cap.fieldLen * srcField,
+                               cap.samples.begin() + cap.fieldLen * (srcField + 1));
+            }
+        }
+    }
+}
+
+}  // namespace
+
+int main(int argc, char **argv)
+{
+    auto a = parseArgs(argc, argv);
+    const std::string mode = a.count("mode") ? a["mode"] : "decode";
+    const int kind = a.count("kind") ? std::atoi(a["kind"].c_str()) : 3;
+    const std::string fmt = a.count("fmt") ? a["fmt"] : "p16";
+    const double threshold = a.count("threshold") ? std::atof(a["threshold"].c_str()) : 0.4;
+    const int first = a.count("first") ? std::atoi(a["first"].c_str()) : 0;
+    const int count = a.count("count") ? std::atoi(a["count"].c_str()) : 1;
+    const bool overcorrect = a.count("overcorrect") && a["overcorrect"] == "1";
+    const bool intra = a.count("intra") && a["intra"] == "1";
+
+    const auto vp = palParams();
+    Capture cap;
+    cap.nfields = std::atoi(a["nfields"].c_str());
+    cap.fieldLen = static_cast<size_t>(vp.fieldWidth) * vp.fieldHeight;
+    cap.samples.resize(cap.fieldLen * cap.nfields);
+    {
+        FILE *fp = std::fopen(a["in"].c_str(), "rb");
+        if (!fp || std::fread(cap.samples.data(), 2, cap.samples.size(), fp) != cap.samples.size()) {
+            std::fprintf(stderr, "ref_harness: cannot read %s\n", a["in"].c_str());
+            return 2;
+        }
+        std::fclose(fp);
+    }
+    cap.dropouts.assign(cap.nfields, chd::metadata::DropOuts());
+    const bool correcting = a.count("dropouts") != 0;
+    if (correcting) {
+        std::ifstream in(a["dropouts"]);
+        int fi, sx, ex, fl;
+        while (in >> fi >> sx >> ex >> fl) {
+            if (fi >= 0 && fi < cap.nfields) cap.dropouts[fi].append(sx, ex, fl);
+        }
+    }
+
+    chd::decoders::palcolour::PalColour::Configuration cfg;
+    cfg.separation = (kind == 2) ? chd::decoders::palcolour::PalColour::transform2DFilter
+                                 : chd::decoders::palcolour::PalColour::transform3DFilter;
+    cfg.transformThreshold = threshold;
+    if (a.count("thresholds")) {
+        std::ifstream in(a["thresholds"]);
+        double v;
+        while (in >> v) cfg.transformThresholds.push_back(v);
+    }
+    const int lookBehind = cfg.getLookBehind();
+    const int lookAhead = cfg.getLookAhead();
+
+    FILE *out = std::fopen(a["out"].c_str(), "wb");
+    if (!out) return 3;
+
+    chd::decoders::palcolour::PalColour pal;
+    pal.updateConfiguration(vp, cfg);
+
+    std::unique_ptr<chd::decoders::palcolour::TransformPal> tp;
+    if (mode == "chroma") {
+        if (kind == 2) tp = std::make_unique<chd::decoders::palcolour::TransformPal2D>();
+        else tp = std::make_unique<chd::decoders::palcolour::TransformPal3D>();
+        tp->updateConfiguration(vp, cfg.transformThreshold, cfg.transformThresholds, cfg.colorConversion);
+    }
+
+    chd::output::OutputWriter writer;
+    chd::output::OutputWriter::Configuration ocfg;
+    ocfg.paddingAmount = 1;
+    ocfg.pixelFormat = chd::output::OutputWriter::YUV444P16;
+    writer.updateConfiguration(vp, ocfg);
+
+    long totalCorrected = 0, totalFailed = 0;
+    long long totalDistance = 0;
+    for (int frame = first; frame < first + count; frame++) {
+        std::vector<chd::decoders::SourceField> fields;
+        int startIndex = 0, endIndex = 0;
+        const int lb = (mode == "dropout") ? 0 : lookBehind;
+        const int la = (mode == "dropout") ? 0 : lookAhead;
+        loadWindow(cap, vp, frame, lb, la, fields, startIndex, endIndex);
+
+        if (correcting) {
+            for (size_t i = 0; i + 1 < fields.size(); i += 2) {
+                if (fields[i].isPadding) continue;
+                if (fields[i].field.dropOuts.empty() && fields[i + 1].field.dropOuts.empty()) continue;
+                chd::dropout::DropoutCorrector corrector(vp);
+                chd::dropout::DropoutCorrectionStats stats;
+                corrector.correctFrame(fields[i], fields[i + 1], overcorrect, intra, &stats);
+                if (static_cast<int>(i) == startIndex) {
+                    totalCorrected += stats.corrected;
+                    totalFailed += stats.failed;
+                    totalDistance += stats.totalDistance;
+                }
+            }
+        }
+
+        if (mode == "dropout") {
+            std::fwrite(fields[startIndex].data.data(), 2, cap.fieldLen, out);
+            std::fwrite(fields[startIndex + 1].data.data(), 2, cap.fieldLen, out);
+            continue;
+        }
+        if (mode == "chroma") {
+            std::vector<const double *> chroma(endIndex - startIndex);
+            tp->filterFields(fields, startIndex, endIndex, chroma);
+            for (const double *c : chroma) std::fwrite(c, sizeof(double), cap.fieldLen, out);
+            continue;
+        }
+
+        std::vector<chd::output::ComponentFrame> frames(1);
+        pal.decodeFrames(fields, startIndex, endIndex, frames);
+        if (fmt == "ps") {
+            std::vector<float> planes[3];
+            writer.convertToFloat(frames[0], planes, true);
+            for (int p = 0; p < 3; p++) std::fwrite(planes[p].data(), sizeof(float), planes[p].size(), out);
+        } else {
+            chd::output::OutputFrame of;
+            writer.convert(frames[0], of);
+            std::fwrite(of.data(), 2, of.size(), out);
+        }
+    }
+    std::fclose(out);
+    std::printf("{\"corrected\": %ld, \"failed\": %ld, \"total_distance\": %lld}\n", totalCorrected, totalFailed,
+                totalDistance);
+    return 0;
+}
