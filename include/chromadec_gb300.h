@@ -1,0 +1,93 @@
+/* SPDX-License-Identifier: GPL-3.0-or-later */
+/*
+ * chromadec_gb300.h -- device-level entry points of libchromadec_gb300.
+ *
+ * These calls have no counterpart in the reference's public ABI: they expose
+ * the GB300 Transform-PAL pipeline on device-resident buffers (CUDA device
+ * pointers, a cudaStream_t passed as void*), for callers that already keep
+ * captures in HBM and for the benchmark's device-resident measurement. The
+ * reference-compatible chd_* ABI in <chromadec/*.h> is built on top of them.
+ *
+ * Conventions: a capture is a device array of uint16 fields, field f at
+ * fields + f * field_stride samples, first field of every frame at an even
+ * index. Frames outside the capture are black padding, as in the reference's
+ * SourceField::loadFields (src/decoders/source_field.cpp:88-170). Every call
+ * returns 0 on success and a negative CHDG_E_* code on failure; failures
+ * also set the thread's chd_last_error() detail.
+ */
+#ifndef CHROMADEC_GB300_H
+#define CHROMADEC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CHDG_E_INVALID_ARG  (-1)
+#define CHDG_E_UNSUPPORTED  (-2)
+#define CHDG_E_CUDA         (-3)
+#define CHDG_E_OOM          (-4)
+
+/* Source geometry and levels (the VideoParameters fields the path reads). */
+typedef struct chdg_geometry {
+    int32_t field_width, field_height;
+    int32_t active_start, active_end;                      /* samples, half-open */
+    int32_t first_active_frame_line, last_active_frame_line; /* inclusive */
+    int32_t burst_start, burst_end;
+    int32_t black, white;
+    double sample_rate, fsc;
+} chdg_geometry;
+
+/* Decoder + output settings (PalColour::Configuration and
+ * OutputWriter::Configuration fields the path reads). */
+typedef struct chdg_config {
+    int32_t kind;                 /* 7 = CHD_DEC_TRANSFORM_2D, 8 = CHD_DEC_TRANSFORM_3D */
+    double threshold;             /* transform_threshold, default 0.4 */
+    const double *thresholds;     /* per-bin thresholds (80 for 2D, 768 for 3D) or NULL */
+    int32_t n_thresholds;
+    double chroma_gain, chroma_phase_deg;
+    int32_t output_format;        /* 0 = yuv444p16, 1 = yuv444ps */
+    int32_t clamp_mode;           /* chd_clamp_t */
+    int32_t padding_multiple;     /* 1 = none */
+    double ecb_from_u, ecr_from_v;
+} chdg_config;
+
+typedef struct chdg_engine chdg_engine;
+
+/* Fill g with the reference's line-locked 4fsc PAL preset and c with the
+ * Transform-PAL decoder defaults for `kind` (7 or 8). */
+void chdg_default_geometry(chdg_geometry *g);
+void chdg_default_config(chdg_config *c, int32_t kind);
+
+/* Create an engine on the current CUDA device. Constant tables are uploaded
+ * once per device; scratch grows on demand. */
+int chdg_engine_create(const chdg_geometry *g, const chdg_config *c, chdg_engine **out);
+void chdg_engine_free(chdg_engine *e);
+
+/* Output frame geometry (after padding) and bytes per output frame. */
+int chdg_output_geometry(const chdg_engine *e, int32_t *width, int32_t *height, size_t *frame_bytes);
+
+/* Decode frames [frame_begin, frame_end) of a device-resident capture of
+ * nfields fields into d_out (frame_end - frame_begin frames, each
+ * [Y | Cb | Cr] planes of width x height, uint16 or float per the format).
+ * Asynchronous on `stream`. */
+int chdg_decode_device(chdg_engine *e, const uint16_t *d_fields, int64_t field_stride, int32_t nfields,
+                       int32_t frame_begin, int32_t frame_end, void *d_out, void *stream);
+
+/* Transform-PAL chroma only: the separated chroma of fields
+ * [2*frame_begin, 2*frame_end) as FP32 planes of (last-first field line + 1)
+ * rows x (active_end - active_start) columns, rows starting at field line
+ * first_active_frame_line / 2. For checking the transform in isolation. */
+int chdg_chroma_device(chdg_engine *e, const uint16_t *d_fields, int64_t field_stride, int32_t nfields,
+                       int32_t frame_begin, int32_t frame_end, float *d_chroma, void *stream);
+
+/* Threshold decisions whose FP32 margin was inside the error bound and were
+ * re-evaluated in double-float, and how many of those FP32 had wrong. */
+int chdg_engine_stats(chdg_engine *e, uint64_t *exact_decisions, uint64_t *fp32_flips);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,270 @@
+// demod.cu -- PALcolour demodulation of Transform-PAL chroma and on-device
+// H.273 quantise/pack, sm_103a.
+//
+// Follows PalColour::decodeField / detectBurst / decodeLine<double, true>
+// (src/decoders/palcolour/palcolour.cpp:307-409, 456-646) and
+// OutputWriter::convertLine / convertToFloat
+// (src/output/output_writer.cpp:402-486, 670-727), restructured:
+//
+//  * 4fsc sampling makes the reference carrier exact: sin(2 pi i fSC/fs) is
+//    {0, 1, 0, -1}[i mod 4] (the reference's double tables differ only by
+//    ~1e-16 residues at the zeros). The burst sums therefore run in exact
+//    integer arithmetic, the V-switch test is an exact int64 comparison, and
+//    each FIR tap touches either the sine or the cosine products, never both.
+//  * The chroma input is the sum of the transform's four overlap-class planes;
+//    chroma lines outside the field's active lines and samples outside the
+//    active window are zero, exactly like the reference's zero-initialised
+//    chroma buffer and its blackLine substitution (palcolour.cpp:466-473).
+//  * Y = composite - chroma, the rotated U/V and the output scaling are fused;
+//    planes are written straight into the frame's [Y | Cb | Cr] layout.
+//
+// One block: 4 field lines of one output field, 512 threads; a thread
+// produces 8 consecutive samples of one line from a register window of the
+// four vertically combined chroma rows.
+#include <cmath>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "tpal_kernels.h"
+
+namespace tpal {
+
+__constant__ float cd_cfilt[8][4];   // PALcolour chroma 2D FIR taps (filterSize = 7)
+static bool g_demod_ready[64];
+
+constexpr int kDemodLines = 4;
+constexpr int kDemodThreads = 512;
+constexpr int kPad = 8;
+
+__device__ __forceinline__ int first_line(int fafl, int off) { return (fafl + 1 - off) / 2; }
+__device__ __forceinline__ int last_line(int lafl, int off) { return ((lafl - off) / 2) + 1; }
+
+__global__ void __launch_bounds__(kDemodThreads) demod_kernel(DemodParams P)
+{
+    extern __shared__ float smem[];
+    const int nblk_per_field = (P.fh + kDemodLines - 1) / kDemodLines;   // upper bound; invalid lines skip
+    const int o = blockIdx.x / nblk_per_field;
+    const int blk = blockIdx.x % nblk_per_field;
+    if (o >= P.nout) return;
+    const int f = P.field_begin + o;
+    const int off = f & 1;
+    const int fl_first = first_line(P.fafl, off);
+    const int fl_last = last_line(P.lafl, off);
+    const int fl0 = fl_first + blk * kDemodLines;
+    if (fl0 >= fl_last) return;
+
+    const int base4 = P.avs & ~3;                     // absolute sample of local index 0
+    const int span = ((P.ave - base4) + 7) & ~7;      // samples covered by threads (multiple of 8)
+    const int SW = span + 2 * kPad;                   // smem row length
+    float *ch = smem;                                  // [10][SW] chroma rows fl0-3 .. fl0+6
+    float *vv = smem + 10 * SW;                        // [4 lines][4 combos][SW]
+    __shared__ float s_bp[kDemodLines], s_bq[kDemodLines], s_vsw[kDemodLines];
+
+    const uint16_t *field = P.fields + (long long)f * P.field_stride;
+    const float *part = P.partial + (long long)o * P.part_field_stride;
+
+    // 1. chroma rows (sum of the overlap-class planes), zero outside
+    for (int idx = threadIdx.x; idx < 10 * SW; idx += blockDim.x) {
+        const int r = idx / SW;
+        const int xl = idx % SW - kPad;
+        const int x = base4 + xl;
+        const int fl = fl0 - 3 + r;
+        float v = 0.f;
+        if (fl >= fl_first && fl < fl_last && x >= P.avs && x < P.ave) {
+            const long long e = (long long)(fl - P.fl_lo) * P.part_row_stride + (x - P.avs);
+            for (int c = 0; c < P.nclasses; c++) v += part[(long long)c * P.part_class_stride + e];
+        }
+        ch[idx] = v;
+    }
+
+    // 2. burst detection: one warp per line (detectBurst, palcolour.cpp:344-409)
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp < kDemodLines) {
+        const int fl = fl0 + warp;
+        long long Ps = 0, Qs = 0, POs = 0, QOs = 0;
+        if (fl < fl_last) {
+            auto px = [&](int line, int i) -> int {
+                return (line < 0 || line >= P.fh) ? 0 : (int)field[(long long)line * P.fw + i];
+            };
+            for (int i = P.burst_start + lane; i < P.burst_end; i += 32) {
+                const int d = 2 * px(fl, i) - px(fl - 2, i) - px(fl + 2, i);   // 4 * ((in0 - (in3+in4)/2) / 2)
+                const int e = px(fl + 1, i) - px(fl - 1, i);                   // 2 * ((in2 - in1) / 2)
+                switch (i & 3) {
+                case 0: Qs += d; QOs += e; break;    // cosine +1
+                case 1: Ps += d; POs += e; break;    // sine +1
+                case 2: Qs -= d; QOs -= e; break;    // cosine -1
+                default: Ps -= d; POs -= e; break;   // sine -1
+                }
+            }
+        }
+#pragma unroll
+        for (int h = 16; h >= 1; h >>= 1) {
+            Ps += __shfl_xor_sync(0xffffffffu, Ps, h);
+            Qs += __shfl_xor_sync(0xffffffffu, Qs, h);
+            POs += __shfl_xor_sync(0xffffffffu, POs, h);
+            QOs += __shfl_xor_sync(0xffffffffu, QOs, h);
+        }
+        if (lane == 0) {
+            const double len = (double)(P.burst_end - P.burst_start);
+            // bp = P/(4 len), bpo = PO/(2 len): the V-switch test scaled by (4 len)^2
+            const long long a = Ps - 2 * POs, b = Qs - 2 * QOs;
+            const bool vpos = (a * a + b * b) < 2 * (Ps * Ps + Qs * Qs);
+            const double bp = (double)(Ps - 2 * QOs) / (8.0 * len);
+            const double bq = (double)(Qs + 2 * POs) / (8.0 * len);
+            const double n = fmax(sqrt(bp * bp + bq * bq), 130000.0 / 128);
+            const double nbp = bp / n, nbq = bq / n;
+            s_bp[warp] = (float)(nbp * P.gain_cos - nbq * P.gain_sin);
+            s_bq[warp] = (float)(nbp * P.gain_sin + nbq * P.gain_cos);
+            s_vsw[warp] = vpos ? 1.f : -1.f;
+        }
+    }
+    __syncthreads();
+
+    // 3. vertical combinations (palcolour.cpp:557-567 without the carrier):
+    //    v0 = c0, v1 = -c(-2) - c(+2), v2 = c(-1) - c(+1), v3 = -c(-3) + c(+3)
+    for (int idx = threadIdx.x; idx < kDemodLines * SW; idx += blockDim.x) {
+        const int t = idx / SW;
+        const int x = idx % SW;
+        const float *r0 = ch + (t + 0) * SW + x;
+        float *d = vv + (t * 4) * SW + x;
+        d[0] = r0[3 * SW];
+        d[SW] = -r0[1 * SW] - r0[5 * SW];
+        d[2 * SW] = r0[2 * SW] - r0[4 * SW];
+        d[3 * SW] = -r0[0] + r0[6 * SW];
+    }
+    __syncthreads();
+
+    // 4. 2D FIR + rotation + pack
+    const int per_line = span / 8;
+    const int t = threadIdx.x / per_line;
+    const int seg = threadIdx.x % per_line;
+    if (t >= kDemodLines) return;
+    const int fl = fl0 + t;
+    if (fl >= fl_last) return;
+    const int xl0 = seg * 8;   // local index of the first sample (absolute base4 + xl0, a multiple of 4)
+    float v[4][22];
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+#pragma unroll
+        for (int q = 0; q < 22; q++) v[k][q] = vv[(t * 4 + k) * SW + kPad + xl0 - 7 + q];
+
+    float PU[8], QU[8], PV[8], QV[8];
+#pragma unroll
+    for (int s = 0; s < 8; s++) {
+        float PA = 0.f, PB = 0.f, QA = 0.f, QB = 0.f;
+#pragma unroll
+        for (int b = 0; b < 8; b++) {
+            const int r = s + b + 7, l = s - b + 7;
+            float sg[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) sg[k] = (b & 1) ? v[k][r] - v[k][l] : v[k][r] + v[k][l];
+            const float A = __fmaf_rn(cd_cfilt[b][1], sg[1], cd_cfilt[b][0] * sg[0]);
+            const float B = __fmaf_rn(cd_cfilt[b][3], sg[3], cd_cfilt[b][2] * sg[2]);
+            switch ((s + b) & 3) {
+            case 1: PA += A; PB += B; break;
+            case 3: PA -= A; PB -= B; break;
+            case 0: QA += A; QB += B; break;
+            default: QA -= A; QB -= B; break;
+            }
+        }
+        PU[s] = PA + QB;
+        PV[s] = PA - QB;
+        QU[s] = QA - PB;
+        QV[s] = QA + PB;
+    }
+
+    const float bp = s_bp[t], bq = s_bq[t], vsw = s_vsw[t];
+    const int frame_row = 2 * fl + off;
+    const int orow = P.top_pad + frame_row - P.fafl;
+    const long long frame = o >> 1;   // field_begin is even: fields 2k, 2k+1 form frame k
+    const long long plane = (long long)P.out_w * P.out_h;
+    const long long rowbase = frame * P.out_frame_stride + (long long)orow * P.out_w + P.left_pad;
+    const uint16_t *comp = field + (long long)fl * P.fw;
+#pragma unroll
+    for (int s = 0; s < 8; s++) {
+        const int x = base4 + xl0 + s;
+        if (x < P.avs || x >= P.ave) continue;
+        const float c0 = v[0][s + 7];
+        const float Y = (float)comp[x] - c0;
+        const float U = -(PU[s] * bp + QU[s] * bq) * 2.0f;
+        const float V = vsw * -(QV[s] * bp - PV[s] * bq) * 2.0f;
+        const float ey = (Y - (float)P.black) * P.ey_scale;
+        const float ecb = U * P.ecb_scale;
+        const float ecr = V * P.ecr_scale;
+        const long long e = rowbase + (x - P.avs);
+        if (P.format == 1) {
+            float *out = (float *)P.out;
+            out[e] = fminf(fmaxf(ey, P.y_lo), P.y_hi);
+            out[e + plane] = fminf(fmaxf(ecb, P.c_lo), P.c_hi);
+            out[e + 2 * plane] = fminf(fmaxf(ecr, P.c_lo), P.c_hi);
+        } else {
+            uint16_t *out = (uint16_t *)P.out;
+            // H.273 Round(x) = Sign(x) * Floor(Abs(x) + 0.5), output_writer.cpp:60-76
+            auto q = [](float x, float lo, float hi) -> uint16_t {
+                const float r = copysignf(floorf(fabsf(x) + 0.5f), x);
+                return (uint16_t)fminf(fmaxf(r, lo), hi);
+            };
+            out[e] = q(__fmaf_rn(219.0f * 256.0f, ey, 16.0f * 256.0f), P.y_lo, P.y_hi);
+            out[e + plane] = q(__fmaf_rn(224.0f * 256.0f, ecb, 128.0f * 256.0f), P.c_lo, P.c_hi);
+            out[e + 2 * plane] = q(__fmaf_rn(224.0f * 256.0f, ecr, 128.0f * 256.0f), P.c_lo, P.c_hi);
+        }
+    }
+}
+
+// PalColour::buildLookUpTables chroma taps (palcolour.cpp:197-276), in double.
+int demod_init_constants(int device, double sample_rate, int /*field_width*/)
+{
+    if (device >= 0 && device < 64 && g_demod_ready[device]) return 0;
+    const double chromaBandwidthHz = 1100000.0 / 0.93;
+    const double ca = 0.5 * sample_rate / chromaBandwidthHz;
+    int fs = 1;
+    if ((int)ca > fs) fs = (int)ca;
+    if (fs != 7) return -2;   // the kernel's tap count is fixed for 4fsc PAL
+    double cf[8][4] = {};
+    double cdiv = 0;
+    for (int f = 0; f <= fs; f++) {
+        const double fc = std::min(ca, (double)f);
+        const double ff = std::min(ca, sqrt((double)(f * f + 4)));
+        const double fff = std::min(ca, sqrt((double)(f * f + 16)));
+        const double ffff = std::min(ca, sqrt((double)(f * f + 36)));
+        const int d = (f == 0) ? 2 : 1;
+        cf[f][0] = (1 + cos(M_PI * fc / ca)) / d;
+        cf[f][2] = (1 + cos(M_PI * ff / ca)) / d;
+        cf[f][1] = (1 + cos(M_PI * fff / ca)) / d;
+        cf[f][3] = (1 + cos(M_PI * ffff / ca)) / d;
+        cdiv += 2 * (1 * cf[f][0] + 2 * cf[f][2] + 2 * cf[f][1] + 2 * cf[f][3]);
+    }
+    float cff[8][4];
+    for (int f = 0; f < 8; f++)
+        for (int i = 0; i < 4; i++) cff[f][i] = (float)(cf[f][i] / cdiv);
+    if (cudaMemcpyToSymbol(cd_cfilt, cff, sizeof(cff)) != cudaSuccess) return -1;
+    if (device >= 0 && device < 64) g_demod_ready[device] = true;
+    return 0;
+}
+
+size_t demod_smem_bytes(int avs, int ave)
+{
+    const int base4 = avs & ~3;
+    const int span = ((ave - base4) + 7) & ~7;
+    const int SW = span + 2 * kPad;
+    return sizeof(float) * (size_t)(10 + 4 * kDemodLines) * SW;
+}
+
+int demod_launch(const DemodParams &P, cudaStream_t stream)
+{
+    if (P.nout <= 0) return 0;
+    const int base4 = P.avs & ~3;
+    const int span = ((P.ave - base4) + 7) & ~7;
+    if ((span / 8) * kDemodLines > kDemodThreads) return -2;   // line too wide for one block
+    const size_t smem = demod_smem_bytes(P.avs, P.ave);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(demod_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr_set = true;
+    }
+    const int nblk_per_field = (P.fh + kDemodLines - 1) / kDemodLines;
+    demod_kernel<<<(unsigned)(P.nout * nblk_per_field), kDemodThreads, smem, stream>>>(P);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace tpal

@@ -1,0 +1,430 @@
+// engine.cu -- host side of the device pipeline: geometry, constant tables,
+// scratch, launches. Implements include/chromadec_gb300.h.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/chromadec_gb300.h"
+#include "engine.h"
+#include "error_state.h"
+#include "tpal_kernels.h"
+
+namespace tpal {
+size_t demod_smem_bytes(int avs, int ave);
+}
+
+namespace chdg {
+
+static int cuda_fail(const char *what, cudaError_t e)
+{
+    chd::detail::set_last_error(std::string("chromadec_gb300: ") + what + ": " + cudaGetErrorString(e));
+    return CHDG_E_CUDA;
+}
+
+static int arg_fail(const std::string &what)
+{
+    chd::detail::set_last_error("chromadec_gb300: " + what);
+    return CHDG_E_INVALID_ARG;
+}
+
+static int first_line(int fafl, int off) { return (fafl + 1 - off) / 2; }
+static int last_line(int lafl, int off) { return ((lafl - off) / 2) + 1; }
+
+void output_geometry(const chdg_geometry &g, int padding, int &w, int &h, int &lp, int &tp)
+{
+    // OutputWriter::updateConfiguration, src/output/output_writer.cpp:195-239
+    const int aw = g.active_end - g.active_start;
+    const int ah = (g.last_active_frame_line - g.first_active_frame_line) + 1;
+    int l = 0, r = 0, t = 0, b = 0, ow = aw, oh = ah;
+    if (padding > 1) {
+        while ((ow % padding) != 0) {
+            if ((ow % 2) == 0) r++;
+            else l++;
+            ow = l + aw + r;
+        }
+        while ((oh % padding) != 0) {
+            if ((oh % 2) == 0) b++;
+            else t++;
+            oh = t + ah + b;
+        }
+    }
+    w = ow;
+    h = oh;
+    lp = l;
+    tp = t;
+}
+
+Engine::~Engine()
+{
+    if (partial_) cudaFree(partial_);
+    if (thr_dev_) cudaFree(thr_dev_);
+    if (stats_dev_) cudaFree(stats_dev_);
+}
+
+int Engine::init(const chdg_geometry &g, const chdg_config &c)
+{
+    g_ = g;
+    c_ = c;
+    if (c.kind != 7 && c.kind != 8) return arg_fail("kind must be CHD_DEC_TRANSFORM_2D (7) or CHD_DEC_TRANSFORM_3D (8)");
+    if (g.field_width <= 0 || g.field_height <= 0 || g.active_start < 0 || g.active_end > g.field_width ||
+        g.active_end <= g.active_start || g.first_active_frame_line < 0 ||
+        g.last_active_frame_line >= 2 * g.field_height - 1 || g.last_active_frame_line < g.first_active_frame_line)
+        return arg_fail("invalid geometry");
+    if (std::fabs(g.fsc / g.sample_rate - 0.25) > 1e-9)
+        return chd::detail::set_last_error("chromadec_gb300: only 4fsc sampling is supported"), CHDG_E_UNSUPPORTED;
+    if (g.active_start - 7 < 0 || g.active_end + 8 > 1135 || g.field_width > 1135)
+        return chd::detail::set_last_error("chromadec_gb300: active window too close to the line ends"),
+               CHDG_E_UNSUPPORTED;
+    if (c.output_format != 0 && c.output_format != 1) return arg_fail("output_format must be 0 or 1");
+    if (c.padding_multiple < 1 || c.padding_multiple > 1024) return arg_fail("padding_multiple out of range");
+    const int nthr = (c.kind == 7) ? 80 : 768;
+    if (c.thresholds != nullptr && c.n_thresholds != nthr)
+        return arg_fail("thresholds table must have " + std::to_string(nthr) + " entries");
+
+    cudaError_t e = cudaGetDevice(&device_);
+    if (e != cudaSuccess) return cuda_fail("cudaGetDevice", e);
+    if (c.kind == 8) {
+        if (tpal::tp3_init_constants(device_) != 0) return cuda_fail("3D constants", cudaGetLastError());
+    } else {
+        if (tpal::tp2_init_constants(device_) != 0) return cuda_fail("2D constants", cudaGetLastError());
+    }
+    if (const int rc = tpal::demod_init_constants(device_, g.sample_rate, g.field_width); rc != 0)
+        return rc == -2 ? (chd::detail::set_last_error("chromadec_gb300: unsupported chroma filter size"),
+                           CHDG_E_UNSUPPORTED)
+                        : cuda_fail("demod constants", cudaGetLastError());
+
+    // Squared thresholds (TransformPal::updateConfiguration, transform_pal.cpp:53-78)
+    const double t2 = c.threshold * c.threshold;
+    t2f_ = (float)t2;
+    t2hi_ = (float)t2;
+    t2lo_ = (float)(t2 - (double)t2hi_);
+    if (c.thresholds != nullptr) {
+        std::vector<float> tab(3 * nthr);
+        for (int i = 0; i < nthr; i++) {
+            const double v = c.thresholds[i] * c.thresholds[i];
+            tab[3 * i] = (float)v;
+            tab[3 * i + 1] = (float)v;
+            tab[3 * i + 2] = (float)(v - (double)(float)v);
+        }
+        if ((e = cudaMalloc(&thr_dev_, sizeof(float) * tab.size())) != cudaSuccess) return cuda_fail("cudaMalloc", e);
+        if ((e = cudaMemcpy(thr_dev_, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+            return cuda_fail("cudaMemcpy", e);
+    }
+    if ((e = cudaMalloc(&stats_dev_, sizeof(unsigned) * 4)) != cudaSuccess) return cuda_fail("cudaMalloc", e);
+    cudaMemset(stats_dev_, 0, sizeof(unsigned) * 4);
+
+    fl_lo_ = g.first_active_frame_line / 2;
+    fl_hi_ = g.last_active_frame_line / 2 + 1;
+    rows_ = fl_hi_ - fl_lo_;
+    cols_ = g.active_end - g.active_start;
+    output_geometry(g, c.padding_multiple, out_w_, out_h_, left_pad_, top_pad_);
+    return 0;
+}
+
+size_t Engine::frame_bytes() const
+{
+    return (size_t)out_w_ * out_h_ * 3 * (c_.output_format == 1 ? sizeof(float) : sizeof(uint16_t));
+}
+
+int Engine::ensure_partial(int nout_fields)
+{
+    const size_t need = (size_t)4 * nout_fields * rows_ * cols_;
+    if (need <= partial_elems_) return 0;
+    if (partial_) cudaFree(partial_);
+    partial_ = nullptr;
+    partial_elems_ = 0;
+    cudaError_t e = cudaMalloc(&partial_, need * sizeof(float));
+    if (e != cudaSuccess) {
+        chd::detail::set_last_error("chromadec_gb300: out of device memory for chroma scratch");
+        return CHDG_E_OOM;
+    }
+    partial_elems_ = need;
+    return 0;
+}
+
+int Engine::run_transform(const uint16_t *fields, long long stride, int nfields, int fb, int fe, float *partial,
+                          cudaStream_t s)
+{
+    const long long cls_stride = (long long)(fe - fb) * 2 * rows_ * cols_;
+    if (c_.kind == 8) {
+        tpal::T3Params P{};
+        P.fields = fields;
+        P.field_stride = stride;
+        P.nfields = nfields;
+        P.fw = g_.field_width;
+        P.avs = g_.active_start;
+        P.ave = g_.active_end;
+        P.fafl = g_.first_active_frame_line;
+        P.lafl = g_.last_active_frame_line;
+        P.black = g_.black;
+        // transform_pal_3d.cpp:151-153 tile grid
+        P.tileX0 = g_.active_start - 8;
+        P.ntx = (g_.active_end - P.tileX0 + 7) / 8;
+        P.tileY0 = g_.first_active_frame_line - 16;
+        P.nty = (g_.last_active_frame_line - P.tileY0) / 16 + 1;
+        P.frame_begin = fb;
+        P.frame_end = fe;
+        P.chunk_frames = chunk_frames_;
+        P.nchunks = (fe - fb + chunk_frames_ - 1) / chunk_frames_;
+        P.partial = partial;
+        P.part_class_stride = cls_stride;
+        P.part_field_stride = (long long)rows_ * cols_;
+        P.part_row_stride = cols_;
+        P.fl_lo = fl_lo_;
+        P.t2f = t2f_;
+        P.t2hi = t2hi_;
+        P.t2lo = t2lo_;
+        P.thr_table = thr_dev_;
+        P.stats = stats_dev_;
+        if (tpal::tp3_launch(P, s) != 0) return cuda_fail("tpal3d launch", cudaGetLastError());
+    } else {
+        tpal::T2Params P{};
+        P.fields = fields;
+        P.field_stride = stride;
+        P.nfields = nfields;
+        P.fw = g_.field_width;
+        P.avs = g_.active_start;
+        P.ave = g_.active_end;
+        P.fafl = g_.first_active_frame_line;
+        P.lafl = g_.last_active_frame_line;
+        P.black = g_.black;
+        P.field_begin = 2 * fb;
+        P.nout = 2 * (fe - fb);
+        P.partial = partial;
+        P.part_class_stride = cls_stride;
+        P.part_field_stride = (long long)rows_ * cols_;
+        P.part_row_stride = cols_;
+        P.fl_lo = fl_lo_;
+        P.t2f = t2f_;
+        P.t2hi = t2hi_;
+        P.t2lo = t2lo_;
+        P.thr_table = thr_dev_;
+        P.stats = stats_dev_;
+        if (tpal::tp2_launch(P, s) != 0) return cuda_fail("tpal2d launch", cudaGetLastError());
+    }
+    return 0;
+}
+
+int Engine::run_demod(const uint16_t *fields, long long stride, int fb, int fe, const float *partial, void *out,
+                      cudaStream_t s)
+{
+    tpal::DemodParams D{};
+    D.fields = fields;
+    D.field_stride = stride;
+    D.field_begin = 2 * fb;
+    D.nout = 2 * (fe - fb);
+    D.fw = g_.field_width;
+    D.fh = g_.field_height;
+    D.avs = g_.active_start;
+    D.ave = g_.active_end;
+    D.fafl = g_.first_active_frame_line;
+    D.lafl = g_.last_active_frame_line;
+    D.burst_start = g_.burst_start;
+    D.burst_end = g_.burst_end;
+    D.black = g_.black;
+    D.white = g_.white;
+    D.partial = partial;
+    D.part_class_stride = (long long)(fe - fb) * 2 * rows_ * cols_;
+    D.part_field_stride = (long long)rows_ * cols_;
+    D.part_row_stride = cols_;
+    D.fl_lo = fl_lo_;
+    D.nclasses = 4;
+    const double th = (c_.chroma_phase_deg * M_PI) / 180;
+    D.gain_cos = (float)(cos(th) * c_.chroma_gain);
+    D.gain_sin = (float)(sin(th) * c_.chroma_gain);
+    D.format = c_.output_format;
+    D.out = out;
+    D.out_frame_stride = (long long)out_w_ * out_h_ * 3;
+    D.out_w = out_w_;
+    D.out_h = out_h_;
+    D.left_pad = left_pad_;
+    D.top_pad = top_pad_;
+    const double range = (double)(g_.white - g_.black);
+    D.ey_scale = (float)(1.0 / range);
+    D.ecb_scale = (float)(c_.ecb_from_u / range);
+    D.ecr_scale = (float)(c_.ecr_from_v / range);
+    // output_writer.cpp:84-143 clamp bounds
+    if (c_.output_format == 1) {
+        switch (c_.clamp_mode) {
+        case 1: D.y_lo = 0.f; D.y_hi = 1.f; D.c_lo = -0.5f; D.c_hi = 0.5f; break;
+        case 3: D.y_lo = -15.0f / 219.0f; D.y_hi = 238.75f / 219.0f; D.c_lo = -127.0f / 224.0f; D.c_hi = 126.75f / 224.0f; break;
+        default: D.y_lo = -INFINITY; D.y_hi = INFINITY; D.c_lo = -INFINITY; D.c_hi = INFINITY;
+        }
+    } else {
+        switch (c_.clamp_mode) {
+        case 1: D.y_lo = 16.f * 256.f; D.y_hi = 235.f * 256.f; D.c_lo = 16.f * 256.f; D.c_hi = 240.f * 256.f; break;
+        case 3: D.y_lo = 256.f; D.y_hi = 254.75f * 256.f; D.c_lo = 256.f; D.c_hi = 254.75f * 256.f; break;
+        default: D.y_lo = 0.f; D.y_hi = 65535.f; D.c_lo = 0.f; D.c_hi = 65535.f;
+        }
+    }
+    if (padded()) {
+        // black border: Y 16*256 / Cb,Cr 128*256 (p16), zeros (ps)
+        const int rc = fill_border(out, fe - fb, s);
+        if (rc != 0) return rc;
+    }
+    const int rc = tpal::demod_launch(D, s);
+    if (rc != 0) return cuda_fail("demod launch", cudaGetLastError());
+    return 0;
+}
+
+__global__ void fill_frames_kernel(uint16_t *o16, float *o32, long long plane, long long nframes, uint16_t y, uint16_t c)
+{
+    const long long n = nframes * 3 * plane;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        if (o16) o16[i] = ((i / plane) % 3 == 0) ? y : c;
+        else o32[i] = 0.f;
+    }
+}
+
+int Engine::fill_border(void *out, int nframes, cudaStream_t s)
+{
+    const long long plane = (long long)out_w_ * out_h_;
+    if (c_.output_format == 1)
+        fill_frames_kernel<<<1024, 256, 0, s>>>(nullptr, (float *)out, plane, nframes, 0, 0);
+    else
+        fill_frames_kernel<<<1024, 256, 0, s>>>((uint16_t *)out, nullptr, plane, nframes, 16 * 256, 128 * 256);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? 0 : cuda_fail("fill", e);
+}
+
+int Engine::decode(const uint16_t *fields, long long stride, int nfields, int fb, int fe, void *out, cudaStream_t s)
+{
+    if (fields == nullptr || out == nullptr || fe < fb || stride < (long long)g_.field_width * g_.field_height)
+        return arg_fail("decode: bad arguments");
+    const int maxb = max_batch_frames_;
+    char *o = (char *)out;
+    for (int b = fb; b < fe; b += maxb) {
+        const int be = std::min(fe, b + maxb);
+        if (const int rc = ensure_partial(2 * (be - b)); rc != 0) return rc;
+        if (const int rc = run_transform(fields, stride, nfields, b, be, partial_, s); rc != 0) return rc;
+        if (const int rc = run_demod(fields, stride, b, be, partial_, o, s); rc != 0) return rc;
+        o += frame_bytes() * (size_t)(be - b);
+    }
+    return 0;
+}
+
+__global__ void sum_classes_kernel(const float *part, long long cls_stride, long long n, float *out)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = part[i] + part[i + cls_stride] + part[i + 2 * cls_stride] + part[i + 3 * cls_stride];
+}
+
+int Engine::chroma(const uint16_t *fields, long long stride, int nfields, int fb, int fe, float *out, cudaStream_t s)
+{
+    if (fields == nullptr || out == nullptr || fe < fb) return arg_fail("chroma: bad arguments");
+    if (const int rc = ensure_partial(2 * (fe - fb)); rc != 0) return rc;
+    if (const int rc = run_transform(fields, stride, nfields, fb, fe, partial_, s); rc != 0) return rc;
+    const long long n = (long long)(fe - fb) * 2 * rows_ * cols_;
+    sum_classes_kernel<<<1024, 256, 0, s>>>(partial_, n, n, out);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? 0 : cuda_fail("sum", e);
+}
+
+int Engine::stats(uint64_t *exact, uint64_t *flips)
+{
+    unsigned h[4];
+    cudaError_t e = cudaMemcpy(h, stats_dev_, sizeof(h), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail("stats", e);
+    if (exact) *exact = h[0];
+    if (flips) *flips = h[1];
+    return 0;
+}
+
+}  // namespace chdg
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+struct chdg_engine {
+    chdg::Engine eng;
+};
+
+#pragma GCC visibility push(default)
+extern "C" {
+
+void chdg_default_geometry(chdg_geometry *g)
+{
+    if (!g) return;
+    // src/format/video_standards.cpp:58-70,116-207 (line-locked PAL preset);
+    // active frame lines from src/metadata/core.cpp:40-50.
+    g->field_width = 1135;
+    g->field_height = 313;
+    g->active_start = 177;
+    g->active_end = 1125;
+    g->first_active_frame_line = 44;
+    g->last_active_frame_line = 619;
+    g->burst_start = 98;
+    g->burst_end = 138;
+    g->black = 256 * 64;
+    g->white = 844 * 64;
+    g->sample_rate = 4.0 * 625.0 * 25.0 * (1135.0 / 4.0 + 1.0 / 625.0);
+    g->fsc = 283.75 * 15625.0 + 25.0;
+}
+
+void chdg_default_config(chdg_config *c, int32_t kind)
+{
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->kind = kind;
+    c->threshold = 0.4;
+    c->chroma_gain = 1.0;
+    c->chroma_phase_deg = 0.0;
+    c->output_format = 0;
+    c->clamp_mode = 0;
+    c->padding_multiple = 1;
+    // src/common/color_conversion.cpp:33-66 at Modern / Scientific
+    const double kb = 0.114, kr = 0.299;
+    c->ecb_from_u = 1.0 / ((2.0 * (1.0 - kb)) * 0.49211104112248356308804691718185);
+    c->ecr_from_v = 1.0 / ((2.0 * (1.0 - kr)) * 0.87728321993817866838972487283129);
+}
+
+int chdg_engine_create(const chdg_geometry *g, const chdg_config *c, chdg_engine **out)
+{
+    if (!g || !c || !out) return chdg::arg_fail("chdg_engine_create: null argument");
+    *out = nullptr;
+    auto e = std::make_unique<chdg_engine>();
+    if (const int rc = e->eng.init(*g, *c); rc != 0) return rc;
+    *out = e.release();
+    return 0;
+}
+
+void chdg_engine_free(chdg_engine *e) { delete e; }
+
+int chdg_output_geometry(const chdg_engine *e, int32_t *width, int32_t *height, size_t *frame_bytes)
+{
+    if (!e) return chdg::arg_fail("chdg_output_geometry: null engine");
+    if (width) *width = e->eng.out_w();
+    if (height) *height = e->eng.out_h();
+    if (frame_bytes) *frame_bytes = e->eng.frame_bytes();
+    return 0;
+}
+
+int chdg_decode_device(chdg_engine *e, const uint16_t *d_fields, int64_t field_stride, int32_t nfields,
+                       int32_t frame_begin, int32_t frame_end, void *d_out, void *stream)
+{
+    if (!e) return chdg::arg_fail("chdg_decode_device: null engine");
+    return e->eng.decode(d_fields, field_stride, nfields, frame_begin, frame_end, d_out, (cudaStream_t)stream);
+}
+
+int chdg_chroma_device(chdg_engine *e, const uint16_t *d_fields, int64_t field_stride, int32_t nfields,
+                       int32_t frame_begin, int32_t frame_end, float *d_chroma, void *stream)
+{
+    if (!e) return chdg::arg_fail("chdg_chroma_device: null engine");
+    return e->eng.chroma(d_fields, field_stride, nfields, frame_begin, frame_end, d_chroma, (cudaStream_t)stream);
+}
+
+int chdg_engine_stats(chdg_engine *e, uint64_t *exact_decisions, uint64_t *fp32_flips)
+{
+    if (!e) return chdg::arg_fail("chdg_engine_stats: null engine");
+    return e->eng.stats(exact_decisions, fp32_flips);
+}
+
+}  // extern "C"
+#pragma GCC visibility pop

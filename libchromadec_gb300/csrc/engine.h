@@ -1,0 +1,63 @@
+// engine.h -- the device pipeline behind chromadec_gb300.h and the chd_* ABI.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "../../include/chromadec_gb300.h"
+
+namespace chdg {
+
+void output_geometry(const chdg_geometry &g, int padding, int &w, int &h, int &lp, int &tp);
+
+class Engine {
+public:
+    Engine() = default;
+    ~Engine();
+    Engine(const Engine &) = delete;
+    Engine &operator=(const Engine &) = delete;
+
+    int init(const chdg_geometry &g, const chdg_config &c);
+    int decode(const uint16_t *fields, long long stride, int nfields, int fb, int fe, void *out, cudaStream_t s);
+    int chroma(const uint16_t *fields, long long stride, int nfields, int fb, int fe, float *out, cudaStream_t s);
+    int stats(uint64_t *exact, uint64_t *flips);
+
+    int out_w() const { return out_w_; }
+    int out_h() const { return out_h_; }
+    int left_pad() const { return left_pad_; }
+    int top_pad() const { return top_pad_; }
+    size_t frame_bytes() const;
+    const chdg_geometry &geometry() const { return g_; }
+    const chdg_config &config() const { return c_; }
+    int look_behind() const { return c_.kind == 8 ? 2 : 0; }   // TransformPal3D::getLookBehind
+    int look_ahead() const { return c_.kind == 8 ? 4 : 0; }    // TransformPal3D::getLookAhead
+    void set_max_batch_frames(int n) { max_batch_frames_ = n > 0 ? n : 1; }
+    void set_chunk_frames(int n) { chunk_frames_ = n > 0 ? n : 1; }
+
+private:
+    bool padded() const { return left_pad_ || top_pad_ || out_w_ != (g_.active_end - g_.active_start) ||
+                                 out_h_ != (g_.last_active_frame_line - g_.first_active_frame_line + 1); }
+    int ensure_partial(int nout_fields);
+    int run_transform(const uint16_t *fields, long long stride, int nfields, int fb, int fe, float *partial,
+                      cudaStream_t s);
+    int run_demod(const uint16_t *fields, long long stride, int fb, int fe, const float *partial, void *out,
+                  cudaStream_t s);
+    int fill_border(void *out, int nframes, cudaStream_t s);
+
+    chdg_geometry g_{};
+    chdg_config c_{};
+    int device_ = 0;
+    float t2f_ = 0.f, t2hi_ = 0.f, t2lo_ = 0.f;
+    float *thr_dev_ = nullptr;
+    unsigned *stats_dev_ = nullptr;
+    float *partial_ = nullptr;
+    size_t partial_elems_ = 0;
+    int fl_lo_ = 0, fl_hi_ = 0, rows_ = 0, cols_ = 0;
+    int out_w_ = 0, out_h_ = 0, left_pad_ = 0, top_pad_ = 0;
+    int max_batch_frames_ = 128;
+    int chunk_frames_ = 16;
+};
+
+}  // namespace chdg

@@ -1,0 +1,79 @@
+// tpal_kernels.h -- launch parameters of the sm_103a kernels (host + device).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace tpal {
+
+// Device field buffer: field f (absolute index in the capture, first field of
+// each frame at even f) starts at fields + f * field_stride. Fields outside
+// [0, nfields) are black padding frames and read as zero after black removal.
+//
+// Chroma partial planes: 4 overlap classes x output fields x rows x cols, in
+// FP32; row r is field line fl_lo + r, column c is sample avs + c. Output
+// field o is field 2 * frame_begin + o.
+
+struct T3Params {
+    const uint16_t *fields;
+    long long field_stride;
+    int nfields;
+    int fw;
+    int avs, ave, fafl, lafl;   // active samples [avs, ave), frame lines [fafl, lafl]
+    int black;
+    int tileX0, ntx, tileY0, nty;
+    int frame_begin, frame_end, chunk_frames, nchunks;
+    float *partial;
+    long long part_class_stride, part_field_stride;
+    int part_row_stride, fl_lo;
+    float t2f, t2hi, t2lo;       // uniform squared threshold (FP32 and double-float)
+    const float *thr_table;      // per-bin squared thresholds [8][32][3] x (f, hi, lo), or null
+    unsigned int *stats;         // [0] exact decisions taken, [1] of which FP32 was wrong
+};
+
+struct T2Params {
+    const uint16_t *fields;
+    long long field_stride;
+    int nfields;
+    int fw;
+    int avs, ave, fafl, lafl;
+    int black;
+    int field_begin, nout;       // output fields [field_begin, field_begin + nout)
+    float *partial;
+    long long part_class_stride, part_field_stride;
+    int part_row_stride, fl_lo;
+    float t2f, t2hi, t2lo;
+    const float *thr_table;      // [16][5] x (f, hi, lo), or null
+    unsigned int *stats;
+};
+
+// PALcolour demodulation + H.273 pack of output fields.
+struct DemodParams {
+    const uint16_t *fields;      // same buffer as the transform's
+    long long field_stride;
+    int field_begin, nout;       // output field o is absolute field field_begin + o
+    int fw, fh;
+    int avs, ave, fafl, lafl;
+    int burst_start, burst_end;
+    int black, white;
+    const float *partial;        // chroma partial planes as above
+    long long part_class_stride, part_field_stride;
+    int part_row_stride, fl_lo;
+    int nclasses;                // 4 for the Transform kinds
+    float gain_cos, gain_sin;    // chroma_gain * (cos, sin)(chroma_phase)
+    int format;                  // 0 = yuv444p16, 1 = yuv444ps
+    void *out;                   // frames: [Y | Cb | Cr] planes of out_w x out_h
+    long long out_frame_stride;  // elements per frame
+    int out_w, out_h, left_pad, top_pad;
+    float ey_scale, ecb_scale, ecr_scale;   // 1/range, ecbFromU/range, ecrFromV/range
+    float y_lo, y_hi, c_lo, c_hi;           // clamp bounds (code units for p16, E' for ps)
+};
+
+int tp3_init_constants(int device);
+int tp3_launch(const T3Params &p, cudaStream_t stream);
+int tp2_init_constants(int device);
+int tp2_launch(const T2Params &p, cudaStream_t stream);
+int demod_init_constants(int device, double sample_rate, int field_width);
+int demod_launch(const DemodParams &p, cudaStream_t stream);
+
+}  // namespace tpal

@@ -1,0 +1,149 @@
+"""ctypes binding of the device-level entry points (include/chromadec_gb300.h).
+
+Device buffers are torch CUDA tensors (plumbing only: allocation, streams);
+all compute runs in libchromadec_gb300.so. There is no CPU fallback: loading
+fails loudly when the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional, Sequence
+
+from . import _build
+
+KIND_TRANSFORM_2D = 7
+KIND_TRANSFORM_3D = 8
+FMT_P16 = 0
+FMT_PS = 1
+
+
+class Geometry(C.Structure):
+    _fields_ = [
+        ("field_width", C.c_int32), ("field_height", C.c_int32),
+        ("active_start", C.c_int32), ("active_end", C.c_int32),
+        ("first_active_frame_line", C.c_int32), ("last_active_frame_line", C.c_int32),
+        ("burst_start", C.c_int32), ("burst_end", C.c_int32),
+        ("black", C.c_int32), ("white", C.c_int32),
+        ("sample_rate", C.c_double), ("fsc", C.c_double),
+    ]
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("threshold", C.c_double),
+        ("thresholds", C.POINTER(C.c_double)), ("n_thresholds", C.c_int32),
+        ("chroma_gain", C.c_double), ("chroma_phase_deg", C.c_double),
+        ("output_format", C.c_int32), ("clamp_mode", C.c_int32), ("padding_multiple", C.c_int32),
+        ("ecb_from_u", C.c_double), ("ecr_from_v", C.c_double),
+    ]
+
+
+_lib = None
+
+
+def lib(build: bool = True):
+    """Load libchromadec_gb300.so (building it in-tree if needed)."""
+    global _lib
+    if _lib is None:
+        path = _build.build() if build else _build.LIB
+        if not os.path.exists(path):
+            raise RuntimeError("libchromadec_gb300.so is missing; run __graft_entry__.build()")
+        L = C.CDLL(path)
+        L.chdg_default_geometry.argtypes = [C.POINTER(Geometry)]
+        L.chdg_default_config.argtypes = [C.POINTER(Config), C.c_int32]
+        L.chdg_engine_create.argtypes = [C.POINTER(Geometry), C.POINTER(Config), C.POINTER(C.c_void_p)]
+        L.chdg_engine_free.argtypes = [C.c_void_p]
+        L.chdg_output_geometry.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                           C.POINTER(C.c_size_t)]
+        L.chdg_decode_device.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
+                                         C.c_void_p, C.c_void_p]
+        L.chdg_chroma_device.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
+                                         C.c_void_p, C.c_void_p]
+        L.chdg_engine_stats.argtypes = [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+        L.chd_last_error.restype = C.c_char_p
+        _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    return lib().chd_last_error().decode(errors="replace")
+
+
+def default_geometry() -> Geometry:
+    g = Geometry()
+    lib().chdg_default_geometry(C.byref(g))
+    return g
+
+
+def default_config(kind: int = KIND_TRANSFORM_3D, fmt: int = FMT_P16, threshold: float = 0.4,
+                   thresholds: Optional[Sequence[float]] = None, **kw) -> Config:
+    c = Config()
+    lib().chdg_default_config(C.byref(c), kind)
+    c.output_format = fmt
+    c.threshold = threshold
+    if thresholds is not None:
+        arr = (C.c_double * len(thresholds))(*thresholds)
+        c._keep = arr
+        c.thresholds = arr
+        c.n_thresholds = len(thresholds)
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+class Engine:
+    """One device pipeline (constant tables + scratch) for a geometry/config."""
+
+    def __init__(self, geometry: Optional[Geometry] = None, config: Optional[Config] = None):
+        self.geometry = geometry or default_geometry()
+        self.config = config or default_config()
+        h = C.c_void_p()
+        rc = lib().chdg_engine_create(C.byref(self.geometry), C.byref(self.config), C.byref(h))
+        if rc != 0:
+            raise RuntimeError(f"chdg_engine_create failed ({rc}): {last_error()}")
+        self._h = h
+        w, hh, fb = C.c_int32(), C.c_int32(), C.c_size_t()
+        lib().chdg_output_geometry(self._h, C.byref(w), C.byref(hh), C.byref(fb))
+        self.out_width, self.out_height, self.frame_bytes = w.value, hh.value, fb.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().chdg_engine_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _stream_ptr(stream):
+        return C.c_void_p(stream.cuda_stream if stream is not None else 0)
+
+    def decode(self, fields, frame_begin: int, frame_end: int, out, stream=None, field_stride: Optional[int] = None,
+               nfields: Optional[int] = None):
+        """fields: uint16 CUDA tensor (nfields, stride) or (nfields, h, w); out: CUDA tensor of
+        (frame_end-frame_begin) frames."""
+        stride = field_stride if field_stride is not None else fields[0].numel()
+        nf = nfields if nfields is not None else fields.shape[0]
+        rc = lib().chdg_decode_device(self._h, C.c_void_p(fields.data_ptr()), stride, nf, frame_begin, frame_end,
+                                      C.c_void_p(out.data_ptr()), self._stream_ptr(stream))
+        if rc != 0:
+            raise RuntimeError(f"chdg_decode_device failed ({rc}): {last_error()}")
+
+    def chroma(self, fields, frame_begin: int, frame_end: int, out, stream=None, field_stride: Optional[int] = None,
+               nfields: Optional[int] = None):
+        stride = field_stride if field_stride is not None else fields[0].numel()
+        nf = nfields if nfields is not None else fields.shape[0]
+        rc = lib().chdg_chroma_device(self._h, C.c_void_p(fields.data_ptr()), stride, nf, frame_begin, frame_end,
+                                      C.c_void_p(out.data_ptr()), self._stream_ptr(stream))
+        if rc != 0:
+            raise RuntimeError(f"chdg_chroma_device failed ({rc}): {last_error()}")
+
+    def stats(self):
+        a, b = C.c_uint64(), C.c_uint64()
+        lib().chdg_engine_stats(self._h, C.byref(a), C.byref(b))
+        return a.value, b.value
