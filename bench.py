@@ -1,0 +1,346 @@
+#!/usr/bin/env python3
+"""Transform-PAL 3D throughput on GB300 (fields/s), one JSON line.
+
+Workload (one "step"): decode every frame of a 500-field synthetic PAL
+capture (1135x313 uint16 fields, seeded encoder, panning 1.5 px/field and
+0.5 line/field plus a static bar region, AWGN 0.5%) with Transform-PAL 3D,
+threshold 0.4, to yuv444p16 (or yuv444ps with --format ps).
+
+  value  -- inputs already resident in HBM; device-timed (CUDA events on the
+            launching stream) over exactly --steps steps.
+  e2e    -- the same decode from pinned HOST buffers through the library's
+            host entry point: field windows uploaded and frames downloaded
+            inside the timed region (overlapped with the kernels).
+  --impl reference -- the reference's algorithm on the host cores (the CPU
+            restatement in oracle/, all threads), on a bounded sample per step.
+
+Multi-GPU: the path does not shard beyond independent replicas; under
+torchrun each rank decodes its own copy of the workload on its own GPU and
+value = fields processed by all ranks / max over ranks of the timed region.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Transform-PAL 3D fields/s on 1 GB300: plain vs TC+NN form at matched chroma PSNR"
+FIELD_BYTES_IN = 1135 * 313 * 2                  # 710,510 B per input field
+OUT_BYTES = {"p16": 948 * 288 * 3 * 2, "ps": 948 * 288 * 3 * 4}   # per output field
+# Algorithmic work per output field (fixed convention of the roofline
+# accounting: 2.5 N log2 N per real FFT each way, window, threshold, OLA,
+# demod+pack), in FLOP; bytes = input field + its output planes.
+FLOP_PER_FIELD_3D = 692_311_680
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--fields", type=int, default=500)
+    ap.add_argument("--format", default="p16", choices=["p16", "ps"])
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def workload_desc(a):
+    return (f"Transform-PAL 3D, {a.fields} PAL fields 1135x313 uint16 (seed {a.seed}, pan 1.5 px/field + "
+            f"0.5 line/field, static 75% bars, AWGN 0.5%), 8x32x16 tiles, threshold 0.4, "
+            f"yuv444{'p16' if a.format == 'p16' else 'ps'} out")
+
+
+def make_capture(a):
+    import numpy as np
+    from libchromadec_gb300 import synth
+    cache = f"/tmp/chdg_bench_{a.fields}_{a.seed}.npy"
+    if os.path.exists(cache):
+        try:
+            return np.load(cache)
+        except Exception:
+            pass
+    cap = synth.make_capture(a.fields, synth.SynthConfig(seed=a.seed, pan_x=1.5, pan_y=0.5))
+    try:
+        np.save(cache, cap.fields)
+    except Exception:
+        pass
+    return cap.fields
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def run_cpu(a, fields, nframes_sample, threads):
+    """Oracle (the reference's algorithm restated in C) on the host cores."""
+    from oracle import oracle as O
+    p = O.params(kind=3, fmt=O.FMT_P16 if a.format == "p16" else O.FMT_PS)
+    t0 = time.perf_counter()
+    O.decode_frames(p, fields, 0, nframes_sample, threads=threads)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(a, fields, budget_s=12.0):
+    threads = cpu_threads()
+    # calibrate on a few frames, then time a sample sized to the budget
+    t1 = run_cpu(a, fields, max(1, min(threads, 4)), threads)
+    per_frame = t1 / max(1, min(threads, 4)) * min(threads, 4) / threads
+    n = int(max(threads, min(fields.shape[0] // 2, budget_s / max(per_frame, 1e-6))))
+    n = min(n, fields.shape[0] // 2)
+    dt = run_cpu(a, fields, n, threads)
+    return {"value": 2 * n / dt, "unit": "fields/s", "cores": threads, "kind": "port",
+            "sample": f"frames 0..{n - 1} ({2 * n} fields) of the same capture, all {threads} host threads, "
+                      f"one decoder instance per thread (chd_decode_frames_async's model), FP64 CPU oracle"}
+
+
+def reference_arm(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    fields = make_capture(a)
+    threads = cpu_threads()
+    # each step: a bounded sample of frames, ~10 s on all host threads
+    t1 = run_cpu(a, fields, max(1, threads), threads)
+    per_frame = t1 / max(1, threads)
+    n = int(max(threads, min(fields.shape[0] // 2, 10.0 / max(per_frame, 1e-6))))
+    n = min(n, fields.shape[0] // 2)
+    for _ in range(a.warmup):
+        run_cpu(a, fields, min(n, threads), threads)
+    times = [run_cpu(a, fields, n, threads) for _ in range(a.steps)]
+    total = sum(times)
+    value = 2 * n * a.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "fields/s", "n_gpus": a.gpus,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1000 * total / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_desc(a), "sample_frames_per_step": n},
+        "cpu_baseline": {"value": value, "unit": "fields/s", "cores": threads, "kind": "port",
+                         "sample": f"{n} frames per step of the same capture, all {threads} host threads; the "
+                                   f"reference's Transform-PAL/PALcolour/OutputWriter restated in C (oracle/), "
+                                   f"FP64 FFT (FFTW is not installed on this host)"},
+        "e2e": {"value": value, "unit": "fields/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        reference_arm(a)
+        return
+    import numpy as np
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    from libchromadec_gb300 import device as D
+
+    fields_np = make_capture(a)
+    nfields = fields_np.shape[0]
+    nframes = nfields // 2
+    fmt = D.FMT_P16 if a.format == "p16" else D.FMT_PS
+    eng = D.Engine(D.default_geometry(), D.default_config(kind=D.KIND_TRANSFORM_3D, fmt=fmt))
+    lib = D.lib()
+    dfields = torch.from_numpy(fields_np.reshape(nfields, -1).view(np.int16)).cuda()
+    out_dtype = torch.int16 if fmt == D.FMT_P16 else torch.float32
+    dout = torch.empty((nframes, 3, eng.out_height, eng.out_width), dtype=out_dtype, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    # ---- device-resident value
+    for _ in range(a.warmup):
+        eng.decode(dfields, 0, nframes, dout, stream)
+    torch.cuda.synchronize()
+    lib.chdg_engine_set_profiling(eng._h, 1)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(a.steps):
+            eng.decode(dfields, 0, nframes, dout, stream)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    import ctypes as C
+    mt, md, nl = C.c_double(), C.c_double(), C.c_int64()
+    lib.chdg_engine_kernel_times(eng._h, C.byref(mt), C.byref(md), C.byref(nl))
+    lib.chdg_engine_set_profiling(eng._h, 0)
+    ms_max = ms
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+    fields_done = nfields * a.steps * world
+    value = fields_done / (ms_max / 1000.0)
+
+    # roofline of the dominant kernel (the transform): launches per step
+    launches_transform = nl.value // 2
+    per_launch_ms = mt.value / max(1, launches_transform)
+    fields_per_launch = nfields * a.steps / max(1, launches_transform)
+    bytes_per_field = FIELD_BYTES_IN + OUT_BYTES[a.format]
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fp:
+            peaks = json.load(fp)
+    except Exception:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    achieved_gbs = fields_per_launch * bytes_per_field / (per_launch_ms / 1000.0) / 1e9
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "tpal3d_traffic.json")) as fp:
+            tr = json.load(fp)
+            traffic = tr["dram_bytes_per_field"] * fields_per_launch
+    except Exception:
+        pass
+    clocks = clk.summary()
+    fp32_peak = 152 * 128 * 2 * (clocks["sm_mhz"] or 2070.0) * 1e6 / 1e12
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "fields/s", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms_max / a.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+        "config": {"workload": workload_desc(a), "fields_per_step": nfields, "frames_per_step": nframes,
+                   "format": "yuv444" + a.format, "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+                   "l2": f"inputs {nfields * FIELD_BYTES_IN / 1e6:.0f} MB > 129 MB L2 (no flush)"},
+        "roofline": {
+            "bound": "hbm", "kernel": "tpal3d_kernel", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+            "frac": achieved_gbs / hbm_peak, "traffic": traffic,
+            "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback 6.8 TB/s",
+            "algorithmic_bytes_per_field": bytes_per_field,
+            "per_launch_ms": per_launch_ms, "fields_per_launch": fields_per_launch,
+            "demod_ms_per_launch": md.value / max(1, launches_transform),
+            "fp32": {"algorithmic_tflops": fields_per_launch * FLOP_PER_FIELD_3D / (per_launch_ms / 1000.0) / 1e12,
+                     "nominal_peak_tflops": fp32_peak,
+                     "note": "convention FLOP count of the full per-tile 3D FFT; the kernel reuses per-field "
+                             "2D spectra across Z tiles, so it executes far fewer FLOPs than counted"},
+        },
+        "clocks": clocks,
+        "gpu_launches": int(nl.value),
+    }
+
+    # ---- end to end from pinned host buffers
+    if not a.no_e2e:
+        hfields = torch.from_numpy(fields_np.reshape(nfields, -1).view(np.int16)).pin_memory()
+        hout = torch.empty((nframes, 3, eng.out_height, eng.out_width), dtype=out_dtype).pin_memory()
+        for _ in range(max(1, a.warmup)):
+            rc = lib.chdg_decode_host(eng._h, C.c_void_p(hfields.data_ptr()), hfields[0].numel(), nfields, 0,
+                                      nframes, C.c_void_p(hout.data_ptr()), C.c_void_p(stream.cuda_stream))
+            if rc != 0:
+                raise RuntimeError(D.last_error())
+        torch.cuda.synchronize()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(a.steps):
+            lib.chdg_decode_host(eng._h, C.c_void_p(hfields.data_ptr()), hfields[0].numel(), nfields, 0, nframes,
+                                 C.c_void_p(hout.data_ptr()), C.c_void_p(stream.cuda_stream))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ems = e0.elapsed_time(e1)
+        if dist is not None:
+            t = torch.tensor([ems], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ems = float(t.item())
+        # bytes actually copied: 32-frame batches, each with its 3D halo
+        B = 32
+        h2d = 0
+        for b in range(0, nframes, B):
+            be = min(nframes, b + B)
+            f0, f1 = max(0, 2 * (b - 2)), min(nfields, 2 * (be + 4))
+            h2d += (f1 - f0) * FIELD_BYTES_IN
+        line["e2e"] = {"value": nfields * a.steps * world / (ems / 1000.0), "unit": "fields/s",
+                       "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": nframes * eng.frame_bytes,
+                       "path": "chdg_decode_host (pinned host buffers, H2D + decode + D2H pipelined)"}
+
+    if rank == 0 and not a.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(a, fields_np)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

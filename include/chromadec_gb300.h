@@ -76,6 +76,20 @@ int chdg_output_geometry(const chdg_engine *e, int32_t *width, int32_t *height, 
 int chdg_decode_device(chdg_engine *e, const uint16_t *d_fields, int64_t field_stride, int32_t nfields,
                        int32_t frame_begin, int32_t frame_end, void *d_out, void *stream);
 
+/* Decode frames [frame_begin, frame_end) of a capture held in HOST memory
+ * (nfields fields, field f at h_fields + f * field_stride samples) into
+ * h_out. Field windows are uploaded and frames downloaded in a double-buffered
+ * pipeline that overlaps the copies with the kernels; use pinned memory for
+ * full-rate copies. Completes asynchronously on `stream`. */
+int chdg_decode_host(chdg_engine *e, const uint16_t *h_fields, int64_t field_stride, int32_t nfields,
+                     int32_t frame_begin, int32_t frame_end, void *h_out, void *stream);
+
+/* Per-kernel timing of the engine's launches (CUDA events on the launching
+ * stream): enable, run, then read the accumulated transform and demodulator
+ * milliseconds and the number of kernel launches. */
+int chdg_engine_set_profiling(chdg_engine *e, int on);
+int chdg_engine_kernel_times(chdg_engine *e, double *ms_transform, double *ms_demod, int64_t *launches);
+
 /* Transform-PAL chroma only: the separated chroma of fields
  * [2*frame_begin, 2*frame_end) as FP32 planes of (last-first field line + 1)
  * rows x (active_end - active_start) columns, rows starting at field line

@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(kDemodThreads) demod_kernel(DemodParams P)
     float *vv = smem + 10 * SW;                        // [4 lines][4 combos][SW]
     __shared__ float s_bp[kDemodLines], s_bq[kDemodLines], s_vsw[kDemodLines];
 
-    const uint16_t *field = P.fields + (long long)f * P.field_stride;
+    const uint16_t *field = P.fields + (long long)(f - P.field_base) * P.field_stride;
     const float *part = P.partial + (long long)o * P.part_field_stride;
 
     // 1. chroma rows (sum of the overlap-class planes), zero outside

@@ -34,8 +34,6 @@ static int arg_fail(const std::string &what)
     return CHDG_E_INVALID_ARG;
 }
 
-static int first_line(int fafl, int off) { return (fafl + 1 - off) / 2; }
-static int last_line(int lafl, int off) { return ((lafl - off) / 2) + 1; }
 
 void output_geometry(const chdg_geometry &g, int padding, int &w, int &h, int &lp, int &tp)
 {
@@ -66,6 +64,15 @@ Engine::~Engine()
     if (partial_) cudaFree(partial_);
     if (thr_dev_) cudaFree(thr_dev_);
     if (stats_dev_) cudaFree(stats_dev_);
+    for (int i = 0; i < 2; i++) {
+        if (hp_fields_[i]) cudaFree(hp_fields_[i]);
+        if (hp_out_[i]) cudaFree(hp_out_[i]);
+        if (ev_h2d_[i]) cudaEventDestroy(ev_h2d_[i]);
+        if (ev_comp_[i]) cudaEventDestroy(ev_comp_[i]);
+        if (ev_d2h_[i]) cudaEventDestroy(ev_d2h_[i]);
+    }
+    if (copy_stream_) cudaStreamDestroy(copy_stream_);
+    reset_kernel_times();
 }
 
 int Engine::init(const chdg_geometry &g, const chdg_config &c)
@@ -149,14 +156,15 @@ int Engine::ensure_partial(int nout_fields)
     return 0;
 }
 
-int Engine::run_transform(const uint16_t *fields, long long stride, int nfields, int fb, int fe, float *partial,
-                          cudaStream_t s)
+int Engine::run_transform(const uint16_t *fields, long long stride, int field_base, int nfields, int fb, int fe,
+                          float *partial, cudaStream_t s)
 {
     const long long cls_stride = (long long)(fe - fb) * 2 * rows_ * cols_;
     if (c_.kind == 8) {
         tpal::T3Params P{};
         P.fields = fields;
         P.field_stride = stride;
+        P.field_base = field_base;
         P.nfields = nfields;
         P.fw = g_.field_width;
         P.avs = g_.active_start;
@@ -188,6 +196,7 @@ int Engine::run_transform(const uint16_t *fields, long long stride, int nfields,
         tpal::T2Params P{};
         P.fields = fields;
         P.field_stride = stride;
+        P.field_base = field_base;
         P.nfields = nfields;
         P.fw = g_.field_width;
         P.avs = g_.active_start;
@@ -212,12 +221,13 @@ int Engine::run_transform(const uint16_t *fields, long long stride, int nfields,
     return 0;
 }
 
-int Engine::run_demod(const uint16_t *fields, long long stride, int fb, int fe, const float *partial, void *out,
-                      cudaStream_t s)
+int Engine::run_demod(const uint16_t *fields, long long stride, int field_base, int fb, int fe, const float *partial,
+                      void *out, cudaStream_t s)
 {
     tpal::DemodParams D{};
     D.fields = fields;
     D.field_stride = stride;
+    D.field_base = field_base;
     D.field_begin = 2 * fb;
     D.nout = 2 * (fe - fb);
     D.fw = g_.field_width;
@@ -294,7 +304,8 @@ int Engine::fill_border(void *out, int nframes, cudaStream_t s)
     return e == cudaSuccess ? 0 : cuda_fail("fill", e);
 }
 
-int Engine::decode(const uint16_t *fields, long long stride, int nfields, int fb, int fe, void *out, cudaStream_t s)
+int Engine::decode(const uint16_t *fields, long long stride, int field_base, int nfields, int fb, int fe, void *out,
+                   cudaStream_t s)
 {
     if (fields == nullptr || out == nullptr || fe < fb || stride < (long long)g_.field_width * g_.field_height)
         return arg_fail("decode: bad arguments");
@@ -303,10 +314,141 @@ int Engine::decode(const uint16_t *fields, long long stride, int nfields, int fb
     for (int b = fb; b < fe; b += maxb) {
         const int be = std::min(fe, b + maxb);
         if (const int rc = ensure_partial(2 * (be - b)); rc != 0) return rc;
-        if (const int rc = run_transform(fields, stride, nfields, b, be, partial_, s); rc != 0) return rc;
-        if (const int rc = run_demod(fields, stride, b, be, partial_, o, s); rc != 0) return rc;
+        Pending ev{};
+        if (profiling_) {
+            cudaEventCreate(&ev.a);
+            cudaEventCreate(&ev.b);
+            cudaEventCreate(&ev.c);
+            cudaEventRecord(ev.a, s);
+        }
+        if (const int rc = run_transform(fields, stride, field_base, nfields, b, be, partial_, s); rc != 0) return rc;
+        if (profiling_) cudaEventRecord(ev.b, s);
+        if (const int rc = run_demod(fields, stride, field_base, b, be, partial_, o, s); rc != 0) return rc;
+        if (profiling_) {
+            cudaEventRecord(ev.c, s);
+            pending_.push_back(ev);
+        }
+        launches_ += 2;
         o += frame_bytes() * (size_t)(be - b);
     }
+    return 0;
+}
+
+void Engine::record_pending()
+{
+    for (auto &p : pending_) {
+        float t1 = 0.f, t2 = 0.f;
+        cudaEventSynchronize(p.c);
+        cudaEventElapsedTime(&t1, p.a, p.b);
+        cudaEventElapsedTime(&t2, p.b, p.c);
+        ms_transform_ += t1;
+        ms_demod_ += t2;
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+        cudaEventDestroy(p.c);
+    }
+    pending_.clear();
+}
+
+int Engine::kernel_times(double *ms_transform, double *ms_demod, long long *launches)
+{
+    record_pending();
+    if (ms_transform) *ms_transform = ms_transform_;
+    if (ms_demod) *ms_demod = ms_demod_;
+    if (launches) *launches = launches_;
+    return 0;
+}
+
+void Engine::reset_kernel_times()
+{
+    record_pending();
+    ms_transform_ = ms_demod_ = 0.0;
+    launches_ = 0;
+}
+
+int Engine::ensure_host_pipeline(size_t field_bytes, size_t out_bytes)
+{
+    cudaError_t e;
+    if (copy_stream_ == nullptr) {
+        if ((e = cudaStreamCreateWithFlags(&copy_stream_, cudaStreamNonBlocking)) != cudaSuccess)
+            return cuda_fail("stream", e);
+        for (int i = 0; i < 2; i++) {
+            cudaEventCreateWithFlags(&ev_h2d_[i], cudaEventDisableTiming);
+            cudaEventCreateWithFlags(&ev_comp_[i], cudaEventDisableTiming);
+            cudaEventCreateWithFlags(&ev_d2h_[i], cudaEventDisableTiming);
+        }
+    }
+    if (field_bytes > hp_field_bytes_) {
+        for (int i = 0; i < 2; i++) {
+            if (hp_fields_[i]) cudaFree(hp_fields_[i]);
+            hp_fields_[i] = nullptr;
+            if ((e = cudaMalloc(&hp_fields_[i], field_bytes)) != cudaSuccess) {
+                hp_field_bytes_ = 0;
+                chd::detail::set_last_error("chromadec_gb300: out of device memory for the field ring");
+                return CHDG_E_OOM;
+            }
+        }
+        hp_field_bytes_ = field_bytes;
+    }
+    if (out_bytes > hp_out_bytes_) {
+        for (int i = 0; i < 2; i++) {
+            if (hp_out_[i]) cudaFree(hp_out_[i]);
+            hp_out_[i] = nullptr;
+            if ((e = cudaMalloc(&hp_out_[i], out_bytes)) != cudaSuccess) {
+                hp_out_bytes_ = 0;
+                chd::detail::set_last_error("chromadec_gb300: out of device memory for output frames");
+                return CHDG_E_OOM;
+            }
+        }
+        hp_out_bytes_ = out_bytes;
+    }
+    return 0;
+}
+
+// Batches of B frames alternate between two device slots: the copy stream
+// uploads batch i+1's field window while the compute stream decodes batch i,
+// and downloads batch i-1's frames. A batch's window is its fields plus the
+// 3D look-behind/ahead halo (frames b-2 .. b+B+3), clipped to the capture.
+int Engine::decode_host(const uint16_t *host_fields, long long host_stride, int nfields, int fb, int fe,
+                        void *host_out, cudaStream_t s)
+{
+    if (host_fields == nullptr || host_out == nullptr || fe < fb) return arg_fail("decode_host: bad arguments");
+    const long long flen = (long long)g_.field_width * g_.field_height;
+    if (host_stride < flen) return arg_fail("decode_host: field stride smaller than a field");
+    const int B = host_batch_frames_;
+    const long long dstride = (flen + 63) & ~63LL;   // 128-byte aligned device fields
+    const int maxWinFields = 2 * (B + look_behind() + look_ahead());
+    if (const int rc = ensure_host_pipeline((size_t)(maxWinFields + 1) * dstride * 2, frame_bytes() * (size_t)B);
+        rc != 0)
+        return rc;
+    cudaError_t e;
+    int i = 0;
+    for (int b = fb; b < fe; b += B, i++) {
+        const int be = std::min(fe, b + B);
+        const int slot = i & 1;
+        const int f0 = std::max(0, 2 * (b - look_behind()));
+        const int f1 = std::min(nfields, 2 * (be + look_ahead()));
+        // slot reuse: batch i-2's compute must be done before overwriting its fields
+        if (i >= 2) cudaStreamWaitEvent(copy_stream_, ev_comp_[slot], 0);
+        if (f1 > f0) {
+            e = cudaMemcpy2DAsync(hp_fields_[slot], dstride * 2, host_fields + (size_t)f0 * host_stride,
+                                  host_stride * 2, flen * 2, f1 - f0, cudaMemcpyHostToDevice, copy_stream_);
+            if (e != cudaSuccess) return cuda_fail("H2D", e);
+        }
+        cudaEventRecord(ev_h2d_[slot], copy_stream_);
+        cudaStreamWaitEvent(s, ev_h2d_[slot], 0);
+        if (i >= 2) cudaStreamWaitEvent(s, ev_d2h_[slot], 0);   // output slot drained
+        if (const int rc = decode(hp_fields_[slot], dstride, f0, nfields, b, be, hp_out_[slot], s); rc != 0) return rc;
+        cudaEventRecord(ev_comp_[slot], s);
+        cudaStreamWaitEvent(copy_stream_, ev_comp_[slot], 0);
+        e = cudaMemcpyAsync((char *)host_out + frame_bytes() * (size_t)(b - fb), hp_out_[slot],
+                            frame_bytes() * (size_t)(be - b), cudaMemcpyDeviceToHost, copy_stream_);
+        if (e != cudaSuccess) return cuda_fail("D2H", e);
+        cudaEventRecord(ev_d2h_[slot], copy_stream_);
+    }
+    // the caller's stream completes after the last download
+    cudaEventRecord(ev_d2h_[0], copy_stream_);
+    cudaStreamWaitEvent(s, ev_d2h_[0], 0);
     return 0;
 }
 
@@ -320,7 +462,7 @@ int Engine::chroma(const uint16_t *fields, long long stride, int nfields, int fb
 {
     if (fields == nullptr || out == nullptr || fe < fb) return arg_fail("chroma: bad arguments");
     if (const int rc = ensure_partial(2 * (fe - fb)); rc != 0) return rc;
-    if (const int rc = run_transform(fields, stride, nfields, fb, fe, partial_, s); rc != 0) return rc;
+    if (const int rc = run_transform(fields, stride, 0, nfields, fb, fe, partial_, s); rc != 0) return rc;
     const long long n = (long long)(fe - fb) * 2 * rows_ * cols_;
     sum_classes_kernel<<<1024, 256, 0, s>>>(partial_, n, n, out);
     cudaError_t e = cudaGetLastError();
@@ -410,7 +552,31 @@ int chdg_decode_device(chdg_engine *e, const uint16_t *d_fields, int64_t field_s
                        int32_t frame_begin, int32_t frame_end, void *d_out, void *stream)
 {
     if (!e) return chdg::arg_fail("chdg_decode_device: null engine");
-    return e->eng.decode(d_fields, field_stride, nfields, frame_begin, frame_end, d_out, (cudaStream_t)stream);
+    return e->eng.decode(d_fields, field_stride, 0, nfields, frame_begin, frame_end, d_out, (cudaStream_t)stream);
+}
+
+int chdg_decode_host(chdg_engine *e, const uint16_t *h_fields, int64_t field_stride, int32_t nfields,
+                     int32_t frame_begin, int32_t frame_end, void *h_out, void *stream)
+{
+    if (!e) return chdg::arg_fail("chdg_decode_host: null engine");
+    return e->eng.decode_host(h_fields, field_stride, nfields, frame_begin, frame_end, h_out, (cudaStream_t)stream);
+}
+
+int chdg_engine_set_profiling(chdg_engine *e, int on)
+{
+    if (!e) return chdg::arg_fail("chdg_engine_set_profiling: null engine");
+    e->eng.set_profiling(on != 0);
+    e->eng.reset_kernel_times();
+    return 0;
+}
+
+int chdg_engine_kernel_times(chdg_engine *e, double *ms_transform, double *ms_demod, int64_t *launches)
+{
+    if (!e) return chdg::arg_fail("chdg_engine_kernel_times: null engine");
+    long long n = 0;
+    const int rc = e->eng.kernel_times(ms_transform, ms_demod, &n);
+    if (launches) *launches = n;
+    return rc;
 }
 
 int chdg_chroma_device(chdg_engine *e, const uint16_t *d_fields, int64_t field_stride, int32_t nfields,

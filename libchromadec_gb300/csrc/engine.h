@@ -3,6 +3,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <vector>
 
 #include <cuda_runtime.h>
 
@@ -20,9 +21,18 @@ public:
     Engine &operator=(const Engine &) = delete;
 
     int init(const chdg_geometry &g, const chdg_config &c);
-    int decode(const uint16_t *fields, long long stride, int nfields, int fb, int fe, void *out, cudaStream_t s);
+    // fields: device buffer holding capture fields [field_base, ...)
+    int decode(const uint16_t *fields, long long stride, int field_base, int nfields, int fb, int fe, void *out,
+               cudaStream_t s);
     int chroma(const uint16_t *fields, long long stride, int nfields, int fb, int fe, float *out, cudaStream_t s);
+    // Host capture -> host frames: pipelined H2D, decode, D2H.
+    int decode_host(const uint16_t *host_fields, long long host_stride, int nfields, int fb, int fe, void *host_out,
+                    cudaStream_t s);
     int stats(uint64_t *exact, uint64_t *flips);
+    // Per-kernel CUDA-event timing of decode()'s launches.
+    void set_profiling(bool on) { profiling_ = on; }
+    int kernel_times(double *ms_transform, double *ms_demod, long long *launches);
+    void reset_kernel_times();
 
     int out_w() const { return out_w_; }
     int out_h() const { return out_h_; }
@@ -40,10 +50,12 @@ private:
     bool padded() const { return left_pad_ || top_pad_ || out_w_ != (g_.active_end - g_.active_start) ||
                                  out_h_ != (g_.last_active_frame_line - g_.first_active_frame_line + 1); }
     int ensure_partial(int nout_fields);
-    int run_transform(const uint16_t *fields, long long stride, int nfields, int fb, int fe, float *partial,
-                      cudaStream_t s);
-    int run_demod(const uint16_t *fields, long long stride, int fb, int fe, const float *partial, void *out,
-                  cudaStream_t s);
+    int run_transform(const uint16_t *fields, long long stride, int field_base, int nfields, int fb, int fe,
+                      float *partial, cudaStream_t s);
+    int run_demod(const uint16_t *fields, long long stride, int field_base, int fb, int fe, const float *partial,
+                  void *out, cudaStream_t s);
+    int ensure_host_pipeline(size_t field_bytes, size_t out_bytes);
+    void record_pending();
     int fill_border(void *out, int nframes, cudaStream_t s);
 
     chdg_geometry g_{};
@@ -58,6 +70,19 @@ private:
     int out_w_ = 0, out_h_ = 0, left_pad_ = 0, top_pad_ = 0;
     int max_batch_frames_ = 128;
     int chunk_frames_ = 16;
+    // host pipeline: two slots of device fields + frames, one copy stream
+    int host_batch_frames_ = 32;
+    uint16_t *hp_fields_[2] = {nullptr, nullptr};
+    void *hp_out_[2] = {nullptr, nullptr};
+    size_t hp_field_bytes_ = 0, hp_out_bytes_ = 0;
+    cudaStream_t copy_stream_ = nullptr;
+    cudaEvent_t ev_h2d_[2] = {nullptr, nullptr}, ev_comp_[2] = {nullptr, nullptr}, ev_d2h_[2] = {nullptr, nullptr};
+    // profiling
+    bool profiling_ = false;
+    struct Pending { cudaEvent_t a, b, c; };
+    std::vector<Pending> pending_;
+    double ms_transform_ = 0.0, ms_demod_ = 0.0;
+    long long launches_ = 0;
 };
 
 }  // namespace chdg

@@ -127,7 +127,7 @@ __device__ __forceinline__ void forward_pair(const T3Params &P, int q, int tileX
     for (int k = 0; k < 5; k++) X[k] = make_float2(0.0f, 0.0f);
     float rowl1 = 0.0f;
     if (valid) {
-        const long long base = (long long)f * P.field_stride + (long long)(L >> 1) * P.fw + tileX;
+        const long long base = (long long)(f - P.field_base) * P.field_stride + (long long)(L >> 1) * P.fw + tileX;
         int a[16];
         int sum = 0;
 #pragma unroll
@@ -232,7 +232,7 @@ __device__ __noinline__ void exact_pair(const T3Params &P, int m, int tileX, int
             const int y = y0 + 2 * i;
             const int L = tileY + y;
             if (L < P.fafl || L > P.lafl) continue;
-            const long long base = (long long)f * P.field_stride + (long long)(L >> 1) * P.fw + tileX;
+            const long long base = (long long)(f - P.field_base) * P.field_stride + (long long)(L >> 1) * P.fw + tileX;
             dfc xb = {{0.f, 0.f}, {0.f, 0.f}}, xr = xb;
             for (int x = 0; x < 16; x++) {
                 long long idx = base + x;

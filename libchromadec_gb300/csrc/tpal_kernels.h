@@ -7,7 +7,8 @@
 namespace tpal {
 
 // Device field buffer: field f (absolute index in the capture, first field of
-// each frame at even f) starts at fields + f * field_stride. Fields outside
+// each frame at even f) starts at fields + (f - field_base) * field_stride;
+// the buffer holds every capture field the launch reads. Fields outside
 // [0, nfields) are black padding frames and read as zero after black removal.
 //
 // Chroma partial planes: 4 overlap classes x output fields x rows x cols, in
@@ -15,8 +16,9 @@ namespace tpal {
 // field o is field 2 * frame_begin + o.
 
 struct T3Params {
-    const uint16_t *fields;
+    const uint16_t *fields;      // buffer holding fields [field_base, ...)
     long long field_stride;
+    int field_base;
     int nfields;
     int fw;
     int avs, ave, fafl, lafl;   // active samples [avs, ave), frame lines [fafl, lafl]
@@ -34,6 +36,7 @@ struct T3Params {
 struct T2Params {
     const uint16_t *fields;
     long long field_stride;
+    int field_base;
     int nfields;
     int fw;
     int avs, ave, fafl, lafl;
@@ -51,6 +54,7 @@ struct T2Params {
 struct DemodParams {
     const uint16_t *fields;      // same buffer as the transform's
     long long field_stride;
+    int field_base;
     int field_begin, nout;       // output field o is absolute field field_begin + o
     int fw, fh;
     int avs, ave, fafl, lafl;

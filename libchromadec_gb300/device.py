@@ -62,6 +62,11 @@ def lib(build: bool = True):
         L.chdg_chroma_device.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
                                          C.c_void_p, C.c_void_p]
         L.chdg_engine_stats.argtypes = [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+        L.chdg_decode_host.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
+                                       C.c_void_p, C.c_void_p]
+        L.chdg_engine_set_profiling.argtypes = [C.c_void_p, C.c_int]
+        L.chdg_engine_kernel_times.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                               C.POINTER(C.c_int64)]
         L.chd_last_error.restype = C.c_char_p
         _lib = L
     return _lib
