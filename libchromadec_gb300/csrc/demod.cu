@@ -18,7 +18,7 @@
 //  * Y = composite - chroma, the rotated U/V and the output scaling are fused;
 //    planes are written straight into the frame's [Y | Cb | Cr] layout.
 //
-// One block: 4 field lines of one output field, 512 threads; a thread
+// One block: 8 field lines of one output field, 256 threads; a work item
 // produces 8 consecutive samples of one line from a register window of the
 // four vertically combined chroma rows.
 #include <cmath>
@@ -32,14 +32,15 @@ namespace tpal {
 __constant__ float cd_cfilt[8][4];   // PALcolour chroma 2D FIR taps (filterSize = 7)
 static bool g_demod_ready[64];
 
-constexpr int kDemodLines = 4;
-constexpr int kDemodThreads = 512;
+constexpr int kDemodLines = 8;
+constexpr int kDemodThreads = 256;
 constexpr int kPad = 8;
+constexpr int kRows = kDemodLines + 6;   // chroma lines fl0-3 .. fl0+L+2
 
 __device__ __forceinline__ int first_line(int fafl, int off) { return (fafl + 1 - off) / 2; }
 __device__ __forceinline__ int last_line(int lafl, int off) { return ((lafl - off) / 2) + 1; }
 
-__global__ void __launch_bounds__(kDemodThreads) demod_kernel(DemodParams P)
+__global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
 {
     extern __shared__ float smem[];
     const int nblk_per_field = (P.fh + kDemodLines - 1) / kDemodLines;   // upper bound; invalid lines skip
@@ -56,25 +57,44 @@ __global__ void __launch_bounds__(kDemodThreads) demod_kernel(DemodParams P)
     const int base4 = P.avs & ~3;                     // absolute sample of local index 0
     const int span = ((P.ave - base4) + 7) & ~7;      // samples covered by threads (multiple of 8)
     const int SW = span + 2 * kPad;                   // smem row length
-    float *ch = smem;                                  // [10][SW] chroma rows fl0-3 .. fl0+6
-    float *vv = smem + 10 * SW;                        // [4 lines][4 combos][SW]
+    float *ch = smem;                                  // [kRows][SW] chroma rows fl0-3 .. fl0+L+2
     __shared__ float s_bp[kDemodLines], s_bq[kDemodLines], s_vsw[kDemodLines];
 
     const uint16_t *field = P.fields + (long long)(f - P.field_base) * P.field_stride;
     const float *part = P.partial + (long long)o * P.part_field_stride;
+    const int cols = P.ave - P.avs;
 
-    // 1. chroma rows (sum of the overlap-class planes), zero outside
-    for (int idx = threadIdx.x; idx < 10 * SW; idx += blockDim.x) {
-        const int r = idx / SW;
-        const int xl = idx % SW - kPad;
-        const int x = base4 + xl;
-        const int fl = fl0 - 3 + r;
-        float v = 0.f;
-        if (fl >= fl_first && fl < fl_last && x >= P.avs && x < P.ave) {
-            const long long e = (long long)(fl - P.fl_lo) * P.part_row_stride + (x - P.avs);
-            for (int c = 0; c < P.nclasses; c++) v += part[(long long)c * P.part_class_stride + e];
+    // 1. chroma rows = sum of the overlap-class planes; zero outside the
+    //    field's active lines and the active window (zero halo included).
+    for (int idx = threadIdx.x; idx < kRows * SW; idx += blockDim.x) ch[idx] = 0.f;
+    __syncthreads();
+    const int c4 = cols >> 2;   // float4 per row (cols is a multiple of 4 when avs is)
+    const bool vec = ((cols & 3) == 0) && ((P.part_row_stride & 3) == 0) && ((P.part_class_stride & 3) == 0) &&
+                     ((P.part_field_stride & 3) == 0);
+    if (vec) {
+        for (int idx = threadIdx.x; idx < kRows * c4; idx += blockDim.x) {
+            const int r = idx / c4, q = idx % c4;
+            const int fl = fl0 - 3 + r;
+            if (fl < fl_first || fl >= fl_last) continue;
+            const float4 *src = reinterpret_cast<const float4 *>(part + (long long)(fl - P.fl_lo) * P.part_row_stride) + q;
+            const long long cs4 = P.part_class_stride >> 2;
+            float4 a = __ldg(src), b = __ldg(src + cs4), c = __ldg(src + 2 * cs4), d = __ldg(src + 3 * cs4);
+            float *dst = ch + r * SW + kPad + (P.avs - base4) + 4 * q;
+            dst[0] = (a.x + b.x) + (c.x + d.x);
+            dst[1] = (a.y + b.y) + (c.y + d.y);
+            dst[2] = (a.z + b.z) + (c.z + d.z);
+            dst[3] = (a.w + b.w) + (c.w + d.w);
         }
-        ch[idx] = v;
+    } else {
+        for (int idx = threadIdx.x; idx < kRows * cols; idx += blockDim.x) {
+            const int r = idx / cols, c = idx % cols;
+            const int fl = fl0 - 3 + r;
+            if (fl < fl_first || fl >= fl_last) continue;
+            const long long e = (long long)(fl - P.fl_lo) * P.part_row_stride + c;
+            float v = 0.f;
+            for (int k = 0; k < P.nclasses; k++) v += part[(long long)k * P.part_class_stride + e];
+            ch[r * SW + kPad + (P.avs - base4) + c] = v;
+        }
     }
 
     // 2. burst detection: one warp per line (detectBurst, palcolour.cpp:344-409)
@@ -120,93 +140,84 @@ __global__ void __launch_bounds__(kDemodThreads) demod_kernel(DemodParams P)
     }
     __syncthreads();
 
-    // 3. vertical combinations (palcolour.cpp:557-567 without the carrier):
-    //    v0 = c0, v1 = -c(-2) - c(+2), v2 = c(-1) - c(+1), v3 = -c(-3) + c(+3)
-    for (int idx = threadIdx.x; idx < kDemodLines * SW; idx += blockDim.x) {
-        const int t = idx / SW;
-        const int x = idx % SW;
-        const float *r0 = ch + (t + 0) * SW + x;
-        float *d = vv + (t * 4) * SW + x;
-        d[0] = r0[3 * SW];
-        d[SW] = -r0[1 * SW] - r0[5 * SW];
-        d[2 * SW] = r0[2 * SW] - r0[4 * SW];
-        d[3 * SW] = -r0[0] + r0[6 * SW];
-    }
-    __syncthreads();
-
-    // 4. 2D FIR + rotation + pack
+    // 3. 2D FIR + rotation + pack; work item = (line, 8-sample segment)
     const int per_line = span / 8;
-    const int t = threadIdx.x / per_line;
-    const int seg = threadIdx.x % per_line;
-    if (t >= kDemodLines) return;
-    const int fl = fl0 + t;
-    if (fl >= fl_last) return;
-    const int xl0 = seg * 8;   // local index of the first sample (absolute base4 + xl0, a multiple of 4)
-    float v[4][22];
-#pragma unroll
-    for (int k = 0; k < 4; k++)
-#pragma unroll
-        for (int q = 0; q < 22; q++) v[k][q] = vv[(t * 4 + k) * SW + kPad + xl0 - 7 + q];
-
-    float PU[8], QU[8], PV[8], QV[8];
-#pragma unroll
-    for (int s = 0; s < 8; s++) {
-        float PA = 0.f, PB = 0.f, QA = 0.f, QB = 0.f;
-#pragma unroll
-        for (int b = 0; b < 8; b++) {
-            const int r = s + b + 7, l = s - b + 7;
-            float sg[4];
-#pragma unroll
-            for (int k = 0; k < 4; k++) sg[k] = (b & 1) ? v[k][r] - v[k][l] : v[k][r] + v[k][l];
-            const float A = __fmaf_rn(cd_cfilt[b][1], sg[1], cd_cfilt[b][0] * sg[0]);
-            const float B = __fmaf_rn(cd_cfilt[b][3], sg[3], cd_cfilt[b][2] * sg[2]);
-            switch ((s + b) & 3) {
-            case 1: PA += A; PB += B; break;
-            case 3: PA -= A; PB -= B; break;
-            case 0: QA += A; QB += B; break;
-            default: QA -= A; QB -= B; break;
-            }
-        }
-        PU[s] = PA + QB;
-        PV[s] = PA - QB;
-        QU[s] = QA - PB;
-        QV[s] = QA + PB;
-    }
-
-    const float bp = s_bp[t], bq = s_bq[t], vsw = s_vsw[t];
-    const int frame_row = 2 * fl + off;
-    const int orow = P.top_pad + frame_row - P.fafl;
-    const long long frame = o >> 1;   // field_begin is even: fields 2k, 2k+1 form frame k
     const long long plane = (long long)P.out_w * P.out_h;
-    const long long rowbase = frame * P.out_frame_stride + (long long)orow * P.out_w + P.left_pad;
-    const uint16_t *comp = field + (long long)fl * P.fw;
+    const long long frame = o >> 1;   // field_begin is even: fields 2k, 2k+1 form frame k
+    for (int item = threadIdx.x; item < kDemodLines * per_line; item += blockDim.x) {
+        const int t = item / per_line;
+        const int seg = item % per_line;
+        const int fl = fl0 + t;
+        if (fl >= fl_last) continue;
+        const int xl0 = seg * 8;   // local index of the first sample (absolute base4 + xl0, a multiple of 4)
+        // vertical combinations (palcolour.cpp:557-567 without the carrier):
+        //   v0 = c0, v1 = -c(-2) - c(+2), v2 = c(-1) - c(+1), v3 = -c(-3) + c(+3)
+        float v[4][22];
+        const float *rw = ch + t * SW + kPad + xl0 - 7;
 #pragma unroll
-    for (int s = 0; s < 8; s++) {
-        const int x = base4 + xl0 + s;
-        if (x < P.avs || x >= P.ave) continue;
-        const float c0 = v[0][s + 7];
-        const float Y = (float)comp[x] - c0;
-        const float U = -(PU[s] * bp + QU[s] * bq) * 2.0f;
-        const float V = vsw * -(QV[s] * bp - PV[s] * bq) * 2.0f;
-        const float ey = (Y - (float)P.black) * P.ey_scale;
-        const float ecb = U * P.ecb_scale;
-        const float ecr = V * P.ecr_scale;
-        const long long e = rowbase + (x - P.avs);
-        if (P.format == 1) {
-            float *out = (float *)P.out;
-            out[e] = fminf(fmaxf(ey, P.y_lo), P.y_hi);
-            out[e + plane] = fminf(fmaxf(ecb, P.c_lo), P.c_hi);
-            out[e + 2 * plane] = fminf(fmaxf(ecr, P.c_lo), P.c_hi);
-        } else {
-            uint16_t *out = (uint16_t *)P.out;
-            // H.273 Round(x) = Sign(x) * Floor(Abs(x) + 0.5), output_writer.cpp:60-76
-            auto q = [](float x, float lo, float hi) -> uint16_t {
-                const float r = copysignf(floorf(fabsf(x) + 0.5f), x);
-                return (uint16_t)fminf(fmaxf(r, lo), hi);
-            };
-            out[e] = q(__fmaf_rn(219.0f * 256.0f, ey, 16.0f * 256.0f), P.y_lo, P.y_hi);
-            out[e + plane] = q(__fmaf_rn(224.0f * 256.0f, ecb, 128.0f * 256.0f), P.c_lo, P.c_hi);
-            out[e + 2 * plane] = q(__fmaf_rn(224.0f * 256.0f, ecr, 128.0f * 256.0f), P.c_lo, P.c_hi);
+        for (int q = 0; q < 22; q++) {
+            v[0][q] = rw[3 * SW + q];
+            v[1][q] = -rw[1 * SW + q] - rw[5 * SW + q];
+            v[2][q] = rw[2 * SW + q] - rw[4 * SW + q];
+            v[3][q] = -rw[q] + rw[6 * SW + q];
+        }
+        float PU[8], QU[8], PV[8], QV[8];
+#pragma unroll
+        for (int s = 0; s < 8; s++) {
+            float PA = 0.f, PB = 0.f, QA = 0.f, QB = 0.f;
+#pragma unroll
+            for (int b = 0; b < 8; b++) {
+                const int r = s + b + 7, l = s - b + 7;
+                float sg[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) sg[k] = (b & 1) ? v[k][r] - v[k][l] : v[k][r] + v[k][l];
+                const float A = __fmaf_rn(cd_cfilt[b][1], sg[1], cd_cfilt[b][0] * sg[0]);
+                const float B = __fmaf_rn(cd_cfilt[b][3], sg[3], cd_cfilt[b][2] * sg[2]);
+                switch ((s + b) & 3) {
+                case 1: PA += A; PB += B; break;
+                case 3: PA -= A; PB -= B; break;
+                case 0: QA += A; QB += B; break;
+                default: QA -= A; QB -= B; break;
+                }
+            }
+            PU[s] = PA + QB;
+            PV[s] = PA - QB;
+            QU[s] = QA - PB;
+            QV[s] = QA + PB;
+        }
+
+        const float bp = s_bp[t], bq = s_bq[t], vsw = s_vsw[t];
+        const int orow = P.top_pad + 2 * fl + off - P.fafl;
+        const long long rowbase = frame * P.out_frame_stride + (long long)orow * P.out_w + P.left_pad;
+        const uint16_t *comp = field + (long long)fl * P.fw;
+#pragma unroll
+        for (int s = 0; s < 8; s++) {
+            const int x = base4 + xl0 + s;
+            if (x < P.avs || x >= P.ave) continue;
+            const float c0 = v[0][s + 7];
+            const float Y = (float)comp[x] - c0;
+            const float U = -(PU[s] * bp + QU[s] * bq) * 2.0f;
+            const float V = vsw * -(QV[s] * bp - PV[s] * bq) * 2.0f;
+            const float ey = (Y - (float)P.black) * P.ey_scale;
+            const float ecb = U * P.ecb_scale;
+            const float ecr = V * P.ecr_scale;
+            const long long e = rowbase + (x - P.avs);
+            if (P.format == 1) {
+                float *out = (float *)P.out;
+                out[e] = fminf(fmaxf(ey, P.y_lo), P.y_hi);
+                out[e + plane] = fminf(fmaxf(ecb, P.c_lo), P.c_hi);
+                out[e + 2 * plane] = fminf(fmaxf(ecr, P.c_lo), P.c_hi);
+            } else {
+                uint16_t *out = (uint16_t *)P.out;
+                // H.273 Round(x) = Sign(x) * Floor(Abs(x) + 0.5), output_writer.cpp:60-76
+                auto q = [](float x, float lo, float hi) -> uint16_t {
+                    const float r = copysignf(floorf(fabsf(x) + 0.5f), x);
+                    return (uint16_t)fminf(fmaxf(r, lo), hi);
+                };
+                out[e] = q(__fmaf_rn(219.0f * 256.0f, ey, 16.0f * 256.0f), P.y_lo, P.y_hi);
+                out[e + plane] = q(__fmaf_rn(224.0f * 256.0f, ecb, 128.0f * 256.0f), P.c_lo, P.c_hi);
+                out[e + 2 * plane] = q(__fmaf_rn(224.0f * 256.0f, ecr, 128.0f * 256.0f), P.c_lo, P.c_hi);
+            }
         }
     }
 }
@@ -247,7 +258,7 @@ size_t demod_smem_bytes(int avs, int ave)
     const int base4 = avs & ~3;
     const int span = ((ave - base4) + 7) & ~7;
     const int SW = span + 2 * kPad;
-    return sizeof(float) * (size_t)(10 + 4 * kDemodLines) * SW;
+    return sizeof(float) * (size_t)kRows * SW;
 }
 
 int demod_launch(const DemodParams &P, cudaStream_t stream)
@@ -255,7 +266,6 @@ int demod_launch(const DemodParams &P, cudaStream_t stream)
     if (P.nout <= 0) return 0;
     const int base4 = P.avs & ~3;
     const int span = ((P.ave - base4) + 7) & ~7;
-    if ((span / 8) * kDemodLines > kDemodThreads) return -2;   // line too wide for one block
     const size_t smem = demod_smem_bytes(P.avs, P.ave);
     static bool attr_set = false;
     if (!attr_set) {

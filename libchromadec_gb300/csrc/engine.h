@@ -68,8 +68,8 @@ private:
     size_t partial_elems_ = 0;
     int fl_lo_ = 0, fl_hi_ = 0, rows_ = 0, cols_ = 0;
     int out_w_ = 0, out_h_ = 0, left_pad_ = 0, top_pad_ = 0;
-    int max_batch_frames_ = 128;
-    int chunk_frames_ = 16;
+    int max_batch_frames_ = 256;
+    int chunk_frames_ = 32;
     // host pipeline: two slots of device fields + frames, one copy stream
     int host_batch_frames_ = 32;
     uint16_t *hp_fields_[2] = {nullptr, nullptr};

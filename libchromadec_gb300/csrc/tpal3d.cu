@@ -106,108 +106,108 @@ __device__ __forceinline__ Thr thr_of(const T3Params &P, int kz, int ky, int kx)
 }
 
 // ---------------------------------------------------------------------------
-// Forward X and Y stages for two consecutive fields (2q, 2q+1).
-// On return lane l holds S_{2q}[kappa(l)][kx] in s0 and S_{2q+1}[kappa(l)][kx]
-// in s1 (kx = 2..6), and the smem bound slots of both fields are written.
+// Per-lane constants of the forward/inverse stages (fixed for the whole walk:
+// lane (j, i) always handles row i of the field with offset j).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void forward_pair(const T3Params &P, int q, int tileX, int tileY, int lane,
-                                             float2 (&s0)[5], float2 (&s1)[5], float *bnd /* [8][8] */)
+struct LaneConst {
+    int j, i, y0, kk;
+    float wy;          // w_y(y0 + 2i)
+    float2 ftw[4];     // radix-2 stage twiddles, h = 8, 4, 2, 1: exp(-2 pi i r / 2h)
+    float2 ptw;        // exp(-2 pi i kk y0 / 32)
+};
+
+__device__ __forceinline__ LaneConst lane_const(int lane, int tileY)
 {
-    const int j = lane >> 4;
-    const int i = lane & 15;
-    const int f = 2 * q + j;
-    const int p = f & 1;                  // field offset: even index = first field
-    const int y0 = (p - tileY) & 1;       // frame-row parity of this field's rows in the tile
-    const int y = y0 + 2 * i;
-    const int L = tileY + y;              // frame line
+    LaneConst c;
+    c.j = lane >> 4;
+    c.i = lane & 15;
+    c.y0 = (c.j - tileY) & 1;
+    c.kk = rev4(c.i);
+    c.wy = c3_wy[c.y0][c.i];
+    int s = 0;
+#pragma unroll
+    for (int h = 8; h >= 1; h >>= 1, s++) c.ftw[s] = c3_tw16[(c.i & (h - 1)) * (8 / h)];
+    c.ptw = c.y0 ? c3_tw32[c.kk] : make_float2(1.f, 0.f);
+    return c;
+}
+
+// ---------------------------------------------------------------------------
+// Forward X and Y stages of fields 2q (half-warp 0) and 2q+1 (half-warp 1).
+// Writes S_f[kappa(l)][kx] into the shared window slot f & 7 and the bound
+// terms of both fields into bnd[f & 7].
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void forward_pair(const T3Params &P, int q, int tileX, int tileY, const LaneConst &LC,
+                                             int lane, float2 *win /* [8][5][32] */, float *bnd /* [8][8] */)
+{
+    const int f = 2 * q + LC.j;
+    const int L = tileY + LC.y0 + 2 * LC.i;   // frame line of this lane's row
     const bool valid = (f >= 0) && (f < P.nfields) && (L >= P.fafl) && (L <= P.lafl);
 
-    float2 X[5];
-#pragma unroll
-    for (int k = 0; k < 5; k++) X[k] = make_float2(0.0f, 0.0f);
+    // Row samples with black and the row mean removed, folded about the
+    // window's centre: s_x = a_x + a_15-x - 2*mean, d_x = a_x - a_15-x
+    // (exact in FP32); the window weight wy is applied to both.
+    float sx[8], dx[8];
     float rowl1 = 0.0f;
     if (valid) {
-        const long long base = (long long)(f - P.field_base) * P.field_stride + (long long)(L >> 1) * P.fw + tileX;
+        const uint16_t *row = P.fields + (long long)(f - P.field_base) * P.field_stride + (long long)(L >> 1) * P.fw;
         int a[16];
         int sum = 0;
 #pragma unroll
         for (int x = 0; x < 16; x++) {
-            long long idx = base + x;
-            idx = idx < 0 ? 0 : idx;
-            a[x] = (int)__ldg(P.fields + idx) - P.black;
+            const int xx = max(tileX + x, -(L >> 1) * P.fw);   // never before the field start
+            a[x] = (int)__ldg(row + xx) - P.black;
             sum += a[x];
         }
-        // s_x = a_x + a_15-x - 2*mean, d_x = a_x - a_15-x (both exact in FP32)
+        const float m16 = (float)sum * 0.0625f;
 #pragma unroll
         for (int x = 0; x < 8; x++) {
-            const float sx = (float)(8 * (a[x] + a[15 - x]) - sum) * 0.125f;
-            const float dx = (float)(a[x] - a[15 - x]);
-#pragma unroll
-            for (int k = 0; k < 5; k++) {
-                X[k].x = __fmaf_rn(c3_cwx[k][x], sx, X[k].x);
-                X[k].y = __fmaf_rn(-c3_swx[k][x], dx, X[k].y);
-            }
-            const float m16 = (float)sum * 0.0625f;
+            sx[x] = (float)(8 * (a[x] + a[15 - x]) - sum) * 0.125f;
+            dx[x] = (float)(a[x] - a[15 - x]);
             rowl1 = __fmaf_rn(c3_wx[x], fabsf((float)a[x] - m16) + fabsf((float)a[15 - x] - m16), rowl1);
         }
-    }
-    const float wy = c3_wy[y0][i];
+    } else {
 #pragma unroll
+        for (int x = 0; x < 8; x++) sx[x] = dx[x] = 0.f;
+    }
+    rowl1 *= LC.wy;
+#pragma unroll
+    for (int h = 1; h < 16; h <<= 1) rowl1 += __shfl_xor_sync(0xffffffffu, rowl1, h);
+    const int fslot = f & 7;
+    if (LC.i == 0) bnd[8 * fslot + 5] = rowl1;
+    const int f0slot = (2 * q) & 7;
+
+#pragma unroll 1
     for (int k = 0; k < 5; k++) {
-        X[k].x *= wy;
-        X[k].y *= wy;
-    }
-    rowl1 *= wy;
-
-    // Bound terms: per field and kx, sum over rows of |X|_1; and the row-L1 sum.
-    float A[6];
+        // column DFT bin kx = k+2 of this row (window and centre phase folded)
+        float2 X = make_float2(0.f, 0.f);
 #pragma unroll
-    for (int k = 0; k < 5; k++) A[k] = l1(X[k]);
-    A[5] = rowl1;
-#pragma unroll
-    for (int h = 1; h < 16; h <<= 1) {
-#pragma unroll
-        for (int k = 0; k < 6; k++) A[k] += __shfl_xor_sync(0xffffffffu, A[k], h);
-    }
-    if (i == 0) {
-        float *b = bnd + 8 * (f & 7);
-#pragma unroll
-        for (int k = 0; k < 6; k++) b[k] = A[k];
-    }
-
-    // 16-point forward DFT over the rows of each half-warp (radix-2 DIF,
-    // bit-reversed output: lane i ends up with bin rev4(i)).
-#pragma unroll
-    for (int h = 8; h >= 1; h >>= 1) {
-        const bool upper = (i & h) != 0;
-        const int r = i & (h - 1);
-        const float2 w = c3_tw16[r * (8 / h)];   // exp(-2 pi i r / (2h))
-#pragma unroll
-        for (int k = 0; k < 5; k++) {
-            const float2 o = shfl_xor2(X[k], h);
-            if (upper) {
-                X[k] = cmul(make_float2(o.x - X[k].x, o.y - X[k].y), w);
-            } else {
-                X[k] = make_float2(X[k].x + o.x, X[k].y + o.y);
-            }
+        for (int x = 0; x < 8; x++) {
+            X.x = __fmaf_rn(c3_cwx[k][x], sx[x], X.x);
+            X.y = __fmaf_rn(-c3_swx[k][x], dx[x], X.y);
         }
-    }
-    // Parity twiddle: S[kk] = exp(-2 pi i kk y0/32) A[kk], S[kk+16] = (-1)^y0 S[kk]
-    const int kk = rev4(i);
-    const float2 tw = y0 ? c3_tw32[kk] : make_float2(1.0f, 0.0f);
-    float2 lo[5], hi[5];
+        X.x *= LC.wy;
+        X.y *= LC.wy;
+        // bound term: sum over the field's rows of |X|_1
+        float A = l1(X);
 #pragma unroll
-    for (int k = 0; k < 5; k++) {
-        lo[k] = cmul(X[k], tw);
-        hi[k] = y0 ? make_float2(-lo[k].x, -lo[k].y) : lo[k];
-    }
-    // Exchange halves so lane l holds both fields at ky = kappa(l).
+        for (int h = 1; h < 16; h <<= 1) A += __shfl_xor_sync(0xffffffffu, A, h);
+        if (LC.i == 0) bnd[8 * fslot + k] = A;
+        // 16-point DFT over the half-warp's rows (radix-2 DIF; lane i ends
+        // with bin rev4(i))
+        int st = 0;
 #pragma unroll
-    for (int k = 0; k < 5; k++) {
-        const float2 send = j ? lo[k] : hi[k];
-        const float2 recv = shfl_xor2(send, 16);
-        s0[k] = j ? recv : lo[k];
-        s1[k] = j ? hi[k] : recv;
+        for (int h = 8; h >= 1; h >>= 1, st++) {
+            const bool upper = (LC.i & h) != 0;
+            const float2 o = shfl_xor2(X, h);
+            X = upper ? cmul(make_float2(o.x - X.x, o.y - X.y), LC.ftw[st]) : make_float2(X.x + o.x, X.y + o.y);
+        }
+        // parity twiddle: S[kk] = exp(-2 pi i kk y0/32) A[kk], S[kk+16] = (-1)^y0 S[kk];
+        // swap halves so lane l holds both fields at ky = kappa(l)
+        const float2 lo = cmul(X, LC.ptw);
+        const float2 hi = LC.y0 ? make_float2(-lo.x, -lo.y) : lo;
+        const float2 recv = shfl_xor2(LC.j ? lo : hi, 16);
+        win[(f0slot * 5 + k) * 32 + lane] = LC.j ? recv : lo;            // field 2q
+        win[((f0slot + 1) * 5 + k) * 32 + lane] = LC.j ? hi : recv;      // field 2q+1
     }
 }
 
@@ -327,8 +327,99 @@ __device__ __forceinline__ void dft8_fwd(const float2 (&in)[8], float2 (&out)[8]
 // ---------------------------------------------------------------------------
 constexpr int kWarps3 = 4;
 constexpr float kBoundFactor = 2.0f;   // guard band, in units of the per-bin error estimate
+constexpr float kEps32 = 5.9604645e-8f;
+constexpr int kWarpSmemF2 = 8 * 5 * 32 + 2 * 2 * 5 * 32 + 32;   // float2 units per warp
 
-__global__ void __launch_bounds__(32 * kWarps3) tpal3d_kernel(T3Params P)
+struct Col {
+    float2 Y[8];
+    float mag[8], ab[8], E;
+};
+
+// 8-point Z DFT of one (ky, kx) column from the shared window, with its
+// magnitudes, L1 magnitudes and error bound.
+__device__ __forceinline__ void z_column(const float2 *win, int m, int k, int lane, float ek, Col &c)
+{
+    float2 col[8];
+    float B = 0.f;
+#pragma unroll
+    for (int z = 0; z < 8; z++) {
+        col[z] = win[((((2 * m + z) & 7) * 5) + k) * 32 + lane];
+        B = __fmaf_rn(c3_wz[z], l1(col[z]), B);
+    }
+    dft8_fwd(col, c.Y);
+#pragma unroll
+    for (int kz = 0; kz < 8; kz++) {
+        c.mag[kz] = __fmaf_rn(c.Y[kz].x, c.Y[kz].x, c.Y[kz].y * c.Y[kz].y);
+        c.ab[kz] = l1(c.Y[kz]);
+    }
+    c.E = kBoundFactor * kEps32 * (ek + B);
+}
+
+// Mask a column, inverse-DFT it to Z slices 0, 1, 4, 5 and overlap-add:
+// R(field 2m) = slice 0 + carried slice 4 of tile 2m-4, R(2m+1) = slice 1 +
+// carried slice 5; then carry this tile's slices 4, 5 for frame m+2.
+__device__ __forceinline__ void z_inverse(const float2 (&Y)[8], unsigned keep, float2 *carry /* [2][5][32] */,
+                                          float2 *RA, float2 *RB /* [5][32] each */, int k, int lane)
+{
+    float2 y[8];
+#pragma unroll
+    for (int kz = 0; kz < 8; kz++) y[kz] = ((keep >> kz) & 1u) ? Y[kz] : make_float2(0.f, 0.f);
+    const float2 E0 = make_float2(y[0].x + y[2].x + y[4].x + y[6].x, y[0].y + y[2].y + y[4].y + y[6].y);
+    const float2 O0 = make_float2(y[1].x + y[3].x + y[5].x + y[7].x, y[1].y + y[3].y + y[5].y + y[7].y);
+    // slice 1: even part y0 + i y2 - y4 - i y6; odd part with powers of exp(+i pi/4)
+    const float2 E1 = make_float2(y[0].x - y[2].y - y[4].x + y[6].y, y[0].y + y[2].x - y[4].y - y[6].x);
+    const float2 o1 = cmul(y[1], make_float2(c3_tw32[4].x, -c3_tw32[4].y));
+    const float2 o3 = cmul(y[3], make_float2(c3_tw32[12].x, -c3_tw32[12].y));
+    const float2 o5 = cmul(y[5], make_float2(c3_tw32[20].x, -c3_tw32[20].y));
+    const float2 o7 = cmul(y[7], make_float2(c3_tw32[28].x, -c3_tw32[28].y));
+    const float2 O1 = make_float2(o1.x + o3.x + o5.x + o7.x, o1.y + o3.y + o5.y + o7.y);
+    const int i4 = k * 32 + lane, i5 = (5 + k) * 32 + lane;
+    const float2 c4 = carry[i4], c5 = carry[i5];
+    RA[k * 32 + lane] = make_float2(E0.x + O0.x + c4.x, E0.y + O0.y + c4.y);
+    RB[k * 32 + lane] = make_float2(E1.x + O1.x + c5.x, E1.y + O1.y + c5.y);
+    carry[i4] = make_float2(E0.x - O0.x, E0.y - O0.y);
+    carry[i5] = make_float2(E1.x - O1.x, E1.y - O1.y);
+}
+
+__device__ __forceinline__ bool fsim(float a, float b, float t) { return (__fmaf_rn(-b, t, a) >= 0.f) && (__fmaf_rn(-a, t, b) >= 0.f); }
+
+__device__ __forceinline__ bool funcertain(float a, float b, float t, float pa, float pb)
+{
+    return (fabsf(__fmaf_rn(-b, t, a)) <= pa + t * pb) || (fabsf(__fmaf_rn(-a, t, b)) <= pb + t * pa);
+}
+
+// Exact resolution of the guard-band decisions of one kx group, one pair at
+// a time, all lanes cooperating (kept out of line: it runs rarely).
+__device__ __noinline__ void resolve_uncertain(const T3Params &P, int m, int tileX, int tileY, int g, int kxa, int lane,
+                                               unsigned &keep, unsigned &unc, unsigned &n_exact, unsigned &n_flip)
+{
+    unsigned any = __ballot_sync(0xffffffffu, unc != 0);
+    while (any) {
+        const int src = __ffs(any) - 1;
+        const unsigned su = __shfl_sync(0xffffffffu, unc, src);
+        const int kz = __ffs(su) - 1;
+        const int kyb = kappa(src);
+        df mb, mr;
+        exact_pair(P, m, tileX, tileY, kz, kyb, kxa, mb, mr);
+        const int kzr = (10 - kz) & 7, kybr = (40 - kyb) & 31;
+        bool sim = df_sim(mb, mr, thr_of(P, kz, kyb, kxa).d);
+        if (kxa == 4) sim |= df_sim(mb, mr, thr_of(P, kzr, kybr, 4).d);
+        if (lane == src) {
+            n_exact++;
+            if ((((keep >> kz) & 1u) != 0) != sim) n_flip++;
+            keep = sim ? (keep | (1u << kz)) : (keep & ~(1u << kz));
+            unc &= ~(1u << kz);
+        }
+        if (g == 2 && lane == kappa(kybr)) {   // kx = 4: the pair's other bin is a visitor too
+            keep = sim ? (keep | (1u << kzr)) : (keep & ~(1u << kzr));
+            unc &= ~(1u << kzr);
+        }
+        any = __ballot_sync(0xffffffffu, unc != 0);
+    }
+}
+
+template <bool PER_BIN>
+__global__ void __launch_bounds__(32 * kWarps3, 3) tpal3d_kernel(T3Params P)
 {
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -344,40 +435,28 @@ __global__ void __launch_bounds__(32 * kWarps3) tpal3d_kernel(T3Params P)
     const int m1 = min(m0 + P.chunk_frames, P.frame_end);
     const int cls = ((ty & 1) << 1) | (tx & 1);
 
-    __shared__ float s_bnd[kWarps3][8 * 8];
-    __shared__ float2 s_carry[kWarps3][2][2][5][32];
-    float *bnd = s_bnd[warp];
+    // Per-warp shared state (dynamic): window of field spectra, Z carries,
+    // Z-stage output spectra and per-field bound terms.
+    extern __shared__ float4 s_dyn[];
+    float2 *wbase = reinterpret_cast<float2 *>(s_dyn) + (size_t)warp * kWarpSmemF2;
+    float2 *win = wbase;                          // [8 slots][5 kx][32 lanes]
+    float2 *carry_base = wbase + 8 * 5 * 32;      // [2][2 slices][5 kx][32 lanes]
+    float *bnd = reinterpret_cast<float *>(carry_base + 2 * 2 * 5 * 32);   // [8 slots][8]
 
+    const LaneConst LC = lane_const(lane, tileY);
     const int my_ky = kappa(lane);
-    const int mirror_lane = kappa((40 - my_ky) & 31);
-
-    // S window: sw[z] = S of field 2m + z at ky = kappa(lane)
-    float2 sw[8][5];
-#pragma unroll
-    for (int z = 0; z < 8; z++)
-#pragma unroll
-        for (int k = 0; k < 5; k++) sw[z][k] = make_float2(0.f, 0.f);
-
-    // Prefill fields 2(m0-2) .. 2(m0-2)+5
-    for (int q = m0 - 2; q < m0 + 1; q++) {
-#pragma unroll
-        for (int z = 0; z < 6; z++)
-#pragma unroll
-            for (int k = 0; k < 5; k++) sw[z][k] = sw[z + 2][k];
-        forward_pair(P, q, tileX, tileY, lane, sw[6], sw[7], bnd);
-    }
+    const int kyr = (40 - my_ky) & 31;
+    const int mirror_lane = kappa(kyr);
 
     unsigned int n_exact = 0, n_flip = 0;
 
-    for (int m = m0 - 2; m < m1; m++) {
+    // Steps m0-5 .. m0-3 only fill the window (fields 2(m0-2) .. 2(m0-2)+5);
+    // steps m0-2 and m0-1 also run the Z stage for the carries; the rest output.
+    for (int m = m0 - 5; m < m1; m++) {
         __syncwarp();
-        // Slide the window and add fields 2m+6, 2m+7.
-#pragma unroll
-        for (int z = 0; z < 6; z++)
-#pragma unroll
-            for (int k = 0; k < 5; k++) sw[z][k] = sw[z + 2][k];
-        forward_pair(P, m + 3, tileX, tileY, lane, sw[6], sw[7], bnd);
+        forward_pair(P, m + 3, tileX, tileY, LC, lane, win, bnd);   // fields 2m+6, 2m+7
         __syncwarp();
+        if (m < m0 - 2) continue;
 
         // Per-kx error-bound base (warp-uniform): sum_z w_z (A_z[kx] + R_z / 2)
         float ek[5];
@@ -390,212 +469,120 @@ __global__ void __launch_bounds__(32 * kWarps3) tpal3d_kernel(T3Params P)
 #pragma unroll
             for (int k = 0; k < 5; k++) ek[k] = __fmaf_rn(c3_wz[z], b[k] + half_r, ek[k]);
         }
+        float2 *carry = carry_base + (m & 1) * (2 * 5 * 32);
 
-        float2 RA[5], RB[5];   // spectra of output fields 2m (A) and 2m+1 (B)
-        const int slot = m & 1;
-
-        // Z stage, per kx group: (2,6), (3,5), (4)
-#pragma unroll
+        // Z stage per kx pair: column A = kx 2+g (visited by the filter),
+        // column B = its mirror kx 6-g (g = 2: kx 4 mirrors onto itself).
+        // Z-stage outputs for fields 2m, 2m+1 go into those fields' window
+        // slots: each column is written after it has been read.
+        float2 *RA = win + ((2 * m) & 7) * 5 * 32;
+        float2 *RB = win + ((2 * m + 1) & 7) * 5 * 32;
+#pragma unroll 1
         for (int g = 0; g < 3; g++) {
-            const int ncol = (g < 2) ? 2 : 1;
-            const int kxs[2] = {2 + g, 6 - g};
-            float2 Y[2][8];
-            float mag[2][8], ab[2][8], E[2];
-#pragma unroll
-            for (int c = 0; c < 2; c++) {
-                if (c >= ncol) break;
-                const int k = kxs[c] - 2;
-                float2 col[8];
-                float B = 0.f;
-#pragma unroll
-                for (int z = 0; z < 8; z++) {
-                    col[z] = sw[z][k];
-                    B = __fmaf_rn(c3_wz[z], l1(sw[z][k]), B);
-                }
-                dft8_fwd(col, Y[c]);
+            const int ka = g, kb = 4 - g;
+            const int kxa = 2 + g;
+            float rmag[8], rab[8], rE;
+            Col B;
+            if (g < 2) {
+                z_column(win, m, kb, lane, g == 0 ? ek[4] : ek[3], B);
 #pragma unroll
                 for (int kz = 0; kz < 8; kz++) {
-                    mag[c][kz] = __fmaf_rn(Y[c][kz].x, Y[c][kz].x, Y[c][kz].y * Y[c][kz].y);
-                    ab[c][kz] = l1(Y[c][kz]);
+                    rmag[kz] = __shfl_sync(0xffffffffu, B.mag[kz], mirror_lane);
+                    rab[kz] = __shfl_sync(0xffffffffu, B.ab[kz], mirror_lane);
                 }
-                E[c] = kBoundFactor * 5.9604645e-8f * (ek[k] + B);
+                rE = __shfl_sync(0xffffffffu, B.E, mirror_lane);
             }
-            // Mirror column data from the mirror lane: for my column c the
-            // mirror column is 8 - kx, held by the mirror lane as its column
-            // (ncol == 2 ? 1 - c : 0).
-            float rmag[2][8], rab[2][8], rE[2];
-#pragma unroll
-            for (int c = 0; c < 2; c++) {
-                if (c >= ncol) break;
-                const int src_c = (ncol == 2) ? 1 - c : 0;
+            Col A;
+            z_column(win, m, ka, lane, g == 0 ? ek[0] : (g == 1 ? ek[1] : ek[2]), A);
+            if (g == 2) {
 #pragma unroll
                 for (int kz = 0; kz < 8; kz++) {
-                    rmag[c][kz] = __shfl_sync(0xffffffffu, mag[src_c][kz], mirror_lane);
-                    rab[c][kz] = __shfl_sync(0xffffffffu, ab[src_c][kz], mirror_lane);
+                    rmag[kz] = __shfl_sync(0xffffffffu, A.mag[kz], mirror_lane);
+                    rab[kz] = __shfl_sync(0xffffffffu, A.ab[kz], mirror_lane);
                 }
-                rE[c] = __shfl_sync(0xffffffffu, E[src_c], mirror_lane);
+                rE = __shfl_sync(0xffffffffu, A.E, mirror_lane);
             }
-            // Decisions
-            unsigned keep = 0, unc = 0;   // bit c*8 + kz
+            // The mirror of my column-A bin kz is bin kzr of the mirror lane's
+            // column B (its column A when g = 2).
+            unsigned keep = 0, unc = 0;
 #pragma unroll
-            for (int c = 0; c < 2; c++) {
-                if (c >= ncol) break;
-                const int kx = kxs[c];
-#pragma unroll
-                for (int kz = 0; kz < 8; kz++) {
-                    const int kzr = (10 - kz) & 7;
-                    const int bit = c * 8 + kz;
-                    const int kyr = (40 - my_ky) & 31;
-                    if (kx == 4 && kz == kzr && my_ky == kyr) {   // its own mirror: a carrier
-                        keep |= 1u << bit;
-                        continue;
-                    }
-                    const float a = mag[c][kz], b = rmag[c][kzr];
-                    const float Ea = E[c], Eb = rE[c];
-                    const float pa = 2.f * Ea * ab[c][kz] + Ea * Ea;
-                    const float pb = 2.f * Eb * rab[c][kzr] + Eb * Eb;
-                    bool sim = false, u = false;
-#pragma unroll
-                    for (int v = 0; v < 2; v++) {
-                        // visit 0: this bin visits (kx <= 4); visit 1: the mirror visits (kx >= 4)
-                        if (v == 0 && kx > 4) continue;
-                        if (v == 1 && kx < 4) continue;
-                        const Thr t = (v == 0) ? thr_of(P, kz, my_ky, kx) : thr_of(P, kzr, kyr, 8 - kx);
-                        const float d1 = __fmaf_rn(-b, t.f, a);
-                        const float d2 = __fmaf_rn(-a, t.f, b);
-                        sim |= (d1 >= 0.f) && (d2 >= 0.f);
-                        u |= (fabsf(d1) <= pa + t.f * pb) || (fabsf(d2) <= pb + t.f * pa);
-                    }
-                    if (sim) keep |= 1u << bit;
-                    if (u) unc |= 1u << bit;
+            for (int kz = 0; kz < 8; kz++) {
+                const int kzr = (10 - kz) & 7;
+                const float a = A.mag[kz], b = rmag[kzr];
+                const float pa = 2.f * A.E * A.ab[kz] + A.E * A.E;
+                const float pb = 2.f * rE * rab[kzr] + rE * rE;
+                float t = P.t2f;
+                if (PER_BIN) t = thr_of(P, kz, my_ky, kxa).f;
+                bool sim = fsim(a, b, t);
+                bool u = funcertain(a, b, t, pa, pb);
+                if (PER_BIN && g == 2) {   // kx = 4: the mirror bin visits too, with its own threshold
+                    const float t2 = thr_of(P, kzr, kyr, 4).f;
+                    sim |= fsim(a, b, t2);
+                    u |= funcertain(a, b, t2, pa, pb);
                 }
+                // a carrier (its own mirror) is always kept
+                const bool self = (g == 2) && (kz == kzr) && (my_ky == kyr);
+                if (sim || self) keep |= 1u << kz;
+                if (u && !self) unc |= 1u << kz;
             }
-            // Resolve uncertain decisions exactly (rare): one pair at a time.
-            unsigned any = __ballot_sync(0xffffffffu, unc != 0);
-            while (any) {
-                const int src = __ffs(any) - 1;
-                const unsigned su = __shfl_sync(0xffffffffu, unc, src);
-                const int bit = __ffs(su) - 1;
-                const int c = bit >> 3, kz = bit & 7;
-                const int kxb = (c == 0) ? 2 + g : 6 - g;
-                const int kyb = kappa(src);
-                df mb, mr;
-                exact_pair(P, m, tileX, tileY, kz, kyb, kxb, mb, mr);
-                const int kzr = (10 - kz) & 7, kyr = (40 - kyb) & 31, kxr = 8 - kxb;
-                bool sim = false;
-                if (kxb <= 4) sim |= df_sim(mb, mr, thr_of(P, kz, kyb, kxb).d);
-                if (kxb >= 4) sim |= df_sim(mb, mr, thr_of(P, kzr, kyr, kxr).d);
-                // update the owning lane of b and of its mirror r
-                const int rl = kappa(kyr);
-                const int rc = (ncol == 2) ? 1 - c : 0;
-                const int rbit = rc * 8 + kzr;
-                if (lane == src) {
-                    const bool was = (keep >> bit) & 1u;
-                    n_exact++;
-                    if (was != sim) n_flip++;
-                    keep = sim ? (keep | (1u << bit)) : (keep & ~(1u << bit));
-                    unc &= ~(1u << bit);
-                }
-                if (lane == rl) {
-                    keep = sim ? (keep | (1u << rbit)) : (keep & ~(1u << rbit));
-                    unc &= ~(1u << rbit);
-                }
-                any = __ballot_sync(0xffffffffu, unc != 0);
-            }
-            // Mask, inverse Z to slices 0, 1, 4, 5, and Z overlap-add.
+            // Resolve decisions inside the guard band exactly (rare).
+            if (__any_sync(0xffffffffu, unc != 0))
+                resolve_uncertain(P, m, tileX, tileY, g, kxa, lane, keep, unc, n_exact, n_flip);
+            z_inverse(A.Y, keep, carry, RA, RB, ka, lane);
+            if (g < 2) {
+                // Column B bins are kept exactly when their mirror visit kept them.
+                const unsigned mk = __shfl_sync(0xffffffffu, keep, mirror_lane);
+                unsigned keepB = 0;
 #pragma unroll
-            for (int c = 0; c < 2; c++) {
-                if (c >= ncol) break;
-                const int k = kxs[c] - 2;
-                float2 y[8];
-#pragma unroll
-                for (int kz = 0; kz < 8; kz++)
-                    y[kz] = ((keep >> (c * 8 + kz)) & 1u) ? Y[c][kz] : make_float2(0.f, 0.f);
-                const float2 E0 = make_float2(y[0].x + y[2].x + y[4].x + y[6].x, y[0].y + y[2].y + y[4].y + y[6].y);
-                const float2 O0 = make_float2(y[1].x + y[3].x + y[5].x + y[7].x, y[1].y + y[3].y + y[5].y + y[7].y);
-                // z = 1: even part y0 + i y2 - y4 - i y6; odd part with w = exp(+i pi/4)
-                const float2 E1 = make_float2(y[0].x - y[2].y - y[4].x + y[6].y, y[0].y + y[2].x - y[4].y - y[6].x);
-                const float2 o1 = cmul(y[1], make_float2(c3_tw32[4].x, -c3_tw32[4].y));    // w
-                const float2 o3 = cmul(y[3], make_float2(c3_tw32[12].x, -c3_tw32[12].y));  // w^3
-                const float2 o5 = cmul(y[5], make_float2(c3_tw32[20].x, -c3_tw32[20].y));  // w^5
-                const float2 o7 = cmul(y[7], make_float2(c3_tw32[28].x, -c3_tw32[28].y));  // w^7
-                const float2 O1 = make_float2(o1.x + o3.x + o5.x + o7.x, o1.y + o3.y + o5.y + o7.y);
-                const float2 z0 = make_float2(E0.x + O0.x, E0.y + O0.y);
-                const float2 z4 = make_float2(E0.x - O0.x, E0.y - O0.y);
-                const float2 z1 = make_float2(E1.x + O1.x, E1.y + O1.y);
-                const float2 z5 = make_float2(E1.x - O1.x, E1.y - O1.y);
-                const float2 c4 = s_carry[warp][slot][0][k][lane];
-                const float2 c5 = s_carry[warp][slot][1][k][lane];
-                RA[k] = make_float2(z0.x + c4.x, z0.y + c4.y);
-                RB[k] = make_float2(z1.x + c5.x, z1.y + c5.y);
-                s_carry[warp][slot][0][k][lane] = z4;
-                s_carry[warp][slot][1][k][lane] = z5;
+                for (int kz = 0; kz < 8; kz++) keepB |= ((mk >> ((10 - kz) & 7)) & 1u) << kz;
+                z_inverse(B.Y, keepB, carry, RA, RB, kb, lane);
             }
         }
-
+        __syncwarp();
         if (m < m0) continue;   // warm-up step: only the carries are needed
 
-        // Inverse Y: fold ky and ky+16 for each output field's row parity.
-        const int j = lane >> 4;
-        const int i = lane & 15;
-        const int kk = rev4(i);
-        const int f = 2 * m + j;
-        const int p = f & 1;
-        const int y0 = (p - tileY) & 1;
-        float2 G[5];
+        // Inverse Y then X, one kx at a time: lane (j, i) folds ky = kk and
+        // kk+16 of output field 2m+j for its row parity, runs a 16-point
+        // inverse DFT over the half-warp, and accumulates row i's cosine and
+        // sine sums of the inverse X transform.
+        float C[8], S[8];
 #pragma unroll
+        for (int x = 0; x < 8; x++) C[x] = S[x] = 0.f;
+        const float2 *Rj = LC.j ? RB : RA;
+#pragma unroll 1
         for (int k = 0; k < 5; k++) {
-            const float2 send = j ? RA[k] : RB[k];
-            const float2 recv = shfl_xor2(send, 16);
-            float2 lo_v, hi_v;   // R[kk], R[kk+16] of this half-warp's field
-            if (j == 0) { lo_v = RA[k]; hi_v = recv; }
-            else { lo_v = recv; hi_v = RB[k]; }
-            float2 s = y0 ? make_float2(lo_v.x - hi_v.x, lo_v.y - hi_v.y) : make_float2(lo_v.x + hi_v.x, lo_v.y + hi_v.y);
-            // exp(+i pi kk y0 / 16) = conj(tw32[kk]) when y0 = 1
-            if (y0) s = cmul(s, make_float2(c3_tw32[kk].x, -c3_tw32[kk].y));
-            G[k] = s;
-        }
-        // 16-point inverse DFT, bit-reversed input -> natural order (DIT)
+            const float2 lo_v = Rj[k * 32 + LC.i];        // R[kk]   (lane kappa^-1(kk) = i)
+            const float2 hi_v = Rj[k * 32 + LC.i + 16];   // R[kk+16]
+            float2 G = LC.y0 ? make_float2(lo_v.x - hi_v.x, lo_v.y - hi_v.y)
+                             : make_float2(lo_v.x + hi_v.x, lo_v.y + hi_v.y);
+            G = cmul(G, make_float2(LC.ptw.x, -LC.ptw.y));   // exp(+i pi kk y0 / 16)
+            // 16-point inverse DFT, bit-reversed input -> natural order (DIT)
+            int st = 3;
 #pragma unroll
-        for (int h = 1; h <= 8; h <<= 1) {
-            const bool upper = (i & h) != 0;
-            const int r = i & (h - 1);
-            const float2 w = make_float2(c3_tw16[r * (8 / h)].x, -c3_tw16[r * (8 / h)].y);   // exp(+2 pi i r/(2h))
-#pragma unroll
-            for (int k = 0; k < 5; k++) {
-                const float2 o = shfl_xor2(G[k], h);
-                if (upper) {
-                    const float2 t = cmul(G[k], w);
-                    G[k] = make_float2(o.x - t.x, o.y - t.y);
-                } else {
-                    const float2 t = cmul(o, w);
-                    G[k] = make_float2(G[k].x + t.x, G[k].y + t.y);
-                }
+            for (int h = 1; h <= 8; h <<= 1, st--) {
+                const bool upper = (LC.i & h) != 0;
+                const float2 w = make_float2(LC.ftw[st].x, -LC.ftw[st].y);   // exp(+2 pi i r/(2h))
+                const float2 o = shfl_xor2(G, h);
+                const float2 t = cmul(upper ? G : o, w);
+                G = upper ? make_float2(o.x - t.x, o.y - t.y) : make_float2(G.x + t.x, G.y + t.y);
             }
-        }
-        // Inverse X and store: lane holds row i of field 2m + j.
-        const int y = y0 + 2 * i;
-        const int L = tileY + y;
-        if (L >= P.fafl && L <= P.lafl) {
-            float o[16];
 #pragma unroll
             for (int x = 0; x < 8; x++) {
-                float C = 0.f, S = 0.f;
-#pragma unroll
-                for (int k = 0; k < 5; k++) {
-                    C = __fmaf_rn(G[k].x, c3_cix[k][x], C);
-                    S = __fmaf_rn(G[k].y, c3_six[k][x], S);
-                }
-                o[x] = C - S;
-                o[15 - x] = C + S;
+                C[x] = __fmaf_rn(G.x, c3_cix[k][x], C[x]);
+                S[x] = __fmaf_rn(G.y, c3_six[k][x], S[x]);
             }
-            const int ofield = 2 * (m - P.frame_begin) + j;
+        }
+        // Store row i of field 2m + j.
+        const int L = tileY + LC.y0 + 2 * LC.i;
+        if (L >= P.fafl && L <= P.lafl) {
+            const int ofield = 2 * (m - P.frame_begin) + LC.j;
             float *dst = P.partial + (long long)cls * P.part_class_stride + (long long)ofield * P.part_field_stride +
                          (long long)((L >> 1) - P.fl_lo) * P.part_row_stride - P.avs;
 #pragma unroll
-            for (int x = 0; x < 16; x++) {
-                const int X = tileX + x;
-                if (X >= P.avs && X < P.ave) dst[X] = o[x];
+            for (int x = 0; x < 8; x++) {
+                const int X0 = tileX + x, X1 = tileX + 15 - x;
+                if (X0 >= P.avs && X0 < P.ave) dst[X0] = C[x] - S[x];
+                if (X1 >= P.avs && X1 < P.ave) dst[X1] = C[x] + S[x];
             }
         }
     }
@@ -678,7 +665,18 @@ int tp3_launch(const T3Params &P, cudaStream_t stream)
     const long long items = (long long)P.ntx * P.nty * P.nchunks;
     if (items <= 0) return 0;
     const unsigned blocks = (unsigned)((items + kWarps3 - 1) / kWarps3);
-    tpal3d_kernel<<<blocks, 32 * kWarps3, 0, stream>>>(P);
+    const size_t smem = sizeof(float2) * (size_t)kWarpSmemF2 * kWarps3;
+    static bool attr_set = false;
+    if (!attr_set) {
+        if (cudaFuncSetAttribute(tpal3d_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(tpal3d_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+                cudaSuccess)
+            return -1;
+        attr_set = true;
+    }
+    if (P.thr_table != nullptr) tpal3d_kernel<true><<<blocks, 32 * kWarps3, smem, stream>>>(P);
+    else tpal3d_kernel<false><<<blocks, 32 * kWarps3, smem, stream>>>(P);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
