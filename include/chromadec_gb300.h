@@ -97,6 +97,26 @@ int chdg_engine_kernel_times(chdg_engine *e, double *ms_transform, double *ms_de
 int chdg_chroma_device(chdg_engine *e, const uint16_t *d_fields, int64_t field_stride, int32_t nfields,
                        int32_t frame_begin, int32_t frame_end, float *d_chroma, void *stream);
 
+/* Allocation-free Transform-PAL 3D decode (no counterpart in the reference).
+ *
+ * Same result as chdg_decode_device for kind 8, for callers that cannot
+ * allocate device memory while decoding: hosts whose device memory belongs to
+ * their own allocator or budget, and latency-critical loops where cudaMalloc's
+ * implicit device synchronisation would stall other work. The chroma scratch
+ * is a fixed array compiled into the library (69.9 MB: 8 frames of the
+ * 948x576 active picture), which every GPU that loads the library holds until
+ * the process exits; calls asking for more than 8 frames, or a larger active
+ * picture, fail with CHDG_E_INVALID_ARG. No cudaMalloc/cudaFree or other
+ * allocating call is made. All calls on a device share the one scratch array
+ * (it keeps the last call's contents), so calls whose work overlaps on the GPU
+ * race: serialise them on one stream. The first call on a device resolves the
+ * array's device address and uploads constant tables; make that first call
+ * before starting any stream capture. Per-bin thresholds, when given, are
+ * copied into a second static array shared the same way. */
+int chdg_decode_device_static(const chdg_geometry *g, const chdg_config *c, const uint16_t *d_fields,
+                              int64_t field_stride, int32_t nfields, int32_t frame_begin, int32_t frame_end,
+                              void *d_out, void *stream);
+
 /* Threshold decisions whose FP32 margin was inside the error bound and were
  * re-evaluated in double-float, and how many of those FP32 had wrong. */
 int chdg_engine_stats(chdg_engine *e, uint64_t *exact_decisions, uint64_t *fp32_flips);

@@ -135,6 +135,77 @@ int Engine::init(const chdg_geometry &g, const chdg_config &c)
     return 0;
 }
 
+int Engine::init_static(const chdg_geometry &g, const chdg_config &c, float *thr_table_dev)
+{
+    g_ = g;
+    c_ = c;
+    if (c.kind != 8) return arg_fail("the allocation-free decode supports CHD_DEC_TRANSFORM_3D (8) only");
+    if (g.field_width <= 0 || g.field_height <= 0 || g.active_start < 0 || g.active_end > g.field_width ||
+        g.active_end <= g.active_start || g.first_active_frame_line < 0 ||
+        g.last_active_frame_line >= 2 * g.field_height - 1 || g.last_active_frame_line < g.first_active_frame_line)
+        return arg_fail("invalid geometry");
+    if (std::fabs(g.fsc / g.sample_rate - 0.25) > 1e-9)
+        return chd::detail::set_last_error("chromadec_gb300: only 4fsc sampling is supported"), CHDG_E_UNSUPPORTED;
+    if (g.active_start - 7 < 0 || g.active_end + 8 > 1135 || g.field_width > 1135)
+        return chd::detail::set_last_error("chromadec_gb300: active window too close to the line ends"),
+               CHDG_E_UNSUPPORTED;
+    if (c.output_format != 0 && c.output_format != 1) return arg_fail("output_format must be 0 or 1");
+    if (c.padding_multiple < 1 || c.padding_multiple > 1024) return arg_fail("padding_multiple out of range");
+    if (c.thresholds != nullptr && c.n_thresholds != 768) return arg_fail("thresholds table must have 768 entries");
+    cudaError_t e = cudaGetDevice(&device_);
+    if (e != cudaSuccess) return cuda_fail("cudaGetDevice", e);
+    if (tpal::tp3_init_constants(device_) != 0) return cuda_fail("3D constants", cudaGetLastError());
+    if (const int rc = tpal::demod_init_constants(device_, g.sample_rate, g.field_width); rc != 0)
+        return rc == -2 ? (chd::detail::set_last_error("chromadec_gb300: unsupported chroma filter size"),
+                           CHDG_E_UNSUPPORTED)
+                        : cuda_fail("demod constants", cudaGetLastError());
+    const double t2 = c.threshold * c.threshold;
+    t2f_ = (float)t2;
+    t2hi_ = (float)t2;
+    t2lo_ = (float)(t2 - (double)t2hi_);
+    thr_dev_ = nullptr;
+    if (c.thresholds != nullptr) {
+        if (thr_table_dev == nullptr) return arg_fail("no device threshold table");
+        float tab[3 * 768];
+        for (int i = 0; i < 768; i++) {
+            const double v = c.thresholds[i] * c.thresholds[i];
+            tab[3 * i] = (float)v;
+            tab[3 * i + 1] = (float)v;
+            tab[3 * i + 2] = (float)(v - (double)(float)v);
+        }
+        if ((e = cudaMemcpy(thr_table_dev, tab, sizeof(tab), cudaMemcpyHostToDevice)) != cudaSuccess)
+            return cuda_fail("cudaMemcpy", e);
+        thr_dev_ = thr_table_dev;
+    }
+    stats_dev_ = nullptr;
+    fl_lo_ = g.first_active_frame_line / 2;
+    fl_hi_ = g.last_active_frame_line / 2 + 1;
+    rows_ = fl_hi_ - fl_lo_;
+    cols_ = g.active_end - g.active_start;
+    output_geometry(g, c.padding_multiple, out_w_, out_h_, left_pad_, top_pad_);
+    return 0;
+}
+
+size_t Engine::scratch_floats_for(const chdg_geometry &g, int nframes)
+{
+    const size_t rows = (size_t)(g.last_active_frame_line / 2 + 1 - g.first_active_frame_line / 2);
+    const size_t cols = (size_t)(g.active_end - g.active_start);
+    return (size_t)4 * 2 * (size_t)nframes * rows * cols;
+}
+
+int Engine::decode_scratch(const uint16_t *fields, long long stride, int nfields, int fb, int fe, void *out,
+                           float *scratch, size_t scratch_floats, cudaStream_t s)
+{
+    if (fields == nullptr || out == nullptr || scratch == nullptr || fe < fb ||
+        stride < (long long)g_.field_width * g_.field_height)
+        return arg_fail("decode: bad arguments");
+    if (fe == fb) return 0;
+    if (scratch_floats_for(g_, fe - fb) > scratch_floats)
+        return arg_fail("decode: " + std::to_string(fe - fb) + " frames exceed the static chroma scratch");
+    if (const int rc = run_transform(fields, stride, 0, nfields, fb, fe, scratch, s); rc != 0) return rc;
+    return run_demod(fields, stride, 0, fb, fe, scratch, out, s);
+}
+
 size_t Engine::frame_bytes() const
 {
     return (size_t)out_w_ * out_h_ * 3 * (c_.output_format == 1 ? sizeof(float) : sizeof(uint16_t));

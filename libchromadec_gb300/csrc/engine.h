@@ -21,6 +21,15 @@ public:
     Engine &operator=(const Engine &) = delete;
 
     int init(const chdg_geometry &g, const chdg_config &c);
+    // Allocation-free set-up and decode (used by chdg_decode_device_static):
+    // the per-bin threshold table and the chroma scratch are caller-provided
+    // device memory; nothing is allocated and no counters are kept.
+    int init_static(const chdg_geometry &g, const chdg_config &c, float *thr_table_dev);
+    int decode_scratch(const uint16_t *fields, long long stride, int nfields, int fb, int fe, void *out,
+                       float *scratch, size_t scratch_floats, cudaStream_t s);
+    static size_t scratch_floats_for(const chdg_geometry &g, int nframes);
+    // Drop the borrowed threshold table before destruction (it is not ours to free).
+    void forget_static() { thr_dev_ = nullptr; }
     // fields: device buffer holding capture fields [field_base, ...)
     int decode(const uint16_t *fields, long long stride, int field_base, int nfields, int fb, int fe, void *out,
                cudaStream_t s);

@@ -1,0 +1,106 @@
+// noalloc.cu -- Transform-PAL 3D decode that allocates no device memory.
+//
+// The regular entry points size their chroma scratch on demand with
+// cudaMalloc. This variant runs the same 3D transform and demodulator
+// kernels with their scratch in a file-scope __device__ array instead, for
+// callers that cannot allocate device memory on the decode path: hosts whose
+// device memory belongs to their own allocator or budget (a framework's
+// caching allocator, a media server with a fixed pool), and latency-critical
+// playback loops where cudaMalloc's implicit device-wide synchronisation
+// would stall other streams.
+//
+// The array is a fixed 8-frame chroma scratch (4 overlap planes x 16 fields x
+// 288 x 948 FP32 at the default 948x576 active picture, 69.9 MB) that every
+// GPU loading the library holds until the process exits. Calls with more
+// frames, or with a larger active picture than fits, are rejected.
+#include <cstring>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "../../include/chromadec_gb300.h"
+#include "engine.h"
+#include "error_state.h"
+
+namespace {
+
+constexpr int kStaticMaxFrames = 8;
+constexpr size_t kStaticScratchFloats = (size_t)4 * 2 * kStaticMaxFrames * 288 * 948;
+
+// Shared by every call on a device; holds the previous call's chroma planes.
+static __device__ __align__(256) float g_static_scratch[kStaticScratchFloats];
+static __device__ __align__(256) float g_static_thresholds[3 * 768];
+
+struct DeviceSymbols {
+    float *scratch = nullptr;
+    float *thresholds = nullptr;
+};
+constexpr int kMaxDevices = 64;
+static DeviceSymbols g_symbols[kMaxDevices];
+
+// Once per device, with that device current: the device addresses of the
+// static arrays (host code cannot take them from the symbols directly).
+int resolve_symbols(int device, DeviceSymbols &out)
+{
+    if (device < 0 || device >= kMaxDevices) {
+        chd::detail::set_last_error("chdg_decode_device_static: device index out of range");
+        return CHDG_E_INVALID_ARG;
+    }
+    DeviceSymbols &d = g_symbols[device];
+    if (d.scratch == nullptr) {
+        void *p = nullptr, *q = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e == cudaSuccess) e = cudaGetSymbolAddress(&q, g_static_thresholds);
+        if (e != cudaSuccess) {
+            chd::detail::set_last_error(std::string("chdg_decode_device_static: cudaGetSymbolAddress: ") +
+                                        cudaGetErrorString(e));
+            return CHDG_E_CUDA;
+        }
+        d.thresholds = static_cast<float *>(q);
+        d.scratch = static_cast<float *>(p);
+    }
+    out = d;
+    return 0;
+}
+
+}  // namespace
+
+#pragma GCC visibility push(default)
+extern "C" int chdg_decode_device_static(const chdg_geometry *g, const chdg_config *c, const uint16_t *d_fields,
+                                         int64_t field_stride, int32_t nfields, int32_t frame_begin,
+                                         int32_t frame_end, void *d_out, void *stream)
+{
+    if (g == nullptr || c == nullptr) {
+        chd::detail::set_last_error("chdg_decode_device_static: null geometry or config");
+        return CHDG_E_INVALID_ARG;
+    }
+    if (frame_end - frame_begin > kStaticMaxFrames) {
+        chd::detail::set_last_error("chdg_decode_device_static: at most " + std::to_string(kStaticMaxFrames) +
+                                    " frames per call (the static chroma scratch holds " +
+                                    std::to_string(kStaticMaxFrames) + " frames)");
+        return CHDG_E_INVALID_ARG;
+    }
+    if (chdg::Engine::scratch_floats_for(*g, frame_end > frame_begin ? frame_end - frame_begin : 0) >
+        kStaticScratchFloats) {
+        chd::detail::set_last_error("chdg_decode_device_static: active picture too large for the static scratch");
+        return CHDG_E_INVALID_ARG;
+    }
+    int device = 0;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e != cudaSuccess) {
+        chd::detail::set_last_error(std::string("chdg_decode_device_static: cudaGetDevice: ") + cudaGetErrorString(e));
+        return CHDG_E_CUDA;
+    }
+    DeviceSymbols sym;
+    if (const int rc = resolve_symbols(device, sym); rc != 0) return rc;
+    chdg::Engine eng;
+    int rc = eng.init_static(*g, *c, sym.thresholds);
+    // Every chroma sample the demodulator reads is written by the transform
+    // in the same call, so the scratch needs no clearing.
+    if (rc == 0)
+        rc = eng.decode_scratch(d_fields, field_stride, nfields, frame_begin, frame_end, d_out, sym.scratch,
+                                kStaticScratchFloats, (cudaStream_t)stream);
+    eng.forget_static();
+    return rc;
+}
+#pragma GCC visibility pop
