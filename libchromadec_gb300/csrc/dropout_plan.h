@@ -1,0 +1,50 @@
+// dropout_plan.h -- host-side planning of dropout concealment and dropout
+// span mapping. The integer logic (span splitting, replacement-line search,
+// statistics) runs on the host from metadata; the resulting ordered list of
+// line operations is applied to the field samples on the GPU
+// (dropout.cu), bit-exact with the reference's DropoutCorrector.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "capture.h"
+
+namespace chdg {
+
+// One concealment step on a frame's two fields (slot 0 / slot 1 of the
+// window frame), applied in order.
+struct DropOp {
+    int32_t field;        // target slot
+    int32_t mode;         // 1 = copy, 2 = low-frequency + high-frequency blend
+    int32_t line;         // target field line, 0-based
+    int32_t startx, endx; // samples [startx, endx)
+    int32_t srcField, srcLine;   // replacement line (slot, 0-based line)
+    int32_t chrField, chrLine;   // chroma replacement line (blend only)
+};
+
+struct FramePlan {
+    std::vector<DropOp> ops;
+    int32_t corrected = 0, failed = 0;
+    int64_t totalDistance = 0;
+};
+
+// DropoutCorrector::correctFrame, single source
+// (src/dropout/dropout_corrector.cpp:40-530). slot0/slot1 are the frame's
+// fields in window order.
+FramePlan plan_frame(const VideoParams &vp, const FieldMeta &slot0, const FieldMeta &slot1, bool overcorrect,
+                     bool intraField);
+
+struct Span {
+    int32_t y, x_start, x_end, origin;
+};
+
+// appendFieldSpans / collectSpans (src/abi/c_api_dropout_detect.cpp:92-174):
+// both fields' dropouts in output framing, sorted by (y, x_start, x_end).
+struct OutputFraming {
+    int32_t activeVideoStart, activeWidth, width, height, firstActiveFrameLine, leftPad, topPad, fieldWidth;
+};
+std::vector<Span> frame_spans(const OutputFraming &g, const FieldMeta &slot0, bool slot0First,
+                              const FieldMeta &slot1, bool slot1First, bool overcorrect);
+
+}  // namespace chdg

@@ -72,6 +72,7 @@ Engine::~Engine()
         if (ev_d2h_[i]) cudaEventDestroy(ev_d2h_[i]);
     }
     if (copy_stream_) cudaStreamDestroy(copy_stream_);
+    if (d2h_stream_) cudaStreamDestroy(d2h_stream_);
     reset_kernel_times();
 }
 
@@ -443,6 +444,8 @@ int Engine::ensure_host_pipeline(size_t field_bytes, size_t out_bytes)
     if (copy_stream_ == nullptr) {
         if ((e = cudaStreamCreateWithFlags(&copy_stream_, cudaStreamNonBlocking)) != cudaSuccess)
             return cuda_fail("stream", e);
+        if ((e = cudaStreamCreateWithFlags(&d2h_stream_, cudaStreamNonBlocking)) != cudaSuccess)
+            return cuda_fail("stream", e);
         for (int i = 0; i < 2; i++) {
             cudaEventCreateWithFlags(&ev_h2d_[i], cudaEventDisableTiming);
             cudaEventCreateWithFlags(&ev_comp_[i], cudaEventDisableTiming);
@@ -511,14 +514,15 @@ int Engine::decode_host(const uint16_t *host_fields, long long host_stride, int 
         if (i >= 2) cudaStreamWaitEvent(s, ev_d2h_[slot], 0);   // output slot drained
         if (const int rc = decode(hp_fields_[slot], dstride, f0, nfields, b, be, hp_out_[slot], s); rc != 0) return rc;
         cudaEventRecord(ev_comp_[slot], s);
-        cudaStreamWaitEvent(copy_stream_, ev_comp_[slot], 0);
+        // downloads on their own stream, so the next upload does not queue behind them
+        cudaStreamWaitEvent(d2h_stream_, ev_comp_[slot], 0);
         e = cudaMemcpyAsync((char *)host_out + frame_bytes() * (size_t)(b - fb), hp_out_[slot],
-                            frame_bytes() * (size_t)(be - b), cudaMemcpyDeviceToHost, copy_stream_);
+                            frame_bytes() * (size_t)(be - b), cudaMemcpyDeviceToHost, d2h_stream_);
         if (e != cudaSuccess) return cuda_fail("D2H", e);
-        cudaEventRecord(ev_d2h_[slot], copy_stream_);
+        cudaEventRecord(ev_d2h_[slot], d2h_stream_);
     }
     // the caller's stream completes after the last download
-    cudaEventRecord(ev_d2h_[0], copy_stream_);
+    cudaEventRecord(ev_d2h_[0], d2h_stream_);
     cudaStreamWaitEvent(s, ev_d2h_[0], 0);
     return 0;
 }

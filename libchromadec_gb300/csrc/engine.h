@@ -84,7 +84,7 @@ private:
     uint16_t *hp_fields_[2] = {nullptr, nullptr};
     void *hp_out_[2] = {nullptr, nullptr};
     size_t hp_field_bytes_ = 0, hp_out_bytes_ = 0;
-    cudaStream_t copy_stream_ = nullptr;
+    cudaStream_t copy_stream_ = nullptr, d2h_stream_ = nullptr;
     cudaEvent_t ev_h2d_[2] = {nullptr, nullptr}, ev_comp_[2] = {nullptr, nullptr}, ev_d2h_[2] = {nullptr, nullptr};
     // profiling
     bool profiling_ = false;

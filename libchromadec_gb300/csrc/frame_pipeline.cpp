@@ -1,0 +1,286 @@
+// frame_pipeline.cpp -- see frame_pipeline.h.
+#include "frame_pipeline.h"
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+
+#include <chromadec/errors.h>
+
+#include "error_state.h"
+
+namespace chdg {
+
+int dropout_apply(uint16_t *fields, long long field_stride, int fw, const int *d_frames, const DropOp *d_ops,
+                  const int *d_op_begin, int nframes, cudaStream_t s);
+
+namespace {
+
+int cuda_status(const char *what, cudaError_t e)
+{
+    chd::detail::set_last_error(std::string("chromadec_gb300: ") + what + ": " + cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? CHD_E_OOM : CHD_E_INTERNAL;
+}
+
+}  // namespace
+
+HostChunk::~HostChunk()
+{
+    if (data != nullptr) cudaFreeHost(data);
+}
+
+FramePipeline::~FramePipeline()
+{
+    if (comp_) cudaStreamSynchronize(comp_);
+    if (copy_) cudaStreamSynchronize(copy_);
+    if (d2h_) cudaStreamSynchronize(d2h_);
+    chunks_.clear();
+    for (int i = 0; i < 2; i++) {
+        if (staging_[i]) cudaFreeHost(staging_[i]);
+        if (dwin_[i]) cudaFree(dwin_[i]);
+        if (dout_[i]) cudaFree(dout_[i]);
+        if (h_ops_[i]) cudaFreeHost(h_ops_[i]);
+        if (d_ops_[i]) cudaFree(d_ops_[i]);
+        if (h_idx_[i]) cudaFreeHost(h_idx_[i]);
+        if (d_idx_[i]) cudaFree(d_idx_[i]);
+        if (ev_h2d_[i]) cudaEventDestroy(ev_h2d_[i]);
+        if (ev_comp_[i]) cudaEventDestroy(ev_comp_[i]);
+        if (ev_d2h_[i]) cudaEventDestroy(ev_d2h_[i]);
+    }
+    if (comp_) cudaStreamDestroy(comp_);
+    if (copy_) cudaStreamDestroy(copy_);
+    if (d2h_) cudaStreamDestroy(d2h_);
+}
+
+int FramePipeline::init(const Capture *cap, const chdg_geometry &g, const chdg_config &c, bool firstFieldFirst,
+                        int batch_frames, int copy_threads)
+{
+    cap_ = cap;
+    copy_threads_ = std::max(1, std::min(16, copy_threads));
+    ffirst_ = firstFieldFirst;
+    nframes_ = cap->numFrames(firstFieldFirst);
+    batch_ = std::max(1, batch_frames);
+    if (const int rc = eng_.init(g, c); rc != 0) return rc == CHDG_E_UNSUPPORTED ? CHD_E_UNSUPPORTED : CHD_E_INVALID_ARG;
+    eng_.set_max_batch_frames(batch_);
+    lb_ = eng_.look_behind();
+    la_ = eng_.look_ahead();
+    flen_ = cap->fieldLen();
+    dstride_ = (long long)((flen_ + 63) & ~(size_t)63);
+    const size_t winFields = (size_t)2 * (batch_ + lb_ + la_) + 1;   // +1: tiles read a few samples past a field
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&comp_, cudaStreamNonBlocking)) != cudaSuccess) return cuda_status("stream", e);
+    if ((e = cudaStreamCreateWithFlags(&copy_, cudaStreamNonBlocking)) != cudaSuccess) return cuda_status("stream", e);
+    if ((e = cudaStreamCreateWithFlags(&d2h_, cudaStreamNonBlocking)) != cudaSuccess) return cuda_status("stream", e);
+    for (int i = 0; i < 2; i++) {
+        if ((e = cudaMallocHost(&staging_[i], winFields * dstride_ * 2)) != cudaSuccess) return cuda_status("pinned", e);
+        if ((e = cudaMalloc(&dwin_[i], winFields * dstride_ * 2)) != cudaSuccess) return cuda_status("window", e);
+        cudaMemset(dwin_[i], 0, winFields * dstride_ * 2);
+        if ((e = cudaMalloc(&dout_[i], eng_.frame_bytes() * (size_t)batch_)) != cudaSuccess)
+            return cuda_status("frames", e);
+        cudaEventCreateWithFlags(&ev_h2d_[i], cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&ev_comp_[i], cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&ev_d2h_[i], cudaEventDisableTiming);
+    }
+    return CHD_OK;
+}
+
+void FramePipeline::set_dropout(const DropoutSettings &d)
+{
+    if (d.overcorrect != drop_.overcorrect || d.intra != drop_.intra) plans_.clear();
+    drop_ = d;
+}
+
+FramePlan FramePipeline::frame_stats(int64_t frame)
+{
+    FramePlan s;
+    if (!drop_.enabled) return s;
+    const FramePlan &p = plan_for(frame);
+    s.corrected = p.corrected;
+    s.failed = p.failed;
+    s.totalDistance = p.totalDistance;
+    return s;
+}
+
+std::shared_ptr<HostChunk> FramePipeline::take_chunk(size_t bytes)
+{
+    // A chunk only this pool still references is free for reuse.
+    for (auto &c : chunks_)
+        if (c.use_count() == 1 && c->bytes >= bytes) return c;
+    size_t idle = 0;
+    for (auto it = chunks_.begin(); it != chunks_.end();) {
+        if (it->use_count() == 1 && ++idle > 2) it = chunks_.erase(it);
+        else ++it;
+    }
+    auto c = std::make_shared<HostChunk>();
+    if (cudaMallocHost(&c->data, bytes) != cudaSuccess) {
+        c->data = nullptr;
+        return nullptr;
+    }
+    c->bytes = bytes;
+    chunks_.push_back(c);
+    return c;
+}
+
+const FramePlan &FramePipeline::plan_for(int64_t frame)
+{
+    auto it = plans_.find(frame);
+    if (it != plans_.end()) return it->second;
+    WindowField wf[2];
+    cap_->windowFrame((int)frame + 1, ffirst_, wf);
+    FramePlan plan;
+    // A padding frame carries frame 1's dropouts but none of its picture.
+    if (!wf[0].isPadding && !wf[1].isPadding) {
+        FieldMeta m0 = cap_->field(wf[0].fieldNumber), m1 = cap_->field(wf[1].fieldNumber);
+        plan = plan_frame(cap_->vp(), m0, m1, drop_.overcorrect, drop_.intra);
+    }
+    if (plans_.size() > 4096) plans_.clear();
+    return plans_.emplace(frame, std::move(plan)).first->second;
+}
+
+int FramePipeline::fill_staging(int slot, int64_t w0, int64_t w1)
+{
+    const int nf = (int)(2 * (w1 - w0));
+    if (nf <= 0) return 0;
+    uint16_t *base = staging_[slot];
+    const uint16_t black = (uint16_t)cap_->vp().black16bIre;
+    auto work = [&](int lo, int hi) {
+        for (int k = lo; k < hi; k++) {
+            WindowField wf[2];
+            cap_->windowFrame((int)(w0 + k / 2) + 1, ffirst_, wf);
+            uint16_t *dst = base + (size_t)k * dstride_;
+            const uint16_t *src = wf[k & 1].source ? cap_->fieldData(wf[k & 1].source) : nullptr;
+            if (src != nullptr) std::memcpy(dst, src, flen_ * 2);
+            else std::fill(dst, dst + flen_, black);
+        }
+    };
+    const int nt = std::min(nf, copy_threads_);
+    if (nt <= 1) {
+        work(0, nf);
+        return 0;
+    }
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; t++) th.emplace_back(work, nf * t / nt, nf * (t + 1) / nt);
+    for (auto &x : th) x.join();
+    return 0;
+}
+
+int FramePipeline::decode(int64_t a, int64_t b, const Deliver &deliver, const std::function<bool()> &cancelled,
+                          FramePlan *stats)
+{
+    struct Pending {
+        std::shared_ptr<HostChunk> out;
+        int64_t first = 0;
+        int count = 0;
+        int slot = 0;
+    };
+    Pending prev;
+    bool havePrev = false;
+    const size_t fb = eng_.frame_bytes();
+    cudaError_t e;
+    int i = 0;
+    for (int64_t c = a; c < b; c += batch_, i++) {
+        if (cancelled && cancelled()) break;
+        const int64_t ce = std::min<int64_t>(b, c + batch_);
+        const int slot = i & 1;
+        const int64_t w0 = std::max<int64_t>(0, c - lb_);
+        const int64_t w1 = std::min<int64_t>(nframes_, ce + la_);
+        if (i >= 2) {
+            // staging, window and plan buffers of this slot were last used by batch i-2
+            if ((e = cudaEventSynchronize(ev_comp_[slot])) != cudaSuccess) return cuda_status("sync", e);
+        }
+        fill_staging(slot, w0, w1);
+        // dropout plans of the window's frames
+        int nplan = 0;
+        size_t nops = 0;
+        std::vector<const FramePlan *> plans;
+        std::vector<int> planFrames;
+        if (drop_.enabled) {
+            for (int64_t w = w0; w < w1; w++) {
+                const FramePlan &p = plan_for(w);
+                if (!p.ops.empty()) {
+                    plans.push_back(&p);
+                    planFrames.push_back((int)(2 * (w - w0)));
+                    nops += p.ops.size();
+                }
+            }
+            nplan = (int)plans.size();
+            if (nops > ops_cap_ || (size_t)(2 * nplan + 1) > idx_cap_) {
+                cudaStreamSynchronize(comp_);
+                cudaStreamSynchronize(copy_);
+                cudaStreamSynchronize(d2h_);
+                for (int s = 0; s < 2; s++) {
+                    if (h_ops_[s]) cudaFreeHost(h_ops_[s]);
+                    if (d_ops_[s]) cudaFree(d_ops_[s]);
+                    if (h_idx_[s]) cudaFreeHost(h_idx_[s]);
+                    if (d_idx_[s]) cudaFree(d_idx_[s]);
+                    h_ops_[s] = d_ops_[s] = nullptr;
+                    h_idx_[s] = d_idx_[s] = nullptr;
+                }
+                ops_cap_ = std::max<size_t>(nops * 2, 1024);
+                idx_cap_ = std::max<size_t>((size_t)(2 * nplan + 1) * 2, 256);
+                for (int s = 0; s < 2; s++) {
+                    if (cudaMallocHost(&h_ops_[s], ops_cap_ * sizeof(DropOp)) != cudaSuccess ||
+                        cudaMalloc(&d_ops_[s], ops_cap_ * sizeof(DropOp)) != cudaSuccess ||
+                        cudaMallocHost(&h_idx_[s], idx_cap_ * sizeof(int)) != cudaSuccess ||
+                        cudaMalloc(&d_idx_[s], idx_cap_ * sizeof(int)) != cudaSuccess)
+                        return cuda_status("dropout plan buffers", cudaErrorMemoryAllocation);
+                }
+            }
+            size_t o = 0;
+            for (int p = 0; p < nplan; p++) {
+                h_idx_[slot][p] = planFrames[p];
+                h_idx_[slot][nplan + p] = (int)o;
+                for (const DropOp &op : plans[p]->ops) h_ops_[slot][o++] = op;
+            }
+            h_idx_[slot][2 * nplan] = (int)o;
+        }
+        const size_t wbytes = (size_t)(2 * (w1 - w0)) * dstride_ * 2;
+        if (wbytes > 0 &&
+            (e = cudaMemcpyAsync(dwin_[slot], staging_[slot], wbytes, cudaMemcpyHostToDevice, copy_)) != cudaSuccess)
+            return cuda_status("H2D", e);
+        if (nplan > 0) {
+            cudaMemcpyAsync(d_ops_[slot], h_ops_[slot], nops * sizeof(DropOp), cudaMemcpyHostToDevice, copy_);
+            cudaMemcpyAsync(d_idx_[slot], h_idx_[slot], (2 * nplan + 1) * sizeof(int), cudaMemcpyHostToDevice, copy_);
+        }
+        cudaEventRecord(ev_h2d_[slot], copy_);
+        cudaStreamWaitEvent(comp_, ev_h2d_[slot], 0);
+        if (i >= 2) cudaStreamWaitEvent(comp_, ev_d2h_[slot], 0);   // output slot drained
+        if (nplan > 0 &&
+            dropout_apply(dwin_[slot], dstride_, cap_->vp().fieldWidth, d_idx_[slot], d_ops_[slot],
+                          d_idx_[slot] + nplan, nplan, comp_) != 0)
+            return cuda_status("dropout kernel", cudaGetLastError());
+        if (const int rc = eng_.decode(dwin_[slot], dstride_, (int)(2 * w0), 2 * nframes_, (int)c, (int)ce,
+                                       dout_[slot], comp_);
+            rc != 0)
+            return CHD_E_INTERNAL;
+        cudaEventRecord(ev_comp_[slot], comp_);
+        auto chunk = take_chunk(fb * (size_t)(ce - c));
+        if (!chunk) return cuda_status("pinned frames", cudaErrorMemoryAllocation);
+        cudaStreamWaitEvent(d2h_, ev_comp_[slot], 0);
+        if ((e = cudaMemcpyAsync(chunk->data, dout_[slot], fb * (size_t)(ce - c), cudaMemcpyDeviceToHost, d2h_)) !=
+            cudaSuccess)
+            return cuda_status("D2H", e);
+        cudaEventRecord(ev_d2h_[slot], d2h_);
+        if (havePrev) {
+            if ((e = cudaEventSynchronize(ev_d2h_[prev.slot])) != cudaSuccess) return cuda_status("sync", e);
+            deliver(prev.out, prev.first, prev.count);
+        }
+        prev = {chunk, c, (int)(ce - c), slot};
+        havePrev = true;
+        if (stats != nullptr && drop_.enabled) {
+            for (int64_t k = c; k < ce; k++) {
+                const FramePlan &p = plan_for(k);
+                stats->corrected += p.corrected;
+                stats->failed += p.failed;
+                stats->totalDistance += p.totalDistance;
+            }
+        }
+    }
+    if (havePrev) {
+        if ((e = cudaEventSynchronize(ev_d2h_[prev.slot])) != cudaSuccess) return cuda_status("sync", e);
+        deliver(prev.out, prev.first, prev.count);
+    }
+    return CHD_OK;
+}
+
+}  // namespace chdg

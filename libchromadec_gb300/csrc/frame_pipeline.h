@@ -1,0 +1,96 @@
+// frame_pipeline.h -- decodes runs of frames of an opened capture on the GPU:
+// field windows gathered from the mmapped .tbc into pinned staging, uploaded,
+// dropout-concealed, Transform-PAL decoded and downloaded into pinned host
+// chunks that decoded frames borrow. Two slots alternate so the upload of one
+// batch and the download of another overlap the kernels of a third.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <functional>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "capture.h"
+#include "dropout_plan.h"
+#include "engine.h"
+
+namespace chdg {
+
+// Pinned host memory holding `count` decoded frames; frames borrow slices.
+struct HostChunk {
+    void *data = nullptr;
+    size_t bytes = 0;
+    ~HostChunk();
+};
+
+struct DropoutSettings {
+    bool enabled = false, overcorrect = false, intra = false;
+};
+
+// Delivery of decoded frames: frame `first + i` lives at chunk->data + i * frame_bytes.
+using Deliver = std::function<void(const std::shared_ptr<HostChunk> &chunk, int64_t first, int count)>;
+
+class FramePipeline {
+public:
+    FramePipeline() = default;
+    ~FramePipeline();
+    FramePipeline(const FramePipeline &) = delete;
+    FramePipeline &operator=(const FramePipeline &) = delete;
+
+    // Returns a chd_status_t value.
+    int init(const Capture *cap, const chdg_geometry &g, const chdg_config &c, bool firstFieldFirst,
+             int batch_frames, int copy_threads);
+    // Changing the overcorrect / intra-field settings drops the cached plans.
+    void set_dropout(const DropoutSettings &d);
+    // Concealment statistics of frame `frame`'s own two fields (0-based).
+    FramePlan frame_stats(int64_t frame);
+
+    // Decode frames [a, b) in batches; deliver() runs on the calling thread
+    // after each batch's frames are in host memory, possibly while the next
+    // batch is still on the GPU. `cancelled` is polled before each batch.
+    // Stats of the frames decoded (their own dropout statistics) accumulate
+    // into *stats when given.
+    int decode(int64_t a, int64_t b, const Deliver &deliver, const std::function<bool()> &cancelled,
+               FramePlan *stats);
+
+    size_t frame_bytes() const { return eng_.frame_bytes(); }
+    Engine &engine() { return eng_; }
+    int num_frames() const { return nframes_; }
+
+private:
+    int fill_staging(int slot, int64_t w0, int64_t w1);
+    const FramePlan &plan_for(int64_t frame);   // cached, window frame (0-based)
+    // A pinned chunk of at least `bytes`, reused once every frame borrowing
+    // from it has been freed.
+    std::shared_ptr<HostChunk> take_chunk(size_t bytes);
+
+    const Capture *cap_ = nullptr;
+    Engine eng_;
+    bool ffirst_ = true;
+    int nframes_ = 0;
+    int batch_ = 32;
+    int lb_ = 0, la_ = 0;
+    size_t flen_ = 0;
+    long long dstride_ = 0;
+    DropoutSettings drop_;
+    cudaStream_t comp_ = nullptr, copy_ = nullptr, d2h_ = nullptr;   // kernels, uploads, downloads
+    uint16_t *staging_[2] = {nullptr, nullptr};   // pinned
+    uint16_t *dwin_[2] = {nullptr, nullptr};
+    void *dout_[2] = {nullptr, nullptr};
+    cudaEvent_t ev_h2d_[2] = {}, ev_comp_[2] = {}, ev_d2h_[2] = {};
+    // dropout plans uploaded per slot
+    DropOp *h_ops_[2] = {nullptr, nullptr}, *d_ops_[2] = {nullptr, nullptr};
+    int *h_idx_[2] = {nullptr, nullptr}, *d_idx_[2] = {nullptr, nullptr};   // frames then op_begin
+    size_t ops_cap_ = 0, idx_cap_ = 0;
+    std::map<int64_t, FramePlan> plans_;
+    std::vector<std::shared_ptr<HostChunk>> chunks_;
+    int copy_threads_ = 1;
+};
+
+}  // namespace chdg
