@@ -14,6 +14,9 @@
 //   mode=decode|chroma|dropout kind=2|3 fmt=p16|ps threshold=0.4
 //   thresholds=<file> in=<fields.u16> nfields=N first=F count=C out=<file>
 //   dropouts=<file> overcorrect=0|1 intra=0|1
+//   gain=<chroma gain> phase=<degrees> clamp=0..3 padding=<multiple>
+//   avs=<first active sample> ave=<one past the last> fafl=<first active
+//   frame line> lafl=<last active frame line>
 // The field file holds N fields of 1135x313 uint16, first field first.
 // The dropout file holds lines "field_index startx endx fieldLine".
 
@@ -127,7 +130,11 @@ int main(int argc, char **argv)
     const bool overcorrect = a.count("overcorrect") && a["overcorrect"] == "1";
     const bool intra = a.count("intra") && a["intra"] == "1";
 
-    const auto vp = palParams();
+    auto vp = palParams();
+    if (a.count("avs")) vp.activeVideoStart = vp.pictureStart = vp.tileReadStart = std::atoi(a["avs"].c_str());
+    if (a.count("ave")) vp.activeVideoEnd = vp.pictureEnd = vp.tileReadEnd = std::atoi(a["ave"].c_str());
+    if (a.count("fafl")) vp.firstActiveFrameLine = std::atoi(a["fafl"].c_str());
+    if (a.count("lafl")) vp.lastActiveFrameLine = std::atoi(a["lafl"].c_str());
     Capture cap;
     cap.nfields = std::atoi(a["nfields"].c_str());
     cap.fieldLen = static_cast<size_t>(vp.fieldWidth) * vp.fieldHeight;
@@ -154,6 +161,8 @@ int main(int argc, char **argv)
     cfg.separation = (kind == 2) ? chd::decoders::palcolour::PalColour::transform2DFilter
                                  : chd::decoders::palcolour::PalColour::transform3DFilter;
     cfg.transformThreshold = threshold;
+    if (a.count("gain")) cfg.chromaGain = std::atof(a["gain"].c_str());
+    if (a.count("phase")) cfg.chromaPhase = std::atof(a["phase"].c_str());
     if (a.count("thresholds")) {
         std::ifstream in(a["thresholds"]);
         double v;
@@ -177,8 +186,10 @@ int main(int argc, char **argv)
 
     chd::output::OutputWriter writer;
     chd::output::OutputWriter::Configuration ocfg;
-    ocfg.paddingAmount = 1;
+    ocfg.paddingAmount = a.count("padding") ? std::atoi(a["padding"].c_str()) : 1;
     ocfg.pixelFormat = chd::output::OutputWriter::YUV444P16;
+    if (a.count("clamp"))
+        ocfg.clampMode = static_cast<chd::output::OutputWriter::ClampMode>(std::atoi(a["clamp"].c_str()));
     writer.updateConfiguration(vp, ocfg);
 
     long totalCorrected = 0, totalFailed = 0;

@@ -1,0 +1,56 @@
+"""The oracle's C restatement against golden vectors from the reference.
+
+tests/golden/golden.json holds, per case, the SHA-256 of what the
+reference's own Transform-PAL / PALcolour / OutputWriter / DropoutCorrector
+sources output (compiled unmodified, oracle/_ref; generator
+tests/golden/make_golden.py). The restatement must reproduce every byte and
+the reference's dropout statistics; the GPU path is then checked against the
+restatement.
+"""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.golden.cases import CASES, case_inputs, thresholds_for
+
+GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "golden.json")))["cases"]
+
+
+def _params(case):
+    p = O.params(case["kind"], O.FMT_PS if case.get("fmt") == "ps" else O.FMT_P16,
+                 threshold=case.get("threshold", 0.4), thresholds=thresholds_for(case))
+    for k in ("chroma_gain", "chroma_phase_deg", "clamp_mode", "padding_multiple", "active_start", "active_end",
+              "first_active_frame_line", "last_active_frame_line"):
+        if k in case:
+            setattr(p, k, case[k])
+    return p
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_restatement_matches_reference_golden(name):
+    case, gold = CASES[name], GOLDEN[name]
+    fields, drops = case_inputs(case)
+    assert hashlib.sha256(fields.tobytes()).hexdigest() == gold["input_sha256"], "synthetic input changed"
+    p = _params(case)
+    oc, intra = bool(case.get("overcorrect", 0)), bool(case.get("intra", 0))
+    if case["mode"] == "decode":
+        out, st = O.decode_frames(p, fields, case["first"], case["count"], dropouts=drops, overcorrect=oc,
+                                  intra=intra, threads=8)
+        data = out.tobytes()
+    elif case["mode"] == "chroma":
+        data = O.transform_chroma(p, fields, case["first"], case["count"]).tobytes()
+        st = (0, 0, 0)
+    else:
+        parts, tot = [], np.zeros(3, dtype=np.int64)
+        for k in range(case["first"], case["first"] + case["count"]):
+            f2, s = O.dropout_correct_frame(p, fields, k, drops, oc, intra)
+            parts.append(f2.tobytes())
+            tot += s
+        data, st = b"".join(parts), tuple(int(x) for x in tot)
+    assert len(data) == gold["output_bytes"]
+    assert hashlib.sha256(data).hexdigest() == gold["output_sha256"]
+    assert list(st) == gold["stats"]
