@@ -20,6 +20,10 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libchromadec_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# The reference's SONAME and symbol version node for release 0.2.x
+# (src/meson.build:238-240, meson.build:53-60: pre-1.0 they track the minor).
+SONAME = "libchromadec.so.0.2"
+VERSION_NODE = "CHROMADEC_0.2"
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden",
               "-I" + INCLUDE, "-I" + CSRC]
 
@@ -72,14 +76,24 @@ def build(force: bool = False, verbose: bool = False) -> str:
         objs = list(ex.map(compile_one, srcs))
     vscript = os.path.join(BUILD, "exports.map")
     with open(vscript, "w") as fp:
-        fp.write("CHROMADEC_GB300 { global: chd_*; chdg_*; local: *; };\n")
+        # chd_* under the reference's version node (meson/chromadec.map.in,
+        # CHROMADEC_<major>.<minor> before 1.0), so binaries linked against
+        # the reference bind to these symbols unchanged; chdg_* under our own.
+        fp.write(f"{VERSION_NODE} {{ global: chd_*; }};\n"
+                 "CHROMADEC_GB300 { global: chdg_*; local: *; };\n")
     tmp = LIB + ".tmp"
     cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + \
-          ["-Xlinker", "--version-script=" + vscript, "-lcudart", "-lpthread"]
+          ["-Xlinker", "--version-script=" + vscript, "-Xlinker", "-soname=" + SONAME, "-lcudart", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    # the reference's file names, for consumers that load libchromadec by name
+    for alias in (SONAME, "libchromadec.so"):
+        ap = os.path.join(HERE, alias)
+        if os.path.lexists(ap):
+            os.remove(ap)
+        os.symlink(os.path.basename(LIB), ap)
     return LIB
 
 

@@ -267,10 +267,16 @@ int demod_launch(const DemodParams &P, cudaStream_t stream)
     const int base4 = P.avs & ~3;
     const int span = ((P.ave - base4) + 7) & ~7;
     const size_t smem = demod_smem_bytes(P.avs, P.ave);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(demod_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr_set = true;
+    // function attributes are per device
+    static bool attr_set[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return -1;
+    if (!attr_set[dev]) {
+        if (cudaFuncSetAttribute(demod_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) !=
+            cudaSuccess)
+            return -1;
+        attr_set[dev] = true;
     }
     const int nblk_per_field = (P.fh + kDemodLines - 1) / kDemodLines;
     demod_kernel<<<(unsigned)(P.nout * nblk_per_field), kDemodThreads, smem, stream>>>(P);

@@ -666,14 +666,18 @@ int tp3_launch(const T3Params &P, cudaStream_t stream)
     if (items <= 0) return 0;
     const unsigned blocks = (unsigned)((items + kWarps3 - 1) / kWarps3);
     const size_t smem = sizeof(float2) * (size_t)kWarpSmemF2 * kWarps3;
-    static bool attr_set = false;
-    if (!attr_set) {
+    // function attributes are per device
+    static bool attr_set[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return -1;
+    if (!attr_set[dev]) {
         if (cudaFuncSetAttribute(tpal3d_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
                 cudaSuccess ||
             cudaFuncSetAttribute(tpal3d_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
                 cudaSuccess)
             return -1;
-        attr_set = true;
+        attr_set[dev] = true;
     }
     if (P.thr_table != nullptr) tpal3d_kernel<true><<<blocks, 32 * kWarps3, smem, stream>>>(P);
     else tpal3d_kernel<false><<<blocks, 32 * kWarps3, smem, stream>>>(P);
