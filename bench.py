@@ -252,8 +252,8 @@ def e2e_abi(a, fields_np, rank, barrier, dist):
     if got[0] != nframes * (a.steps + max(1, a.warmup)):
         raise RuntimeError(f"chd_decode_frames_async delivered {got[0]} frames")
     value, dt = replica_throughput(nfields, a.steps, dt, dist)
-    # uploaded per step: 32-frame batches, each with its 2 + 4 frame window halo
-    B, h2d = 32, 0
+    # uploaded per step: 64-frame batches, each with its 2 + 4 frame window halo
+    B, h2d = 64, 0
     for b in range(0, nframes, B):
         be = min(nframes, b + B)
         h2d += (min(nframes, be + 4) - max(0, b - 2)) * 2 * FIELD_BYTES_IN

@@ -115,7 +115,7 @@ namespace chdg {
 
 // Builds a pipeline for the committed decoder on its device; returns a
 // chd_status_t and sets the last error on failure.
-int make_pipeline(chd_decoder_t *d, std::unique_ptr<FramePipeline> &out);
+int make_pipeline(chd_decoder_t *d, std::unique_ptr<FramePipeline> &out, int batch_frames);
 // A frame handle for `count` frames' chunk slice `index`.
 chd_frame_t *make_frame(chd_decoder_t *d, const std::shared_ptr<HostChunk> &chunk, size_t offset, int64_t index);
 

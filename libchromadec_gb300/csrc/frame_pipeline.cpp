@@ -13,6 +13,8 @@ namespace chdg {
 
 int dropout_apply(uint16_t *fields, long long field_stride, int fw, const int *d_frames, const DropOp *d_ops,
                   const int *d_op_begin, int nframes, cudaStream_t s);
+int fill_fields(uint16_t *fields, long long field_stride, long long field_len, int nfields, uint16_t value,
+                cudaStream_t s);
 
 namespace {
 
@@ -36,7 +38,6 @@ FramePipeline::~FramePipeline()
     if (d2h_) cudaStreamSynchronize(d2h_);
     chunks_.clear();
     for (int i = 0; i < 2; i++) {
-        if (staging_[i]) cudaFreeHost(staging_[i]);
         if (dwin_[i]) cudaFree(dwin_[i]);
         if (dout_[i]) cudaFree(dout_[i]);
         if (h_ops_[i]) cudaFreeHost(h_ops_[i]);
@@ -53,10 +54,9 @@ FramePipeline::~FramePipeline()
 }
 
 int FramePipeline::init(const Capture *cap, const chdg_geometry &g, const chdg_config &c, bool firstFieldFirst,
-                        int batch_frames, int copy_threads)
+                        int batch_frames)
 {
     cap_ = cap;
-    copy_threads_ = std::max(1, std::min(16, copy_threads));
     ffirst_ = firstFieldFirst;
     nframes_ = cap->numFrames(firstFieldFirst);
     batch_ = std::max(1, batch_frames);
@@ -72,7 +72,6 @@ int FramePipeline::init(const Capture *cap, const chdg_geometry &g, const chdg_c
     if ((e = cudaStreamCreateWithFlags(&copy_, cudaStreamNonBlocking)) != cudaSuccess) return cuda_status("stream", e);
     if ((e = cudaStreamCreateWithFlags(&d2h_, cudaStreamNonBlocking)) != cudaSuccess) return cuda_status("stream", e);
     for (int i = 0; i < 2; i++) {
-        if ((e = cudaMallocHost(&staging_[i], winFields * dstride_ * 2)) != cudaSuccess) return cuda_status("pinned", e);
         if ((e = cudaMalloc(&dwin_[i], winFields * dstride_ * 2)) != cudaSuccess) return cuda_status("window", e);
         cudaMemset(dwin_[i], 0, winFields * dstride_ * 2);
         if ((e = cudaMalloc(&dout_[i], eng_.frame_bytes() * (size_t)batch_)) != cudaSuccess)
@@ -133,35 +132,39 @@ const FramePlan &FramePipeline::plan_for(int64_t frame)
         FieldMeta m0 = cap_->field(wf[0].fieldNumber), m1 = cap_->field(wf[1].fieldNumber);
         plan = plan_frame(cap_->vp(), m0, m1, drop_.overcorrect, drop_.intra);
     }
-    if (plans_.size() > 4096) plans_.clear();
     return plans_.emplace(frame, std::move(plan)).first->second;
 }
 
-int FramePipeline::fill_staging(int slot, int64_t w0, int64_t w1)
+int FramePipeline::upload_window(int slot, int64_t w0, int64_t w1)
 {
     const int nf = (int)(2 * (w1 - w0));
-    if (nf <= 0) return 0;
-    uint16_t *base = staging_[slot];
     const uint16_t black = (uint16_t)cap_->vp().black16bIre;
-    auto work = [&](int lo, int hi) {
-        for (int k = lo; k < hi; k++) {
-            WindowField wf[2];
-            cap_->windowFrame((int)(w0 + k / 2) + 1, ffirst_, wf);
-            uint16_t *dst = base + (size_t)k * dstride_;
-            const uint16_t *src = wf[k & 1].source ? cap_->fieldData(wf[k & 1].source) : nullptr;
-            if (src != nullptr) std::memcpy(dst, src, flen_ * 2);
-            else std::fill(dst, dst + flen_, black);
-        }
-    };
-    const int nt = std::min(nf, copy_threads_);
-    if (nt <= 1) {
-        work(0, nf);
-        return 0;
+    const size_t fbytes = flen_ * 2;
+    // window field k comes from capture field src[k] (1-based, 0 = black)
+    std::vector<int> src((size_t)std::max(nf, 0));
+    for (int k = 0; k < nf; k += 2) {
+        WindowField wf[2];
+        cap_->windowFrame((int)(w0 + k / 2) + 1, ffirst_, wf);
+        src[k] = wf[0].source;
+        src[k + 1] = wf[1].source;
     }
-    std::vector<std::thread> th;
-    for (int t = 0; t < nt; t++) th.emplace_back(work, nf * t / nt, nf * (t + 1) / nt);
-    for (auto &x : th) x.join();
-    return 0;
+    cudaError_t e;
+    for (int k = 0; k < nf;) {
+        int n = 1;
+        if (src[k] == 0) {
+            while (k + n < nf && src[k + n] == 0) n++;
+            if (fill_fields(dwin_[slot] + (size_t)k * dstride_, dstride_, (long long)flen_, n, black, copy_) != 0)
+                return cuda_status("black fields", cudaGetLastError());
+        } else {
+            while (k + n < nf && src[k + n] == src[k] + n) n++;
+            if ((e = cudaMemcpy2DAsync(dwin_[slot] + (size_t)k * dstride_, (size_t)dstride_ * 2,
+                                       cap_->fieldData(src[k]), fbytes, fbytes, (size_t)n, cudaMemcpyHostToDevice,
+                                       copy_)) != cudaSuccess)
+                return cuda_status("H2D", e);
+        }
+        k += n;
+    }
+    return CHD_OK;
 }
 
 int FramePipeline::decode(int64_t a, int64_t b, const Deliver &deliver, const std::function<bool()> &cancelled,
@@ -184,11 +187,15 @@ int FramePipeline::decode(int64_t a, int64_t b, const Deliver &deliver, const st
         const int slot = i & 1;
         const int64_t w0 = std::max<int64_t>(0, c - lb_);
         const int64_t w1 = std::min<int64_t>(nframes_, ce + la_);
+        // bound the plan cache; plans behind the window are not needed again
+        // by this run (references into the map stay valid: only others go)
+        if (plans_.size() > 4096) plans_.erase(plans_.begin(), plans_.lower_bound(w0));
         if (i >= 2) {
-            // staging, window and plan buffers of this slot were last used by batch i-2
-            if ((e = cudaEventSynchronize(ev_comp_[slot])) != cudaSuccess) return cuda_status("sync", e);
+            // the window of this slot was last read by batch i-2's kernels, and
+            // its plan buffers were last uploaded for batch i-2
+            cudaStreamWaitEvent(copy_, ev_comp_[slot], 0);
+            if ((e = cudaEventSynchronize(ev_h2d_[slot])) != cudaSuccess) return cuda_status("sync", e);
         }
-        fill_staging(slot, w0, w1);
         // dropout plans of the window's frames
         int nplan = 0;
         size_t nops = 0;
@@ -234,10 +241,7 @@ int FramePipeline::decode(int64_t a, int64_t b, const Deliver &deliver, const st
             }
             h_idx_[slot][2 * nplan] = (int)o;
         }
-        const size_t wbytes = (size_t)(2 * (w1 - w0)) * dstride_ * 2;
-        if (wbytes > 0 &&
-            (e = cudaMemcpyAsync(dwin_[slot], staging_[slot], wbytes, cudaMemcpyHostToDevice, copy_)) != cudaSuccess)
-            return cuda_status("H2D", e);
+        if (const int rc = upload_window(slot, w0, w1); rc != CHD_OK) return rc;
         if (nplan > 0) {
             cudaMemcpyAsync(d_ops_[slot], h_ops_[slot], nops * sizeof(DropOp), cudaMemcpyHostToDevice, copy_);
             cudaMemcpyAsync(d_idx_[slot], h_idx_[slot], (2 * nplan + 1) * sizeof(int), cudaMemcpyHostToDevice, copy_);

@@ -1,5 +1,8 @@
 // frame_pipeline.h -- decodes runs of frames of an opened capture on the GPU:
-// field windows gathered from the mmapped .tbc into pinned staging, uploaded,
+// field windows copied straight from the mmapped .tbc into device memory
+// (runs of consecutive fields as one 2D copy; on Grace the GPU reads the
+// page-cached mapping over NVLink-C2C at the rate of pinned memory, so no
+// host staging copy is made), black padding fields filled on the device,
 // dropout-concealed, Transform-PAL decoded and downloaded into pinned host
 // chunks that decoded frames borrow. Two slots alternate so the upload of one
 // batch and the download of another overlap the kernels of a third.
@@ -45,7 +48,7 @@ public:
 
     // Returns a chd_status_t value.
     int init(const Capture *cap, const chdg_geometry &g, const chdg_config &c, bool firstFieldFirst,
-             int batch_frames, int copy_threads);
+             int batch_frames);
     // Changing the overcorrect / intra-field settings drops the cached plans.
     void set_dropout(const DropoutSettings &d);
     // Concealment statistics of frame `frame`'s own two fields (0-based).
@@ -64,7 +67,8 @@ public:
     int num_frames() const { return nframes_; }
 
 private:
-    int fill_staging(int slot, int64_t w0, int64_t w1);
+    // Enqueue the window fields of frames [w0, w1) into dwin_[slot] on copy_.
+    int upload_window(int slot, int64_t w0, int64_t w1);
     const FramePlan &plan_for(int64_t frame);   // cached, window frame (0-based)
     // A pinned chunk of at least `bytes`, reused once every frame borrowing
     // from it has been freed.
@@ -80,7 +84,6 @@ private:
     long long dstride_ = 0;
     DropoutSettings drop_;
     cudaStream_t comp_ = nullptr, copy_ = nullptr, d2h_ = nullptr;   // kernels, uploads, downloads
-    uint16_t *staging_[2] = {nullptr, nullptr};   // pinned
     uint16_t *dwin_[2] = {nullptr, nullptr};
     void *dout_[2] = {nullptr, nullptr};
     cudaEvent_t ev_h2d_[2] = {}, ev_comp_[2] = {}, ev_d2h_[2] = {};
@@ -90,7 +93,6 @@ private:
     size_t ops_cap_ = 0, idx_cap_ = 0;
     std::map<int64_t, FramePlan> plans_;
     std::vector<std::shared_ptr<HostChunk>> chunks_;
-    int copy_threads_ = 1;
 };
 
 }  // namespace chdg

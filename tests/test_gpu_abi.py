@@ -173,3 +173,22 @@ def test_thresholds_file_through_abi(cuda, tbc, tmp_path):
     for k in range(NF // 2):
         fr = d.decode(k)
         _compare(fr.planes(), ref[k], "yuv444p16")
+
+
+def test_truncated_capture_decodes_missing_frames_as_black(cuda, tmp_path):
+    """A .tbc shorter than its sidecar: frames whose fields are missing enter
+    the window as black fields (SourceField::loadFields' blank fallback,
+    src/decoders/source_field.cpp:110-158), uploaded by the device fill."""
+    cap = capture(NF, 23)
+    path = str(tmp_path / "short.tbc")
+    synth.write_tbc(path, cap)
+    with open(path, "r+b") as fp:
+        fp.truncate(13 * cap.fields[0].nbytes)       # fields 14..16 (1-based) missing
+    black = cap.fields.copy()
+    black[12:] = synth.BLACK                          # frames 6 and 7 become blank
+    ref, _ = O.decode_frames(O.params(3, O.FMT_P16), black, 0, NF // 2, threads=8)
+    v, d = _decoder(path)
+    res = d.decode_async(list(range(NF // 2)))
+    assert [s for s, _, _ in res] == [abi.OK] * (NF // 2)
+    for _, i, planes in res:
+        _compare(planes, ref[i], "yuv444p16")
