@@ -20,6 +20,10 @@ REF_HARNESS = os.path.join(HERE, "_ref", "chd_ref_harness")
 
 FMT_P16 = 0
 FMT_PS = 1
+FMT_RGB48 = 2
+FMT_RGBS = 3
+FMT_GRAY16 = 4
+FMT_GRAYS = 5
 
 
 class Params(C.Structure):
@@ -37,6 +41,8 @@ class Params(C.Structure):
         ("chroma_gain", C.c_double), ("chroma_phase_deg", C.c_double),
         ("output_format", C.c_int32), ("clamp_mode", C.c_int32), ("padding_multiple", C.c_int32),
         ("ecb_from_u", C.c_double), ("ecr_from_v", C.c_double),
+        ("kr", C.c_double), ("kb", C.c_double), ("u_reduction", C.c_double), ("v_reduction", C.c_double),
+        ("y_nr_level", C.c_double), ("first_field_offset", C.c_int32), ("sc_locked", C.c_int32),
     ]
 
 
@@ -112,6 +118,29 @@ def params(kind: int = 3, fmt: int = FMT_P16, threshold: float = 0.4,
     return p
 
 
+def frame_dtype(p: Params):
+    return np.float32 if p.output_format in (FMT_PS, FMT_RGBS, FMT_GRAYS) else np.uint16
+
+
+def frame_shape(p: Params, count: int, w: int, h: int):
+    """Array shape of `count` output frames: planar formats (count, planes,
+    h, w); RGB48 is interleaved (count, h, w, 3) as OutputWriter packs it."""
+    if p.output_format == FMT_RGB48:
+        return (count, h, w, 3)
+    planes = 1 if p.output_format in (FMT_GRAY16, FMT_GRAYS) else 3
+    return (count, planes, h, w)
+
+
+def colour_precision(p: Params, difference: str = "modern", scaling: str = "scientific") -> None:
+    """ColorConversion for the two precision options (color_conversion.cpp:33-66)."""
+    p.kr, p.kb = (0.30, 0.11) if difference == "classic" else (0.299, 0.114)
+    p.u_reduction, p.v_reduction = {"classic": (0.493, 0.877), "modern": (0.492111, 0.877283),
+                                    "scientific": (0.49211104112248356308804691718185,
+                                                   0.87728321993817866838972487283129)}[scaling]
+    p.ecb_from_u = 1.0 / ((2.0 * (1.0 - p.kb)) * p.u_reduction)
+    p.ecr_from_v = 1.0 / ((2.0 * (1.0 - p.kr)) * p.v_reduction)
+
+
 def output_geometry(p: Params) -> Tuple[int, int, int, int]:
     w, h, lp, tp = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
     lib().tpo_output_geometry(C.byref(p), C.byref(w), C.byref(h), C.byref(lp), C.byref(tp))
@@ -143,8 +172,7 @@ def decode_frames(p: Params, fields: np.ndarray, first: int, count: int, dropout
     fields = np.ascontiguousarray(fields, dtype=np.uint16)
     nfields = fields.shape[0]
     w, h, _, _ = output_geometry(p)
-    dtype = np.float32 if p.output_format == FMT_PS else np.uint16
-    out = np.empty((count, 3, h, w), dtype=dtype)
+    out = np.empty(frame_shape(p, count, w, h), dtype=frame_dtype(p))
     arr, nd = _dropout_array(dropouts)
     st = Stats()
     rc = lib().tpo_decode_frames(C.byref(p), fields.ctypes.data, nfields, arr, nd, int(overcorrect), int(intra),

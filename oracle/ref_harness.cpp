@@ -17,6 +17,10 @@
 //   gain=<chroma gain> phase=<degrees> clamp=0..3 padding=<multiple>
 //   avs=<first active sample> ave=<one past the last> fafl=<first active
 //   frame line> lafl=<last active frame line>
+//   kind=1 (PALcolour 2D filter alone) fmt=rgb48|rgbs|gray16|grays
+//   ynr=<luma_nr_level> sff=1 (window slot 0 holds second fields: the
+//   reversed pairing) sclocked=1 (subcarrier-locked: slot-1 fields shifted)
+//   cdp=classic|modern bsp=classic|modern|scientific
 // The field file holds N fields of 1135x313 uint16, first field first.
 // The dropout file holds lines "field_index startx endx fieldLine".
 
@@ -29,6 +33,7 @@
 #include <string>
 #include <vector>
 
+#include "common/color_conversion.h"
 #include "decoders/palcolour/palcolour.h"
 #include "decoders/palcolour/transform_pal_2d.h"
 #include "decoders/palcolour/transform_pal_3d.h"
@@ -90,7 +95,8 @@ struct Capture {
 // Field window for frames [firstFrame - lookBehind, firstFrame + 1 + lookAhead),
 // black padding outside the capture (source_field.cpp:88-170).
 void loadWindow(const Capture &cap, const LdDecodeMetaData::VideoParameters &vp, int frame, int lookBehind,
-                int lookAhead, std::vector<chd::decoders::SourceField> &fields, int &startIndex, int &endIndex)
+                int lookAhead, bool slot0IsSecond, std::vector<chd::decoders::SourceField> &fields,
+                int &startIndex, int &endIndex)
 {
     startIndex = 2 * lookBehind;
     endIndex = startIndex + 2;
@@ -101,7 +107,7 @@ void loadWindow(const Capture &cap, const LdDecodeMetaData::VideoParameters &vp,
         const bool pad = f < 0 || f >= numFrames;
         for (int j = 0; j < 2; j++) {
             auto &sf = fields[i + j];
-            sf.field.isFirstField = (j == 0);
+            sf.field.isFirstField = slot0IsSecond ? (j == 1) : (j == 0);
             sf.isPadding = pad;
             const int srcField = pad ? j : 2 * f + j;
             sf.fieldNumber = srcField + 1;
@@ -111,6 +117,9 @@ void loadWindow(const Capture &cap, const LdDecodeMetaData::VideoParameters &vp,
             } else {
                 sf.data.assign(cap.samples.begin() + cap.fieldLen * srcField,
                                cap.samples.begin() + cap.fieldLen * (srcField + 1));
+                if (j == 1 && chd::decoders::SourceField::secondFieldIsShifted(vp))
+                    chd::decoders::SourceField::shiftSecondField(sf.data, sf.field.dropOuts,
+                                                                 static_cast<uint16_t>(vp.black16bIre));
             }
         }
     }
@@ -135,6 +144,8 @@ int main(int argc, char **argv)
     if (a.count("ave")) vp.activeVideoEnd = vp.pictureEnd = vp.tileReadEnd = std::atoi(a["ave"].c_str());
     if (a.count("fafl")) vp.firstActiveFrameLine = std::atoi(a["fafl"].c_str());
     if (a.count("lafl")) vp.lastActiveFrameLine = std::atoi(a["lafl"].c_str());
+    if (a.count("sclocked") && a["sclocked"] == "1") vp.isSubcarrierLocked = true;
+    const bool slot0IsSecond = a.count("sff") && a["sff"] == "1";
     Capture cap;
     cap.nfields = std::atoi(a["nfields"].c_str());
     cap.fieldLen = static_cast<size_t>(vp.fieldWidth) * vp.fieldHeight;
@@ -158,8 +169,15 @@ int main(int argc, char **argv)
     }
 
     chd::decoders::palcolour::PalColour::Configuration cfg;
-    cfg.separation = (kind == 2) ? chd::decoders::palcolour::PalColour::transform2DFilter
-                                 : chd::decoders::palcolour::PalColour::transform3DFilter;
+    cfg.separation = (kind == 1)   ? chd::decoders::palcolour::PalColour::palColourFilter
+                     : (kind == 2) ? chd::decoders::palcolour::PalColour::transform2DFilter
+                                   : chd::decoders::palcolour::PalColour::transform3DFilter;
+    if (a.count("ynr")) cfg.yNRLevel = std::atof(a["ynr"].c_str());
+    chd::color::ColorDifferencePrecision cdp = chd::color::ColorDifferencePrecision::Modern;
+    chd::color::BroadcastScalingPrecision bsp = chd::color::BroadcastScalingPrecision::Scientific;
+    if (a.count("cdp")) cdp = *chd::color::parseColorDifferencePrecision(a["cdp"]);
+    if (a.count("bsp")) bsp = *chd::color::parseBroadcastScalingPrecision(a["bsp"]);
+    cfg.colorConversion = chd::color::resolveColorConversion(cdp, bsp);
     cfg.transformThreshold = threshold;
     if (a.count("gain")) cfg.chromaGain = std::atof(a["gain"].c_str());
     if (a.count("phase")) cfg.chromaPhase = std::atof(a["phase"].c_str());
@@ -187,7 +205,11 @@ int main(int argc, char **argv)
     chd::output::OutputWriter writer;
     chd::output::OutputWriter::Configuration ocfg;
     ocfg.paddingAmount = a.count("padding") ? std::atoi(a["padding"].c_str()) : 1;
-    ocfg.pixelFormat = chd::output::OutputWriter::YUV444P16;
+    ocfg.pixelFormat = (fmt == "rgb48") ? chd::output::OutputWriter::RGB48
+                       : (fmt == "gray16") ? chd::output::OutputWriter::GRAY16
+                                           : chd::output::OutputWriter::YUV444P16;
+    ocfg.colorDifferencePrecision = cdp;
+    ocfg.broadcastScalingPrecision = bsp;
     if (a.count("clamp"))
         ocfg.clampMode = static_cast<chd::output::OutputWriter::ClampMode>(std::atoi(a["clamp"].c_str()));
     writer.updateConfiguration(vp, ocfg);
@@ -199,7 +221,7 @@ int main(int argc, char **argv)
         int startIndex = 0, endIndex = 0;
         const int lb = (mode == "dropout") ? 0 : lookBehind;
         const int la = (mode == "dropout") ? 0 : lookAhead;
-        loadWindow(cap, vp, frame, lb, la, fields, startIndex, endIndex);
+        loadWindow(cap, vp, frame, lb, la, slot0IsSecond, fields, startIndex, endIndex);
 
         if (correcting) {
             for (size_t i = 0; i + 1 < fields.size(); i += 2) {
@@ -207,6 +229,7 @@ int main(int argc, char **argv)
                 if (fields[i].field.dropOuts.empty() && fields[i + 1].field.dropOuts.empty()) continue;
                 chd::dropout::DropoutCorrector corrector(vp);
                 chd::dropout::DropoutCorrectionStats stats;
+                // correctFrame orders the pair by isFirstField itself
                 corrector.correctFrame(fields[i], fields[i + 1], overcorrect, intra, &stats);
                 if (static_cast<int>(i) == startIndex) {
                     totalCorrected += stats.corrected;
@@ -230,9 +253,13 @@ int main(int argc, char **argv)
 
         std::vector<chd::output::ComponentFrame> frames(1);
         pal.decodeFrames(fields, startIndex, endIndex, frames);
-        if (fmt == "ps") {
+        if (fmt == "ps" || fmt == "grays") {
             std::vector<float> planes[3];
-            writer.convertToFloat(frames[0], planes, true);
+            writer.convertToFloat(frames[0], planes, fmt == "ps");
+            for (int p = 0; p < 3; p++) std::fwrite(planes[p].data(), sizeof(float), planes[p].size(), out);
+        } else if (fmt == "rgbs") {
+            std::vector<float> planes[3];
+            writer.convertToFloatRGB(frames[0], planes);
             for (int p = 0; p < 3; p++) std::fwrite(planes[p].data(), sizeof(float), planes[p].size(), out);
         } else {
             chd::output::OutputFrame of;

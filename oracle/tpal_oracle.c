@@ -52,13 +52,15 @@ void tpo_default_params(tpo_params *p, int32_t kind)
     p->clamp_mode = TPO_CLAMP_NONE;
     p->padding_multiple = 1;
     /* color_conversion.cpp:33-66 at Modern / Scientific */
-    {
-        const double kb = 0.114, kr = 0.299;
-        const double uRed = 0.49211104112248356308804691718185;
-        const double vRed = 0.87728321993817866838972487283129;
-        p->ecb_from_u = 1.0 / ((2.0 * (1.0 - kb)) * uRed);
-        p->ecr_from_v = 1.0 / ((2.0 * (1.0 - kr)) * vRed);
-    }
+    p->kb = 0.114;
+    p->kr = 0.299;
+    p->u_reduction = 0.49211104112248356308804691718185;
+    p->v_reduction = 0.87728321993817866838972487283129;
+    p->ecb_from_u = 1.0 / ((2.0 * (1.0 - p->kb)) * p->u_reduction);
+    p->ecr_from_v = 1.0 / ((2.0 * (1.0 - p->kr)) * p->v_reduction);
+    p->y_nr_level = 0.0;
+    p->first_field_offset = 0;
+    p->sc_locked = 0;
 }
 
 /* Field-line range of a field, src/decoders/source_field.h:86-91 */
@@ -100,7 +102,10 @@ size_t tpo_frame_bytes(const tpo_params *p)
 {
     int32_t w, h;
     tpo_output_geometry(p, &w, &h, NULL, NULL);
-    return (size_t)w * (size_t)h * 3 * (p->output_format == TPO_FMT_PS ? sizeof(float) : sizeof(uint16_t));
+    const size_t planes = (p->output_format == TPO_FMT_GRAY16 || p->output_format == TPO_FMT_GRAYS) ? 1 : 3;
+    const size_t bytes = (p->output_format == TPO_FMT_PS || p->output_format == TPO_FMT_RGBS ||
+                          p->output_format == TPO_FMT_GRAYS) ? sizeof(float) : sizeof(uint16_t);
+    return (size_t)w * (size_t)h * planes * bytes;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -129,6 +134,7 @@ static int tp_init(tp_ctx *t, const tpo_params *p)
 {
     memset(t, 0, sizeof(*t));
     t->kind = p->kind;
+    if (p->kind == 1) return 0;   /* PALcolour 2D filter alone: no transform */
     if (p->kind == 2) {
         t->window = (double *)malloc(sizeof(double) * 16 * 32);
         for (int32_t y = 0; y < 16; y++) {
@@ -442,22 +448,82 @@ typedef struct component_frame {
     double *y, *u, *v;
 } component_frame;
 
-/* PalColour::decodeLine<double, true>, palcolour.cpp:456-646 (the
- * pre-filtered-chroma path; simplePAL is not reachable from the ABI). */
+/* The 25-tap high-pass of doYNR, c_nrpal_b (src/decoders/filter/deemp.h:620-628). */
+static const double kNrPal[25] = {
+    1.141291975113614e-04, -1.857019211291029e-03, -4.499636864042073e-03, -5.577680979937061e-03,
+    -4.423694440267179e-04, 1.309163063177155e-02, 2.861211356202848e-02, 3.029931283148555e-02,
+    1.098965697652802e-03, -6.398130386469833e-02, -1.492080690537196e-01, -2.223459379380252e-01,
+    7.479077367478024e-01, -2.223459379380252e-01, -1.492080690537196e-01, -6.398130386469833e-02,
+    1.098965697652803e-03, 3.029931283148557e-02, 2.861211356202848e-02, 1.309163063177156e-02,
+    -4.423694440267185e-04, -5.577680979937061e-03, -4.499636864042074e-03, -1.857019211291030e-03,
+    1.141291975113614e-04};
+
+/* PalColour::doYNR, palcolour.cpp:412-449, with IIRFilter<25,1>::feed
+ * (src/decoders/filter/iirfilter.h:69-83): output = b0*x[t] then b[i]*x[t-i]
+ * for i = 24 down to 1; zeros fed before and after the active samples. */
+static void do_ynr(const tpo_params *p, double *Yline, double *hist, double *hpY)
+{
+    const double irescale = (double)((p->white - p->black) / 100);   /* integer division, as the reference */
+    const double nr_y = p->y_nr_level * irescale;
+    const int32_t delay = 25 / 2;
+    for (int32_t i = 0; i < 25; i++) hist[i] = 0.0;
+    /* feed(v): y0 = b0*v + sum_{i=24..1} b[i]*x[i] (x shifted first) */
+#define YNR_FEED(v, outv)                                              \
+    do {                                                               \
+        double y0 = kNrPal[0] * (v);                                   \
+        for (int32_t i = 24; i >= 1; i--) {                            \
+            hist[i] = hist[i - 1];                                     \
+            y0 += kNrPal[i] * hist[i];                                 \
+        }                                                              \
+        hist[0] = (v);                                                 \
+        outv = y0;                                                     \
+    } while (0)
+    double sink;
+    for (int32_t h = p->active_start - delay; h < p->active_start; h++) YNR_FEED(0.0, sink);
+    (void)sink;
+    for (int32_t h = p->active_start; h < p->active_end; h++) YNR_FEED(Yline[h], hpY[h]);
+    for (int32_t h = p->active_end; h < p->active_end + delay; h++) YNR_FEED(0.0, hpY[h]);
+#undef YNR_FEED
+    for (int32_t h = p->active_start; h < p->active_end; h++) {
+        double a = hpY[h + delay];
+        if (fabs(a) > nr_y) a = (a > 0) ? nr_y : -nr_y;
+        Yline[h] -= a;
+    }
+}
+
+/* PalColour::decodeLine, palcolour.cpp:456-646: decodeLine<double, true> on
+ * Transform-PAL chroma (kinds 2, 3) and decodeLine<uint16_t, false> on the
+ * composite (kind 1, the PALcolour 2D filter with luma resynthesised from
+ * the Y filter). simplePAL is not reachable from the ABI. */
 static void decode_line(const pal_ctx *c, const tpo_params *p, const src_field *f, const double *chromaData,
                         const line_info *line, component_frame *cf, double (*m)[MAX_WIDTH],
-                        double (*n)[MAX_WIDTH], double *pu, double *qu, double *pv, double *qv)
+                        double (*n)[MAX_WIDTH], double *pu, double *qu, double *pv, double *qv, double *py,
+                        double *qy, double *scratch)
 {
     const int32_t fw = p->field_width;
     const int32_t firstLine = first_active_line(p, f->offset);
     const int32_t lastLine = last_active_line(p, f->offset);
-    const double *in0 = chromaData + (line->number * fw);
-    const double *in1 = (line->number - 1) < firstLine ? kBlackLineD : (chromaData + ((line->number - 1) * fw));
-    const double *in2 = (line->number + 1) >= lastLine ? kBlackLineD : (chromaData + ((line->number + 1) * fw));
-    const double *in3 = (line->number - 2) < firstLine ? kBlackLineD : (chromaData + ((line->number - 2) * fw));
-    const double *in4 = (line->number + 2) >= lastLine ? kBlackLineD : (chromaData + ((line->number + 2) * fw));
-    const double *in5 = (line->number - 3) < firstLine ? kBlackLineD : (chromaData + ((line->number - 3) * fw));
-    const double *in6 = (line->number + 3) >= lastLine ? kBlackLineD : (chromaData + ((line->number + 3) * fw));
+    const int prefiltered = (p->kind != 1);
+    /* input rows as doubles: chroma for the transform kinds, composite for kind 1 (blackLine = 0) */
+    const double *rows[7];
+    const int32_t dl[7] = {0, -1, 1, -2, 2, -3, 3};
+    double *tmp = scratch;   /* 7 rows of MAX_WIDTH for the composite case */
+    for (int r = 0; r < 7; r++) {
+        const int32_t ln = line->number + dl[r];
+        const int outside = (r == 0) ? 0 : ((dl[r] < 0) ? (ln < firstLine) : (ln >= lastLine));
+        if (outside) {
+            rows[r] = kBlackLineD;
+        } else if (prefiltered) {
+            rows[r] = chromaData + (ln * fw);
+        } else {
+            const uint16_t *src = f->data + (ln * fw);
+            double *d = tmp + (size_t)r * MAX_WIDTH;
+            for (int32_t i = 0; i < fw; i++) d[i] = src[i];
+            rows[r] = d;
+        }
+    }
+    const double *in0 = rows[0], *in1 = rows[1], *in2 = rows[2], *in3 = rows[3], *in4 = rows[4], *in5 = rows[5],
+                 *in6 = rows[6];
     const int32_t endPos = imin(p->active_end, MAX_WIDTH);
     const int32_t filterSize = c->filterSize;
     const int32_t fillStart = imax(0, p->active_start - filterSize);
@@ -474,11 +540,13 @@ static void decode_line(const pal_ctx *c, const tpo_params *p, const src_field *
         n[3][i] = -in5[i] * cosine[i] + in6[i] * cosine[i];
     }
     for (int32_t i = p->active_start; i < endPos; i++) {
-        double PU = 0, QU = 0, PV = 0, QV = 0;
+        double PU = 0, QU = 0, PV = 0, QV = 0, PY = 0, QY = 0;
         for (int32_t b = 0; b <= filterSize; b++) {
             const int32_t l = imax(fillStart, i - b);
             const int32_t r = imin(fillEnd - 1, i + b);
             const double *cf4 = c->cfilt[b];
+            PY += (m[0][r] + m[0][l]) * c->yfilt[b][0] + (m[1][r] + m[1][l]) * c->yfilt[b][1];
+            QY += (n[0][r] + n[0][l]) * c->yfilt[b][0] + (n[1][r] + n[1][l]) * c->yfilt[b][1];
             PU += (m[0][r] + m[0][l]) * cf4[0] + (m[1][r] + m[1][l]) * cf4[1] + (n[2][r] + n[2][l]) * cf4[2] +
                   (n[3][r] + n[3][l]) * cf4[3];
             QU += (n[0][r] + n[0][l]) * cf4[0] + (n[1][r] + n[1][l]) * cf4[1] - (m[2][r] + m[2][l]) * cf4[2] -
@@ -492,6 +560,8 @@ static void decode_line(const pal_ctx *c, const tpo_params *p, const src_field *
         qu[i] = QU;
         pv[i] = PV;
         qv[i] = QV;
+        py[i] = PY;
+        qy[i] = QY;
     }
     const uint16_t *comp = f->data + (line->number * fw);
     const int32_t lineNumber = (line->number * 2) + f->offset;
@@ -499,15 +569,18 @@ static void decode_line(const pal_ctx *c, const tpo_params *p, const src_field *
     double *outU = cf->u + (size_t)lineNumber * cf->width;
     double *outV = cf->v + (size_t)lineNumber * cf->width;
     for (int32_t i = p->active_start; i < endPos; i++) {
-        outY[i] = comp[i] - in0[i];
+        if (prefiltered) outY[i] = comp[i] - in0[i];
+        else outY[i] = comp[i] - ((py[i] * sine[i] + qy[i] * cosine[i]) * 2.0);
         outU[i] = -(pu[i] * line->bp + qu[i] * line->bq) * 2.0;
         outV[i] = line->Vsw * -(qv[i] * line->bp - pv[i] * line->bq) * 2.0;
     }
+    if (p->y_nr_level > 0.0) do_ynr(p, outY, scratch + 7 * (size_t)MAX_WIDTH, scratch + 8 * (size_t)MAX_WIDTH);
 }
 
 typedef struct demod_scratch {
     double m[4][MAX_WIDTH], n[4][MAX_WIDTH];
-    double pu[MAX_WIDTH], qu[MAX_WIDTH], pv[MAX_WIDTH], qv[MAX_WIDTH];
+    double pu[MAX_WIDTH], qu[MAX_WIDTH], pv[MAX_WIDTH], qv[MAX_WIDTH], py[MAX_WIDTH], qy[MAX_WIDTH];
+    double rows[9 * MAX_WIDTH + 64];   /* composite rows, yNR history and high-pass output */
 } demod_scratch;
 
 /* PalColour::decodeField, palcolour.cpp:307-335 */
@@ -524,7 +597,7 @@ static void decode_field(const pal_ctx *c, const tpo_params *p, const src_field 
         const double theta = (p->chroma_phase_deg * M_PI) / 180;
         line.bp = (oldBp * cos(theta) - oldBq * sin(theta)) * p->chroma_gain;
         line.bq = (oldBp * sin(theta) + oldBq * cos(theta)) * p->chroma_gain;
-        decode_line(c, p, f, chroma, &line, cf, s->m, s->n, s->pu, s->qu, s->pv, s->qv);
+        decode_line(c, p, f, chroma, &line, cf, s->m, s->n, s->pu, s->qu, s->pv, s->qv, s->py, s->qy, s->rows);
     }
 }
 
@@ -565,7 +638,41 @@ static void float_bounds(int32_t mode, float *b)
     }
 }
 
-/* OutputWriter::convert (YUV444P16) and convertToFloat, output_writer.cpp:340-486, 670-727 */
+/* floatRGBBounds, output_writer.cpp:149-190 */
+static void float_rgb_bounds(const tpo_params *p, float *b)
+{
+    const float inf = INFINITY;
+    switch (p->clamp_mode) {
+    case TPO_CLAMP_LEGAL_RGB_SDR:
+        for (int i = 0; i < 3; i++) { b[2 * i] = 0.0f; b[2 * i + 1] = 1.0f; }
+        break;
+    case TPO_CLAMP_LEGAL_RGB_HDR:
+        for (int i = 0; i < 3; i++) { b[2 * i] = 0.0f; b[2 * i + 1] = inf; }
+        break;
+    case TPO_CLAMP_LEGAL_YCBCR_BT601: {
+        float yb[4];
+        float_bounds(p->clamp_mode, yb);
+        const double kg = 1.0 - p->kr - p->kb;
+        const double bds = 2.0 * (1.0 - p->kb), rds = 2.0 * (1.0 - p->kr);
+        const double gFromCb = (p->kb * bds) / kg;
+        const double gFromCr = (p->kr * rds) / kg;
+        b[0] = (float)(yb[0] + rds * yb[2]);
+        b[1] = (float)(yb[1] + rds * yb[3]);
+        b[2] = (float)(yb[0] - (gFromCb + gFromCr) * yb[3]);
+        b[3] = (float)(yb[1] - (gFromCb + gFromCr) * yb[2]);
+        b[4] = (float)(yb[0] + bds * yb[2]);
+        b[5] = (float)(yb[1] + bds * yb[3]);
+        break;
+    }
+    default:
+        for (int i = 0; i < 3; i++) { b[2 * i] = -inf; b[2 * i + 1] = inf; }
+    }
+}
+
+/* OutputWriter::convert / convertLine (YUV444P16, RGB48, GRAY16),
+ * convertToFloat (YUV444PS, GRAYS) and convertToFloatRGB (RGBS),
+ * output_writer.cpp:340-486, 670-779, with ColorConversion's derived
+ * scalars (color_conversion.cpp:33-66). */
 static void write_output(const tpo_params *p, const component_frame *cf, void *out)
 {
     int32_t ow, oh, lp, tpad;
@@ -579,11 +686,20 @@ static void write_output(const tpo_params *p, const component_frame *cf, void *o
     const double eyScale = 1.0 / yRange;
     const double ecbScale = p->ecb_from_u / uvRange;
     const double ecrScale = p->ecr_from_v / uvRange;
-    if (p->output_format == TPO_FMT_PS) {
+    const double kg = 1.0 - p->kr - p->kb;
+    const double rFromV = 1.0 / p->v_reduction;
+    const double gFromU = -(p->kb / kg) / p->u_reduction;
+    const double gFromV = -(p->kr / kg) / p->v_reduction;
+    const double bFromU = 1.0 / p->u_reduction;
+    const int32_t fmt = p->output_format;
+    const int padded = (ow != activeWidth || oh != activeHeight);
+    if (fmt == TPO_FMT_PS || fmt == TPO_FMT_GRAYS || fmt == TPO_FMT_RGBS) {
         float *pl = (float *)out;
-        float b[4];
-        float_bounds(p->clamp_mode, b);
-        memset(pl, 0, sizeof(float) * planeSize * 3);
+        const int nplanes = (fmt == TPO_FMT_GRAYS) ? 1 : 3;
+        memset(pl, 0, sizeof(float) * planeSize * nplanes);
+        float b[6] = {0, 0, 0, 0, 0, 0};
+        if (fmt == TPO_FMT_RGBS) float_rgb_bounds(p, b);
+        else float_bounds(p->clamp_mode, b);
         for (int32_t y = 0; y < activeHeight; y++) {
             const int32_t inputLine = p->first_active_frame_line + y;
             const double *inY = cf->y + (size_t)inputLine * cf->width + p->active_start;
@@ -591,33 +707,68 @@ static void write_output(const tpo_params *p, const component_frame *cf, void *o
             const double *inV = cf->v + (size_t)inputLine * cf->width + p->active_start;
             const size_t rowOff = (size_t)ow * (tpad + y) + lp;
             for (int32_t x = 0; x < activeWidth; x++) {
+                if (fmt == TPO_FMT_RGBS) {
+                    const double rY = (inY[x] - yOffset) * eyScale;
+                    const double rU = inU[x] * (1.0 / uvRange);
+                    const double rV = inV[x] * (1.0 / uvRange);
+                    pl[rowOff + x] = fclamp((float)(rY + rFromV * rV), b[0], b[1]);
+                    pl[planeSize + rowOff + x] = fclamp((float)(rY + gFromU * rU + gFromV * rV), b[2], b[3]);
+                    pl[2 * planeSize + rowOff + x] = fclamp((float)(rY + bFromU * rU), b[4], b[5]);
+                    continue;
+                }
                 pl[rowOff + x] = fclamp((float)((inY[x] - yOffset) * eyScale), b[0], b[1]);
+                if (fmt == TPO_FMT_GRAYS) continue;
                 pl[planeSize + rowOff + x] = fclamp((float)(inU[x] * ecbScale), b[2], b[3]);
                 pl[2 * planeSize + rowOff + x] = fclamp((float)(inV[x] * ecrScale), b[2], b[3]);
             }
         }
-    } else {
-        uint16_t *pl = (uint16_t *)out;
-        double b[4];
-        int_bounds(p->clamp_mode, b);
-        if (ow != activeWidth || oh != activeHeight) {
-            for (size_t i = 0; i < planeSize; i++) {
-                pl[i] = (uint16_t)(16.0 * 256.0);
-                pl[planeSize + i] = (uint16_t)(128.0 * 256.0);
-                pl[2 * planeSize + i] = (uint16_t)(128.0 * 256.0);
-            }
-        }
+        return;
+    }
+    uint16_t *pl = (uint16_t *)out;
+    double b[4];
+    int_bounds(p->clamp_mode, b);
+    if (fmt == TPO_FMT_RGB48) {
+        if (padded) memset(pl, 0, sizeof(uint16_t) * planeSize * 3);
+        const double yScale = 65535.0 / yRange;
+        const double uvScale = 65535.0 / uvRange;
         for (int32_t y = 0; y < activeHeight; y++) {
             const int32_t inputLine = p->first_active_frame_line + y;
             const double *inY = cf->y + (size_t)inputLine * cf->width + p->active_start;
             const double *inU = cf->u + (size_t)inputLine * cf->width + p->active_start;
             const double *inV = cf->v + (size_t)inputLine * cf->width + p->active_start;
-            const size_t rowOff = (size_t)ow * (tpad + y) + lp;
+            uint16_t *o = pl + ((size_t)ow * (tpad + y) + lp) * 3;
             for (int32_t x = 0; x < activeWidth; x++) {
-                pl[rowOff + x] = (uint16_t)dclamp(h273_round(219.0 * 256.0 * ((inY[x] - yOffset) * eyScale) + 16.0 * 256.0), b[0], b[1]);
-                pl[planeSize + rowOff + x] = (uint16_t)dclamp(h273_round(224.0 * 256.0 * (inU[x] * ecbScale) + 128.0 * 256.0), b[2], b[3]);
-                pl[2 * planeSize + rowOff + x] = (uint16_t)dclamp(h273_round(224.0 * 256.0 * (inV[x] * ecrScale) + 128.0 * 256.0), b[2], b[3]);
+                const double rY = dclamp((inY[x] - yOffset) * yScale, 0.0, 65535.0);
+                const double rU = inU[x] * uvScale;
+                const double rV = inV[x] * uvScale;
+                o[3 * x] = (uint16_t)dclamp(rY + (rFromV * rV), 0.0, 65535.0);
+                o[3 * x + 1] = (uint16_t)dclamp(rY + (gFromU * rU) + (gFromV * rV), 0.0, 65535.0);
+                o[3 * x + 2] = (uint16_t)dclamp(rY + (bFromU * rU), 0.0, 65535.0);
             }
+        }
+        return;
+    }
+    const int nplanes = (fmt == TPO_FMT_GRAY16) ? 1 : 3;
+    if (padded) {
+        for (size_t i = 0; i < planeSize; i++) {
+            pl[i] = (uint16_t)(16.0 * 256.0);
+            if (nplanes == 3) {
+                pl[planeSize + i] = (uint16_t)(128.0 * 256.0);
+                pl[2 * planeSize + i] = (uint16_t)(128.0 * 256.0);
+            }
+        }
+    }
+    for (int32_t y = 0; y < activeHeight; y++) {
+        const int32_t inputLine = p->first_active_frame_line + y;
+        const double *inY = cf->y + (size_t)inputLine * cf->width + p->active_start;
+        const double *inU = cf->u + (size_t)inputLine * cf->width + p->active_start;
+        const double *inV = cf->v + (size_t)inputLine * cf->width + p->active_start;
+        const size_t rowOff = (size_t)ow * (tpad + y) + lp;
+        for (int32_t x = 0; x < activeWidth; x++) {
+            pl[rowOff + x] = (uint16_t)dclamp(h273_round(219.0 * 256.0 * ((inY[x] - yOffset) * eyScale) + 16.0 * 256.0), b[0], b[1]);
+            if (nplanes == 1) continue;
+            pl[planeSize + rowOff + x] = (uint16_t)dclamp(h273_round(224.0 * 256.0 * (inU[x] * ecbScale) + 128.0 * 256.0), b[2], b[3]);
+            pl[2 * planeSize + rowOff + x] = (uint16_t)dclamp(h273_round(224.0 * 256.0 * (inV[x] * ecrScale) + 128.0 * 256.0), b[2], b[3]);
         }
     }
 }
@@ -855,19 +1006,22 @@ static void correct_field(const tpo_params *p, const do_list *thisD, const do_li
 }
 
 /* DropoutCorrector::correctFrame (single source), dropout_corrector.cpp:40-114.
- * first/second are the two fields of capture frame `frame` (first field
- * first, so the broadcast order equals the stored order). */
-static void correct_frame(const tpo_params *p, const tpo_dropout *d, int32_t nd, int32_t frame, uint16_t *first,
-                          uint16_t *second, int32_t overCorrect, int32_t intraField, tpo_stats *stats)
+ * The two fields are taken in broadcast order: `first` is the field whose
+ * metadata says isFirstField (capture field index fi_first), `second` the
+ * other one. d holds the frame's dropouts as loaded (shifted for a
+ * subcarrier-locked second field). */
+static void correct_frame(const tpo_params *p, const tpo_dropout *d, int32_t nd, int32_t fi_first,
+                          int32_t fi_second, uint16_t *first, uint16_t *second, int32_t overCorrect,
+                          int32_t intraField, tpo_stats *stats)
 {
     do_list fd = {0}, sd = {0};
-    populate(p, d, nd, 2 * frame, overCorrect, &fd);
-    populate(p, d, nd, 2 * frame + 1, overCorrect, &sd);
+    populate(p, d, nd, fi_first, overCorrect, &fd);
+    populate(p, d, nd, fi_second, overCorrect, &sd);
     /* "Skip if no dropouts in primary fields" tests the metadata lists, which
      * also hold entries populate() drops for being off the field. */
     int32_t any = 0;
     for (int32_t i = 0; i < nd; i++)
-        if (d[i].field == 2 * frame || d[i].field == 2 * frame + 1) any = 1;
+        if (d[i].field == fi_first || d[i].field == fi_second) any = 1;
     if (any) {
         if (fd.n) set_locations(p, &fd);
         if (sd.n) set_locations(p, &sd);
@@ -878,11 +1032,52 @@ static void correct_frame(const tpo_params *p, const tpo_dropout *d, int32_t nd,
     free(sd.v);
 }
 
-static int32_t frame_has_dropouts(const tpo_dropout *d, int32_t nd, int32_t frame)
+/* The dropouts of frame `frame` as SourceField::loadFields leaves them: a
+ * subcarrier-locked slot-1 field's dropouts move 2 samples left and vanish
+ * when they end at or before sample 0 (source_field.cpp:51-66). Returns the
+ * count; *out is malloc'd (free it). */
+static int32_t frame_dropouts(const tpo_params *p, const tpo_dropout *d, int32_t nd, int32_t frame,
+                              tpo_dropout **out)
 {
+    *out = NULL;
+    int32_t n = 0;
     for (int32_t i = 0; i < nd; i++)
-        if (d[i].field == 2 * frame || d[i].field == 2 * frame + 1) return 1;
-    return 0;
+        if (d[i].field == 2 * frame || d[i].field == 2 * frame + 1) n++;
+    if (n == 0) return 0;
+    tpo_dropout *v = (tpo_dropout *)malloc(sizeof(tpo_dropout) * (size_t)n);
+    int32_t k = 0;
+    for (int32_t i = 0; i < nd; i++) {
+        if (d[i].field != 2 * frame && d[i].field != 2 * frame + 1) continue;
+        tpo_dropout x = d[i];
+        if (p->sc_locked && x.field == 2 * frame + 1) {
+            const int32_t endx = x.endx - 2;
+            if (endx <= 0) continue;
+            x.startx = imax(x.startx - 2, 0);
+            x.endx = endx;
+        }
+        v[k++] = x;
+    }
+    *out = v;
+    return k;
+}
+
+/* shiftSecondField's samples: drop the first 2, append 2 black (source_field.cpp:51-57). */
+static void shift_field(const tpo_params *p, const uint16_t *src, uint16_t *dst)
+{
+    const size_t fl = (size_t)p->field_width * p->field_height;
+    memcpy(dst, src + 2, sizeof(uint16_t) * (fl - 2));
+    dst[fl - 2] = (uint16_t)p->black;
+    dst[fl - 1] = (uint16_t)p->black;
+}
+
+/* Correct frame f's fields c0 (slot 0) and c1 (slot 1) in place; stats of the correction. */
+static void correct_slots(const tpo_params *p, const tpo_dropout *fd, int32_t nfd, int32_t f, uint16_t *c0,
+                          uint16_t *c1, int32_t overcorrect, int32_t intra, tpo_stats *st)
+{
+    if (p->first_field_offset == 0)
+        correct_frame(p, fd, nfd, 2 * f, 2 * f + 1, c0, c1, overcorrect, intra, st);
+    else
+        correct_frame(p, fd, nfd, 2 * f + 1, 2 * f, c1, c0, overcorrect, intra, st);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -896,7 +1091,7 @@ typedef struct decoder {
     demod_scratch *scratch;
     component_frame cf;
     uint16_t *black;       /* one black field */
-    uint16_t *corrected;   /* window frames' corrected copies, 2 fields per frame */
+    uint16_t *corrected;   /* window frames' corrected / shifted copies, 2 fields per frame */
 } decoder;
 
 static int decoder_init(decoder *d, const tpo_params *p)
@@ -928,7 +1123,7 @@ static void decoder_free(decoder *d)
     free(d->corrected);
 }
 
-static int32_t look_behind(const tpo_params *p) { return p->kind == 3 ? (4 + 1) / 2 : 0; } /* transform_pal_3d.cpp:111-115 */
+static int32_t look_behind(const tpo_params *p) { return p->kind == 3 ? (4 + 1) / 2 : 0; } /* transform_pal_3d.cpp:111-115; 0 for 2D and PALcolour */
 static int32_t look_ahead(const tpo_params *p) { return p->kind == 3 ? (8 - 1 + 1) / 2 : 0; } /* :117-121 */
 
 /* Window of frames [frame-lb, frame+1+la) with black padding outside the
@@ -944,8 +1139,8 @@ static int32_t load_window(decoder *d, const uint16_t *fields, int32_t nfields, 
     const int32_t n = 2 * (lb + 1 + la);
     for (int32_t i = 0; i < n; i += 2) {
         const int32_t f = frame - lb + i / 2;
-        win[i].offset = 0;
-        win[i + 1].offset = 1;
+        win[i].offset = p->first_field_offset;
+        win[i + 1].offset = 1 - p->first_field_offset;
         if (f < 0 || f >= numFrames) {
             win[i].data = d->black;
             win[i + 1].data = d->black;
@@ -953,13 +1148,19 @@ static int32_t load_window(decoder *d, const uint16_t *fields, int32_t nfields, 
         }
         win[i].data = fields + fl * (size_t)(2 * f);
         win[i + 1].data = fields + fl * (size_t)(2 * f + 1);
-        if (drops && frame_has_dropouts(drops, nd, f)) {
-            uint16_t *c0 = d->corrected + fl * (size_t)i;
-            uint16_t *c1 = c0 + fl;
-            memcpy(c0, win[i].data, sizeof(uint16_t) * fl);
-            memcpy(c1, win[i + 1].data, sizeof(uint16_t) * fl);
+        uint16_t *c0 = d->corrected + fl * (size_t)i;
+        uint16_t *c1 = c0 + fl;
+        if (p->sc_locked) {   /* SourceField::shiftSecondField on slot 1 */
+            shift_field(p, win[i + 1].data, c1);
+            win[i + 1].data = c1;
+        }
+        tpo_dropout *fd = NULL;
+        const int32_t nfd = drops ? frame_dropouts(p, drops, nd, f, &fd) : 0;
+        if (nfd > 0) {
+            if (win[i].data != c0) memcpy(c0, win[i].data, sizeof(uint16_t) * fl);
+            if (win[i + 1].data != c1) memcpy(c1, win[i + 1].data, sizeof(uint16_t) * fl);
             tpo_stats st = {0, 0, 0};
-            correct_frame(p, drops, nd, f, c0, c1, overcorrect, intra, &st);
+            correct_slots(p, fd, nfd, f, c0, c1, overcorrect, intra, &st);
             if (f == frame && stats) {
                 stats->corrected += st.corrected;
                 stats->failed += st.failed;
@@ -968,6 +1169,7 @@ static int32_t load_window(decoder *d, const uint16_t *fields, int32_t nfields, 
             win[i].data = c0;
             win[i + 1].data = c1;
         }
+        free(fd);
     }
     return 2 * lb; /* startIndex */
 }
@@ -993,7 +1195,7 @@ static int decode_one(decoder *d, const uint16_t *fields, int32_t nfields, const
     if (p->kind == 2) {
         filter_field_2d(&d->tp, p, &win[startIndex], chroma[0]);
         filter_field_2d(&d->tp, p, &win[startIndex + 1], chroma[1]);
-    } else {
+    } else if (p->kind == 3) {
         filter_fields_3d(&d->tp, p, win, startIndex, startIndex + 2, chroma);
     }
     const size_t n = (size_t)d->cf.width * d->cf.height;
@@ -1049,7 +1251,8 @@ int tpo_decode_frames(const tpo_params *p, const uint16_t *fields, int32_t nfiel
                       int32_t ndropouts, int32_t overcorrect, int32_t intra_field, int32_t first, int32_t count,
                       void *out, int32_t nthreads, tpo_stats *stats)
 {
-    if (!p || !fields || !out || count < 0 || (p->kind != 2 && p->kind != 3)) return -1;
+    if (!p || !fields || !out || count < 0 || (p->kind != 1 && p->kind != 2 && p->kind != 3)) return -1;
+    if (p->output_format < TPO_FMT_P16 || p->output_format > TPO_FMT_GRAYS) return -1;
     if (p->thresholds && p->n_thresholds != (p->kind == 2 ? 80 : 768)) return -1;
     job j;
     j.p = p;
@@ -1114,10 +1317,14 @@ int tpo_dropout_correct_frame(const tpo_params *p, const uint16_t *fields, int32
 {
     const size_t fl = (size_t)p->field_width * p->field_height;
     if (frame < 0 || 2 * frame + 1 >= nfields) return -1;
-    memcpy(out, fields + fl * (size_t)(2 * frame), sizeof(uint16_t) * fl * 2);
+    memcpy(out, fields + fl * (size_t)(2 * frame), sizeof(uint16_t) * fl);
+    if (p->sc_locked) shift_field(p, fields + fl * (size_t)(2 * frame + 1), out + fl);
+    else memcpy(out + fl, fields + fl * (size_t)(2 * frame + 1), sizeof(uint16_t) * fl);
     tpo_stats st = {0, 0, 0};
-    if (frame_has_dropouts(dropouts, ndropouts, frame))
-        correct_frame(p, dropouts, ndropouts, frame, out, out + fl, overcorrect, intra_field, &st);
+    tpo_dropout *fd = NULL;
+    const int32_t nfd = frame_dropouts(p, dropouts, ndropouts, frame, &fd);
+    if (nfd > 0) correct_slots(p, fd, nfd, frame, out, out + fl, overcorrect, intra_field, &st);
+    free(fd);
     if (stats) *stats = st;
     return 0;
 }
@@ -1140,14 +1347,17 @@ int32_t tpo_dropout_spans(const tpo_params *p, const tpo_dropout *d, int32_t nd,
     const int32_t avs = p->active_start;
     const int32_t ave = p->active_end;
     int32_t n = 0;
+    tpo_dropout *fd = NULL;
+    const int32_t nfd = frame_dropouts(p, d, nd, frame, &fd);
     for (int32_t j = 0; j < 2; j++) {
         const int32_t field = 2 * frame + j;
-        for (int32_t i = 0; i < nd; i++) {
-            if (d[i].field != field) continue;
-            const int32_t frameRow = (2 * (d[i].field_line - 1)) + j;
+        const int32_t offset = j ^ p->first_field_offset;   /* SourceField::getOffset */
+        for (int32_t i = 0; i < nfd; i++) {
+            if (fd[i].field != field) continue;
+            const int32_t frameRow = (2 * (fd[i].field_line - 1)) + offset;
             const int32_t y = tpad + frameRow - p->first_active_frame_line;
             if (y < 0 || y >= oh) continue;
-            int32_t x0 = d[i].startx, x1 = d[i].endx;
+            int32_t x0 = fd[i].startx, x1 = fd[i].endx;
             if (mode == 1) {
                 const int32_t dots = 24;
                 x0 = (x0 > dots) ? x0 - dots : 0;
@@ -1165,6 +1375,7 @@ int32_t tpo_dropout_spans(const tpo_params *p, const tpo_dropout *d, int32_t nd,
             n++;
         }
     }
+    free(fd);
     qsort(out, (size_t)(n < cap ? n : cap), sizeof(tpo_span), span_cmp);
     return n;
 }

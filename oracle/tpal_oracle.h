@@ -12,7 +12,10 @@
  *   TransformPal 2D / 3D           src/decoders/palcolour/transform_pal_2d.cpp:107-287
  *                                  src/decoders/palcolour/transform_pal_3d.cpp:64-333
  *   PALcolour demodulator          src/decoders/palcolour/palcolour.cpp:150-646
- *   H.273 output                   src/output/output_writer.cpp:52-143,195-239,402-486,670-727
+ *     (Transform PAL chroma, or the PALcolour 2D filter on the composite,
+ *      and the optional luma noise coring doYNR)
+ *   second-field shift (scLocked)  src/decoders/source_field.cpp:45-66
+ *   output formats                 src/output/output_writer.cpp:52-143,195-239,340-486,670-779
  *   dropout concealment            src/dropout/dropout_corrector.cpp:50-530
  *   dropout spans / mask           src/abi/c_api_dropout_detect.cpp:92-295
  * Operation order follows the reference so results agree to the last bit
@@ -29,7 +32,9 @@
 extern "C" {
 #endif
 
-enum { TPO_FMT_P16 = 0, TPO_FMT_PS = 1 };
+/* Output formats, numbered as chd_pixel_format_t. */
+enum { TPO_FMT_P16 = 0, TPO_FMT_PS = 1, TPO_FMT_RGB48 = 2, TPO_FMT_RGBS = 3, TPO_FMT_GRAY16 = 4, TPO_FMT_GRAYS = 5 };
+/* Decoder kinds: 1 = PALcolour 2D filter alone, 2 = Transform PAL 2D, 3 = Transform PAL 3D. */
 enum { TPO_CLAMP_NONE = 0, TPO_CLAMP_LEGAL_RGB_SDR = 1, TPO_CLAMP_LEGAL_RGB_HDR = 2, TPO_CLAMP_LEGAL_YCBCR_BT601 = 3 };
 
 typedef struct tpo_params {
@@ -52,6 +57,11 @@ typedef struct tpo_params {
     int32_t clamp_mode;         /* TPO_CLAMP_* */
     int32_t padding_multiple;   /* 1 = none */
     double ecb_from_u, ecr_from_v;  /* colour-difference scalars (color_conversion.cpp:59-60) */
+    /* ColorConversion inputs for the RGB formats (color_conversion.cpp:33-66) */
+    double kr, kb, u_reduction, v_reduction;
+    double y_nr_level;          /* luma_nr_level; 0 = off */
+    int32_t first_field_offset; /* offset of window slot 0: 0 = first field (normal), 1 = reversed pairing */
+    int32_t sc_locked;          /* subcarrier-locked PAL: slot-1 fields shifted left by 2 samples */
 } tpo_params;
 
 typedef struct tpo_dropout {
@@ -71,14 +81,15 @@ void tpo_default_params(tpo_params *p, int32_t kind);
 void tpo_output_geometry(const tpo_params *p, int32_t *width, int32_t *height,
                          int32_t *left_pad, int32_t *top_pad);
 
-/* Bytes of one output frame (3 planes). */
+/* Bytes of one output frame. */
 size_t tpo_frame_bytes(const tpo_params *p);
 
 /* Decode frames [first, first+count) of a capture of nfields fields
- * (field_width*field_height uint16 each, first field first). Dropouts, when
+ * (field_width*field_height uint16 each, in pairing order: frame k is fields
+ * 2k and 2k+1, slot 0 having offset first_field_offset). Dropouts, when
  * given, are concealed before decoding exactly as the reference does.
- * Output: count frames back to back, each [Y | Cb | Cr] planes (uint16 for
- * p16, float for ps). nthreads >= 1 decodes frames in parallel, one decoder
+ * Output: count frames back to back in the output format's layout
+ * (OutputFrame / float planes). nthreads >= 1 decodes frames in parallel, one decoder
  * instance per thread (chd_decode_frames_async's model). stats (optional)
  * receives the sum over the decoded frames of their own dropout stats.
  * Returns 0 on success. */

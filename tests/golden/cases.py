@@ -36,7 +36,40 @@ CASES = {
                        overcorrect=1),
     "chroma2d": dict(mode="chroma", kind=2, nfields=8, seed=31, first=0, count=4),
     "chroma3d": dict(mode="chroma", kind=3, nfields=12, seed=32, first=0, count=6),
+    # PALcolour 2D filter alone (CHD_DEC_PAL_2D)
+    "pal2d_p16": dict(mode="decode", kind=1, fmt="p16", nfields=8, seed=34, first=0, count=4),
+    "pal2d_ps_ynr": dict(mode="decode", kind=1, fmt="ps", nfields=8, seed=34, first=1, count=2, y_nr_level=2.5),
+    # luma noise coring on the Transform paths
+    "t3d_ynr": dict(mode="decode", kind=3, fmt="p16", nfields=12, seed=32, first=1, count=3, y_nr_level=1.5),
+    "t2d_ynr_ps": dict(mode="decode", kind=2, fmt="ps", nfields=8, seed=31, first=0, count=2, y_nr_level=4.0),
+    # output formats and colour-conversion precisions
+    "t3d_rgb48": dict(mode="decode", kind=3, fmt="rgb48", nfields=12, seed=32, first=2, count=2),
+    "t3d_rgbs_bt601": dict(mode="decode", kind=3, fmt="rgbs", nfields=12, seed=32, first=2, count=2, clamp_mode=3,
+                           cdp="classic", bsp="modern"),
+    "t3d_rgbs_hdr": dict(mode="decode", kind=3, fmt="rgbs", nfields=12, seed=32, first=3, count=1, clamp_mode=2),
+    "t2d_gray16_pad": dict(mode="decode", kind=2, fmt="gray16", nfields=8, seed=31, first=0, count=2,
+                           padding_multiple=16, clamp_mode=1),
+    "t2d_grays": dict(mode="decode", kind=2, fmt="grays", nfields=8, seed=31, first=1, count=2, clamp_mode=3),
+    "t3d_p16_classic": dict(mode="decode", kind=3, fmt="p16", nfields=12, seed=32, first=2, count=1,
+                            cdp="classic", bsp="classic"),
+    # reversed field pairing (reverse_field_order): slot 0 holds second fields
+    "t3d_rev": dict(mode="decode", kind=3, fmt="p16", nfields=13, seed=35, first=0, count=6, sff=1,
+                    dropouts=0.02),
+    "t2d_rev_ps": dict(mode="decode", kind=2, fmt="ps", nfields=9, seed=35, first=0, count=4, sff=1),
+    "conceal_rev": dict(mode="dropout", kind=3, fmt="p16", nfields=13, seed=35, first=0, count=6, sff=1,
+                        dropouts=0.02),
+    # subcarrier-locked PAL: second fields shifted by 2 samples
+    "t3d_sclocked": dict(mode="decode", kind=3, fmt="p16", nfields=12, seed=33, first=0, count=6, sc_locked=1,
+                         dropouts=0.02),
+    "conceal_sclocked": dict(mode="dropout", kind=3, fmt="p16", nfields=12, seed=33, first=0, count=6,
+                             sc_locked=1, dropouts=0.02, overcorrect=1),
 }
+
+# harness argument of each optional case key
+HARNESS_ARGS = {"chroma_gain": "gain", "chroma_phase_deg": "phase", "clamp_mode": "clamp",
+                "padding_multiple": "padding", "active_start": "avs", "active_end": "ave",
+                "first_active_frame_line": "fafl", "last_active_frame_line": "lafl", "y_nr_level": "ynr",
+                "sff": "sff", "sc_locked": "sclocked", "cdp": "cdp", "bsp": "bsp"}
 
 
 @functools.lru_cache(maxsize=8)
@@ -46,12 +79,17 @@ def _capture(nfields: int, seed: int, dropouts: float):
 
 
 def case_inputs(case: dict):
-    """(fields uint16 (n, 313, 1135), flat dropouts [(field, startx, endx, fieldLine)] or None)."""
+    """(fields uint16 (n, 313, 1135), flat dropouts [(field, startx, endx, fieldLine)] or None).
+
+    For the reversed pairing (sff) the capture's first field is dropped, so
+    the array starts with a second field and frame k is fields 2k, 2k+1 of
+    the array, slot 0 being a second field."""
     cap = _capture(case["nfields"], case["seed"], case.get("dropouts", 0.0))
+    skip = 1 if case.get("sff") else 0
     flat = None
     if case.get("dropouts", 0.0) > 0:
-        flat = [(f, s[0], s[1], s[2]) for f, spans in enumerate(cap.dropouts) for s in spans]
-    return np.ascontiguousarray(cap.fields), flat
+        flat = [(f - skip, s[0], s[1], s[2]) for f, spans in enumerate(cap.dropouts) for s in spans if f >= skip]
+    return np.ascontiguousarray(cap.fields[skip:]), flat
 
 
 def thresholds_for(case: dict):

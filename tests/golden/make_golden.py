@@ -25,7 +25,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from tests.golden.cases import CASES, case_inputs, thresholds_for  # noqa: E402
+from tests.golden.cases import CASES, HARNESS_ARGS, case_inputs, thresholds_for  # noqa: E402
 from oracle import oracle  # noqa: E402
 
 
@@ -54,9 +54,7 @@ def run_case(harness: str, case: dict, tmp: str) -> dict:
         with open(tpath, "w") as fp:
             fp.write("\n".join(repr(float(t)) for t in thr))
         args.append(f"thresholds={tpath}")
-    for key, arg in (("chroma_gain", "gain"), ("chroma_phase_deg", "phase"), ("clamp_mode", "clamp"),
-                     ("padding_multiple", "padding"), ("active_start", "avs"), ("active_end", "ave"),
-                     ("first_active_frame_line", "fafl"), ("last_active_frame_line", "lafl")):
+    for key, arg in HARNESS_ARGS.items():
         if key in case:
             args.append(f"{arg}={case[key]}")
     r = subprocess.run(args, capture_output=True, text=True, check=True)

@@ -20,13 +20,20 @@ from tests.golden.cases import CASES, case_inputs, thresholds_for
 GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "golden.json")))["cases"]
 
 
+FMTS = {"p16": O.FMT_P16, "ps": O.FMT_PS, "rgb48": O.FMT_RGB48, "rgbs": O.FMT_RGBS, "gray16": O.FMT_GRAY16,
+        "grays": O.FMT_GRAYS}
+
+
 def _params(case):
-    p = O.params(case["kind"], O.FMT_PS if case.get("fmt") == "ps" else O.FMT_P16,
-                 threshold=case.get("threshold", 0.4), thresholds=thresholds_for(case))
+    p = O.params(case["kind"], FMTS[case.get("fmt", "p16")], threshold=case.get("threshold", 0.4),
+                 thresholds=thresholds_for(case))
     for k in ("chroma_gain", "chroma_phase_deg", "clamp_mode", "padding_multiple", "active_start", "active_end",
-              "first_active_frame_line", "last_active_frame_line"):
+              "first_active_frame_line", "last_active_frame_line", "y_nr_level"):
         if k in case:
             setattr(p, k, case[k])
+    p.first_field_offset = int(case.get("sff", 0))
+    p.sc_locked = int(case.get("sc_locked", 0))
+    O.colour_precision(p, case.get("cdp", "modern"), case.get("bsp", "scientific"))
     return p
 
 
