@@ -9,8 +9,8 @@
  * reference-compatible chd_* ABI in <chromadec/*.h> is built on top of them.
  *
  * Conventions: a capture is a device array of uint16 fields, field f at
- * fields + f * field_stride samples, first field of every frame at an even
- * index. Frames outside the capture are black padding, as in the reference's
+ * fields + f * field_stride samples, frame k made of fields 2k and 2k+1 (the
+ * first field at the even index unless first_field_offset says otherwise). Frames outside the capture are black padding, as in the reference's
  * SourceField::loadFields (src/decoders/source_field.cpp:88-170). Every call
  * returns 0 on success and a negative CHDG_E_* code on failure; failures
  * also set the thread's chd_last_error() detail.
@@ -43,21 +43,26 @@ typedef struct chdg_geometry {
 /* Decoder + output settings (PalColour::Configuration and
  * OutputWriter::Configuration fields the path reads). */
 typedef struct chdg_config {
-    int32_t kind;                 /* 7 = CHD_DEC_TRANSFORM_2D, 8 = CHD_DEC_TRANSFORM_3D */
+    int32_t kind;                 /* 6 = CHD_DEC_PAL_2D, 7 = CHD_DEC_TRANSFORM_2D, 8 = CHD_DEC_TRANSFORM_3D */
     double threshold;             /* transform_threshold, default 0.4 */
     const double *thresholds;     /* per-bin thresholds (80 for 2D, 768 for 3D) or NULL */
     int32_t n_thresholds;
     double chroma_gain, chroma_phase_deg;
-    int32_t output_format;        /* 0 = yuv444p16, 1 = yuv444ps */
+    int32_t output_format;        /* chd_pixel_format_t: 0 yuv444p16, 1 yuv444ps, 2 rgb48, 3 rgbs, 4 gray16, 5 grays */
     int32_t clamp_mode;           /* chd_clamp_t */
     int32_t padding_multiple;     /* 1 = none */
     double ecb_from_u, ecr_from_v;
+    /* ColorConversion inputs (src/common/color_conversion.cpp:33-66): luma
+     * coefficients and the composite U/V reductions, for the RGB formats */
+    double kr, kb, u_reduction, v_reduction;
+    double y_nr_level;            /* luma_nr_level (doYNR); 0 = off */
+    int32_t first_field_offset;   /* 1: field 2k of every frame is its second field (reverse_field_order) */
 } chdg_config;
 
 typedef struct chdg_engine chdg_engine;
 
 /* Fill g with the reference's line-locked 4fsc PAL preset and c with the
- * Transform-PAL decoder defaults for `kind` (7 or 8). */
+ * decoder defaults for `kind` (6, 7 or 8). */
 void chdg_default_geometry(chdg_geometry *g);
 void chdg_default_config(chdg_config *c, int32_t kind);
 
@@ -70,8 +75,9 @@ void chdg_engine_free(chdg_engine *e);
 int chdg_output_geometry(const chdg_engine *e, int32_t *width, int32_t *height, size_t *frame_bytes);
 
 /* Decode frames [frame_begin, frame_end) of a device-resident capture of
- * nfields fields into d_out (frame_end - frame_begin frames, each
- * [Y | Cb | Cr] planes of width x height, uint16 or float per the format).
+ * nfields fields into d_out (frame_end - frame_begin frames, each in the
+ * output format's layout: [Y | Cb | Cr] or [R | G | B] planes, interleaved
+ * R'G'B' for rgb48, one plane for the gray formats).
  * Asynchronous on `stream`. */
 int chdg_decode_device(chdg_engine *e, const uint16_t *d_fields, int64_t field_stride, int32_t nfields,
                        int32_t frame_begin, int32_t frame_end, void *d_out, void *stream);

@@ -4,8 +4,8 @@ This is the binding a Python consumer of the reference would write against
 its C ABI: the same calls, structs and status codes (reference
 include/chromadec/{video,decoder,frame,dropout,pipeline,errors}.h), with thin
 classes that raise ChdError on a non-OK status. The library underneath
-decodes CHD_DEC_TRANSFORM_2D / CHD_DEC_TRANSFORM_3D on the GPU; there is no
-CPU fallback.
+decodes CHD_DEC_PAL_2D, CHD_DEC_TRANSFORM_2D and CHD_DEC_TRANSFORM_3D on the
+GPU; there is no CPU fallback.
 """
 from __future__ import annotations
 
@@ -35,6 +35,7 @@ E_UNSUPPORTED = 17
 # chd_decoder_kind_t (decoder.h)
 DEC_AUTO = 0
 DEC_MONO = 1
+DEC_NTSC_2D = 3
 DEC_PAL_2D = 6
 DEC_TRANSFORM_2D = 7
 DEC_TRANSFORM_3D = 8
@@ -43,9 +44,12 @@ DEC_NONE = 13
 # chd_pixel_format_t, chd_plane_t, detect modes
 PIXEL_YUV444P16 = 0
 PIXEL_YUV444PS = 1
+PIXEL_RGB48 = 2
+PIXEL_RGBS = 3
 PIXEL_GRAY16 = 4
 PIXEL_GRAYS = 5
 PLANE_Y, PLANE_CB, PLANE_CR = 0, 1, 2
+PLANE_R, PLANE_G, PLANE_B = 3, 4, 5
 DROPOUT_DETECTED = 0
 DROPOUT_OVERCORRECT = 1
 
@@ -197,7 +201,14 @@ class Frame:
         data = C.c_void_p()
         stride = C.c_ssize_t()
         w, h = self.info.width, self.info.height
-        if self.info.format in (PIXEL_YUV444PS, PIXEL_GRAYS):
+        if self.info.format == PIXEL_RGB48:
+            check(L.chd_frame_get_plane(self._h, p, C.byref(data), C.byref(stride)), "chd_frame_get_plane")
+            n = (h - 1) * (stride.value // 2) + 3 * w - 2
+            buf = (C.c_uint16 * n).from_address(data.value)
+            a = np.frombuffer(buf, dtype=np.uint16)
+            rows = [a[y * (stride.value // 2):y * (stride.value // 2) + 3 * w:3] for y in range(h)]
+            return np.stack(rows).copy()
+        if self.info.format in (PIXEL_YUV444PS, PIXEL_GRAYS, PIXEL_RGBS):
             check(L.chd_frame_get_plane_float(self._h, p, C.byref(data), C.byref(stride)), "chd_frame_get_plane_float")
             buf = (C.c_float * (h * stride.value // 4)).from_address(data.value)
             return np.frombuffer(buf, dtype=np.float32).reshape(h, stride.value // 4)[:, :w].copy()
@@ -206,6 +217,12 @@ class Frame:
         return np.frombuffer(buf, dtype=np.uint16).reshape(h, stride.value // 2)[:, :w].copy()
 
     def planes(self) -> np.ndarray:
+        """Y'CbCr / gray formats: (planes, h, w); rgbs: (3, h, w) R, G, B;
+        rgb48: (h, w, 3), the packed layout."""
+        if self.info.format == PIXEL_RGB48:
+            return np.stack([self.plane(p) for p in (PLANE_R, PLANE_G, PLANE_B)], axis=-1)
+        if self.info.format == PIXEL_RGBS:
+            return np.stack([self.plane(p) for p in (PLANE_R, PLANE_G, PLANE_B)])
         n = self.info.num_planes
         return np.stack([self.plane(p) for p in range(n)])
 

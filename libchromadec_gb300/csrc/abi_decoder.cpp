@@ -230,7 +230,7 @@ chd_frame_t *make_frame(chd_decoder_t *d, const std::shared_ptr<HostChunk> &chun
     f->info.format = f->format;
     f->info.width = f->width;
     f->info.height = f->height;
-    f->info.num_planes = 3;
+    f->info.num_planes = (f->format == CHD_PIXEL_GRAY16 || f->format == CHD_PIXEL_GRAYS) ? 1 : 3;
     f->info.frame_index = index;
     return f;
 }
@@ -433,9 +433,13 @@ CHD_API chd_status_t chd_decoder_commit(chd_decoder_t *d)
     output_geometry(g, padding, w, h, lp, tp);
 
     chdg_config c{};
-    chdg_default_config(&c, resolved == CHD_DEC_TRANSFORM_2D ? 7 : 8);
+    chdg_default_config(&c, (int32_t)resolved);
     c.clamp_mode = clamp;
     c.padding_multiple = padding;
+    c.kr = kr;
+    c.kb = kb;
+    c.u_reduction = uRed;
+    c.v_reduction = vRed;
     c.ecb_from_u = 1.0 / ((2.0 * (1.0 - kb)) * uRed);
     c.ecr_from_v = 1.0 / ((2.0 * (1.0 - kr)) * vRed);
 
@@ -464,31 +468,26 @@ CHD_API chd_status_t chd_decoder_commit(chd_decoder_t *d)
     }
     if (!known_kind(resolved))
         return fail(CHD_E_DECODER_UNKNOWN, "chd_decoder_commit: unknown or unsupported decoder kind");
-    if (resolved != CHD_DEC_TRANSFORM_2D && resolved != CHD_DEC_TRANSFORM_3D)
-        return fail(CHD_E_UNSUPPORTED, "chd_decoder_commit: this library decodes CHD_DEC_TRANSFORM_2D and "
-                                       "CHD_DEC_TRANSFORM_3D only");
+    if (resolved != CHD_DEC_PAL_2D && resolved != CHD_DEC_TRANSFORM_2D && resolved != CHD_DEC_TRANSFORM_3D)
+        return fail(CHD_E_UNSUPPORTED, "chd_decoder_commit: this library decodes CHD_DEC_PAL_2D, "
+                                       "CHD_DEC_TRANSFORM_2D and CHD_DEC_TRANSFORM_3D only");
     // PalDecoder::configure (src/decoders/palcolour/pal_decoder.cpp:38-43)
     if (src.system != SYS_PAL && src.system != SYS_PAL_M) {
         log_returned(CHD_LOG_ERROR, "This decoder is for PAL video sources only");
         return fail(CHD_E_DECODER_INCOMPATIBLE, "chd_decoder_commit: This decoder is for PAL video sources only");
     }
-    // what the GPU path covers
+    // what the GPU path covers: the 625-line 4fsc raster
     if (src.system != SYS_PAL)
-        return fail(CHD_E_UNSUPPORTED, "chd_decoder_commit: the GPU Transform-PAL path decodes 625-line PAL only");
-    if (src.isSubcarrierLocked)
-        return fail(CHD_E_UNSUPPORTED, "chd_decoder_commit: subcarrier-locked captures are not decoded by the GPU path");
-    if (fmt != CHD_PIXEL_YUV444P16 && fmt != CHD_PIXEL_YUV444PS)
-        return fail(CHD_E_UNSUPPORTED, "chd_decoder_commit: the GPU path writes yuv444p16 and yuv444ps");
-    if (find_or(o.f64, CHD_OPT_LUMA_NR_LEVEL, 0.0) > 0.0)
-        return fail(CHD_E_UNSUPPORTED, "chd_decoder_commit: luma_nr_level > 0 is not implemented on the GPU path");
-    if (reverse)
-        return fail(CHD_E_UNSUPPORTED, "chd_decoder_commit: reverse_field_order is not implemented on the GPU path");
+        return fail(CHD_E_UNSUPPORTED, "chd_decoder_commit: the GPU path decodes 625-line PAL only");
     c.threshold = find_or(o.f64, CHD_OPT_TRANSFORM_THRESHOLD, c.threshold);
     c.chroma_gain = find_or(o.f64, CHD_OPT_CHROMA_GAIN, c.chroma_gain);
     c.chroma_phase_deg = find_or(o.f64, CHD_OPT_CHROMA_PHASE_DEG, c.chroma_phase_deg);
-    c.output_format = fmt == CHD_PIXEL_YUV444PS ? 1 : 0;
+    // doYNR runs only for yNRLevel > 0.0 (palcolour.cpp:644-646); anything else is off
+    c.y_nr_level = std::max(0.0, find_or(o.f64, CHD_OPT_LUMA_NR_LEVEL, 0.0));
+    c.output_format = (int32_t)fmt;   // chd_pixel_format_t 0..5 (4:4:0 was rejected above)
     std::vector<double> thr;
-    if (auto it = o.str.find(CHD_OPT_TRANSFORM_THRESHOLDS_FILE); it != o.str.end() && !it->second.empty()) {
+    if (auto it = o.str.find(CHD_OPT_TRANSFORM_THRESHOLDS_FILE);
+        resolved != CHD_DEC_PAL_2D && it != o.str.end() && !it->second.empty()) {
         thr = read_thresholds(it->second);
         const size_t need = resolved == CHD_DEC_TRANSFORM_2D ? 80 : 768;
         // TransformPal::updateConfiguration asserts this count (transform_pal.cpp:62-72)

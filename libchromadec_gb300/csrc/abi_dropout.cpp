@@ -36,7 +36,9 @@ chd_status_t collect(const chd_decoder_t *d, int64_t frame, chd_dropout_detect_m
     WindowField wf[2];
     d->video->cap.windowFrame((int)frame + 1, d->firstFieldFirst(), wf);
     const FieldMeta &m0 = d->video->cap.field(wf[0].fieldNumber);
-    const FieldMeta &m1 = d->video->cap.field(wf[1].fieldNumber);
+    FieldMeta m1 = d->video->cap.field(wf[1].fieldNumber);
+    // the spans of the fields as loaded: a shifted second field's dropouts moved too
+    if (second_field_shifted(d->video->cap.vp())) m1 = shift_dropouts(m1);
     spans = frame_spans(d->framing, m0, wf[0].isFirstField, m1, wf[1].isFirstField, mode == CHD_DROPOUT_OVERCORRECT);
     return CHD_OK;
 }

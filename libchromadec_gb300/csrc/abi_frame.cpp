@@ -1,8 +1,9 @@
 // abi_frame.cpp -- decoded-frame accessors of the chd_* ABI
 // (include/chromadec/frame.h; reference: src/abi/c_api_frame.cpp). Planes
 // are borrowed from the frame: yuv444p16 is [Y | Cb | Cr] with a row stride
-// of width * 2 bytes, yuv444ps three float planes; dropout masks are one
-// GRAY16 or GRAYS plane.
+// of width * 2 bytes, yuv444ps and rgbs three float planes, rgb48 packed
+// R'G'B' (row pitch width * 6 bytes); gray16 / grays frames and dropout
+// masks are one plane.
 #include "abi_handles.h"
 #include "error_state.h"
 
@@ -92,6 +93,16 @@ CHD_API chd_status_t chd_frame_get_plane(const chd_frame_t *f, chd_plane_t plane
         *out_data = base;
         *out_stride_bytes = (ptrdiff_t)f->width * 2;
         return CHD_OK;
+    case CHD_PIXEL_RGB48:
+        // packed R'G'B': the three accessors share the row pitch, offset 0/1/2 samples
+        switch (plane) {
+        case CHD_PLANE_R: *out_data = base; break;
+        case CHD_PLANE_G: *out_data = base + 1; break;
+        case CHD_PLANE_B: *out_data = base + 2; break;
+        default: return fail(CHD_E_INVALID_ARG, "chd_frame_get_plane: plane not valid for RGB48");
+        }
+        *out_stride_bytes = (ptrdiff_t)f->width * 3 * 2;
+        return CHD_OK;
     default:
         if (is_float(f->format))
             return fail(CHD_E_INVALID_ARG, "chd_frame_get_plane: use chd_frame_get_plane_float for float pixel formats");
@@ -110,12 +121,21 @@ CHD_API chd_status_t chd_frame_get_plane_float(const chd_frame_t *f, chd_plane_t
     if (f->format == CHD_PIXEL_GRAYS && plane != CHD_PLANE_Y)
         return fail(CHD_E_INVALID_ARG, "chd_frame_get_plane_float: CHD_PIXEL_GRAYS only has CHD_PLANE_Y");
     int idx;
-    switch (plane) {
-    case CHD_PLANE_Y: idx = 0; break;
-    case CHD_PLANE_CB: idx = 1; break;
-    case CHD_PLANE_CR: idx = 2; break;
-    default:
-        return fail(CHD_E_INVALID_ARG, "chd_frame_get_plane_float: Y'CbCr float frame plane must be Y, Cb, or Cr");
+    if (f->format == CHD_PIXEL_RGBS) {
+        switch (plane) {
+        case CHD_PLANE_R: idx = 0; break;
+        case CHD_PLANE_G: idx = 1; break;
+        case CHD_PLANE_B: idx = 2; break;
+        default: return fail(CHD_E_INVALID_ARG, "chd_frame_get_plane_float: CHD_PIXEL_RGBS plane must be R, G, or B");
+        }
+    } else {
+        switch (plane) {
+        case CHD_PLANE_Y: idx = 0; break;
+        case CHD_PLANE_CB: idx = 1; break;
+        case CHD_PLANE_CR: idx = 2; break;
+        default:
+            return fail(CHD_E_INVALID_ARG, "chd_frame_get_plane_float: Y'CbCr float frame plane must be Y, Cb, or Cr");
+        }
     }
     *out_data = static_cast<const float *>(f->pixels) + (size_t)idx * f->width * f->height;
     *out_stride_bytes = (ptrdiff_t)f->width * (ptrdiff_t)sizeof(float);

@@ -18,6 +18,15 @@
 //  * Y = composite - chroma, the rotated U/V and the output scaling are fused;
 //    planes are written straight into the frame's [Y | Cb | Cr] layout.
 //
+//  * CHD_DEC_PAL_2D (partial == NULL): the same 2D FIR runs on the composite
+//    rows themselves (decodeLine<uint16_t, false>) and luma is the composite
+//    minus the chroma the Y filter extracts, resynthesised on the carrier.
+//  * luma_nr_level > 0: doYNR (palcolour.cpp:412-449) -- the 25-tap
+//    high-pass of each line's luma, cored to +-nr_y and subtracted -- after a
+//    pre-pass that puts the block's luma lines in shared memory.
+//  * Every output format of the ABI is packed here: yuv444p16/ps, rgb48
+//    (interleaved, truncating), rgbs, gray16, grays.
+//
 // One block: 8 field lines of one output field, 256 threads; a work item
 // produces 8 consecutive samples of one line from a register window of the
 // four vertically combined chroma rows.
@@ -30,16 +39,131 @@
 namespace tpal {
 
 __constant__ float cd_cfilt[8][4];   // PALcolour chroma 2D FIR taps (filterSize = 7)
+__constant__ float cd_yfilt[8][2];   // PALcolour luma-extraction taps
+__constant__ float cd_nrpal[25];     // doYNR high-pass (c_nrpal_b)
 static bool g_demod_ready[64];
 
 constexpr int kDemodLines = 8;
 constexpr int kDemodThreads = 256;
 constexpr int kPad = 8;
 constexpr int kRows = kDemodLines + 6;   // chroma lines fl0-3 .. fl0+L+2
+constexpr int kNrHalf = 12;              // half length of the yNR filter
 
 __device__ __forceinline__ int first_line(int fafl, int off) { return (fafl + 1 - off) / 2; }
 __device__ __forceinline__ int last_line(int lafl, int off) { return ((lafl - off) / 2) + 1; }
 
+__host__ __device__ __forceinline__ int demod_span(int avs, int ave) { return ((ave - (avs & ~3)) + 7) & ~7; }
+
+// 4fsc reference carrier at sample x: sine {0, 1, 0, -1}, cosine {1, 0, -1, 0}.
+__device__ __forceinline__ float carrier_sin(int x) { return (x & 1) ? ((x & 2) ? -1.f : 1.f) : 0.f; }
+__device__ __forceinline__ float carrier_cos(int x) { return (x & 1) ? 0.f : ((x & 2) ? -1.f : 1.f); }
+
+// The 2D FIR of one work item: PU, QU, PV, QV (and PY, QY from the luma
+// taps when WITH_Y) for 8 samples from the 4 vertical combinations v.
+template <bool WITH_Y>
+__device__ __forceinline__ void item_fir(const float (&v)[4][22], float (&PU)[8], float (&QU)[8], float (&PV)[8],
+                                         float (&QV)[8], float (&PY)[8], float (&QY)[8])
+{
+#pragma unroll
+    for (int s = 0; s < 8; s++) {
+        float PA = 0.f, PB = 0.f, QA = 0.f, QB = 0.f, PYs = 0.f, QYs = 0.f;
+#pragma unroll
+        for (int b = 0; b < 8; b++) {
+            const int r = s + b + 7, l = s - b + 7;
+            float sg[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) sg[k] = (b & 1) ? v[k][r] - v[k][l] : v[k][r] + v[k][l];
+            const float A = __fmaf_rn(cd_cfilt[b][1], sg[1], cd_cfilt[b][0] * sg[0]);
+            const float B = __fmaf_rn(cd_cfilt[b][3], sg[3], cd_cfilt[b][2] * sg[2]);
+            float AY = 0.f;
+            if (WITH_Y) AY = __fmaf_rn(cd_yfilt[b][1], sg[1], cd_yfilt[b][0] * sg[0]);
+            switch ((s + b) & 3) {
+            case 1: PA += A; PB += B; if (WITH_Y) PYs += AY; break;
+            case 3: PA -= A; PB -= B; if (WITH_Y) PYs -= AY; break;
+            case 0: QA += A; QB += B; if (WITH_Y) QYs += AY; break;
+            default: QA -= A; QB -= B; if (WITH_Y) QYs -= AY; break;
+            }
+        }
+        PU[s] = PA + QB;
+        PV[s] = PA - QB;
+        QU[s] = QA - PB;
+        QV[s] = QA + PB;
+        PY[s] = PYs;
+        QY[s] = QYs;
+    }
+}
+
+// Vertical combinations (palcolour.cpp:557-567 without the carrier):
+//   v0 = c0, v1 = -c(-2) - c(+2), v2 = c(-1) - c(+1), v3 = -c(-3) + c(+3)
+__device__ __forceinline__ void item_window(const float *rw, int SW, float (&v)[4][22])
+{
+#pragma unroll
+    for (int q = 0; q < 22; q++) {
+        v[0][q] = rw[3 * SW + q];
+        v[1][q] = -rw[1 * SW + q] - rw[5 * SW + q];
+        v[2][q] = rw[2 * SW + q] - rw[4 * SW + q];
+        v[3][q] = -rw[q] + rw[6 * SW + q];
+    }
+}
+
+// H.273 Round(x) = Sign(x) * Floor(Abs(x) + 0.5) then clamp (output_writer.cpp:60-76)
+__device__ __forceinline__ uint16_t h273q(float x, float lo, float hi)
+{
+    const float r = copysignf(floorf(fabsf(x) + 0.5f), x);
+    return (uint16_t)fminf(fmaxf(r, lo), hi);
+}
+
+// Pack one sample in the output format (OutputWriter::convertLine,
+// convertToFloat, convertToFloatRGB; output_writer.cpp:402-486, 670-779).
+__device__ __forceinline__ void pack_sample(const DemodParams &P, long long frame, long long pix, float Y, float U,
+                                            float V)
+{
+    const long long plane = (long long)P.out_w * P.out_h;
+    const long long e = frame * P.out_frame_stride + pix;
+    const float ey = (Y - (float)P.black) * P.ey_scale;
+    switch (P.format) {
+    case 0: {
+        uint16_t *o = (uint16_t *)P.out;
+        o[e] = h273q(__fmaf_rn(219.0f * 256.0f, ey, 16.0f * 256.0f), P.y_lo, P.y_hi);
+        o[e + plane] = h273q(__fmaf_rn(224.0f * 256.0f, U * P.ecb_scale, 128.0f * 256.0f), P.c_lo, P.c_hi);
+        o[e + 2 * plane] = h273q(__fmaf_rn(224.0f * 256.0f, V * P.ecr_scale, 128.0f * 256.0f), P.c_lo, P.c_hi);
+        break;
+    }
+    case 1: {
+        float *o = (float *)P.out;
+        o[e] = fminf(fmaxf(ey, P.y_lo), P.y_hi);
+        o[e + plane] = fminf(fmaxf(U * P.ecb_scale, P.c_lo), P.c_hi);
+        o[e + 2 * plane] = fminf(fmaxf(V * P.ecr_scale, P.c_lo), P.c_hi);
+        break;
+    }
+    case 2: {   // interleaved R'G'B' 0..65535, truncating stores
+        uint16_t *o = (uint16_t *)P.out + frame * P.out_frame_stride + 3 * pix;
+        const float rY = fminf(fmaxf((Y - (float)P.black) * P.rgb_y_scale, 0.f), 65535.f);
+        const float rU = U * P.rgb_uv_scale, rV = V * P.rgb_uv_scale;
+        o[0] = (uint16_t)__float2uint_rz(fminf(fmaxf(__fmaf_rn(P.r_from_v, rV, rY), 0.f), 65535.f));
+        o[1] = (uint16_t)__float2uint_rz(
+            fminf(fmaxf(__fmaf_rn(P.g_from_v, rV, __fmaf_rn(P.g_from_u, rU, rY)), 0.f), 65535.f));
+        o[2] = (uint16_t)__float2uint_rz(fminf(fmaxf(__fmaf_rn(P.b_from_u, rU, rY), 0.f), 65535.f));
+        break;
+    }
+    case 3: {
+        float *o = (float *)P.out;
+        const float rU = U * P.rgb_uv_scale, rV = V * P.rgb_uv_scale;
+        o[e] = fminf(fmaxf(__fmaf_rn(P.r_from_v, rV, ey), P.r_lo), P.r_hi);
+        o[e + plane] = fminf(fmaxf(__fmaf_rn(P.g_from_v, rV, __fmaf_rn(P.g_from_u, rU, ey)), P.g_lo), P.g_hi);
+        o[e + 2 * plane] = fminf(fmaxf(__fmaf_rn(P.b_from_u, rU, ey), P.b_lo), P.b_hi);
+        break;
+    }
+    case 4:
+        ((uint16_t *)P.out)[e] = h273q(__fmaf_rn(219.0f * 256.0f, ey, 16.0f * 256.0f), P.y_lo, P.y_hi);
+        break;
+    default:
+        ((float *)P.out)[e] = fminf(fmaxf(ey, P.y_lo), P.y_hi);
+        break;
+    }
+}
+
+template <bool COMPOSITE, bool YNR>
 __global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
 {
     extern __shared__ float smem[];
@@ -48,52 +172,69 @@ __global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
     const int blk = blockIdx.x % nblk_per_field;
     if (o >= P.nout) return;
     const int f = P.field_begin + o;
-    const int off = f & 1;
+    const int off = (f & 1) ^ P.swap;   // SourceField::getOffset
     const int fl_first = first_line(P.fafl, off);
     const int fl_last = last_line(P.lafl, off);
     const int fl0 = fl_first + blk * kDemodLines;
     if (fl0 >= fl_last) return;
 
     const int base4 = P.avs & ~3;                     // absolute sample of local index 0
-    const int span = ((P.ave - base4) + 7) & ~7;      // samples covered by threads (multiple of 8)
+    const int span = demod_span(P.avs, P.ave);        // samples covered by threads (multiple of 8)
     const int SW = span + 2 * kPad;                   // smem row length
-    float *ch = smem;                                  // [kRows][SW] chroma rows fl0-3 .. fl0+L+2
+    const int YW = span + 2 * kNrHalf;                // luma line length (yNR)
+    float *ch = smem;                                  // [kRows][SW] rows fl0-3 .. fl0+L+2
+    float *ys = smem + kRows * SW;                     // [kDemodLines][YW] luma before coring (yNR only)
     __shared__ float s_bp[kDemodLines], s_bq[kDemodLines], s_vsw[kDemodLines];
 
     const uint16_t *field = P.fields + (long long)(f - P.field_base) * P.field_stride;
-    const float *part = P.partial + (long long)o * P.part_field_stride;
     const int cols = P.ave - P.avs;
 
-    // 1. chroma rows = sum of the overlap-class planes; zero outside the
-    //    field's active lines and the active window (zero halo included).
+    // 1. input rows, zero outside the field's active lines: the summed
+    //    overlap-class chroma planes (zero outside the active window, the
+    //    reference's zero-initialised chroma buffer), or the composite
+    //    itself for the PALcolour filter (blackLine = 0, palcolour.cpp:466-473).
     for (int idx = threadIdx.x; idx < kRows * SW; idx += blockDim.x) ch[idx] = 0.f;
+    if (YNR)
+        for (int idx = threadIdx.x; idx < kDemodLines * YW; idx += blockDim.x) ys[idx] = 0.f;
     __syncthreads();
-    const int c4 = cols >> 2;   // float4 per row (cols is a multiple of 4 when avs is)
-    const bool vec = ((cols & 3) == 0) && ((P.part_row_stride & 3) == 0) && ((P.part_class_stride & 3) == 0) &&
-                     ((P.part_field_stride & 3) == 0);
-    if (vec) {
-        for (int idx = threadIdx.x; idx < kRows * c4; idx += blockDim.x) {
-            const int r = idx / c4, q = idx % c4;
+    if (COMPOSITE) {
+        for (int idx = threadIdx.x; idx < kRows * SW; idx += blockDim.x) {
+            const int r = idx / SW, c = idx % SW;
             const int fl = fl0 - 3 + r;
-            if (fl < fl_first || fl >= fl_last) continue;
-            const float4 *src = reinterpret_cast<const float4 *>(part + (long long)(fl - P.fl_lo) * P.part_row_stride) + q;
-            const long long cs4 = P.part_class_stride >> 2;
-            float4 a = __ldg(src), b = __ldg(src + cs4), c = __ldg(src + 2 * cs4), d = __ldg(src + 3 * cs4);
-            float *dst = ch + r * SW + kPad + (P.avs - base4) + 4 * q;
-            dst[0] = (a.x + b.x) + (c.x + d.x);
-            dst[1] = (a.y + b.y) + (c.y + d.y);
-            dst[2] = (a.z + b.z) + (c.z + d.z);
-            dst[3] = (a.w + b.w) + (c.w + d.w);
+            const int x = base4 - kPad + c;
+            if (fl < fl_first || fl >= fl_last || x < 0 || x >= P.fw) continue;
+            ch[idx] = (float)field[(long long)fl * P.fw + x];
         }
     } else {
-        for (int idx = threadIdx.x; idx < kRows * cols; idx += blockDim.x) {
-            const int r = idx / cols, c = idx % cols;
-            const int fl = fl0 - 3 + r;
-            if (fl < fl_first || fl >= fl_last) continue;
-            const long long e = (long long)(fl - P.fl_lo) * P.part_row_stride + c;
-            float v = 0.f;
-            for (int k = 0; k < P.nclasses; k++) v += part[(long long)k * P.part_class_stride + e];
-            ch[r * SW + kPad + (P.avs - base4) + c] = v;
+        const float *part = P.partial + (long long)o * P.part_field_stride;
+        const int c4 = cols >> 2;   // float4 per row (cols is a multiple of 4 when avs is)
+        const bool vec = ((cols & 3) == 0) && ((P.part_row_stride & 3) == 0) && ((P.part_class_stride & 3) == 0) &&
+                         ((P.part_field_stride & 3) == 0);
+        if (vec) {
+            for (int idx = threadIdx.x; idx < kRows * c4; idx += blockDim.x) {
+                const int r = idx / c4, q = idx % c4;
+                const int fl = fl0 - 3 + r;
+                if (fl < fl_first || fl >= fl_last) continue;
+                const float4 *src =
+                    reinterpret_cast<const float4 *>(part + (long long)(fl - P.fl_lo) * P.part_row_stride) + q;
+                const long long cs4 = P.part_class_stride >> 2;
+                float4 a = __ldg(src), b = __ldg(src + cs4), c = __ldg(src + 2 * cs4), d = __ldg(src + 3 * cs4);
+                float *dst = ch + r * SW + kPad + (P.avs - base4) + 4 * q;
+                dst[0] = (a.x + b.x) + (c.x + d.x);
+                dst[1] = (a.y + b.y) + (c.y + d.y);
+                dst[2] = (a.z + b.z) + (c.z + d.z);
+                dst[3] = (a.w + b.w) + (c.w + d.w);
+            }
+        } else {
+            for (int idx = threadIdx.x; idx < kRows * cols; idx += blockDim.x) {
+                const int r = idx / cols, c = idx % cols;
+                const int fl = fl0 - 3 + r;
+                if (fl < fl_first || fl >= fl_last) continue;
+                const long long e = (long long)(fl - P.fl_lo) * P.part_row_stride + c;
+                float v = 0.f;
+                for (int k = 0; k < P.nclasses; k++) v += part[(long long)k * P.part_class_stride + e];
+                ch[r * SW + kPad + (P.avs - base4) + c] = v;
+            }
         }
     }
 
@@ -140,84 +281,82 @@ __global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
     }
     __syncthreads();
 
-    // 3. 2D FIR + rotation + pack; work item = (line, 8-sample segment)
     const int per_line = span / 8;
-    const long long plane = (long long)P.out_w * P.out_h;
     const long long frame = o >> 1;   // field_begin is even: fields 2k, 2k+1 form frame k
+
+    // 3. yNR pre-pass: the block's luma lines (zero outside the active window)
+    if (YNR) {
+        for (int item = threadIdx.x; item < kDemodLines * per_line; item += blockDim.x) {
+            const int t = item / per_line, seg = item % per_line;
+            const int fl = fl0 + t;
+            if (fl >= fl_last) continue;
+            const int xl0 = seg * 8;
+            const uint16_t *comp = field + (long long)fl * P.fw;
+            float Yv[8];
+            if (COMPOSITE) {
+                float v[4][22];
+                item_window(ch + t * SW + kPad + xl0 - 7, SW, v);
+                float PU[8], QU[8], PV[8], QV[8], PY[8], QY[8];
+                item_fir<true>(v, PU, QU, PV, QV, PY, QY);
+#pragma unroll
+                for (int s = 0; s < 8; s++) {
+                    const int x = base4 + xl0 + s;
+                    Yv[s] = (float)comp[x < P.fw ? x : P.fw - 1] -
+                            2.0f * __fmaf_rn(PY[s], carrier_sin(x), QY[s] * carrier_cos(x));
+                }
+            } else {
+#pragma unroll
+                for (int s = 0; s < 8; s++) {
+                    const int x = base4 + xl0 + s;
+                    Yv[s] = (float)comp[x < P.fw ? x : P.fw - 1] - ch[(t + 3) * SW + kPad + xl0 + s];
+                }
+            }
+#pragma unroll
+            for (int s = 0; s < 8; s++) {
+                const int x = base4 + xl0 + s;
+                if (x >= P.avs && x < P.ave) ys[t * YW + kNrHalf + xl0 + s] = Yv[s];
+            }
+        }
+        __syncthreads();
+    }
+
+    // 4. 2D FIR + rotation + pack; work item = (line, 8-sample segment)
     for (int item = threadIdx.x; item < kDemodLines * per_line; item += blockDim.x) {
         const int t = item / per_line;
         const int seg = item % per_line;
         const int fl = fl0 + t;
         if (fl >= fl_last) continue;
         const int xl0 = seg * 8;   // local index of the first sample (absolute base4 + xl0, a multiple of 4)
-        // vertical combinations (palcolour.cpp:557-567 without the carrier):
-        //   v0 = c0, v1 = -c(-2) - c(+2), v2 = c(-1) - c(+1), v3 = -c(-3) + c(+3)
         float v[4][22];
-        const float *rw = ch + t * SW + kPad + xl0 - 7;
-#pragma unroll
-        for (int q = 0; q < 22; q++) {
-            v[0][q] = rw[3 * SW + q];
-            v[1][q] = -rw[1 * SW + q] - rw[5 * SW + q];
-            v[2][q] = rw[2 * SW + q] - rw[4 * SW + q];
-            v[3][q] = -rw[q] + rw[6 * SW + q];
-        }
-        float PU[8], QU[8], PV[8], QV[8];
-#pragma unroll
-        for (int s = 0; s < 8; s++) {
-            float PA = 0.f, PB = 0.f, QA = 0.f, QB = 0.f;
-#pragma unroll
-            for (int b = 0; b < 8; b++) {
-                const int r = s + b + 7, l = s - b + 7;
-                float sg[4];
-#pragma unroll
-                for (int k = 0; k < 4; k++) sg[k] = (b & 1) ? v[k][r] - v[k][l] : v[k][r] + v[k][l];
-                const float A = __fmaf_rn(cd_cfilt[b][1], sg[1], cd_cfilt[b][0] * sg[0]);
-                const float B = __fmaf_rn(cd_cfilt[b][3], sg[3], cd_cfilt[b][2] * sg[2]);
-                switch ((s + b) & 3) {
-                case 1: PA += A; PB += B; break;
-                case 3: PA -= A; PB -= B; break;
-                case 0: QA += A; QB += B; break;
-                default: QA -= A; QB -= B; break;
-                }
-            }
-            PU[s] = PA + QB;
-            PV[s] = PA - QB;
-            QU[s] = QA - PB;
-            QV[s] = QA + PB;
-        }
+        item_window(ch + t * SW + kPad + xl0 - 7, SW, v);
+        float PU[8], QU[8], PV[8], QV[8], PY[8], QY[8];
+        item_fir<COMPOSITE && !YNR>(v, PU, QU, PV, QV, PY, QY);
 
         const float bp = s_bp[t], bq = s_bq[t], vsw = s_vsw[t];
         const int orow = P.top_pad + 2 * fl + off - P.fafl;
-        const long long rowbase = frame * P.out_frame_stride + (long long)orow * P.out_w + P.left_pad;
+        const long long rowpix = (long long)orow * P.out_w + P.left_pad;
         const uint16_t *comp = field + (long long)fl * P.fw;
 #pragma unroll
         for (int s = 0; s < 8; s++) {
             const int x = base4 + xl0 + s;
             if (x < P.avs || x >= P.ave) continue;
-            const float c0 = v[0][s + 7];
-            const float Y = (float)comp[x] - c0;
+            float Y;
+            if (YNR) {
+                // doYNR: a = sum_i b_i Y[x + 12 - i], cored to +-nr_y, subtracted
+                const float *yl = ys + t * YW + kNrHalf + xl0 + s;
+                float a = 0.f;
+#pragma unroll
+                for (int i = 0; i < 25; i++) a = __fmaf_rn(cd_nrpal[i], yl[kNrHalf - i], a);
+                a = fminf(fmaxf(a, -P.nr_y), P.nr_y);
+                Y = yl[0] - a;
+            } else if (COMPOSITE) {
+                Y = (float)comp[x] - 2.0f * __fmaf_rn(PY[s], carrier_sin(x), QY[s] * carrier_cos(x));
+            } else {
+                Y = (float)comp[x] - v[0][s + 7];
+            }
             const float U = -(PU[s] * bp + QU[s] * bq) * 2.0f;
             const float V = vsw * -(QV[s] * bp - PV[s] * bq) * 2.0f;
-            const float ey = (Y - (float)P.black) * P.ey_scale;
-            const float ecb = U * P.ecb_scale;
-            const float ecr = V * P.ecr_scale;
-            const long long e = rowbase + (x - P.avs);
-            if (P.format == 1) {
-                float *out = (float *)P.out;
-                out[e] = fminf(fmaxf(ey, P.y_lo), P.y_hi);
-                out[e + plane] = fminf(fmaxf(ecb, P.c_lo), P.c_hi);
-                out[e + 2 * plane] = fminf(fmaxf(ecr, P.c_lo), P.c_hi);
-            } else {
-                uint16_t *out = (uint16_t *)P.out;
-                // H.273 Round(x) = Sign(x) * Floor(Abs(x) + 0.5), output_writer.cpp:60-76
-                auto q = [](float x, float lo, float hi) -> uint16_t {
-                    const float r = copysignf(floorf(fabsf(x) + 0.5f), x);
-                    return (uint16_t)fminf(fmaxf(r, lo), hi);
-                };
-                out[e] = q(__fmaf_rn(219.0f * 256.0f, ey, 16.0f * 256.0f), P.y_lo, P.y_hi);
-                out[e + plane] = q(__fmaf_rn(224.0f * 256.0f, ecb, 128.0f * 256.0f), P.c_lo, P.c_hi);
-                out[e + 2 * plane] = q(__fmaf_rn(224.0f * 256.0f, ecr, 128.0f * 256.0f), P.c_lo, P.c_hi);
-            }
+            pack_sample(P, frame, rowpix + (x - P.avs), Y, U, V);
         }
     }
 }
@@ -231,8 +370,8 @@ int demod_init_constants(int device, double sample_rate, int /*field_width*/)
     int fs = 1;
     if ((int)ca > fs) fs = (int)ca;
     if (fs != 7) return -2;   // the kernel's tap count is fixed for 4fsc PAL
-    double cf[8][4] = {};
-    double cdiv = 0;
+    double cf[8][4] = {}, yf[8][2] = {};
+    double cdiv = 0, ydiv = 0;
     for (int f = 0; f <= fs; f++) {
         const double fc = std::min(ca, (double)f);
         const double ff = std::min(ca, sqrt((double)(f * f + 4)));
@@ -244,42 +383,77 @@ int demod_init_constants(int device, double sample_rate, int /*field_width*/)
         cf[f][1] = (1 + cos(M_PI * fff / ca)) / d;
         cf[f][3] = (1 + cos(M_PI * ffff / ca)) / d;
         cdiv += 2 * (1 * cf[f][0] + 2 * cf[f][2] + 2 * cf[f][1] + 2 * cf[f][3]);
+        // luma-extraction taps (ya = ca at this bandwidth)
+        const double fy = std::min(ca, (double)f);
+        const double fffy = std::min(ca, sqrt((double)(f * f + 16)));
+        yf[f][0] = (1 + cos(M_PI * fy / ca)) / d;
+        yf[f][1] = 0.2 * (1 + cos(M_PI * fffy / ca)) / d;
+        ydiv += 2 * (1 * yf[f][0] + 2 * yf[f][1]);
     }
-    float cff[8][4];
-    for (int f = 0; f < 8; f++)
+    float cff[8][4], yff[8][2];
+    for (int f = 0; f < 8; f++) {
         for (int i = 0; i < 4; i++) cff[f][i] = (float)(cf[f][i] / cdiv);
+        for (int i = 0; i < 2; i++) yff[f][i] = (float)(yf[f][i] / ydiv);
+    }
+    // c_nrpal_b, src/decoders/filter/deemp.h:620-628
+    static const double nrpal[25] = {
+        1.141291975113614e-04, -1.857019211291029e-03, -4.499636864042073e-03, -5.577680979937061e-03,
+        -4.423694440267179e-04, 1.309163063177155e-02, 2.861211356202848e-02, 3.029931283148555e-02,
+        1.098965697652802e-03, -6.398130386469833e-02, -1.492080690537196e-01, -2.223459379380252e-01,
+        7.479077367478024e-01, -2.223459379380252e-01, -1.492080690537196e-01, -6.398130386469833e-02,
+        1.098965697652803e-03, 3.029931283148557e-02, 2.861211356202848e-02, 1.309163063177156e-02,
+        -4.423694440267185e-04, -5.577680979937061e-03, -4.499636864042074e-03, -1.857019211291030e-03,
+        1.141291975113614e-04};
+    float nrf[25];
+    for (int i = 0; i < 25; i++) nrf[i] = (float)nrpal[i];
     if (cudaMemcpyToSymbol(cd_cfilt, cff, sizeof(cff)) != cudaSuccess) return -1;
+    if (cudaMemcpyToSymbol(cd_yfilt, yff, sizeof(yff)) != cudaSuccess) return -1;
+    if (cudaMemcpyToSymbol(cd_nrpal, nrf, sizeof(nrf)) != cudaSuccess) return -1;
     if (device >= 0 && device < 64) g_demod_ready[device] = true;
     return 0;
 }
 
-size_t demod_smem_bytes(int avs, int ave)
+size_t demod_smem_bytes(int avs, int ave, bool ynr)
 {
-    const int base4 = avs & ~3;
-    const int span = ((ave - base4) + 7) & ~7;
-    const int SW = span + 2 * kPad;
-    return sizeof(float) * (size_t)kRows * SW;
+    const int span = demod_span(avs, ave);
+    const size_t rows = sizeof(float) * (size_t)kRows * (span + 2 * kPad);
+    return rows + (ynr ? sizeof(float) * (size_t)kDemodLines * (span + 2 * kNrHalf) : 0);
 }
 
 int demod_launch(const DemodParams &P, cudaStream_t stream)
 {
     if (P.nout <= 0) return 0;
-    const int base4 = P.avs & ~3;
-    const int span = ((P.ave - base4) + 7) & ~7;
-    const size_t smem = demod_smem_bytes(P.avs, P.ave);
+    const bool composite = P.partial == nullptr;
+    const bool ynr = P.nr_y > 0.f;
+    const size_t smem = demod_smem_bytes(P.avs, P.ave, ynr);
+    if (smem > 110 * 1024) return -1;   // two blocks per SM
     // function attributes are per device
     static bool attr_set[64] = {};
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64) return -1;
     if (!attr_set[dev]) {
-        if (cudaFuncSetAttribute(demod_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) !=
-            cudaSuccess)
+        const int lim = 110 * 1024;
+        if (cudaFuncSetAttribute(demod_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(demod_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(demod_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(demod_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim) !=
+                cudaSuccess)
             return -1;
         attr_set[dev] = true;
     }
     const int nblk_per_field = (P.fh + kDemodLines - 1) / kDemodLines;
-    demod_kernel<<<(unsigned)(P.nout * nblk_per_field), kDemodThreads, smem, stream>>>(P);
+    const dim3 grid((unsigned)(P.nout * nblk_per_field));
+    if (composite) {
+        if (ynr) demod_kernel<true, true><<<grid, kDemodThreads, smem, stream>>>(P);
+        else demod_kernel<true, false><<<grid, kDemodThreads, smem, stream>>>(P);
+    } else {
+        if (ynr) demod_kernel<false, true><<<grid, kDemodThreads, smem, stream>>>(P);
+        else demod_kernel<false, false><<<grid, kDemodThreads, smem, stream>>>(P);
+    }
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -179,6 +179,22 @@ void plan_field(const VideoParams &vp, const std::vector<DLoc> &thisD, const std
 
 }  // namespace
 
+bool second_field_shifted(const VideoParams &vp)
+{
+    return (vp.system == SYS_PAL || vp.system == SYS_PAL_M) && vp.isSubcarrierLocked;
+}
+
+FieldMeta shift_dropouts(const FieldMeta &f)
+{
+    FieldMeta out = f;
+    out.dropouts.clear();
+    for (const Dropout &d : f.dropouts) {
+        const int32_t endx = d.endx - 2;
+        if (endx > 0) out.dropouts.push_back({std::max(d.startx - 2, 0), endx, d.fieldLine});
+    }
+    return out;
+}
+
 FramePlan plan_frame(const VideoParams &vp, const FieldMeta &slot0, const FieldMeta &slot1, bool overcorrect,
                      bool intraField)
 {

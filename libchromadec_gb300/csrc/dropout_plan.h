@@ -29,6 +29,14 @@ struct FramePlan {
     int64_t totalDistance = 0;
 };
 
+// SourceField::secondFieldIsShifted (src/decoders/source_field.cpp:45-49):
+// subcarrier-locked PAL and PAL-M captures store the second field of each
+// window frame 2 samples late.
+bool second_field_shifted(const VideoParams &vp);
+// shiftSecondField's dropout move (source_field.cpp:59-65): 2 samples left,
+// dropped when they end at or before sample 0.
+FieldMeta shift_dropouts(const FieldMeta &f);
+
 // DropoutCorrector::correctFrame, single source
 // (src/dropout/dropout_corrector.cpp:40-530). slot0/slot1 are the frame's
 // fields in window order.

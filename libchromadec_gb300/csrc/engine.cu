@@ -17,7 +17,6 @@
 #include "tpal_kernels.h"
 
 namespace tpal {
-size_t demod_smem_bytes(int avs, int ave);
 }
 
 namespace chdg {
@@ -80,7 +79,8 @@ int Engine::init(const chdg_geometry &g, const chdg_config &c)
 {
     g_ = g;
     c_ = c;
-    if (c.kind != 7 && c.kind != 8) return arg_fail("kind must be CHD_DEC_TRANSFORM_2D (7) or CHD_DEC_TRANSFORM_3D (8)");
+    if (c.kind != 6 && c.kind != 7 && c.kind != 8)
+        return arg_fail("kind must be CHD_DEC_PAL_2D (6), CHD_DEC_TRANSFORM_2D (7) or CHD_DEC_TRANSFORM_3D (8)");
     if (g.field_width <= 0 || g.field_height <= 0 || g.active_start < 0 || g.active_end > g.field_width ||
         g.active_end <= g.active_start || g.first_active_frame_line < 0 ||
         g.last_active_frame_line >= 2 * g.field_height - 1 || g.last_active_frame_line < g.first_active_frame_line)
@@ -90,9 +90,12 @@ int Engine::init(const chdg_geometry &g, const chdg_config &c)
     if (g.active_start - 7 < 0 || g.active_end + 8 > 1135 || g.field_width > 1135)
         return chd::detail::set_last_error("chromadec_gb300: active window too close to the line ends"),
                CHDG_E_UNSUPPORTED;
-    if (c.output_format != 0 && c.output_format != 1) return arg_fail("output_format must be 0 or 1");
+    if (c.output_format < 0 || c.output_format > 5) return arg_fail("output_format must be 0..5");
     if (c.padding_multiple < 1 || c.padding_multiple > 1024) return arg_fail("padding_multiple out of range");
+    if (c.first_field_offset != 0 && c.first_field_offset != 1) return arg_fail("first_field_offset must be 0 or 1");
+    if (!(c.y_nr_level >= 0.0)) return arg_fail("y_nr_level must be >= 0");
     const int nthr = (c.kind == 7) ? 80 : 768;
+    if (c.kind == 6 && c.thresholds != nullptr) return arg_fail("CHD_DEC_PAL_2D takes no thresholds");
     if (c.thresholds != nullptr && c.n_thresholds != nthr)
         return arg_fail("thresholds table must have " + std::to_string(nthr) + " entries");
 
@@ -100,7 +103,7 @@ int Engine::init(const chdg_geometry &g, const chdg_config &c)
     if (e != cudaSuccess) return cuda_fail("cudaGetDevice", e);
     if (c.kind == 8) {
         if (tpal::tp3_init_constants(device_) != 0) return cuda_fail("3D constants", cudaGetLastError());
-    } else {
+    } else if (c.kind == 7) {
         if (tpal::tp2_init_constants(device_) != 0) return cuda_fail("2D constants", cudaGetLastError());
     }
     if (const int rc = tpal::demod_init_constants(device_, g.sample_rate, g.field_width); rc != 0)
@@ -150,8 +153,10 @@ int Engine::init_static(const chdg_geometry &g, const chdg_config &c, float *thr
     if (g.active_start - 7 < 0 || g.active_end + 8 > 1135 || g.field_width > 1135)
         return chd::detail::set_last_error("chromadec_gb300: active window too close to the line ends"),
                CHDG_E_UNSUPPORTED;
-    if (c.output_format != 0 && c.output_format != 1) return arg_fail("output_format must be 0 or 1");
+    if (c.output_format < 0 || c.output_format > 5) return arg_fail("output_format must be 0..5");
     if (c.padding_multiple < 1 || c.padding_multiple > 1024) return arg_fail("padding_multiple out of range");
+    if (c.first_field_offset != 0 && c.first_field_offset != 1) return arg_fail("first_field_offset must be 0 or 1");
+    if (!(c.y_nr_level >= 0.0)) return arg_fail("y_nr_level must be >= 0");
     if (c.thresholds != nullptr && c.n_thresholds != 768) return arg_fail("thresholds table must have 768 entries");
     cudaError_t e = cudaGetDevice(&device_);
     if (e != cudaSuccess) return cuda_fail("cudaGetDevice", e);
@@ -207,9 +212,14 @@ int Engine::decode_scratch(const uint16_t *fields, long long stride, int nfields
     return run_demod(fields, stride, 0, fb, fe, scratch, out, s);
 }
 
+// Elements per output frame and their size: three planes (or interleaved
+// R'G'B') except the gray formats; float for yuv444ps, rgbs and grays.
+static size_t format_planes(int fmt) { return (fmt == 4 || fmt == 5) ? 1 : 3; }
+static size_t format_elem(int fmt) { return (fmt == 1 || fmt == 3 || fmt == 5) ? sizeof(float) : sizeof(uint16_t); }
+
 size_t Engine::frame_bytes() const
 {
-    return (size_t)out_w_ * out_h_ * 3 * (c_.output_format == 1 ? sizeof(float) : sizeof(uint16_t));
+    return (size_t)out_w_ * out_h_ * format_planes(c_.output_format) * format_elem(c_.output_format);
 }
 
 int Engine::ensure_partial(int nout_fields)
@@ -232,6 +242,7 @@ int Engine::run_transform(const uint16_t *fields, long long stride, int field_ba
                           float *partial, cudaStream_t s)
 {
     const long long cls_stride = (long long)(fe - fb) * 2 * rows_ * cols_;
+    if (c_.kind == 6) return 0;   // the PALcolour filter demodulates the composite directly
     if (c_.kind == 8) {
         tpal::T3Params P{};
         P.fields = fields;
@@ -244,6 +255,7 @@ int Engine::run_transform(const uint16_t *fields, long long stride, int field_ba
         P.fafl = g_.first_active_frame_line;
         P.lafl = g_.last_active_frame_line;
         P.black = g_.black;
+        P.swap = c_.first_field_offset;
         // transform_pal_3d.cpp:151-153 tile grid
         P.tileX0 = g_.active_start - 8;
         P.ntx = (g_.active_end - P.tileX0 + 7) / 8;
@@ -276,6 +288,7 @@ int Engine::run_transform(const uint16_t *fields, long long stride, int field_ba
         P.fafl = g_.first_active_frame_line;
         P.lafl = g_.last_active_frame_line;
         P.black = g_.black;
+        P.swap = c_.first_field_offset;
         P.field_begin = 2 * fb;
         P.nout = 2 * (fe - fb);
         P.partial = partial;
@@ -312,18 +325,23 @@ int Engine::run_demod(const uint16_t *fields, long long stride, int field_base, 
     D.burst_end = g_.burst_end;
     D.black = g_.black;
     D.white = g_.white;
-    D.partial = partial;
+    D.partial = (c_.kind == 6) ? nullptr : partial;
     D.part_class_stride = (long long)(fe - fb) * 2 * rows_ * cols_;
     D.part_field_stride = (long long)rows_ * cols_;
     D.part_row_stride = cols_;
     D.fl_lo = fl_lo_;
     D.nclasses = 4;
+    D.swap = c_.first_field_offset;
     const double th = (c_.chroma_phase_deg * M_PI) / 180;
     D.gain_cos = (float)(cos(th) * c_.chroma_gain);
     D.gain_sin = (float)(sin(th) * c_.chroma_gain);
-    D.format = c_.output_format;
+    // doYNR coring level: yNRLevel * ((white - black) / 100), the division in
+    // integers as in the reference (palcolour.cpp:415-416)
+    D.nr_y = (float)(c_.y_nr_level * (double)((g_.white - g_.black) / 100));
+    const int fmt = c_.output_format;
+    D.format = fmt;
     D.out = out;
-    D.out_frame_stride = (long long)out_w_ * out_h_ * 3;
+    D.out_frame_stride = (long long)out_w_ * out_h_ * (long long)format_planes(fmt);
     D.out_w = out_w_;
     D.out_h = out_h_;
     D.left_pad = left_pad_;
@@ -332,8 +350,8 @@ int Engine::run_demod(const uint16_t *fields, long long stride, int field_base, 
     D.ey_scale = (float)(1.0 / range);
     D.ecb_scale = (float)(c_.ecb_from_u / range);
     D.ecr_scale = (float)(c_.ecr_from_v / range);
-    // output_writer.cpp:84-143 clamp bounds
-    if (c_.output_format == 1) {
+    // output_writer.cpp:84-143 Y'CbCr clamp bounds
+    if (fmt == 1 || fmt == 5) {
         switch (c_.clamp_mode) {
         case 1: D.y_lo = 0.f; D.y_hi = 1.f; D.c_lo = -0.5f; D.c_hi = 0.5f; break;
         case 3: D.y_lo = -15.0f / 219.0f; D.y_hi = 238.75f / 219.0f; D.c_lo = -127.0f / 224.0f; D.c_hi = 126.75f / 224.0f; break;
@@ -346,6 +364,36 @@ int Engine::run_demod(const uint16_t *fields, long long stride, int field_base, 
         default: D.y_lo = 0.f; D.y_hi = 65535.f; D.c_lo = 0.f; D.c_hi = 65535.f;
         }
     }
+    // R'G'B': ColorConversion's matrix (color_conversion.cpp:60-64) and the
+    // floatRGBBounds box (output_writer.cpp:149-190)
+    const double kg = 1.0 - c_.kr - c_.kb;
+    D.r_from_v = (float)(1.0 / c_.v_reduction);
+    D.g_from_u = (float)(-(c_.kb / kg) / c_.u_reduction);
+    D.g_from_v = (float)(-(c_.kr / kg) / c_.v_reduction);
+    D.b_from_u = (float)(1.0 / c_.u_reduction);
+    D.rgb_y_scale = (float)(65535.0 / range);
+    D.rgb_uv_scale = (float)((fmt == 2 ? 65535.0 : 1.0) / range);
+    {
+        const float inf = INFINITY;
+        float b[6] = {-inf, inf, -inf, inf, -inf, inf};
+        if (c_.clamp_mode == 1) {
+            for (int i = 0; i < 3; i++) b[2 * i] = 0.f, b[2 * i + 1] = 1.f;
+        } else if (c_.clamp_mode == 2) {
+            for (int i = 0; i < 3; i++) b[2 * i] = 0.f, b[2 * i + 1] = inf;
+        } else if (c_.clamp_mode == 3) {
+            const float eyLo = -15.0f / 219.0f, eyHi = 238.75f / 219.0f;
+            const float ecLo = -127.0f / 224.0f, ecHi = 126.75f / 224.0f;
+            const double bds = 2.0 * (1.0 - c_.kb), rds = 2.0 * (1.0 - c_.kr);
+            const double gcb = (c_.kb * bds) / kg, gcr = (c_.kr * rds) / kg;
+            b[0] = (float)(eyLo + rds * ecLo);
+            b[1] = (float)(eyHi + rds * ecHi);
+            b[2] = (float)(eyLo - (gcb + gcr) * ecHi);
+            b[3] = (float)(eyHi - (gcb + gcr) * ecLo);
+            b[4] = (float)(eyLo + bds * ecLo);
+            b[5] = (float)(eyHi + bds * ecHi);
+        }
+        D.r_lo = b[0], D.r_hi = b[1], D.g_lo = b[2], D.g_hi = b[3], D.b_lo = b[4], D.b_hi = b[5];
+    }
     if (padded()) {
         // black border: Y 16*256 / Cb,Cr 128*256 (p16), zeros (ps)
         const int rc = fill_border(out, fe - fb, s);
@@ -356,22 +404,30 @@ int Engine::run_demod(const uint16_t *fields, long long stride, int field_base, 
     return 0;
 }
 
-__global__ void fill_frames_kernel(uint16_t *o16, float *o32, long long plane, long long nframes, uint16_t y, uint16_t c)
+// Black border of padded frames (OutputWriter::fillBlack, output_writer.cpp:371-400):
+// Y 16*256 and Cb/Cr 128*256 for yuv444p16, 16*256 for gray16, zero for
+// rgb48 and every float format.
+__global__ void fill_frames_kernel(uint16_t *o16, float *o32, long long frame_elems, long long plane, long long nframes,
+                                   uint16_t y, uint16_t c)
 {
-    const long long n = nframes * 3 * plane;
+    const long long n = nframes * frame_elems;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        if (o16) o16[i] = ((i / plane) % 3 == 0) ? y : c;
+        if (o16) o16[i] = (((i % frame_elems) / plane) == 0) ? y : c;
         else o32[i] = 0.f;
     }
 }
 
 int Engine::fill_border(void *out, int nframes, cudaStream_t s)
 {
+    const int fmt = c_.output_format;
     const long long plane = (long long)out_w_ * out_h_;
-    if (c_.output_format == 1)
-        fill_frames_kernel<<<1024, 256, 0, s>>>(nullptr, (float *)out, plane, nframes, 0, 0);
+    const long long elems = plane * (long long)format_planes(fmt);
+    if (format_elem(fmt) == sizeof(float))
+        fill_frames_kernel<<<1024, 256, 0, s>>>(nullptr, (float *)out, elems, plane, nframes, 0, 0);
+    else if (fmt == 2)
+        fill_frames_kernel<<<1024, 256, 0, s>>>((uint16_t *)out, nullptr, elems, plane, nframes, 0, 0);
     else
-        fill_frames_kernel<<<1024, 256, 0, s>>>((uint16_t *)out, nullptr, plane, nframes, 16 * 256, 128 * 256);
+        fill_frames_kernel<<<1024, 256, 0, s>>>((uint16_t *)out, nullptr, elems, plane, nframes, 16 * 256, 128 * 256);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? 0 : cuda_fail("fill", e);
 }
@@ -385,7 +441,8 @@ int Engine::decode(const uint16_t *fields, long long stride, int field_base, int
     char *o = (char *)out;
     for (int b = fb; b < fe; b += maxb) {
         const int be = std::min(fe, b + maxb);
-        if (const int rc = ensure_partial(2 * (be - b)); rc != 0) return rc;
+        if (c_.kind != 6)
+            if (const int rc = ensure_partial(2 * (be - b)); rc != 0) return rc;
         Pending ev{};
         if (profiling_) {
             cudaEventCreate(&ev.a);
@@ -536,6 +593,7 @@ __global__ void sum_classes_kernel(const float *part, long long cls_stride, long
 int Engine::chroma(const uint16_t *fields, long long stride, int nfields, int fb, int fe, float *out, cudaStream_t s)
 {
     if (fields == nullptr || out == nullptr || fe < fb) return arg_fail("chroma: bad arguments");
+    if (c_.kind == 6) return arg_fail("chroma: CHD_DEC_PAL_2D has no Transform-PAL stage");
     if (const int rc = ensure_partial(2 * (fe - fb)); rc != 0) return rc;
     if (const int rc = run_transform(fields, stride, 0, nfields, fb, fe, partial_, s); rc != 0) return rc;
     const long long n = (long long)(fe - fb) * 2 * rows_ * cols_;
@@ -597,9 +655,14 @@ void chdg_default_config(chdg_config *c, int32_t kind)
     c->clamp_mode = 0;
     c->padding_multiple = 1;
     // src/common/color_conversion.cpp:33-66 at Modern / Scientific
-    const double kb = 0.114, kr = 0.299;
-    c->ecb_from_u = 1.0 / ((2.0 * (1.0 - kb)) * 0.49211104112248356308804691718185);
-    c->ecr_from_v = 1.0 / ((2.0 * (1.0 - kr)) * 0.87728321993817866838972487283129);
+    c->kb = 0.114;
+    c->kr = 0.299;
+    c->u_reduction = 0.49211104112248356308804691718185;
+    c->v_reduction = 0.87728321993817866838972487283129;
+    c->ecb_from_u = 1.0 / ((2.0 * (1.0 - c->kb)) * c->u_reduction);
+    c->ecr_from_v = 1.0 / ((2.0 * (1.0 - c->kr)) * c->v_reduction);
+    c->y_nr_level = 0.0;
+    c->first_field_offset = 0;
 }
 
 int chdg_engine_create(const chdg_geometry *g, const chdg_config *c, chdg_engine **out)

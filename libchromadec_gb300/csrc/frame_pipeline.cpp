@@ -15,6 +15,7 @@ int dropout_apply(uint16_t *fields, long long field_stride, int fw, const int *d
                   const int *d_op_begin, int nframes, cudaStream_t s);
 int fill_fields(uint16_t *fields, long long field_stride, long long field_len, int nfields, uint16_t value,
                 cudaStream_t s);
+int fill_samples(uint16_t *p, long long n, uint16_t value, cudaStream_t s);
 
 namespace {
 
@@ -130,6 +131,7 @@ const FramePlan &FramePipeline::plan_for(int64_t frame)
     // A padding frame carries frame 1's dropouts but none of its picture.
     if (!wf[0].isPadding && !wf[1].isPadding) {
         FieldMeta m0 = cap_->field(wf[0].fieldNumber), m1 = cap_->field(wf[1].fieldNumber);
+        if (second_field_shifted(cap_->vp())) m1 = shift_dropouts(m1);
         plan = plan_frame(cap_->vp(), m0, m1, drop_.overcorrect, drop_.intra);
     }
     return plans_.emplace(frame, std::move(plan)).first->second;
@@ -149,14 +151,26 @@ int FramePipeline::upload_window(int slot, int64_t w0, int64_t w1)
         src[k + 1] = wf[1].source;
     }
     cudaError_t e;
+    const bool shifted = second_field_shifted(cap_->vp());
     for (int k = 0; k < nf;) {
         int n = 1;
+        if (shifted && (k & 1) && src[k] != 0) {
+            // shiftSecondField: samples 2.. of the field, then 2 black
+            uint16_t *dst = dwin_[slot] + (size_t)k * dstride_;
+            if ((e = cudaMemcpyAsync(dst, cap_->fieldData(src[k]) + 2, fbytes - 4, cudaMemcpyHostToDevice, copy_)) !=
+                cudaSuccess)
+                return cuda_status("H2D", e);
+            if (fill_samples(dst + flen_ - 2, 2, black, copy_) != 0) return cuda_status("black tail", cudaGetLastError());
+            k += 1;
+            continue;
+        }
         if (src[k] == 0) {
             while (k + n < nf && src[k + n] == 0) n++;
             if (fill_fields(dwin_[slot] + (size_t)k * dstride_, dstride_, (long long)flen_, n, black, copy_) != 0)
                 return cuda_status("black fields", cudaGetLastError());
         } else {
-            while (k + n < nf && src[k + n] == src[k] + n) n++;
+            // a run of consecutive fields (slot-0 fields only when slot 1 is shifted)
+            while (k + n < nf && src[k + n] == src[k] + n && !(shifted && ((k + n) & 1))) n++;
             if ((e = cudaMemcpy2DAsync(dwin_[slot] + (size_t)k * dstride_, (size_t)dstride_ * 2,
                                        cap_->fieldData(src[k]), fbytes, fbytes, (size_t)n, cudaMemcpyHostToDevice,
                                        copy_)) != cudaSuccess)

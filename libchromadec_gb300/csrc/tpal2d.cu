@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(32 * kWarps2) tpal2d_kernel(T2Params P)
     const int t = (int)(item % per_field);
     const int tx = t % ntx, ty = t / ntx;
     const int f = P.field_begin + o;
-    const int off = f & 1;
+    const int off = (f & 1) ^ P.swap;   // SourceField::getOffset
     const int fl_first = (P.fafl + 1 - off) / 2;   // SourceField::getFirstActiveLine
     const int fl_last = ((P.lafl - off) / 2) + 1;  // SourceField::getLastActiveLine
     const int tileY = fl_first - 8 + 8 * ty;

@@ -116,12 +116,12 @@ struct LaneConst {
     float2 ptw;        // exp(-2 pi i kk y0 / 32)
 };
 
-__device__ __forceinline__ LaneConst lane_const(int lane, int tileY)
+__device__ __forceinline__ LaneConst lane_const(int lane, int tileY, int swap)
 {
     LaneConst c;
     c.j = lane >> 4;
     c.i = lane & 15;
-    c.y0 = (c.j - tileY) & 1;
+    c.y0 = ((c.j ^ swap) - tileY) & 1;   // field offset (j ^ swap): its rows have that parity
     c.kk = rev4(c.i);
     c.wy = c3_wy[c.y0][c.i];
     int s = 0;
@@ -223,7 +223,7 @@ __device__ __noinline__ void exact_pair(const T3Params &P, int m, int tileX, int
     const int z = lane >> 2;
     const int part = lane & 3;
     const int f = 2 * m + z;
-    const int p = f & 1;
+    const int p = (f & 1) ^ P.swap;   // SourceField::getOffset of window field f
     const int y0 = (p - tileY) & 1;
     dfc accb = {{0.f, 0.f}, {0.f, 0.f}}, accr = accb;
     if (f >= 0 && f < P.nfields) {
@@ -443,7 +443,7 @@ __global__ void __launch_bounds__(32 * kWarps3, 3) tpal3d_kernel(T3Params P)
     float2 *carry_base = wbase + 8 * 5 * 32;      // [2][2 slices][5 kx][32 lanes]
     float *bnd = reinterpret_cast<float *>(carry_base + 2 * 2 * 5 * 32);   // [8 slots][8]
 
-    const LaneConst LC = lane_const(lane, tileY);
+    const LaneConst LC = lane_const(lane, tileY, P.swap);
     const int my_ky = kappa(lane);
     const int kyr = (40 - my_ky) & 31;
     const int mirror_lane = kappa(kyr);

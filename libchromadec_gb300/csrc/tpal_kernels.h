@@ -23,6 +23,7 @@ struct T3Params {
     int fw;
     int avs, ave, fafl, lafl;   // active samples [avs, ave), frame lines [fafl, lafl]
     int black;
+    int swap;                    // 1: even fields are second fields (reversed pairing)
     int tileX0, ntx, tileY0, nty;
     int frame_begin, frame_end, chunk_frames, nchunks;
     float *partial;
@@ -41,6 +42,7 @@ struct T2Params {
     int fw;
     int avs, ave, fafl, lafl;
     int black;
+    int swap;                    // 1: even fields are second fields (reversed pairing)
     int field_begin, nout;       // output fields [field_begin, field_begin + nout)
     float *partial;
     long long part_class_stride, part_field_stride;
@@ -60,17 +62,22 @@ struct DemodParams {
     int avs, ave, fafl, lafl;
     int burst_start, burst_end;
     int black, white;
-    const float *partial;        // chroma partial planes as above
+    const float *partial;        // chroma partial planes as above (NULL: demodulate the composite)
     long long part_class_stride, part_field_stride;
     int part_row_stride, fl_lo;
     int nclasses;                // 4 for the Transform kinds
+    int swap;                    // 1: even window fields are second fields (offset = (f & 1) ^ swap)
     float gain_cos, gain_sin;    // chroma_gain * (cos, sin)(chroma_phase)
-    int format;                  // 0 = yuv444p16, 1 = yuv444ps
-    void *out;                   // frames: [Y | Cb | Cr] planes of out_w x out_h
+    float nr_y;                  // luma coring level in sample units (0 = off)
+    int format;                  // chd_pixel_format_t: 0 yuv444p16, 1 yuv444ps, 2 rgb48, 3 rgbs, 4 gray16, 5 grays
+    void *out;                   // frames in the format's layout, out_w x out_h
     long long out_frame_stride;  // elements per frame
     int out_w, out_h, left_pad, top_pad;
     float ey_scale, ecb_scale, ecr_scale;   // 1/range, ecbFromU/range, ecrFromV/range
-    float y_lo, y_hi, c_lo, c_hi;           // clamp bounds (code units for p16, E' for ps)
+    float y_lo, y_hi, c_lo, c_hi;           // Y'CbCr clamp bounds (code units for p16/gray16, E' for ps/grays)
+    float rgb_y_scale, rgb_uv_scale;        // rgb48: 65535/range; rgbs: 1/range
+    float r_from_v, g_from_u, g_from_v, b_from_u;
+    float r_lo, r_hi, g_lo, g_hi, b_lo, b_hi;   // R'G'B' clamp bounds
 };
 
 int tp3_init_constants(int device);

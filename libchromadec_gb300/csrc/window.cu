@@ -1,4 +1,5 @@
-// window.cu -- black padding fields of a decode window, on the device.
+// window.cu -- black padding fields of a decode window, and the black tail of
+// a shifted subcarrier-locked second field, on the device.
 //
 // Frames outside the capture (and frames whose metadata is unusable) enter
 // the Transform-PAL window as fields filled with the black level
@@ -27,6 +28,22 @@ int fill_fields(uint16_t *fields, long long field_stride, long long field_len, i
     if (nfields <= 0) return 0;
     if ((reinterpret_cast<uintptr_t>(fields) & 15) != 0 || (field_stride & 7) != 0) return -1;
     fill_fields_kernel<<<dim3(64, (unsigned)nfields), 256, 0, s>>>(fields, field_stride, field_len, value);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+__global__ void fill_samples_kernel(uint16_t *p, long long n, uint16_t value)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        p[i] = value;
+}
+
+// Any run of samples, no alignment needed (the 2 black samples a shifted
+// second field ends with).
+int fill_samples(uint16_t *p, long long n, uint16_t value, cudaStream_t s)
+{
+    if (n <= 0) return 0;
+    const unsigned blocks = (unsigned)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024);
+    fill_samples_kernel<<<blocks, 256, 0, s>>>(p, n, value);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -37,6 +37,8 @@ class Config(C.Structure):
         ("chroma_gain", C.c_double), ("chroma_phase_deg", C.c_double),
         ("output_format", C.c_int32), ("clamp_mode", C.c_int32), ("padding_multiple", C.c_int32),
         ("ecb_from_u", C.c_double), ("ecr_from_v", C.c_double),
+        ("kr", C.c_double), ("kb", C.c_double), ("u_reduction", C.c_double), ("v_reduction", C.c_double),
+        ("y_nr_level", C.c_double), ("first_field_offset", C.c_int32),
     ]
 
 

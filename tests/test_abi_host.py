@@ -187,9 +187,13 @@ def test_commit_validation_order(pal_tbc, tmp_path):
                           last_active_frame_line=200)[0] == abi.E_INVALID_ARG
     assert _commit_status(v, 99)[0] == abi.E_DECODER_UNKNOWN
     assert _commit_status(v, abi.DEC_MONO)[0] == abi.E_UNSUPPORTED
-    assert _commit_status(v, abi.DEC_AUTO)[0] == abi.E_UNSUPPORTED     # AUTO resolves to PAL_2D
-    assert _commit_status(v, abi.DEC_TRANSFORM_3D, output_format="rgb48")[0] == abi.E_UNSUPPORTED
-    assert _commit_status(v, abi.DEC_TRANSFORM_3D, luma_nr_level=1.0)[0] == abi.E_UNSUPPORTED
+    assert _commit_status(v, abi.DEC_NTSC_2D)[0] == abi.E_UNSUPPORTED
+    # supported configurations pass validation; without a GPU the commit
+    # then stops at the device (no CPU fallback)
+    for kind, opts in ((abi.DEC_AUTO, {}), (abi.DEC_PAL_2D, {"luma_nr_level": 2.0}),
+                       (abi.DEC_TRANSFORM_3D, {"output_format": "rgb48"}),
+                       (abi.DEC_TRANSFORM_2D, {"output_format": "grays", "reverse_field_order": True})):
+        assert _commit_status(v, kind, **opts)[0] in (abi.OK, abi.E_INTERNAL)
     thr = tmp_path / "short.txt"
     thr.write_text(" ".join(["0.5"] * 100))
     assert _commit_status(v, abi.DEC_TRANSFORM_3D, transform_thresholds_file=str(thr))[0] == \
