@@ -192,6 +192,24 @@ def reference_arm(a):
     print(json.dumps(line), flush=True)
 
 
+def pipeline_batches(a: int, b: int, batch: int, edge: int):
+    """The batch boundaries FramePipeline::decode uses for frames [a, b)."""
+    out, c = [], a
+    edge = min(edge, batch)
+    if b - a <= batch:
+        return [(a, b)] if b > a else []
+    out.append((c, c + edge))
+    c += edge
+    while b - c > batch + edge:
+        out.append((c, c + batch))
+        c += batch
+    if b - c > edge:
+        out.append((c, b - edge))
+        c = b - edge
+    out.append((c, b))
+    return out
+
+
 def max_over_ranks(x: float, dist, device: str = "cuda") -> float:
     """The slowest rank's time: replicas are timed together and the job takes
     as long as its slowest GPU."""
@@ -252,10 +270,10 @@ def e2e_abi(a, fields_np, rank, barrier, dist):
     if got[0] != nframes * (a.steps + max(1, a.warmup)):
         raise RuntimeError(f"chd_decode_frames_async delivered {got[0]} frames")
     value, dt = replica_throughput(nfields, a.steps, dt, dist)
-    # uploaded per step: 64-frame batches, each with its 2 + 4 frame window halo
-    B, h2d = 64, 0
-    for b in range(0, nframes, B):
-        be = min(nframes, b + B)
+    # uploaded per step: the pipeline's batches (16 frames first and last,
+    # 64 in between), each with its 2 + 4 frame window halo
+    h2d = 0
+    for b, be in pipeline_batches(0, nframes, 64, 16):
         h2d += (min(nframes, be + 4) - max(0, b - 2)) * 2 * FIELD_BYTES_IN
     frame_bytes = oi.width * oi.height * 3 * (2 if a.format == "p16" else 4)
     d.close()

@@ -27,9 +27,9 @@
 //  * Every output format of the ABI is packed here: yuv444p16/ps, rgb48
 //    (interleaved, truncating), rgbs, gray16, grays.
 //
-// One block: 8 field lines of one output field, 256 threads; a work item
-// produces 8 consecutive samples of one line from a register window of the
-// four vertically combined chroma rows.
+// One block: 16 field lines (8 with yNR) of one output field, 256 threads; a
+// work item produces 8 consecutive samples of one line from a register window
+// of the four vertically combined chroma rows.
 #include <cmath>
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -43,11 +43,12 @@ __constant__ float cd_yfilt[8][2];   // PALcolour luma-extraction taps
 __constant__ float cd_nrpal[25];     // doYNR high-pass (c_nrpal_b)
 static bool g_demod_ready[64];
 
-constexpr int kDemodLines = 8;
 constexpr int kDemodThreads = 256;
 constexpr int kPad = 8;
-constexpr int kRows = kDemodLines + 6;   // chroma lines fl0-3 .. fl0+L+2
 constexpr int kNrHalf = 12;              // half length of the yNR filter
+// Field lines per block: 16 (a 6-line halo re-read per 16 lines), 8 with
+// yNR, whose luma lines also live in shared memory.
+__host__ __device__ constexpr int demod_lines(bool ynr) { return ynr ? 8 : 16; }
 
 __device__ __forceinline__ int first_line(int fafl, int off) { return (fafl + 1 - off) / 2; }
 __device__ __forceinline__ int last_line(int lafl, int off) { return ((lafl - off) / 2) + 1; }
@@ -166,6 +167,8 @@ __device__ __forceinline__ void pack_sample(const DemodParams &P, long long fram
 template <bool COMPOSITE, bool YNR>
 __global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
 {
+    constexpr int kDemodLines = demod_lines(YNR);
+    constexpr int kRows = kDemodLines + 6;   // input lines fl0-3 .. fl0+L+2
     extern __shared__ float smem[];
     const int nblk_per_field = (P.fh + kDemodLines - 1) / kDemodLines;   // upper bound; invalid lines skip
     const int o = blockIdx.x / nblk_per_field;
@@ -211,6 +214,7 @@ __global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
         const bool vec = ((cols & 3) == 0) && ((P.part_row_stride & 3) == 0) && ((P.part_class_stride & 3) == 0) &&
                          ((P.part_field_stride & 3) == 0);
         if (vec) {
+#pragma unroll 4
             for (int idx = threadIdx.x; idx < kRows * c4; idx += blockDim.x) {
                 const int r = idx / c4, q = idx % c4;
                 const int fl = fl0 - 3 + r;
@@ -240,8 +244,8 @@ __global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
 
     // 2. burst detection: one warp per line (detectBurst, palcolour.cpp:344-409)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (warp < kDemodLines) {
-        const int fl = fl0 + warp;
+    for (int ln = warp; ln < kDemodLines; ln += kDemodThreads / 32) {
+        const int fl = fl0 + ln;
         long long Ps = 0, Qs = 0, POs = 0, QOs = 0;
         if (fl < fl_last) {
             auto px = [&](int line, int i) -> int {
@@ -274,9 +278,9 @@ __global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
             const double bq = (double)(Qs + 2 * POs) / (8.0 * len);
             const double n = fmax(sqrt(bp * bp + bq * bq), 130000.0 / 128);
             const double nbp = bp / n, nbq = bq / n;
-            s_bp[warp] = (float)(nbp * P.gain_cos - nbq * P.gain_sin);
-            s_bq[warp] = (float)(nbp * P.gain_sin + nbq * P.gain_cos);
-            s_vsw[warp] = vpos ? 1.f : -1.f;
+            s_bp[ln] = (float)(nbp * P.gain_cos - nbq * P.gain_sin);
+            s_bq[ln] = (float)(nbp * P.gain_sin + nbq * P.gain_cos);
+            s_vsw[ln] = vpos ? 1.f : -1.f;
         }
     }
     __syncthreads();
@@ -416,8 +420,9 @@ int demod_init_constants(int device, double sample_rate, int /*field_width*/)
 size_t demod_smem_bytes(int avs, int ave, bool ynr)
 {
     const int span = demod_span(avs, ave);
-    const size_t rows = sizeof(float) * (size_t)kRows * (span + 2 * kPad);
-    return rows + (ynr ? sizeof(float) * (size_t)kDemodLines * (span + 2 * kNrHalf) : 0);
+    const int lines = demod_lines(ynr);
+    const size_t rows = sizeof(float) * (size_t)(lines + 6) * (span + 2 * kPad);
+    return rows + (ynr ? sizeof(float) * (size_t)lines * (span + 2 * kNrHalf) : 0);
 }
 
 int demod_launch(const DemodParams &P, cudaStream_t stream)
@@ -445,7 +450,8 @@ int demod_launch(const DemodParams &P, cudaStream_t stream)
             return -1;
         attr_set[dev] = true;
     }
-    const int nblk_per_field = (P.fh + kDemodLines - 1) / kDemodLines;
+    const int lines = demod_lines(ynr);
+    const int nblk_per_field = (P.fh + lines - 1) / lines;
     const dim3 grid((unsigned)(P.nout * nblk_per_field));
     if (composite) {
         if (ynr) demod_kernel<true, true><<<grid, kDemodThreads, smem, stream>>>(P);

@@ -195,9 +195,32 @@ int FramePipeline::decode(int64_t a, int64_t b, const Deliver &deliver, const st
     const size_t fb = eng_.frame_bytes();
     cudaError_t e;
     int i = 0;
-    for (int64_t c = a; c < b; c += batch_, i++) {
+    // Batch boundaries: full batches in the middle, short ones at both ends,
+    // so the first upload and the last download -- the parts no kernel
+    // overlaps -- stay small.
+    std::vector<std::pair<int64_t, int64_t>> batches;
+    {
+        const int64_t edge = std::min<int64_t>(kEdgeFrames, batch_);
+        int64_t c = a;
+        if (b - a <= batch_) {
+            if (b > a) batches.emplace_back(a, b);
+        } else {
+            batches.emplace_back(c, c + edge);
+            c += edge;
+            while (b - c > batch_ + edge) {
+                batches.emplace_back(c, c + batch_);
+                c += batch_;
+            }
+            if (b - c > edge) {
+                batches.emplace_back(c, b - edge);
+                c = b - edge;
+            }
+            batches.emplace_back(c, b);
+        }
+    }
+    for (const auto &bt : batches) {
         if (cancelled && cancelled()) break;
-        const int64_t ce = std::min<int64_t>(b, c + batch_);
+        const int64_t c = bt.first, ce = bt.second;
         const int slot = i & 1;
         const int64_t w0 = std::max<int64_t>(0, c - lb_);
         const int64_t w1 = std::min<int64_t>(nframes_, ce + la_);
@@ -279,6 +302,7 @@ int FramePipeline::decode(int64_t a, int64_t b, const Deliver &deliver, const st
             cudaSuccess)
             return cuda_status("D2H", e);
         cudaEventRecord(ev_d2h_[slot], d2h_);
+        i++;
         if (havePrev) {
             if ((e = cudaEventSynchronize(ev_d2h_[prev.slot])) != cudaSuccess) return cuda_status("sync", e);
             deliver(prev.out, prev.first, prev.count);

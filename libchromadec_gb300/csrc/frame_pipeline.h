@@ -41,6 +41,8 @@ using Deliver = std::function<void(const std::shared_ptr<HostChunk> &chunk, int6
 
 class FramePipeline {
 public:
+    static constexpr int kEdgeFrames = 16;   // size of the first and last batch of a long run
+
     FramePipeline() = default;
     ~FramePipeline();
     FramePipeline(const FramePipeline &) = delete;
