@@ -46,10 +46,11 @@ namespace tpal {
 // ---------------------------------------------------------------------------
 // Constant tables (filled by tp3_init_constants from double precision)
 // ---------------------------------------------------------------------------
-__constant__ float c3_cwx[5][8];   // forward X: w(x) cos(theta_kx), theta = 2 pi kx (x - 7.5) / 16
-__constant__ float c3_swx[5][8];   // forward X: w(x) sin(theta_kx)
-__constant__ float c3_cix[5][8];   // inverse X: (2/4096) cos(theta)
-__constant__ float c3_six[5][8];   // inverse X: (2/4096) sin(theta)
+// X-stage tables as (re, im) pairs for the paired FP32 instructions
+// (fma.rn.f32x2: two independent round-to-nearest FMAs, the same results as
+// two scalar FMAs, in one instruction):
+__constant__ float2 c3_xf[5][8];   // forward X: w(x) (cos theta_kx, -sin theta_kx), theta = 2 pi kx (x - 7.5) / 16
+__constant__ float2 c3_xi[5][8];   // inverse X: (2/4096) (cos theta, sin theta)
 __constant__ float c3_wy[2][16];   // w_y(y0 + 2i), 32-point raised cosine
 __constant__ float c3_wx[16];      // w_x(x)
 __constant__ float c3_wz[8];       // w_z(z)
@@ -73,6 +74,13 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 }
 
 __device__ __forceinline__ float l1(float2 a) { return fabsf(a.x) + fabsf(a.y); }
+
+// Paired FP32 (sm_100+): each lane of the pair rounds exactly like the scalar op.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+// multiply by -i: (y, -x); by the tables' exp(-i pi/2) = (6e-17, -1), whose
+// tiny real part is below the rounding of any non-degenerate product
+__device__ __forceinline__ float2 mul_negi(float2 a) { return make_float2(a.y, -a.x); }
 
 __device__ __forceinline__ float2 shfl_xor2(float2 v, int m)
 {
@@ -146,7 +154,7 @@ __device__ __forceinline__ void forward_pair(const T3Params &P, int q, int tileX
     // Row samples with black and the row mean removed, folded about the
     // window's centre: s_x = a_x + a_15-x - 2*mean, d_x = a_x - a_15-x
     // (exact in FP32); the window weight wy is applied to both.
-    float sx[8], dx[8];
+    float2 sd[8];   // (s_x, d_x)
     float rowl1 = 0.0f;
     if (valid) {
         const uint16_t *row = P.fields + (long long)(f - P.field_base) * P.field_stride + (long long)(L >> 1) * P.fw;
@@ -161,13 +169,12 @@ __device__ __forceinline__ void forward_pair(const T3Params &P, int q, int tileX
         const float m16 = (float)sum * 0.0625f;
 #pragma unroll
         for (int x = 0; x < 8; x++) {
-            sx[x] = (float)(8 * (a[x] + a[15 - x]) - sum) * 0.125f;
-            dx[x] = (float)(a[x] - a[15 - x]);
+            sd[x] = make_float2((float)(8 * (a[x] + a[15 - x]) - sum) * 0.125f, (float)(a[x] - a[15 - x]));
             rowl1 = __fmaf_rn(c3_wx[x], fabsf((float)a[x] - m16) + fabsf((float)a[15 - x] - m16), rowl1);
         }
     } else {
 #pragma unroll
-        for (int x = 0; x < 8; x++) sx[x] = dx[x] = 0.f;
+        for (int x = 0; x < 8; x++) sd[x] = make_float2(0.f, 0.f);
     }
     rowl1 *= LC.wy;
 #pragma unroll
@@ -181,12 +188,8 @@ __device__ __forceinline__ void forward_pair(const T3Params &P, int q, int tileX
         // column DFT bin kx = k+2 of this row (window and centre phase folded)
         float2 X = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int x = 0; x < 8; x++) {
-            X.x = __fmaf_rn(c3_cwx[k][x], sx[x], X.x);
-            X.y = __fmaf_rn(-c3_swx[k][x], dx[x], X.y);
-        }
-        X.x *= LC.wy;
-        X.y *= LC.wy;
+        for (int x = 0; x < 8; x++) X = __ffma2_rn(c3_xf[k][x], sd[x], X);
+        X = __fmul2_rn(X, make_float2(LC.wy, LC.wy));
         // bound term: sum over the field's rows of |X|_1
         float A = l1(X);
 #pragma unroll
@@ -285,38 +288,37 @@ __device__ __forceinline__ bool df_sim(df a, df b, df t)
     return !(df_sign(d1) < 0 || df_sign(d2) < 0);
 }
 
-// 8-point forward DFT of windowed column values (natural order in/out).
+// 8-point forward DFT of windowed column values (natural order in/out),
+// radix-2 with paired FP32 butterflies; the twiddles 1 and -i are applied
+// exactly, exp(-i pi/4) and exp(-3i pi/4) by complex multiplication.
 __device__ __forceinline__ void dft8_fwd(const float2 (&in)[8], float2 (&out)[8])
 {
     float2 a[8];
 #pragma unroll
-    for (int z = 0; z < 8; z++) a[z] = make_float2(in[z].x * c3_wz[z], in[z].y * c3_wz[z]);
-    // stage 1: pairs (z, z+4)
+    for (int z = 0; z < 8; z++) a[z] = __fmul2_rn(in[z], make_float2(c3_wz[z], c3_wz[z]));
+    // stage 1: pairs (z, z+4), twiddles exp(-2 pi i z / 8)
     float2 b[8];
 #pragma unroll
-    for (int z = 0; z < 4; z++) {
-        b[z] = make_float2(a[z].x + a[z + 4].x, a[z].y + a[z + 4].y);
-        const float2 d = make_float2(a[z].x - a[z + 4].x, a[z].y - a[z + 4].y);
-        b[z + 4] = cmul(d, c3_tw32[4 * z]);   // exp(-2 pi i z / 8)
-    }
-    // stage 2: pairs (z, z+2) within each half
+    for (int z = 0; z < 4; z++) b[z] = add2(a[z], a[z + 4]);
+    b[4] = sub2(a[0], a[4]);
+    b[5] = cmul(sub2(a[1], a[5]), c3_tw32[4]);
+    b[6] = mul_negi(sub2(a[2], a[6]));
+    b[7] = cmul(sub2(a[3], a[7]), c3_tw32[12]);
+    // stage 2: pairs (z, z+2) within each half, twiddles 1 and -i
     float2 c[8];
 #pragma unroll
     for (int hb = 0; hb < 8; hb += 4) {
-#pragma unroll
-        for (int z = 0; z < 2; z++) {
-            const float2 u = b[hb + z], v = b[hb + z + 2];
-            c[hb + z] = make_float2(u.x + v.x, u.y + v.y);
-            const float2 d = make_float2(u.x - v.x, u.y - v.y);
-            c[hb + z + 2] = cmul(d, c3_tw32[8 * z]);   // exp(-2 pi i z / 4)
-        }
+        c[hb] = add2(b[hb], b[hb + 2]);
+        c[hb + 1] = add2(b[hb + 1], b[hb + 3]);
+        c[hb + 2] = sub2(b[hb], b[hb + 2]);
+        c[hb + 3] = mul_negi(sub2(b[hb + 1], b[hb + 3]));
     }
     // stage 3: pairs (z, z+1); outputs in bit-reversed order
     float2 d[8];
 #pragma unroll
     for (int z = 0; z < 8; z += 2) {
-        d[z] = make_float2(c[z].x + c[z + 1].x, c[z].y + c[z + 1].y);
-        d[z + 1] = make_float2(c[z].x - c[z + 1].x, c[z].y - c[z + 1].y);
+        d[z] = add2(c[z], c[z + 1]);
+        d[z + 1] = sub2(c[z], c[z + 1]);
     }
     out[0] = d[0]; out[4] = d[1]; out[2] = d[2]; out[6] = d[3];
     out[1] = d[4]; out[5] = d[5]; out[3] = d[6]; out[7] = d[7];
@@ -364,21 +366,21 @@ __device__ __forceinline__ void z_inverse(const float2 (&Y)[8], unsigned keep, f
     float2 y[8];
 #pragma unroll
     for (int kz = 0; kz < 8; kz++) y[kz] = ((keep >> kz) & 1u) ? Y[kz] : make_float2(0.f, 0.f);
-    const float2 E0 = make_float2(y[0].x + y[2].x + y[4].x + y[6].x, y[0].y + y[2].y + y[4].y + y[6].y);
-    const float2 O0 = make_float2(y[1].x + y[3].x + y[5].x + y[7].x, y[1].y + y[3].y + y[5].y + y[7].y);
+    const float2 E0 = add2(add2(add2(y[0], y[2]), y[4]), y[6]);
+    const float2 O0 = add2(add2(add2(y[1], y[3]), y[5]), y[7]);
     // slice 1: even part y0 + i y2 - y4 - i y6; odd part with powers of exp(+i pi/4)
     const float2 E1 = make_float2(y[0].x - y[2].y - y[4].x + y[6].y, y[0].y + y[2].x - y[4].y - y[6].x);
     const float2 o1 = cmul(y[1], make_float2(c3_tw32[4].x, -c3_tw32[4].y));
     const float2 o3 = cmul(y[3], make_float2(c3_tw32[12].x, -c3_tw32[12].y));
     const float2 o5 = cmul(y[5], make_float2(c3_tw32[20].x, -c3_tw32[20].y));
     const float2 o7 = cmul(y[7], make_float2(c3_tw32[28].x, -c3_tw32[28].y));
-    const float2 O1 = make_float2(o1.x + o3.x + o5.x + o7.x, o1.y + o3.y + o5.y + o7.y);
+    const float2 O1 = add2(add2(add2(o1, o3), o5), o7);
     const int i4 = k * 32 + lane, i5 = (5 + k) * 32 + lane;
     const float2 c4 = carry[i4], c5 = carry[i5];
-    RA[k * 32 + lane] = make_float2(E0.x + O0.x + c4.x, E0.y + O0.y + c4.y);
-    RB[k * 32 + lane] = make_float2(E1.x + O1.x + c5.x, E1.y + O1.y + c5.y);
-    carry[i4] = make_float2(E0.x - O0.x, E0.y - O0.y);
-    carry[i5] = make_float2(E1.x - O1.x, E1.y - O1.y);
+    RA[k * 32 + lane] = add2(add2(E0, O0), c4);
+    RB[k * 32 + lane] = add2(add2(E1, O1), c5);
+    carry[i4] = sub2(E0, O0);
+    carry[i5] = sub2(E1, O1);
 }
 
 __device__ __forceinline__ bool fsim(float a, float b, float t) { return (__fmaf_rn(-b, t, a) >= 0.f) && (__fmaf_rn(-a, t, b) >= 0.f); }
@@ -545,9 +547,9 @@ __global__ void __launch_bounds__(32 * kWarps3, 3) tpal3d_kernel(T3Params P)
         // kk+16 of output field 2m+j for its row parity, runs a 16-point
         // inverse DFT over the half-warp, and accumulates row i's cosine and
         // sine sums of the inverse X transform.
-        float C[8], S[8];
+        float2 CS[8];   // (cosine sum, sine sum) of row i
 #pragma unroll
-        for (int x = 0; x < 8; x++) C[x] = S[x] = 0.f;
+        for (int x = 0; x < 8; x++) CS[x] = make_float2(0.f, 0.f);
         const float2 *Rj = LC.j ? RB : RA;
 #pragma unroll 1
         for (int k = 0; k < 5; k++) {
@@ -567,10 +569,7 @@ __global__ void __launch_bounds__(32 * kWarps3, 3) tpal3d_kernel(T3Params P)
                 G = upper ? make_float2(o.x - t.x, o.y - t.y) : make_float2(G.x + t.x, G.y + t.y);
             }
 #pragma unroll
-            for (int x = 0; x < 8; x++) {
-                C[x] = __fmaf_rn(G.x, c3_cix[k][x], C[x]);
-                S[x] = __fmaf_rn(G.y, c3_six[k][x], S[x]);
-            }
+            for (int x = 0; x < 8; x++) CS[x] = __ffma2_rn(G, c3_xi[k][x], CS[x]);
         }
         // Store row i of field 2m + j.
         const int L = tileY + LC.y0 + 2 * LC.i;
@@ -581,8 +580,8 @@ __global__ void __launch_bounds__(32 * kWarps3, 3) tpal3d_kernel(T3Params P)
 #pragma unroll
             for (int x = 0; x < 8; x++) {
                 const int X0 = tileX + x, X1 = tileX + 15 - x;
-                if (X0 >= P.avs && X0 < P.ave) dst[X0] = C[x] - S[x];
-                if (X1 >= P.avs && X1 < P.ave) dst[X1] = C[x] + S[x];
+                if (X0 >= P.avs && X0 < P.ave) dst[X0] = CS[x].x - CS[x].y;
+                if (X1 >= P.avs && X1 < P.ave) dst[X1] = CS[x].x + CS[x].y;
             }
         }
     }
@@ -642,10 +641,14 @@ int tp3_init_constants(int device)
     }
 #define TPAL_CPY(sym, src)                                                  \
     if (cudaMemcpyToSymbol(sym, src, sizeof(src)) != cudaSuccess) return -1;
-    TPAL_CPY(c3_cwx, cwx);
-    TPAL_CPY(c3_swx, swx);
-    TPAL_CPY(c3_cix, cix);
-    TPAL_CPY(c3_six, six);
+    float2 xf[5][8], xi[5][8];
+    for (int k = 0; k < 5; k++)
+        for (int x = 0; x < 8; x++) {
+            xf[k][x] = make_float2(cwx[k][x], -swx[k][x]);
+            xi[k][x] = make_float2(cix[k][x], six[k][x]);
+        }
+    TPAL_CPY(c3_xf, xf);
+    TPAL_CPY(c3_xi, xi);
     TPAL_CPY(c3_wy, wy);
     TPAL_CPY(c3_wx, wx);
     TPAL_CPY(c3_wz, wz);
