@@ -1,0 +1,130 @@
+"""The 500-field benchmark workload at full size, and capture-shape edge cases.
+
+Full size: the oracle cannot decode 250 3D frames in test time, so parity is
+checked on sampled frames (both ends of the capture, where the 3D window is
+padded, and the middle), and the rest through properties that hold at any
+size: the device path is deterministic (bit-identical on repeat), and the
+reference-facing ABI over a .tbc gives exactly the device path's frames.
+
+Edge cases (as SourceField::loadFields / LdDecodeMetaData pair fields,
+src/decoders/source_field.cpp:68-171, src/metadata/core.cpp:1092-1190): a
+capture that starts with a second field, an odd field count, a one-frame
+3D capture, an empty capture.
+"""
+import json
+
+import numpy as np
+import pytest
+
+from libchromadec_gb300 import abi, synth
+from oracle import oracle as O
+from tests._capture import capture
+
+pytestmark = pytest.mark.gpu
+
+
+def _p16_close(got, ref):
+    d = np.abs(got.astype(np.int32) - ref.astype(np.int32))
+    assert d.max() <= 1, (d.max(), (d > 0).mean())
+
+
+@pytest.fixture(scope="module")
+def workload():
+    cfg = synth.SynthConfig(seed=1, pan_x=1.5, pan_y=0.5)
+    return synth.make_capture(500, cfg)
+
+
+def test_full_workload_determinism_abi_and_sampled_parity(cuda, workload, tmp_path_factory):
+    torch = cuda
+    from libchromadec_gb300 import device as D
+    fields = workload.fields
+    n = fields.shape[0]
+    nfr = n // 2
+    eng = D.Engine(D.default_geometry(), D.default_config(kind=D.KIND_TRANSFORM_3D, fmt=D.FMT_P16))
+    dfields = torch.from_numpy(fields.reshape(n, -1).view(np.int16)).cuda()
+    out1 = torch.empty((nfr, 3, 576, 948), dtype=torch.int16, device="cuda")
+    out2 = torch.empty_like(out1)
+    eng.decode(dfields, 0, nfr, out1)
+    eng.decode(dfields, 0, nfr, out2)
+    torch.cuda.synchronize()
+    assert torch.equal(out1, out2)                         # deterministic: no atomics in the data path
+    dev = out1.cpu().numpy().view(np.uint16)
+
+    path = str(tmp_path_factory.mktemp("full") / "w.tbc")
+    synth.write_tbc(path, workload)
+    v = abi.Video(path)
+    d = abi.Decoder(v, abi.DEC_TRANSFORM_3D)
+    d.commit()
+    res = d.decode_async(list(range(nfr)))
+    assert len(res) == nfr and all(s == abi.OK for s, _, _ in res)
+    for _, i, planes in res:
+        assert np.array_equal(planes, dev[i]), i           # same kernels, same frames
+
+    for k in (0, 1, 2, 124, 125, 247, 248, 249):
+        ref, _ = O.decode_frames(O.params(3, O.FMT_P16), fields, k, 1, threads=8)
+        _p16_close(dev[k], ref[0])
+
+
+def _write_flags(tmp_path, fields, first_flags, name):
+    cap = synth.SynthCapture(fields=np.ascontiguousarray(fields), dropouts=[[] for _ in range(len(fields))])
+    path = str(tmp_path / name)
+    jpath = synth.write_tbc(path, cap)
+    meta = json.load(open(jpath))
+    for f, flag in zip(meta["fields"], first_flags):
+        f["isFirstField"] = bool(flag)
+    json.dump(meta, open(jpath, "w"))
+    return path
+
+
+def _decode_abi(path, kind=abi.DEC_TRANSFORM_3D):
+    v = abi.Video(path)
+    d = abi.Decoder(v, kind)
+    d.commit()
+    n = d.output_info().num_frames
+    return (np.stack([d.decode(k).planes() for k in range(n)]) if n > 0 else np.zeros((0,))), n, d
+
+
+def test_capture_starting_with_a_second_field(cuda, tmp_path):
+    cap = capture(17, 51)
+    flags = [i % 2 == 1 for i in range(17)]               # field 1 is a second field
+    path = _write_flags(tmp_path, cap.fields, flags, "s.tbc")
+    got, n, _ = _decode_abi(path)
+    assert n == 7                                         # pairs (2,3), (4,5), ... (1-based)
+    # frames beyond the 7th are black padding in the window, so give the oracle exactly 7 frames
+    ref, _ = O.decode_frames(O.params(3, O.FMT_P16), np.ascontiguousarray(cap.fields[1:15]), 0, n, threads=8)
+    _p16_close(got, ref)
+
+
+def test_odd_field_count_and_single_frame(cuda, tmp_path):
+    cap = capture(15, 52)
+    path = _write_flags(tmp_path, cap.fields, [i % 2 == 0 for i in range(15)], "o.tbc")
+    got, n, _ = _decode_abi(path)
+    assert n == 7                                         # the unpaired last field is not a frame
+    ref, _ = O.decode_frames(O.params(3, O.FMT_P16), cap.fields, 0, n, threads=8)
+    _p16_close(got, ref)
+    one = capture(2, 53)
+    path1 = _write_flags(tmp_path, one.fields, [True, False], "one.tbc")
+    for kind, okind in ((abi.DEC_TRANSFORM_3D, 3), (abi.DEC_TRANSFORM_2D, 2), (abi.DEC_PAL_2D, 1)):
+        got1, n1, _ = _decode_abi(path1, kind)
+        assert n1 == 1
+        ref1, _ = O.decode_frames(O.params(okind, O.FMT_P16), one.fields, 0, 1, threads=2)
+        _p16_close(got1, ref1)
+
+
+def test_empty_capture(cuda, tmp_path):
+    path = str(tmp_path / "e.tbc")
+    open(path, "wb").close()
+    meta = {"videoParameters": synth.video_parameters_json(0), "fields": []}
+    json.dump(meta, open(path + ".json", "w"))
+    v = abi.Video(path)
+    # getNumberOfFrames: 0 fields / 2 minus 1 because the (missing) field 1 is
+    # not a first field -- the reference reports -1 (src/metadata/core.cpp:1092-1107)
+    assert v.info().num_frames == -1
+    d = abi.Decoder(v, abi.DEC_TRANSFORM_3D)
+    d.commit()
+    assert d.output_info().num_frames == -1
+    with pytest.raises(abi.ChdError) as e:
+        d.decode(0)
+    assert e.value.status == abi.E_OUT_OF_RANGE
+    res = d.decode_async([0, 3])
+    assert sorted(s for s, _, _ in res) == [abi.E_OUT_OF_RANGE, abi.E_OUT_OF_RANGE]
