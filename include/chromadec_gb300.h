@@ -123,6 +123,44 @@ int chdg_decode_device_static(const chdg_geometry *g, const chdg_config *c, cons
                               int64_t field_stride, int32_t nfields, int32_t frame_begin, int32_t frame_end,
                               void *d_out, void *stream);
 
+/* Batches of captures (no counterpart in the reference, which decodes one
+ * capture per decoder). Many captures of uneven length and mixed
+ * Transform-PAL 2D/3D modes, each with its own threshold, are decoded by one
+ * transform and one demodulator launch per mode, reading every capture's
+ * fields in place through a table of field pointers: the 3D captures share
+ * one frame index space in which 3 black frames separate neighbours -- the
+ * black the reference pads every window with -- so every frame equals the
+ * single-capture decode. The first decode of a batch shape runs eagerly,
+ * the second captures its launches into a CUDA graph, and later
+ * decodes of the same captures (same pointers and sizes) replay the graph
+ * with one launch. chdg_batch_autotune times the schedule candidates on the
+ * caller's batch and keeps the fastest. Captures and outputs are device
+ * buffers; the configuration's output format applies to every capture
+ * (padding_multiple 1, no per-bin thresholds). Asynchronous on `stream`;
+ * graphs need a created stream (on the legacy default stream, NULL, every
+ * decode runs eagerly). */
+typedef struct chdg_capture {
+    const uint16_t *fields;       /* device: field f at fields + f * field_stride */
+    int64_t field_stride;
+    int32_t nfields;              /* frames = nfields / 2 */
+    int32_t kind;                 /* 7 = Transform 2D, 8 = Transform 3D */
+    double threshold;             /* transform_threshold of this capture */
+    void *out;                    /* device: nfields / 2 output frames */
+} chdg_capture;
+
+typedef struct chdg_batch chdg_batch;
+
+typedef struct chdg_batch_tuning {
+    int32_t chunk_frames;         /* frames per 3D work item */
+    int32_t max_blocks;           /* 3D grid cap (0 = full grid, else persistent) */
+    float ms;                     /* the winner's time for the batch */
+} chdg_batch_tuning;
+
+int chdg_batch_create(const chdg_geometry *g, const chdg_config *c, chdg_batch **out);
+void chdg_batch_free(chdg_batch *b);
+int chdg_batch_decode(chdg_batch *b, const chdg_capture *caps, int32_t n, void *stream);
+int chdg_batch_autotune(chdg_batch *b, const chdg_capture *caps, int32_t n, void *stream, chdg_batch_tuning *out);
+
 /* Threshold decisions whose FP32 margin was inside the error bound and were
  * re-evaluated in double-float, and how many of those FP32 had wrong. */
 int chdg_engine_stats(chdg_engine *e, uint64_t *exact_decisions, uint64_t *fp32_flips);

@@ -116,29 +116,29 @@ __device__ __forceinline__ uint16_t h273q(float x, float lo, float hi)
 
 // Pack one sample in the output format (OutputWriter::convertLine,
 // convertToFloat, convertToFloatRGB; output_writer.cpp:402-486, 670-779).
-__device__ __forceinline__ void pack_sample(const DemodParams &P, long long frame, long long pix, float Y, float U,
-                                            float V)
+__device__ __forceinline__ void pack_sample(const DemodParams &P, void *out, long long frame, long long pix, float Y,
+                                            float U, float V)
 {
     const long long plane = (long long)P.out_w * P.out_h;
     const long long e = frame * P.out_frame_stride + pix;
     const float ey = (Y - (float)P.black) * P.ey_scale;
     switch (P.format) {
     case 0: {
-        uint16_t *o = (uint16_t *)P.out;
+        uint16_t *o = (uint16_t *)out;
         o[e] = h273q(__fmaf_rn(219.0f * 256.0f, ey, 16.0f * 256.0f), P.y_lo, P.y_hi);
         o[e + plane] = h273q(__fmaf_rn(224.0f * 256.0f, U * P.ecb_scale, 128.0f * 256.0f), P.c_lo, P.c_hi);
         o[e + 2 * plane] = h273q(__fmaf_rn(224.0f * 256.0f, V * P.ecr_scale, 128.0f * 256.0f), P.c_lo, P.c_hi);
         break;
     }
     case 1: {
-        float *o = (float *)P.out;
+        float *o = (float *)out;
         o[e] = fminf(fmaxf(ey, P.y_lo), P.y_hi);
         o[e + plane] = fminf(fmaxf(U * P.ecb_scale, P.c_lo), P.c_hi);
         o[e + 2 * plane] = fminf(fmaxf(V * P.ecr_scale, P.c_lo), P.c_hi);
         break;
     }
     case 2: {   // interleaved R'G'B' 0..65535, truncating stores
-        uint16_t *o = (uint16_t *)P.out + frame * P.out_frame_stride + 3 * pix;
+        uint16_t *o = (uint16_t *)out + frame * P.out_frame_stride + 3 * pix;
         const float rY = fminf(fmaxf((Y - (float)P.black) * P.rgb_y_scale, 0.f), 65535.f);
         const float rU = U * P.rgb_uv_scale, rV = V * P.rgb_uv_scale;
         o[0] = (uint16_t)__float2uint_rz(fminf(fmaxf(__fmaf_rn(P.r_from_v, rV, rY), 0.f), 65535.f));
@@ -148,7 +148,7 @@ __device__ __forceinline__ void pack_sample(const DemodParams &P, long long fram
         break;
     }
     case 3: {
-        float *o = (float *)P.out;
+        float *o = (float *)out;
         const float rU = U * P.rgb_uv_scale, rV = V * P.rgb_uv_scale;
         o[e] = fminf(fmaxf(__fmaf_rn(P.r_from_v, rV, ey), P.r_lo), P.r_hi);
         o[e + plane] = fminf(fmaxf(__fmaf_rn(P.g_from_v, rV, __fmaf_rn(P.g_from_u, rU, ey)), P.g_lo), P.g_hi);
@@ -156,10 +156,10 @@ __device__ __forceinline__ void pack_sample(const DemodParams &P, long long fram
         break;
     }
     case 4:
-        ((uint16_t *)P.out)[e] = h273q(__fmaf_rn(219.0f * 256.0f, ey, 16.0f * 256.0f), P.y_lo, P.y_hi);
+        ((uint16_t *)out)[e] = h273q(__fmaf_rn(219.0f * 256.0f, ey, 16.0f * 256.0f), P.y_lo, P.y_hi);
         break;
     default:
-        ((float *)P.out)[e] = fminf(fmaxf(ey, P.y_lo), P.y_hi);
+        ((float *)out)[e] = fminf(fmaxf(ey, P.y_lo), P.y_hi);
         break;
     }
 }
@@ -189,7 +189,18 @@ __global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
     float *ys = smem + kRows * SW;                     // [kDemodLines][YW] luma before coring (yNR only)
     __shared__ float s_bp[kDemodLines], s_bq[kDemodLines], s_vsw[kDemodLines];
 
-    const uint16_t *field = P.fields + (long long)(f - P.field_base) * P.field_stride;
+    // where this field's frame goes: the frame slot of the output array, or
+    // (batches of captures) the frame's own pointer, absent for the black
+    // gap frames between captures
+    void *out_base = P.out;
+    long long frame_slot = o >> 1;   // field_begin is even: fields 2k, 2k+1 form frame k
+    if (P.frame_out != nullptr) {
+        out_base = P.frame_out[f >> 1];
+        frame_slot = 0;
+        if (out_base == nullptr) return;
+    }
+    const uint16_t *field = field_at(P, f);
+    if (field == nullptr) return;   // a black batch gap: nothing to write
     const int cols = P.ave - P.avs;
 
     // 1. input rows, zero outside the field's active lines: the summed
@@ -286,7 +297,6 @@ __global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
     __syncthreads();
 
     const int per_line = span / 8;
-    const long long frame = o >> 1;   // field_begin is even: fields 2k, 2k+1 form frame k
 
     // 3. yNR pre-pass: the block's luma lines (zero outside the active window)
     if (YNR) {
@@ -360,7 +370,7 @@ __global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
             }
             const float U = -(PU[s] * bp + QU[s] * bq) * 2.0f;
             const float V = vsw * -(QV[s] * bp - PV[s] * bq) * 2.0f;
-            pack_sample(P, frame, rowpix + (x - P.avs), Y, U, V);
+            pack_sample(P, out_base, frame_slot, rowpix + (x - P.avs), Y, U, V);
         }
     }
 }

@@ -246,6 +246,7 @@ int Engine::run_transform(const uint16_t *fields, long long stride, int field_ba
     if (c_.kind == 8) {
         tpal::T3Params P{};
         P.fields = fields;
+        P.field_ptrs = field_ptrs_;
         P.field_stride = stride;
         P.field_base = field_base;
         P.nfields = nfields;
@@ -274,11 +275,13 @@ int Engine::run_transform(const uint16_t *fields, long long stride, int field_ba
         P.t2hi = t2hi_;
         P.t2lo = t2lo_;
         P.thr_table = thr_dev_;
+        P.frame_t2 = frame_t2_;
         P.stats = stats_dev_;
-        if (tpal::tp3_launch(P, s) != 0) return cuda_fail("tpal3d launch", cudaGetLastError());
+        if (tpal::tp3_launch(P, s, max_blocks3_) != 0) return cuda_fail("tpal3d launch", cudaGetLastError());
     } else {
         tpal::T2Params P{};
         P.fields = fields;
+        P.field_ptrs = field_ptrs_;
         P.field_stride = stride;
         P.field_base = field_base;
         P.nfields = nfields;
@@ -300,6 +303,7 @@ int Engine::run_transform(const uint16_t *fields, long long stride, int field_ba
         P.t2hi = t2hi_;
         P.t2lo = t2lo_;
         P.thr_table = thr_dev_;
+        P.frame_t2 = frame_t2_;
         P.stats = stats_dev_;
         if (tpal::tp2_launch(P, s) != 0) return cuda_fail("tpal2d launch", cudaGetLastError());
     }
@@ -311,6 +315,7 @@ int Engine::run_demod(const uint16_t *fields, long long stride, int field_base, 
 {
     tpal::DemodParams D{};
     D.fields = fields;
+    D.field_ptrs = field_ptrs_;
     D.field_stride = stride;
     D.field_base = field_base;
     D.field_begin = 2 * fb;
@@ -341,6 +346,7 @@ int Engine::run_demod(const uint16_t *fields, long long stride, int field_base, 
     const int fmt = c_.output_format;
     D.format = fmt;
     D.out = out;
+    D.frame_out = frame_out_;
     D.out_frame_stride = (long long)out_w_ * out_h_ * (long long)format_planes(fmt);
     D.out_w = out_w_;
     D.out_h = out_h_;
@@ -394,7 +400,7 @@ int Engine::run_demod(const uint16_t *fields, long long stride, int field_base, 
         }
         D.r_lo = b[0], D.r_hi = b[1], D.g_lo = b[2], D.g_hi = b[3], D.b_lo = b[4], D.b_hi = b[5];
     }
-    if (padded()) {
+    if (padded() && frame_out_ == nullptr) {
         // black border: Y 16*256 / Cb,Cr 128*256 (p16), zeros (ps)
         const int rc = fill_border(out, fe - fb, s);
         if (rc != 0) return rc;

@@ -54,6 +54,22 @@ public:
     int look_ahead() const { return c_.kind == 8 ? 4 : 0; }    // TransformPal3D::getLookAhead
     void set_max_batch_frames(int n) { max_batch_frames_ = n > 0 ? n : 1; }
     void set_chunk_frames(int n) { chunk_frames_ = n > 0 ? n : 1; }
+    int chunk_frames() const { return chunk_frames_; }
+    // Cap on the 3D transform's grid (0 = one block per 4 work items); a
+    // capped grid walks the items persistently.
+    void set_max_blocks(int n) { max_blocks3_ = n > 0 ? n : 0; }
+    int max_blocks() const { return max_blocks3_; }
+    // Batches of captures in one frame index space: every field's first
+    // sample (null for the black gap fields between captures), every frame's
+    // squared threshold (f, hi, lo) and output pointer (null for gap frames).
+    // Device arrays indexed by field / frame; null restores the
+    // single-capture behaviour.
+    void set_frame_tables(const uint16_t *const *d_field_ptrs, const float *d_frame_t2, void *const *d_frame_out)
+    {
+        field_ptrs_ = d_field_ptrs;
+        frame_t2_ = d_frame_t2;
+        frame_out_ = d_frame_out;
+    }
 
 private:
     bool padded() const { return left_pad_ || top_pad_ || out_w_ != (g_.active_end - g_.active_start) ||
@@ -79,6 +95,10 @@ private:
     int out_w_ = 0, out_h_ = 0, left_pad_ = 0, top_pad_ = 0;
     int max_batch_frames_ = 256;
     int chunk_frames_ = 32;
+    int max_blocks3_ = 0;
+    const uint16_t *const *field_ptrs_ = nullptr;
+    const float *frame_t2_ = nullptr;
+    void *const *frame_out_ = nullptr;
     // host pipeline: two slots of device fields + frames, one copy stream
     int host_batch_frames_ = 32;
     uint16_t *hp_fields_[2] = {nullptr, nullptr};

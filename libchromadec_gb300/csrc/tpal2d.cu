@@ -63,9 +63,15 @@ struct Thr2 {
     df d;
 };
 
-__device__ __forceinline__ Thr2 thr2(const T2Params &P, int ky, int kx)
+__device__ __forceinline__ Thr2 thr2(const T2Params &P, int frame, int ky, int kx)
 {
-    if (P.thr_table == nullptr) return {P.t2f, {P.t2hi, P.t2lo}};
+    if (P.thr_table == nullptr) {
+        if (P.frame_t2 != nullptr) {   // a batch of captures: the threshold of this frame's capture
+            const float *t = P.frame_t2 + 3 * frame;
+            return {t[0], {t[1], t[2]}};
+        }
+        return {P.t2f, {P.t2hi, P.t2lo}};
+    }
     const float *t = P.thr_table + 3 * (ky * 5 + (kx - 4));
     return {t[0], {t[1], t[2]}};
 }
@@ -80,8 +86,9 @@ __device__ __noinline__ void exact_pair2(const T2Params &P, int f, int tileX, in
     const int kx = h ? 16 - kxb : kxb;
     const int fl = tileY + i;
     dfc acc = {{0.f, 0.f}, {0.f, 0.f}};
-    if (fl >= fl_first && fl < fl_last) {
-        const uint16_t *row = P.fields + (long long)(f - P.field_base) * P.field_stride + (long long)fl * P.fw;
+    const uint16_t *fp = field_at(P, f);   // f is an output field: inside the buffer or the table
+    if (fp != nullptr && fl >= fl_first && fl < fl_last) {
+        const uint16_t *row = fp + (long long)fl * P.fw;
         dfc x1 = acc;
         for (int x = 0; x < 32; x++) {
             const int xx = max(tileX + x, -fl * P.fw);
@@ -152,11 +159,12 @@ __global__ void __launch_bounds__(32 * kWarps2) tpal2d_kernel(T2Params P)
 
     // --- forward X: row i, DC/black removed, folded about the window centre
     const int fl = tileY + i;
-    const bool valid = (f >= 0) && (f < P.nfields) && (fl >= fl_first) && (fl < fl_last);
+    const uint16_t *fp = (f >= 0 && f < P.nfields) ? field_at(P, f) : nullptr;
+    const bool valid = (fp != nullptr) && (fl >= fl_first) && (fl < fl_last);
     float sx[16], dx[16];
     float rowl1 = 0.f;
     if (valid) {
-        const uint16_t *row = P.fields + (long long)(f - P.field_base) * P.field_stride + (long long)fl * P.fw;
+        const uint16_t *row = fp + (long long)fl * P.fw;
         int a[32];
         int sum = 0;
 #pragma unroll
@@ -255,12 +263,12 @@ __global__ void __launch_bounds__(32 * kWarps2) tpal2d_kernel(T2Params P)
             const float a = mag[k], b = rm[k];
             const float pa = 2.f * E[k] * ab[k] + E[k] * E[k];
             const float pb = 2.f * rE[k] * ra[k] + rE[k] * rE[k];
-            float tt = P.t2f;
-            if (PER_BIN) tt = thr2(P, ky, kx).f;
+            float tt = (P.frame_t2 != nullptr) ? P.frame_t2[3 * (f >> 1)] : P.t2f;
+            if (PER_BIN) tt = thr2(P, f >> 1, ky, kx).f;
             bool sm = sim2(a, b, tt);
             bool u = unc2(a, b, tt, pa, pb);
             if (PER_BIN && kx == 8) {   // the mirror (also kx 8) visits with its own threshold
-                const float t2 = thr2(P, kyr, 8).f;
+                const float t2 = thr2(P, f >> 1, kyr, 8).f;
                 sm |= sim2(a, b, t2);
                 u |= unc2(a, b, t2, pa, pb);
             }
@@ -278,8 +286,8 @@ __global__ void __launch_bounds__(32 * kWarps2) tpal2d_kernel(T2Params P)
         df mb, mr;
         exact_pair2(P, f, tileX, tileY, fl_first, fl_last, kyb, kxb, mb, mr);
         const int kybr = (8 - kyb) & 15;
-        bool sm = df_sim2(mb, mr, thr2(P, kyb, kxb).d);
-        if (kxb == 8) sm |= df_sim2(mb, mr, thr2(P, kybr, 8).d);
+        bool sm = df_sim2(mb, mr, thr2(P, f >> 1, kyb, kxb).d);
+        if (kxb == 8) sm |= df_sim2(mb, mr, thr2(P, f >> 1, kybr, 8).d);
         if (lane == src) {
             n_exact++;
             if ((((keep >> k) & 1u) != 0) != sm) n_flip++;

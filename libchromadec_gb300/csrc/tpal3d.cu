@@ -106,9 +106,15 @@ struct Thr {
     df d;
 };
 
-__device__ __forceinline__ Thr thr_of(const T3Params &P, int kz, int ky, int kx)
+__device__ __forceinline__ Thr thr_of(const T3Params &P, int m, int kz, int ky, int kx)
 {
-    if (P.thr_table == nullptr) return {P.t2f, {P.t2hi, P.t2lo}};
+    if (P.thr_table == nullptr) {
+        if (P.frame_t2 != nullptr) {   // a batch of captures: the threshold of frame m's capture
+            const float *t = P.frame_t2 + 3 * m;
+            return {t[0], {t[1], t[2]}};
+        }
+        return {P.t2f, {P.t2hi, P.t2lo}};
+    }
     const float *t = P.thr_table + 3 * ((kz * 32 + ky) * 3 + (kx - 2));
     return {t[0], {t[1], t[2]}};
 }
@@ -149,7 +155,8 @@ __device__ __forceinline__ void forward_pair(const T3Params &P, int q, int tileX
 {
     const int f = 2 * q + LC.j;
     const int L = tileY + LC.y0 + 2 * LC.i;   // frame line of this lane's row
-    const bool valid = (f >= 0) && (f < P.nfields) && (L >= P.fafl) && (L <= P.lafl);
+    const uint16_t *fp = (f >= 0 && f < P.nfields) ? field_at(P, f) : nullptr;
+    const bool valid = (fp != nullptr) && (L >= P.fafl) && (L <= P.lafl);
 
     // Row samples with black and the row mean removed, folded about the
     // window's centre: s_x = a_x + a_15-x - 2*mean, d_x = a_x - a_15-x
@@ -157,7 +164,7 @@ __device__ __forceinline__ void forward_pair(const T3Params &P, int q, int tileX
     float2 sd[8];   // (s_x, d_x)
     float rowl1 = 0.0f;
     if (valid) {
-        const uint16_t *row = P.fields + (long long)(f - P.field_base) * P.field_stride + (long long)(L >> 1) * P.fw;
+        const uint16_t *row = fp + (long long)(L >> 1) * P.fw;
         int a[16];
         int sum = 0;
 #pragma unroll
@@ -229,18 +236,19 @@ __device__ __noinline__ void exact_pair(const T3Params &P, int m, int tileX, int
     const int p = (f & 1) ^ P.swap;   // SourceField::getOffset of window field f
     const int y0 = (p - tileY) & 1;
     dfc accb = {{0.f, 0.f}, {0.f, 0.f}}, accr = accb;
-    if (f >= 0 && f < P.nfields) {
+    const uint16_t *fp = (f >= 0 && f < P.nfields) ? field_at(P, f) : nullptr;
+    if (fp != nullptr) {
         for (int r4 = 0; r4 < 4; r4++) {
             const int i = part * 4 + r4;
             const int y = y0 + 2 * i;
             const int L = tileY + y;
             if (L < P.fafl || L > P.lafl) continue;
-            const long long base = (long long)(f - P.field_base) * P.field_stride + (long long)(L >> 1) * P.fw + tileX;
+            const long long base = (long long)(L >> 1) * P.fw + tileX;   // within the field
             dfc xb = {{0.f, 0.f}, {0.f, 0.f}}, xr = xb;
             for (int x = 0; x < 16; x++) {
                 long long idx = base + x;
                 idx = idx < 0 ? 0 : idx;
-                const float a = (float)((int)__ldg(P.fields + idx) - P.black);
+                const float a = (float)((int)__ldg(fp + idx) - P.black);
                 const float *cb = c3_dfx[kxb - 2][x];
                 const float *cr = c3_dfx[kxr - 2][x];
                 xb.re = df_add(xb.re, df_mul_f({cb[0], cb[1]}, a));
@@ -404,8 +412,8 @@ __device__ __noinline__ void resolve_uncertain(const T3Params &P, int m, int til
         df mb, mr;
         exact_pair(P, m, tileX, tileY, kz, kyb, kxa, mb, mr);
         const int kzr = (10 - kz) & 7, kybr = (40 - kyb) & 31;
-        bool sim = df_sim(mb, mr, thr_of(P, kz, kyb, kxa).d);
-        if (kxa == 4) sim |= df_sim(mb, mr, thr_of(P, kzr, kybr, 4).d);
+        bool sim = df_sim(mb, mr, thr_of(P, m, kz, kyb, kxa).d);
+        if (kxa == 4) sim |= df_sim(mb, mr, thr_of(P, m, kzr, kybr, 4).d);
         if (lane == src) {
             n_exact++;
             if ((((keep >> kz) & 1u) != 0) != sim) n_flip++;
@@ -420,14 +428,19 @@ __device__ __noinline__ void resolve_uncertain(const T3Params &P, int m, int til
     }
 }
 
-template <bool PER_BIN>
+// TMODE: 0 = one uniform threshold, 1 = per-bin table, 2 = per-frame
+// thresholds (batches of captures).
+template <int TMODE>
 __global__ void __launch_bounds__(32 * kWarps3, 3) tpal3d_kernel(T3Params P)
 {
+    constexpr bool PER_BIN = (TMODE == 1);
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int ntiles = P.ntx * P.nty;
-    const int item = blockIdx.x * kWarps3 + warp;
-    if (item >= ntiles * P.nchunks) return;
+    unsigned int n_exact = 0, n_flip = 0;
+    // Work items (tile position, chunk of frames); a grid smaller than the
+    // item count walks them persistently.
+    for (int item = blockIdx.x * kWarps3 + warp; item < ntiles * P.nchunks; item += gridDim.x * kWarps3) {
     const int tile = item % ntiles;
     const int chunk = item / ntiles;
     const int tx = tile % P.ntx, ty = tile / P.ntx;
@@ -450,8 +463,6 @@ __global__ void __launch_bounds__(32 * kWarps3, 3) tpal3d_kernel(T3Params P)
     const int kyr = (40 - my_ky) & 31;
     const int mirror_lane = kappa(kyr);
 
-    unsigned int n_exact = 0, n_flip = 0;
-
     // Steps m0-5 .. m0-3 only fill the window (fields 2(m0-2) .. 2(m0-2)+5);
     // steps m0-2 and m0-1 also run the Z stage for the carries; the rest output.
     for (int m = m0 - 5; m < m1; m++) {
@@ -472,6 +483,7 @@ __global__ void __launch_bounds__(32 * kWarps3, 3) tpal3d_kernel(T3Params P)
             for (int k = 0; k < 5; k++) ek[k] = __fmaf_rn(c3_wz[z], b[k] + half_r, ek[k]);
         }
         float2 *carry = carry_base + (m & 1) * (2 * 5 * 32);
+        const float tf_m = (TMODE == 2) ? P.frame_t2[3 * m] : P.t2f;   // uniform threshold of frame m
 
         // Z stage per kx pair: column A = kx 2+g (visited by the filter),
         // column B = its mirror kx 6-g (g = 2: kx 4 mirrors onto itself).
@@ -513,12 +525,12 @@ __global__ void __launch_bounds__(32 * kWarps3, 3) tpal3d_kernel(T3Params P)
                 const float a = A.mag[kz], b = rmag[kzr];
                 const float pa = 2.f * A.E * A.ab[kz] + A.E * A.E;
                 const float pb = 2.f * rE * rab[kzr] + rE * rE;
-                float t = P.t2f;
-                if (PER_BIN) t = thr_of(P, kz, my_ky, kxa).f;
+                float t = tf_m;
+                if (PER_BIN) t = thr_of(P, m, kz, my_ky, kxa).f;
                 bool sim = fsim(a, b, t);
                 bool u = funcertain(a, b, t, pa, pb);
                 if (PER_BIN && g == 2) {   // kx = 4: the mirror bin visits too, with its own threshold
-                    const float t2 = thr_of(P, kzr, kyr, 4).f;
+                    const float t2 = thr_of(P, m, kzr, kyr, 4).f;
                     sim |= fsim(a, b, t2);
                     u |= funcertain(a, b, t2, pa, pb);
                 }
@@ -584,6 +596,8 @@ __global__ void __launch_bounds__(32 * kWarps3, 3) tpal3d_kernel(T3Params P)
                 if (X1 >= P.avs && X1 < P.ave) dst[X1] = CS[x].x + CS[x].y;
             }
         }
+    }
+    __syncwarp();   // the next item reuses this warp's shared window
     }
     if (P.stats != nullptr) {
         if (n_exact) atomicAdd(P.stats + 0, n_exact);
@@ -663,11 +677,12 @@ int tp3_init_constants(int device)
     return 0;
 }
 
-int tp3_launch(const T3Params &P, cudaStream_t stream)
+int tp3_launch(const T3Params &P, cudaStream_t stream, int max_blocks)
 {
     const long long items = (long long)P.ntx * P.nty * P.nchunks;
     if (items <= 0) return 0;
-    const unsigned blocks = (unsigned)((items + kWarps3 - 1) / kWarps3);
+    unsigned blocks = (unsigned)((items + kWarps3 - 1) / kWarps3);
+    if (max_blocks > 0 && blocks > (unsigned)max_blocks) blocks = (unsigned)max_blocks;   // persistent grid
     const size_t smem = sizeof(float2) * (size_t)kWarpSmemF2 * kWarps3;
     // function attributes are per device
     static bool attr_set[64] = {};
@@ -675,15 +690,18 @@ int tp3_launch(const T3Params &P, cudaStream_t stream)
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64) return -1;
     if (!attr_set[dev]) {
-        if (cudaFuncSetAttribute(tpal3d_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        if (cudaFuncSetAttribute(tpal3d_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
                 cudaSuccess ||
-            cudaFuncSetAttribute(tpal3d_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaFuncSetAttribute(tpal3d_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(tpal3d_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
                 cudaSuccess)
             return -1;
         attr_set[dev] = true;
     }
-    if (P.thr_table != nullptr) tpal3d_kernel<true><<<blocks, 32 * kWarps3, smem, stream>>>(P);
-    else tpal3d_kernel<false><<<blocks, 32 * kWarps3, smem, stream>>>(P);
+    if (P.thr_table != nullptr) tpal3d_kernel<1><<<blocks, 32 * kWarps3, smem, stream>>>(P);
+    else if (P.frame_t2 != nullptr) tpal3d_kernel<2><<<blocks, 32 * kWarps3, smem, stream>>>(P);
+    else tpal3d_kernel<0><<<blocks, 32 * kWarps3, smem, stream>>>(P);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

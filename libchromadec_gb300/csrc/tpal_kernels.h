@@ -15,8 +15,18 @@ namespace tpal {
 // FP32; row r is field line fl_lo + r, column c is sample avs + c. Output
 // field o is field 2 * frame_begin + o.
 
+// Field f's first sample: from the batch table when there is one (null for
+// a black field), else field f of the contiguous buffer.
+template <typename Params>
+__device__ __forceinline__ const uint16_t *field_at(const Params &P, int f)
+{
+    if (P.field_ptrs != nullptr) return P.field_ptrs[f];
+    return P.fields + (long long)(f - P.field_base) * P.field_stride;
+}
+
 struct T3Params {
     const uint16_t *fields;      // buffer holding fields [field_base, ...)
+    const uint16_t *const *field_ptrs;   // or (batches) each field's first sample by index, null = black
     long long field_stride;
     int field_base;
     int nfields;
@@ -31,11 +41,13 @@ struct T3Params {
     int part_row_stride, fl_lo;
     float t2f, t2hi, t2lo;       // uniform squared threshold (FP32 and double-float)
     const float *thr_table;      // per-bin squared thresholds [8][32][3] x (f, hi, lo), or null
+    const float *frame_t2;       // per-frame squared threshold (f, hi, lo) by frame index, or null (batches)
     unsigned int *stats;         // [0] exact decisions taken, [1] of which FP32 was wrong
 };
 
 struct T2Params {
     const uint16_t *fields;
+    const uint16_t *const *field_ptrs;   // or (batches) each field's first sample by index, null = black
     long long field_stride;
     int field_base;
     int nfields;
@@ -49,12 +61,14 @@ struct T2Params {
     int part_row_stride, fl_lo;
     float t2f, t2hi, t2lo;
     const float *thr_table;      // [16][5] x (f, hi, lo), or null
+    const float *frame_t2;       // per-frame squared threshold (f, hi, lo) by frame index, or null (batches)
     unsigned int *stats;
 };
 
 // PALcolour demodulation + H.273 pack of output fields.
 struct DemodParams {
     const uint16_t *fields;      // same buffer as the transform's
+    const uint16_t *const *field_ptrs;   // or (batches) each field's first sample by index, null = black
     long long field_stride;
     int field_base;
     int field_begin, nout;       // output field o is absolute field field_begin + o
@@ -71,6 +85,7 @@ struct DemodParams {
     float nr_y;                  // luma coring level in sample units (0 = off)
     int format;                  // chd_pixel_format_t: 0 yuv444p16, 1 yuv444ps, 2 rgb48, 3 rgbs, 4 gray16, 5 grays
     void *out;                   // frames in the format's layout, out_w x out_h
+    void *const *frame_out;      // per-frame output pointers by frame index (null entry: not written), or null
     long long out_frame_stride;  // elements per frame
     int out_w, out_h, left_pad, top_pad;
     float ey_scale, ecb_scale, ecr_scale;   // 1/range, ecbFromU/range, ecrFromV/range
@@ -81,7 +96,8 @@ struct DemodParams {
 };
 
 int tp3_init_constants(int device);
-int tp3_launch(const T3Params &p, cudaStream_t stream);
+// max_blocks > 0 caps the grid; the blocks then walk the work items persistently.
+int tp3_launch(const T3Params &p, cudaStream_t stream, int max_blocks = 0);
 int tp2_init_constants(int device);
 int tp2_launch(const T2Params &p, cudaStream_t stream);
 int demod_init_constants(int device, double sample_rate, int field_width);

@@ -42,6 +42,16 @@ class Config(C.Structure):
     ]
 
 
+class Capture(C.Structure):
+    """chdg_capture: one capture of a batch (device buffers)."""
+    _fields_ = [("fields", C.c_void_p), ("field_stride", C.c_int64), ("nfields", C.c_int32), ("kind", C.c_int32),
+                ("threshold", C.c_double), ("out", C.c_void_p)]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("chunk_frames", C.c_int32), ("max_blocks", C.c_int32), ("ms", C.c_float)]
+
+
 _lib = None
 
 
@@ -67,6 +77,11 @@ def lib(build: bool = True):
         L.chdg_decode_host.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
                                        C.c_void_p, C.c_void_p]
         L.chdg_engine_set_profiling.argtypes = [C.c_void_p, C.c_int]
+        L.chdg_batch_create.argtypes = [C.POINTER(Geometry), C.POINTER(Config), C.POINTER(C.c_void_p)]
+        L.chdg_batch_free.argtypes = [C.c_void_p]
+        L.chdg_batch_decode.argtypes = [C.c_void_p, C.POINTER(Capture), C.c_int32, C.c_void_p]
+        L.chdg_batch_autotune.argtypes = [C.c_void_p, C.POINTER(Capture), C.c_int32, C.c_void_p,
+                                          C.POINTER(BatchTuning)]
         L.chdg_engine_kernel_times.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                                C.POINTER(C.c_int64)]
         L.chd_last_error.restype = C.c_char_p
@@ -154,3 +169,48 @@ class Engine:
         a, b = C.c_uint64(), C.c_uint64()
         lib().chdg_engine_stats(self._h, C.byref(a), C.byref(b))
         return a.value, b.value
+
+
+class Batch:
+    """chdg_batch: many captures (mixed Transform 2D/3D, one threshold each)
+    decoded by one launch per mode, replayed from a CUDA graph."""
+
+    def __init__(self, geometry: Optional[Geometry] = None, config: Optional[Config] = None):
+        self.geometry = geometry or default_geometry()
+        self.config = config or default_config()
+        h = C.c_void_p()
+        rc = lib().chdg_batch_create(C.byref(self.geometry), C.byref(self.config), C.byref(h))
+        if rc != 0:
+            raise RuntimeError(f"chdg_batch_create failed ({rc}): {last_error()}")
+        self._h = h
+
+    @staticmethod
+    def captures(items):
+        """items: (fields tensor (n, stride), kind, threshold, out tensor) tuples."""
+        arr = (Capture * len(items))()
+        for i, (f, kind, thr, out) in enumerate(items):
+            arr[i] = Capture(f.data_ptr(), f[0].numel(), f.shape[0], kind, thr, out.data_ptr())
+        return arr
+
+    def decode(self, caps, stream=None):
+        rc = lib().chdg_batch_decode(self._h, caps, len(caps), Engine._stream_ptr(stream))
+        if rc != 0:
+            raise RuntimeError(f"chdg_batch_decode failed ({rc}): {last_error()}")
+
+    def autotune(self, caps, stream=None) -> BatchTuning:
+        t = BatchTuning()
+        rc = lib().chdg_batch_autotune(self._h, caps, len(caps), Engine._stream_ptr(stream), C.byref(t))
+        if rc != 0:
+            raise RuntimeError(f"chdg_batch_autotune failed ({rc}): {last_error()}")
+        return t
+
+    def close(self):
+        if self._h:
+            lib().chdg_batch_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
