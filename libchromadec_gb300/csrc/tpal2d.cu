@@ -119,7 +119,10 @@ __device__ __forceinline__ bool sim2(float a, float b, float t)
 
 __device__ __forceinline__ bool unc2(float a, float b, float t, float pa, float pb)
 {
-    return (fabsf(__fmaf_rn(-b, t, a)) <= pa + t * pb) || (fabsf(__fmaf_rn(-a, t, b)) <= pb + t * pa);
+    // Two bins that are exactly zero with a zero error bound (a flat or
+    // black tile) need no exact pass: both outputs are zero either way.
+    return ((fabsf(__fmaf_rn(-b, t, a)) <= pa + t * pb) || (fabsf(__fmaf_rn(-a, t, b)) <= pb + t * pa)) &&
+           (a + b + pa + pb > 0.f);
 }
 
 __device__ __forceinline__ bool df_sim2(df a, df b, df t)

@@ -110,7 +110,7 @@ __device__ __forceinline__ Thr thr_of(const T3Params &P, int m, int kz, int ky, 
 {
     if (P.thr_table == nullptr) {
         if (P.frame_t2 != nullptr) {   // a batch of captures: the threshold of frame m's capture
-            const float *t = P.frame_t2 + 3 * m;
+            const float *t = P.frame_t2 + 3 * max(m, 0);   // warm-up steps before frame 0 take frame 0's
             return {t[0], {t[1], t[2]}};
         }
         return {P.t2f, {P.t2hi, P.t2lo}};
@@ -483,7 +483,7 @@ __global__ void __launch_bounds__(32 * kWarps3, 3) tpal3d_kernel(T3Params P)
             for (int k = 0; k < 5; k++) ek[k] = __fmaf_rn(c3_wz[z], b[k] + half_r, ek[k]);
         }
         float2 *carry = carry_base + (m & 1) * (2 * 5 * 32);
-        const float tf_m = (TMODE == 2) ? P.frame_t2[3 * m] : P.t2f;   // uniform threshold of frame m
+        const float tf_m = (TMODE == 2) ? P.frame_t2[3 * max(m, 0)] : P.t2f;   // uniform threshold of frame m
 
         // Z stage per kx pair: column A = kx 2+g (visited by the filter),
         // column B = its mirror kx 6-g (g = 2: kx 4 mirrors onto itself).
@@ -539,6 +539,9 @@ __global__ void __launch_bounds__(32 * kWarps3, 3) tpal3d_kernel(T3Params P)
                 if (sim || self) keep |= 1u << kz;
                 if (u && !self) unc |= 1u << kz;
             }
+            // A zero error bound on both columns means a flat or black tile:
+            // every visited bin is exactly zero, and so is either decision's output.
+            if (A.E == 0.f && rE == 0.f) unc = 0;
             // Resolve decisions inside the guard band exactly (rare).
             if (__any_sync(0xffffffffu, unc != 0))
                 resolve_uncertain(P, m, tileX, tileY, g, kxa, lane, keep, unc, n_exact, n_flip);
