@@ -161,6 +161,19 @@ void chdg_batch_free(chdg_batch *b);
 int chdg_batch_decode(chdg_batch *b, const chdg_capture *caps, int32_t n, void *stream);
 int chdg_batch_autotune(chdg_batch *b, const chdg_capture *caps, int32_t n, void *stream, chdg_batch_tuning *out);
 
+/* Multi-source concealment alignment (MultiSourceAlignment::
+ * sourceFrameForPrimaryFrame, src/dropout/multi_source_alignment.cpp:54-71):
+ * the 0-based frame of extra source `source` (1 = the first added with
+ * chd_video_add_extra_source_*) that holds the same disc frame as the
+ * primary's 0-based frame `primary_frame`, matched by CAV picture number or
+ * CLV time code when both captures carry them and positionally otherwise;
+ * -1 when that source does not hold it. Both captures pair their fields in
+ * their own order, swapped when reverse_field_order is non-zero. Returns a
+ * chd_status_t (CHD_E_OUT_OF_RANGE for an unknown source). */
+struct chd_video;
+int chdg_video_source_frame(const struct chd_video *v, int32_t reverse_field_order, int32_t source,
+                            int32_t primary_frame, int32_t *out_frame);
+
 /* Threshold decisions whose FP32 margin was inside the error bound and were
  * re-evaluated in double-float, and how many of those FP32 had wrong. */
 int chdg_engine_stats(chdg_engine *e, uint64_t *exact_decisions, uint64_t *fp32_flips);

@@ -118,6 +118,7 @@ _SIGS = {
     "chd_video_row_sample_to_standard_sample": ([_P, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
     "chd_video_add_extra_source_composite": ([_P, C.c_char_p, C.c_char_p], C.c_int),
     "chd_video_add_extra_source_yc": ([_P, C.c_char_p, C.c_char_p, C.c_char_p], C.c_int),
+    "chdg_video_source_frame": ([_P, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
     "chd_decoder_create": ([_P, C.c_int, _PP], C.c_int), "chd_decoder_free": ([_P], None),
     "chd_decoder_set_option_f64": ([_P, C.c_char_p, C.c_double], C.c_int),
     "chd_decoder_set_option_i32": ([_P, C.c_char_p, C.c_int32], C.c_int),

@@ -140,6 +140,33 @@ DropoutSettings dropout_settings(const chd_decoder_t *d)
     return s;
 }
 
+// The settings a decode runs with: dropout_settings plus, when concealment
+// is on, the video's extra sources. The first such decode freezes the
+// extras and builds their alignment once (c_api_decoder.cpp:219-241).
+DropoutSettings decode_dropout_settings(chd_decoder_t *d)
+{
+    DropoutSettings s = dropout_settings(d);
+    if (!s.enabled) return s;
+    chd_video_t *v = d->video;
+    v->extrasFrozen.store(true, std::memory_order_release);
+    if (v->extras.empty()) return s;
+    std::lock_guard<std::mutex> l(d->sourcesMutex);
+    if (!d->multiSource) {
+        auto ms = std::make_shared<MultiSource>();
+        std::vector<AlignedSource> all;
+        all.push_back({&v->cap, d->firstFieldFirst()});
+        for (const auto &x : v->extras) {
+            const AlignedSource a{x.get(), x->isFirstFieldFirst() != d->reverseFieldOrder};
+            all.push_back(a);
+            ms->extras.push_back(a);
+        }
+        ms->alignment = SourceAlignment(std::move(all));
+        d->multiSource = std::move(ms);
+    }
+    s.sources = d->multiSource;
+    return s;
+}
+
 void publish_stats(chd_decoder_t *d, const FramePlan &p)
 {
     std::lock_guard<std::mutex> l(d->statsMutex);
@@ -535,7 +562,7 @@ CHD_API chd_status_t chd_decode_frame(chd_decoder_t *d, int64_t frame_index, chd
         const int64_t end = std::min<int64_t>(d->numFrames, frame_index + n);
         FramePipeline &p = *d->syncPipe;
         cudaSetDevice(d->device);
-        p.set_dropout(dropout_settings(d));
+        p.set_dropout(decode_dropout_settings(d));
         const size_t fb = p.frame_bytes();
         const int rc = p.decode(
             frame_index, end,
@@ -609,7 +636,7 @@ CHD_API chd_status_t chd_decode_frames_async(chd_decoder_t *d, const int64_t *in
 
     if (failure == CHD_OK) {
         cudaSetDevice(d->device);
-        pipe->set_dropout(dropout_settings(d));
+        pipe->set_dropout(decode_dropout_settings(d));
         const size_t fb = pipe->frame_bytes();
         size_t k = 0;
         while (k < order.size() && failure == CHD_OK && !is_cancelled()) {

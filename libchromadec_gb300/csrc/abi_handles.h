@@ -1,6 +1,7 @@
 // abi_handles.h -- what the opaque chd_* handles hold in this library.
 //
-// chd_video owns an opened capture (mmapped .tbc + parsed sidecar).
+// chd_video owns an opened capture (mmapped .tbc + parsed sidecar) and the
+// extra captures of the same disc that multi-source concealment reads.
 // chd_decoder stashes options until commit (the reference's two-phase
 // lifecycle, src/abi/handles.h:76-200), then owns the GPU frame pipelines:
 // one for chd_decode_frame, which decodes ahead in batches while requests
@@ -25,6 +26,7 @@
 #include "capture.h"
 #include "dropout_plan.h"
 #include "frame_pipeline.h"
+#include "multi_source.h"
 
 #define CHD_API extern "C" __attribute__((visibility("default")))
 
@@ -54,6 +56,12 @@ struct CachedFrame {
 
 struct chd_video {
     chdg::Capture cap;
+    // chd_video_add_extra_source_*: composite extras (and a Y/C extra's
+    // luma), plus the chroma planes of Y/C extras, kept open for their
+    // lifetime; frozen by the first decode with concealment on
+    // (src/abi/handles.h:68-73).
+    std::vector<std::unique_ptr<chdg::Capture>> extras, chromaExtras;
+    std::atomic<bool> extrasFrozen{false};
 };
 
 struct chd_decoder {
@@ -91,6 +99,10 @@ struct chd_decoder {
     // chd_decode_frames_async: idle pipelines.
     std::mutex poolMutex;
     std::vector<std::unique_ptr<chdg::FramePipeline>> pool;
+
+    // The extras' alignment, built on the first decode with concealment on.
+    std::mutex sourcesMutex;
+    std::shared_ptr<const chdg::MultiSource> multiSource;
 };
 
 struct chd_frame {

@@ -5,7 +5,10 @@
 // reference lines it mirrors.
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <string>
+
+#include <sys/stat.h>
 
 #include "abi_handles.h"
 #include "error_state.h"
@@ -230,21 +233,107 @@ CHD_API chd_status_t chd_video_row_sample_to_standard_sample(const chd_video_t *
     return CHD_OK;
 }
 
-// Multi-source concealment (c_api_video.cpp:859-897) needs VBI alignment of
-// several captures, which the single-source GPU concealment does not do.
-CHD_API chd_status_t chd_video_add_extra_source_composite(chd_video_t *v, const char *path, const char *)
+// ---- extra sources for multi-source concealment (c_api_video.cpp:586-897) ---
+
+namespace {
+
+bool exists(const std::string &p)
 {
-    if (v == nullptr || path == nullptr)
-        return fail(CHD_E_INVALID_ARG, "chd_video_add_extra_source_composite: null argument");
-    return fail(CHD_E_UNSUPPORTED, "chd_video_add_extra_source_composite: multi-source dropout correction is not "
-                                   "part of the GPU path");
+    struct stat st;
+    return ::stat(p.c_str(), &st) == 0 && S_ISREG(st.st_mode);
 }
 
-CHD_API chd_status_t chd_video_add_extra_source_yc(chd_video_t *v, const char *luma_path, const char *chroma_path,
-                                                   const char *)
+// Open one extra capture the way the primary is opened (no parameter
+// override); its failure detail is re-attributed to `fn`.
+int open_extra(const std::string &fn, const char *path, const char *sidecar, std::unique_ptr<chdg::Capture> &out)
 {
+    auto c = std::make_unique<chdg::Capture>();
+    const int rc = c->open(path, sidecar, nullptr);
+    if (rc != CHD_OK) {
+        std::string detail = chd::detail::get_last_error();
+        const std::string prefix = "chd_video_open_composite: ";
+        if (detail.compare(0, prefix.size(), prefix) == 0) detail.erase(0, prefix.size());
+        chd::detail::set_last_error(fn + ": " + detail);
+        return rc;
+    }
+    out = std::move(c);
+    return CHD_OK;
+}
+
+// The concealment kernel reads an extra's replacement lines with the
+// primary's field geometry, so an extra must share it.
+int check_geometry(const std::string &fn, const chd_video_t *v, const chdg::Capture &x)
+{
+    if (x.vp().fieldWidth != v->cap.vp().fieldWidth || x.vp().fieldHeight != v->cap.vp().fieldHeight)
+        return fail(CHD_E_FORMAT_UNSUPPORTED, fn + ": the extra source's field geometry differs from the primary's");
+    return CHD_OK;
+}
+
+}  // namespace
+
+CHD_API chd_status_t chd_video_add_extra_source_composite(chd_video_t *v, const char *path,
+                                                          const char *metadata_path_or_null)
+{
+    const std::string fn = "chd_video_add_extra_source_composite";
+    if (v == nullptr || path == nullptr) return fail(CHD_E_INVALID_ARG, fn + ": null argument");
+    if (v->extrasFrozen.load(std::memory_order_acquire))
+        return fail(CHD_E_INVALID_ARG, fn + ": a decode has already run with dropout correction on");
+    if (!exists(path)) return fail(CHD_E_FILE_NOT_FOUND, fn + ": file does not exist: " + path);
+    std::unique_ptr<chdg::Capture> x;
+    if (const int rc = open_extra(fn, path, metadata_path_or_null, x); rc != CHD_OK) return (chd_status_t)rc;
+    if (const int rc = check_geometry(fn, v, *x); rc != CHD_OK) return (chd_status_t)rc;
+    v->extras.push_back(std::move(x));
+    return CHD_OK;
+}
+
+// A luma extra corrects the luma plane and a chroma extra the separately
+// decoded chroma plane of a Y/C decode; for the composite decodes of this
+// library the luma capture is the extra, as in the reference, and the chroma
+// capture is opened and checked but not read.
+CHD_API chd_status_t chd_video_add_extra_source_yc(chd_video_t *v, const char *luma_path, const char *chroma_path,
+                                                   const char *metadata_path_or_null)
+{
+    const std::string fn = "chd_video_add_extra_source_yc";
     if (v == nullptr || luma_path == nullptr || chroma_path == nullptr)
-        return fail(CHD_E_INVALID_ARG, "chd_video_add_extra_source_yc: null argument");
-    return fail(CHD_E_UNSUPPORTED, "chd_video_add_extra_source_yc: multi-source dropout correction is not part of "
-                                   "the GPU path");
+        return fail(CHD_E_INVALID_ARG, fn + ": null argument");
+    if (v->extrasFrozen.load(std::memory_order_acquire))
+        return fail(CHD_E_INVALID_ARG, fn + ": a decode has already run with dropout correction on");
+    if (!exists(luma_path) || !exists(chroma_path))
+        return fail(CHD_E_FILE_NOT_FOUND, fn + ": luma/chroma file does not exist");
+    // openYcPair (c_api_video.cpp:586-629): the chroma plane's own sidecar,
+    // else the luma's
+    const std::string lumaSidecar =
+        metadata_path_or_null != nullptr ? std::string(metadata_path_or_null) : std::string(luma_path) + ".json";
+    std::unique_ptr<chdg::Capture> luma, chroma;
+    if (const int rc = open_extra(fn + " (luma)", luma_path, metadata_path_or_null, luma); rc != CHD_OK)
+        return (chd_status_t)rc;
+    const bool chromaOwn = exists(std::string(chroma_path) + ".json") || exists(std::string(chroma_path) + ".db");
+    if (const int rc = open_extra(fn + " (chroma)", chroma_path, chromaOwn ? nullptr : lumaSidecar.c_str(), chroma);
+        rc != CHD_OK)
+        return (chd_status_t)rc;
+    if (luma->vp().fieldWidth != chroma->vp().fieldWidth || luma->vp().fieldHeight != chroma->vp().fieldHeight)
+        return fail(CHD_E_FORMAT_UNSUPPORTED, fn + ": luma and chroma have mismatched dimensions");
+    if (luma->numFrames(luma->isFirstFieldFirst()) != chroma->numFrames(chroma->isFirstFieldFirst()))
+        return fail(CHD_E_FORMAT_UNSUPPORTED, fn + ": luma and chroma have different frame counts");
+    if (const int rc = check_geometry(fn, v, *luma); rc != CHD_OK) return (chd_status_t)rc;
+    v->extras.push_back(std::move(luma));
+    v->chromaExtras.push_back(std::move(chroma));
+    return CHD_OK;
+}
+
+CHD_API int chdg_video_source_frame(const chd_video_t *v, int32_t reverse_field_order, int32_t source,
+                                    int32_t primary_frame, int32_t *out_frame)
+{
+    if (v == nullptr || out_frame == nullptr) return fail(CHD_E_INVALID_ARG, "chdg_video_source_frame: null argument");
+    if (source < 0 || (size_t)source > v->extras.size())
+        return fail(CHD_E_OUT_OF_RANGE, "chdg_video_source_frame: no such source");
+    const bool rev = reverse_field_order != 0;
+    std::vector<chdg::AlignedSource> all;
+    all.push_back({&v->cap, v->cap.isFirstFieldFirst() != rev});
+    for (const auto &x : v->extras) all.push_back({x.get(), x->isFirstFieldFirst() != rev});
+    const chdg::SourceAlignment a(all, false);
+    const int32_t f = a.frameFor(primary_frame + 1, source);
+    const int frames = all[(size_t)source].cap->numFrames(all[(size_t)source].firstFieldFirst);
+    *out_frame = (f >= 1 && f <= frames) ? f - 1 : -1;
+    return CHD_OK;
 }

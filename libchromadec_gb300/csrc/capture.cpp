@@ -161,8 +161,14 @@ int Capture::open(const char *path, const char *meta_or_null, const chd_video_pa
         for (const auto &fv : fa->arr) {
             FieldMeta fm;
             if (const json::Value *x = fv.get("isFirstField"); x && x->kind == json::Value::Bool) fm.isFirstField = x->b;
+            if (const json::Value *x = fv.get("pad"); x && x->kind == json::Value::Bool) fm.pad = x->b;
             if (const json::Value *vm = fv.get("vitsMetrics"))
                 if (const json::Value *b = vm->get("bPSNR"); b && b->is_number()) fm.bPSNR = b->num;
+            // Vbi::read (ld_metadata_json.cpp:34-56): up to 3 values, the rest 0
+            if (const json::Value *vb = fv.get("vbi"))
+                if (const json::Value *vd = vb->get("vbiData"); vd && vd->kind == json::Value::Array)
+                    for (size_t i = 0; i < 3; i++)
+                        fm.vbi[i] = (i < vd->arr.size()) ? (int32_t)vd->arr[i].num : 0;
             if (const json::Value *d = fv.get("dropOuts"); d && d->kind == json::Value::Object) {
                 const json::Value *sx = d->get("startx"), *ex = d->get("endx"), *fl = d->get("fieldLine");
                 const size_t n = sx && sx->kind == json::Value::Array ? sx->arr.size() : 0;

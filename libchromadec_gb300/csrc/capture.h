@@ -33,7 +33,9 @@ struct Dropout {
 
 struct FieldMeta {
     bool isFirstField = false;
+    bool pad = false;
     double bPSNR = 0.0;
+    int32_t vbi[3] = {0, 0, 0};   // VBI lines 16-18 (Vbi::vbiData, src/metadata/core.h:46-53)
     std::vector<Dropout> dropouts;
 };
 

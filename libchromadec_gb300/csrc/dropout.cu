@@ -33,20 +33,26 @@ __device__ __forceinline__ uint16_t luma_fir(const uint16_t *line, int fw, int x
 
 // frames: per planned frame, the device field index of its slot 0 (slot 1
 // is the next field); ops[op_begin[b] .. op_begin[b+1]) are frame b's.
+// extras: the batch's extra-capture fields (same stride), which ops with
+// srcExtra / chrExtra >= 0 read their replacement lines from.
 __global__ void dropout_apply_kernel(uint16_t *fields, long long field_stride, int fw, const int *frames,
-                                     const DropOp *ops, const int *op_begin)
+                                     const DropOp *ops, const int *op_begin, const uint16_t *extras)
 {
     const int b = blockIdx.x;
     uint16_t *base = fields + (long long)frames[b] * field_stride;
     for (int i = op_begin[b]; i < op_begin[b + 1]; i++) {
         const DropOp op = ops[i];
         uint16_t *target = base + (long long)op.field * field_stride + (long long)op.line * fw;
-        const uint16_t *src = base + (long long)op.srcField * field_stride + (long long)op.srcLine * fw;
+        const uint16_t *src = (op.srcExtra >= 0 ? extras + (long long)op.srcExtra * field_stride
+                                                : base + (long long)op.srcField * field_stride) +
+                              (long long)op.srcLine * fw;
         const int x0 = max(op.startx, 0), x1 = min(op.endx, fw);
         if (op.mode == 1) {
             for (int x = x0 + (int)threadIdx.x; x < x1; x += blockDim.x) target[x] = src[x];
         } else {
-            const uint16_t *chr = base + (long long)op.chrField * field_stride + (long long)op.chrLine * fw;
+            const uint16_t *chr = (op.chrExtra >= 0 ? extras + (long long)op.chrExtra * field_stride
+                                                    : base + (long long)op.chrField * field_stride) +
+                                  (long long)op.chrLine * fw;
             for (int x = x0 + (int)threadIdx.x; x < x1; x += blockDim.x) {
                 const uint16_t lf = luma_fir(src, fw, x);
                 const uint16_t lfc = luma_fir(chr, fw, x);
@@ -58,10 +64,10 @@ __global__ void dropout_apply_kernel(uint16_t *fields, long long field_stride, i
 }
 
 int dropout_apply(uint16_t *fields, long long field_stride, int fw, const int *d_frames, const DropOp *d_ops,
-                  const int *d_op_begin, int nframes, cudaStream_t s)
+                  const int *d_op_begin, int nframes, const uint16_t *extras, cudaStream_t s)
 {
     if (nframes <= 0) return 0;
-    dropout_apply_kernel<<<nframes, 256, 0, s>>>(fields, field_stride, fw, d_frames, d_ops, d_op_begin);
+    dropout_apply_kernel<<<nframes, 256, 0, s>>>(fields, field_stride, fw, d_frames, d_ops, d_op_begin, extras);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

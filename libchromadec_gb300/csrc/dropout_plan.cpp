@@ -61,14 +61,23 @@ void set_locations(const VideoParams &vp, std::vector<DLoc> &d)
 struct Rep {
     bool sameField = true;
     int32_t fieldLine = -1;
+    int32_t source = 0;
     double quality = -1.0;
     int32_t distance = 0;
 };
 
-// findPotentialReplacementLine, dropout_corrector.cpp:417-466
+// Every source's share of one frame: index 0 is the primary.
+struct Sources {
+    std::vector<const VideoParams *> vp;
+    std::vector<std::vector<DLoc>> first, second;   // located dropouts, broadcast / pairing order
+    std::vector<double> quality;
+};
+
+// findPotentialReplacementLine, dropout_corrector.cpp:417-466 (vp: the
+// source's video parameters)
 void find_potential(const VideoParams &vp, const std::vector<DLoc> &target, size_t ti,
-                    const std::vector<DLoc> &source, bool sameField, int32_t offset, int32_t step, double quality,
-                    std::vector<Rep> &cands)
+                    const std::vector<DLoc> &source, bool sameField, int32_t offset, int32_t step, int32_t sourceNo,
+                    double quality, std::vector<Rep> &cands)
 {
     const int32_t firstF = (vp.firstActiveFrameLine + 1) / 2;   // firstActiveFieldLine()
     const int32_t lastF = vp.lastActiveFrameLine / 2;           // lastActiveFieldLine()
@@ -87,6 +96,7 @@ void find_potential(const VideoParams &vp, const std::vector<DLoc> &target, size
             Rep r;
             r.sameField = sameField;
             r.fieldLine = line;
+            r.source = sourceNo;
             r.quality = quality;
             cands.push_back(r);
             return;
@@ -94,10 +104,13 @@ void find_potential(const VideoParams &vp, const std::vector<DLoc> &target, size
     }
 }
 
-// findReplacementLine, dropout_corrector.cpp:248-414 (single source)
-Rep find_replacement(const VideoParams &vp, const std::vector<DLoc> &thisD, const std::vector<DLoc> &otherD,
-                     size_t idx, bool thisFieldIsFirst, bool matchChromaPhase, bool isColourBurst, bool intraField,
-                     double quality)
+// findReplacementLine, dropout_corrector.cpp:248-414: every source in turn
+// (this field up and down, then the other field), nearest frame line first,
+// the higher quality among equally near candidates. thisD / otherD are the
+// per-source lists of this field and the other; the target is thisD[0][idx].
+Rep find_replacement(const VideoParams &vp, const Sources &S, const std::vector<std::vector<DLoc>> &thisD,
+                     const std::vector<std::vector<DLoc>> &otherD, size_t idx, bool thisFieldIsFirst,
+                     bool matchChromaPhase, bool isColourBurst, bool intraField)
 {
     int32_t step, otherOffset;
     if (!matchChromaPhase) {
@@ -114,18 +127,23 @@ Rep find_replacement(const VideoParams &vp, const std::vector<DLoc> &thisD, cons
         otherOffset = -1;
     }
     std::vector<Rep> cands;
-    find_potential(vp, thisD, idx, thisD, true, 0, -step, quality, cands);
-    find_potential(vp, thisD, idx, thisD, true, step, step, quality, cands);
-    if (!isColourBurst && !intraField) {
-        find_potential(vp, thisD, idx, otherD, false, otherOffset, -step, quality, cands);
-        find_potential(vp, thisD, idx, otherD, false, otherOffset + step, step, quality, cands);
+    const std::vector<DLoc> &target = thisD[0];
+    for (size_t s = 0; s < thisD.size(); s++) {
+        const VideoParams &sv = *S.vp[s];
+        const double q = S.quality[s];
+        find_potential(sv, target, idx, thisD[s], true, 0, -step, (int32_t)s, q, cands);
+        find_potential(sv, target, idx, thisD[s], true, step, step, (int32_t)s, q, cands);
+        if (!isColourBurst && !intraField) {
+            find_potential(sv, target, idx, otherD[s], false, otherOffset, -step, (int32_t)s, q, cands);
+            find_potential(sv, target, idx, otherD[s], false, otherOffset + step, step, (int32_t)s, q, cands);
+        }
     }
     Rep rep;
     if (!cands.empty()) {
         rep.distance = 1000000;
         rep.quality = -1;
         for (const Rep &c : cands) {
-            const int32_t dropLine = (2 * thisD[idx].fieldLine) + (thisFieldIsFirst ? 0 : 1);
+            const int32_t dropLine = (2 * target[idx].fieldLine) + (thisFieldIsFirst ? 0 : 1);
             const int32_t srcLine = (2 * c.fieldLine) + (c.sameField ? (thisFieldIsFirst ? 0 : 1) : (thisFieldIsFirst ? 1 : 0));
             const int32_t distance = std::abs(dropLine - srcLine);
             if (distance < rep.distance) {
@@ -141,17 +159,29 @@ Rep find_replacement(const VideoParams &vp, const std::vector<DLoc> &thisD, cons
 }
 
 // correctField + correctDropOut's choice of operation
-// (dropout_corrector.cpp:117-157, 469-530)
-void plan_field(const VideoParams &vp, const std::vector<DLoc> &thisD, const std::vector<DLoc> &otherD, int thisSlot,
-                int otherSlot, bool thisFieldIsFirst, bool intraField, double quality, FramePlan &plan)
+// (dropout_corrector.cpp:117-157, 469-530). A replacement from source s >= 1
+// reads that source's field of the same or the other parity: plan.extras
+// holds each extra source's first and second field at 2(s-1) and 2(s-1)+1.
+void plan_field(const VideoParams &vp, const Sources &S, const std::vector<std::vector<DLoc>> &thisD,
+                const std::vector<std::vector<DLoc>> &otherD, int thisSlot, int otherSlot, bool thisFieldIsFirst,
+                bool intraField, FramePlan &plan)
 {
-    for (size_t i = 0; i < thisD.size(); i++) {
+    auto where = [&](const Rep &r, int32_t &slot, int32_t &extra) {
+        slot = r.sameField ? thisSlot : otherSlot;
+        extra = -1;
+        if (r.source > 0) {
+            const bool first = (r.sameField == thisFieldIsFirst);   // the extra's first-field list
+            extra = 2 * (r.source - 1) + (first ? 0 : 1);
+        }
+    };
+    const std::vector<DLoc> &target = thisD[0];
+    for (size_t i = 0; i < target.size(); i++) {
         Rep rep, crep;
-        if (thisD[i].location == BURST)
-            rep = find_replacement(vp, thisD, otherD, i, thisFieldIsFirst, true, true, intraField, quality);
-        if (thisD[i].location == VISIBLE) {
-            rep = find_replacement(vp, thisD, otherD, i, thisFieldIsFirst, false, false, intraField, quality);
-            crep = find_replacement(vp, thisD, otherD, i, thisFieldIsFirst, true, false, intraField, quality);
+        if (target[i].location == BURST)
+            rep = find_replacement(vp, S, thisD, otherD, i, thisFieldIsFirst, true, true, intraField);
+        if (target[i].location == VISIBLE) {
+            rep = find_replacement(vp, S, thisD, otherD, i, thisFieldIsFirst, false, false, intraField);
+            crep = find_replacement(vp, S, thisD, otherD, i, thisFieldIsFirst, true, false, intraField);
         }
         if (rep.fieldLine == -1) {
             plan.failed++;
@@ -161,16 +191,17 @@ void plan_field(const VideoParams &vp, const std::vector<DLoc> &thisD, const std
         plan.totalDistance += rep.distance;
         DropOp op{};
         op.field = thisSlot;
-        op.line = thisD[i].fieldLine - 1;
-        op.startx = thisD[i].startx;
-        op.endx = thisD[i].endx;
-        op.srcField = rep.sameField ? thisSlot : otherSlot;
+        op.line = target[i].fieldLine - 1;
+        op.startx = target[i].startx;
+        op.endx = target[i].endx;
+        where(rep, op.srcField, op.srcExtra);
         op.srcLine = rep.fieldLine - 1;
-        if (crep.fieldLine == -1 || (thisD[i].fieldLine == rep.fieldLine && thisD[i].fieldLine == crep.fieldLine)) {
+        op.chrExtra = -1;
+        if (crep.fieldLine == -1 || (target[i].fieldLine == rep.fieldLine && target[i].fieldLine == crep.fieldLine)) {
             op.mode = 1;
         } else {
             op.mode = 2;
-            op.chrField = crep.sameField ? thisSlot : otherSlot;
+            where(crep, op.chrField, op.chrExtra);
             op.chrLine = crep.fieldLine - 1;
         }
         plan.ops.push_back(op);
@@ -196,7 +227,7 @@ FieldMeta shift_dropouts(const FieldMeta &f)
 }
 
 FramePlan plan_frame(const VideoParams &vp, const FieldMeta &slot0, const FieldMeta &slot1, bool overcorrect,
-                     bool intraField)
+                     bool intraField, const std::vector<ExtraFrame> &extras)
 {
     FramePlan plan;
     // broadcast order (dropout_corrector.cpp:56-57)
@@ -205,18 +236,31 @@ FramePlan plan_frame(const VideoParams &vp, const FieldMeta &slot0, const FieldM
     const FieldMeta &bs = s0first ? slot1 : slot0;
     const int bfSlot = s0first ? 0 : 1, bsSlot = s0first ? 1 : 0;
     if (bf.dropouts.empty() && bs.dropouts.empty()) return plan;
-    const double quality = (bf.bPSNR + bs.bPSNR) / 2.0;
-    std::vector<DLoc> fd, sd;
-    if (!bf.dropouts.empty()) {
-        fd = populate(vp, bf, overcorrect);
-        set_locations(vp, fd);
+    // sources: the primary, then the extras (dropout_corrector.cpp:60-103)
+    const size_t n = 1 + extras.size();
+    Sources S;
+    S.vp.assign(n, &vp);
+    S.first.assign(n, {});
+    S.second.assign(n, {});
+    S.quality.assign(n, 0.0);
+    S.quality[0] = (bf.bPSNR + bs.bPSNR) / 2.0;
+    auto locate = [&](const VideoParams &svp, const FieldMeta &f, std::vector<DLoc> &out) {
+        if (f.dropouts.empty()) return;
+        out = populate(svp, f, overcorrect);
+        set_locations(vp, out);   // the corrector's own (primary) video parameters
+    };
+    locate(vp, bf, S.first[0]);
+    locate(vp, bs, S.second[0]);
+    for (size_t e = 0; e < extras.size(); e++) {
+        S.vp[e + 1] = &extras[e].vp;
+        S.quality[e + 1] = extras[e].quality;
+        locate(extras[e].vp, extras[e].first, S.first[e + 1]);
+        locate(extras[e].vp, extras[e].second, S.second[e + 1]);
+        plan.extras.push_back(extras[e].firstField);
+        plan.extras.push_back(extras[e].secondField);
     }
-    if (!bs.dropouts.empty()) {
-        sd = populate(vp, bs, overcorrect);
-        set_locations(vp, sd);
-    }
-    plan_field(vp, fd, sd, bfSlot, bsSlot, true, intraField, quality, plan);
-    plan_field(vp, sd, fd, bsSlot, bfSlot, false, intraField, quality, plan);
+    plan_field(vp, S, S.first, S.second, bfSlot, bsSlot, true, intraField, plan);
+    plan_field(vp, S, S.second, S.first, bsSlot, bfSlot, false, intraField, plan);
     return plan;
 }
 

@@ -12,7 +12,7 @@
 namespace chdg {
 
 int dropout_apply(uint16_t *fields, long long field_stride, int fw, const int *d_frames, const DropOp *d_ops,
-                  const int *d_op_begin, int nframes, cudaStream_t s);
+                  const int *d_op_begin, int nframes, const uint16_t *extras, cudaStream_t s);
 int fill_fields(uint16_t *fields, long long field_stride, long long field_len, int nfields, uint16_t value,
                 cudaStream_t s);
 int fill_samples(uint16_t *p, long long n, uint16_t value, cudaStream_t s);
@@ -45,6 +45,7 @@ FramePipeline::~FramePipeline()
         if (d_ops_[i]) cudaFree(d_ops_[i]);
         if (h_idx_[i]) cudaFreeHost(h_idx_[i]);
         if (d_idx_[i]) cudaFree(d_idx_[i]);
+        if (dext_[i]) cudaFree(dext_[i]);
         if (ev_h2d_[i]) cudaEventDestroy(ev_h2d_[i]);
         if (ev_comp_[i]) cudaEventDestroy(ev_comp_[i]);
         if (ev_d2h_[i]) cudaEventDestroy(ev_d2h_[i]);
@@ -86,7 +87,7 @@ int FramePipeline::init(const Capture *cap, const chdg_geometry &g, const chdg_c
 
 void FramePipeline::set_dropout(const DropoutSettings &d)
 {
-    if (d.overcorrect != drop_.overcorrect || d.intra != drop_.intra) plans_.clear();
+    if (d.overcorrect != drop_.overcorrect || d.intra != drop_.intra || d.sources != drop_.sources) plans_.clear();
     drop_ = d;
 }
 
@@ -132,7 +133,32 @@ const FramePlan &FramePipeline::plan_for(int64_t frame)
     if (!wf[0].isPadding && !wf[1].isPadding) {
         FieldMeta m0 = cap_->field(wf[0].fieldNumber), m1 = cap_->field(wf[1].fieldNumber);
         if (second_field_shifted(cap_->vp())) m1 = shift_dropouts(m1);
-        plan = plan_frame(cap_->vp(), m0, m1, drop_.overcorrect, drop_.intra);
+        std::vector<ExtraFrame> extras;
+        if (drop_.sources && !(m0.dropouts.empty() && m1.dropouts.empty())) {
+            // The extras that hold this window frame, matched by VBI disc frame
+            // or positionally, each read by its own pairing
+            // (src/abi/c_api_decoder.cpp:245-282)
+            const MultiSource &ms = *drop_.sources;
+            for (size_t i = 0; i < ms.extras.size(); i++) {
+                const AlignedSource &x = ms.extras[i];
+                const int exFrame = ms.alignment.frameFor((int)frame + 1, (int)i + 1);
+                if (exFrame < 1 || exFrame > x.cap->numFrames(x.firstFieldFirst)) continue;
+                const int a = x.cap->fieldNumber(exFrame, 1, x.firstFieldFirst);
+                const int b = x.cap->fieldNumber(exFrame, 2, x.firstFieldFirst);
+                ExtraFrame ef;
+                ef.vp = x.cap->vp();
+                ef.first = x.cap->field(a);
+                ef.second = x.cap->field(b);
+                ef.quality = (ef.first.bPSNR + ef.second.bPSNR) / 2.0;
+                const bool sh = second_field_shifted(ef.vp);
+                if (sh) ef.second = shift_dropouts(ef.second);
+                const uint16_t black = (uint16_t)ef.vp.black16bIre;
+                ef.firstField = {x.cap, a, false, black};
+                ef.secondField = {x.cap, b, sh, black};
+                extras.push_back(std::move(ef));
+            }
+        }
+        plan = plan_frame(cap_->vp(), m0, m1, drop_.overcorrect, drop_.intra, extras);
     }
     return plans_.emplace(frame, std::move(plan)).first->second;
 }
@@ -193,6 +219,7 @@ int FramePipeline::decode(int64_t a, int64_t b, const Deliver &deliver, const st
     Pending prev;
     bool havePrev = false;
     const size_t fb = eng_.frame_bytes();
+    std::vector<ExtraField> extFields;   // this batch's extra-source fields, in buffer order
     cudaError_t e;
     int i = 0;
     // Batch boundaries: full batches in the middle, short ones at both ends,
@@ -271,14 +298,64 @@ int FramePipeline::decode(int64_t a, int64_t b, const Deliver &deliver, const st
                 }
             }
             size_t o = 0;
+            extFields.clear();
+            std::map<std::pair<const Capture *, int32_t>, int32_t> extIndex;
+            auto ext_slot = [&](const FramePlan &pl, int32_t k) -> int32_t {
+                if (k < 0) return -1;
+                const ExtraField &xf = pl.extras[(size_t)k];
+                auto it = extIndex.find({xf.cap, xf.seq});
+                if (it != extIndex.end()) return it->second;
+                const int32_t idx = (int32_t)extFields.size();
+                extFields.push_back(xf);
+                extIndex.emplace(std::make_pair(xf.cap, xf.seq), idx);
+                return idx;
+            };
             for (int p = 0; p < nplan; p++) {
                 h_idx_[slot][p] = planFrames[p];
                 h_idx_[slot][nplan + p] = (int)o;
-                for (const DropOp &op : plans[p]->ops) h_ops_[slot][o++] = op;
+                for (const DropOp &op : plans[p]->ops) {
+                    DropOp d = op;
+                    d.srcExtra = ext_slot(*plans[p], op.srcExtra);
+                    d.chrExtra = (op.mode == 2) ? ext_slot(*plans[p], op.chrExtra) : -1;
+                    h_ops_[slot][o++] = d;
+                }
             }
             h_idx_[slot][2 * nplan] = (int)o;
         }
         if (const int rc = upload_window(slot, w0, w1); rc != CHD_OK) return rc;
+        if (!extFields.empty()) {
+            if (extFields.size() > ext_cap_) {
+                cudaStreamSynchronize(comp_);
+                cudaStreamSynchronize(copy_);
+                for (int s = 0; s < 2; s++) {
+                    if (dext_[s]) cudaFree(dext_[s]);
+                    dext_[s] = nullptr;
+                }
+                ext_cap_ = std::max<size_t>(extFields.size() * 2, 8);
+                for (int s = 0; s < 2; s++)
+                    if ((e = cudaMalloc(&dext_[s], ext_cap_ * (size_t)dstride_ * 2)) != cudaSuccess)
+                        return cuda_status("extra source fields", e);
+            }
+            const size_t fbytes = flen_ * 2;
+            for (size_t k = 0; k < extFields.size(); k++) {
+                const ExtraField &xf = extFields[k];
+                const uint16_t *src = xf.cap->fieldData(xf.seq);
+                if (src == nullptr) {
+                    chd::detail::set_last_error("chromadec_gb300: extra source field " + std::to_string(xf.seq) +
+                                                " is outside its .tbc file");
+                    return CHD_E_INTERNAL;
+                }
+                uint16_t *dst = dext_[slot] + k * (size_t)dstride_;
+                if (xf.shifted) {   // shiftSecondField (src/decoders/source_field.cpp:51-57)
+                    if ((e = cudaMemcpyAsync(dst, src + 2, fbytes - 4, cudaMemcpyHostToDevice, copy_)) != cudaSuccess)
+                        return cuda_status("H2D", e);
+                    if (fill_samples(dst + flen_ - 2, 2, xf.black, copy_) != 0)
+                        return cuda_status("black tail", cudaGetLastError());
+                } else if ((e = cudaMemcpyAsync(dst, src, fbytes, cudaMemcpyHostToDevice, copy_)) != cudaSuccess) {
+                    return cuda_status("H2D", e);
+                }
+            }
+        }
         if (nplan > 0) {
             cudaMemcpyAsync(d_ops_[slot], h_ops_[slot], nops * sizeof(DropOp), cudaMemcpyHostToDevice, copy_);
             cudaMemcpyAsync(d_idx_[slot], h_idx_[slot], (2 * nplan + 1) * sizeof(int), cudaMemcpyHostToDevice, copy_);
@@ -288,7 +365,7 @@ int FramePipeline::decode(int64_t a, int64_t b, const Deliver &deliver, const st
         if (i >= 2) cudaStreamWaitEvent(comp_, ev_d2h_[slot], 0);   // output slot drained
         if (nplan > 0 &&
             dropout_apply(dwin_[slot], dstride_, cap_->vp().fieldWidth, d_idx_[slot], d_ops_[slot],
-                          d_idx_[slot] + nplan, nplan, comp_) != 0)
+                          d_idx_[slot] + nplan, nplan, dext_[slot], comp_) != 0)
             return cuda_status("dropout kernel", cudaGetLastError());
         if (const int rc = eng_.decode(dwin_[slot], dstride_, (int)(2 * w0), 2 * nframes_, (int)c, (int)ce,
                                        dout_[slot], comp_);

@@ -22,6 +22,7 @@
 #include "capture.h"
 #include "dropout_plan.h"
 #include "engine.h"
+#include "multi_source.h"
 
 namespace chdg {
 
@@ -34,6 +35,8 @@ struct HostChunk {
 
 struct DropoutSettings {
     bool enabled = false, overcorrect = false, intra = false;
+    // extra captures to conceal from (null: the primary alone)
+    std::shared_ptr<const MultiSource> sources;
 };
 
 // Delivery of decoded frames: frame `first + i` lives at chunk->data + i * frame_bytes.
@@ -51,7 +54,8 @@ public:
     // Returns a chd_status_t value.
     int init(const Capture *cap, const chdg_geometry &g, const chdg_config &c, bool firstFieldFirst,
              int batch_frames);
-    // Changing the overcorrect / intra-field settings drops the cached plans.
+    // Changing the overcorrect / intra-field settings or the sources drops
+    // the cached plans.
     void set_dropout(const DropoutSettings &d);
     // Concealment statistics of frame `frame`'s own two fields (0-based).
     FramePlan frame_stats(int64_t frame);
@@ -93,6 +97,9 @@ private:
     DropOp *h_ops_[2] = {nullptr, nullptr}, *d_ops_[2] = {nullptr, nullptr};
     int *h_idx_[2] = {nullptr, nullptr}, *d_idx_[2] = {nullptr, nullptr};   // frames then op_begin
     size_t ops_cap_ = 0, idx_cap_ = 0;
+    // extra captures' fields that a batch's plans read replacement lines from
+    uint16_t *dext_[2] = {nullptr, nullptr};
+    size_t ext_cap_ = 0;   // fields per slot
     std::map<int64_t, FramePlan> plans_;
     std::vector<std::shared_ptr<HostChunk>> chunks_;
 };

@@ -70,6 +70,10 @@ class SynthConfig:
     dropout_min_len: int = 20
     dropout_max_len: int = 400
     saturation_edges: bool = False
+    # Another capture of the same disc: the same pictures (content seeded by
+    # `seed`) with its own noise and dropouts.
+    noise_seed: Optional[int] = None
+    dropout_seed: Optional[int] = None
 
 
 @dataclass
@@ -149,7 +153,7 @@ class PalEncoder:
         self.zp_cx = 0.5 * (ACTIVE_START + ACTIVE_END) + rng.uniform(-40, 40)
         self.zp_cy = 420.0 + rng.uniform(-20, 20)
         self.zp_r = 240.0
-        self.noise_rng = np.random.default_rng(cfg.seed + 7919)
+        self.noise_rng = np.random.default_rng(cfg.seed + 7919 if cfg.noise_seed is None else cfg.noise_seed)
         x = np.arange(FIELD_WIDTH, dtype=np.float64)
         # Raised-cosine gate for the active region (4-sample edges).
         self.active_gate = np.clip(np.minimum(x - (ACTIVE_START - 4), (ACTIVE_END + 3) - x) / 4.0, 0.0, 1.0)
@@ -277,7 +281,7 @@ def make_capture(nfields: int, cfg: SynthConfig, truth: bool = False) -> SynthCa
             ys[f], us[f], vs[f], cs[f] = Y, U, V, C
     dropouts: List[List[Tuple[int, int, int]]] = [[] for _ in range(nfields)]
     if cfg.dropout_line_fraction > 0:
-        drng = np.random.default_rng(cfg.seed + 104729)
+        drng = np.random.default_rng(cfg.seed + 104729 if cfg.dropout_seed is None else cfg.dropout_seed)
         for f in range(nfields):
             for line in range(FIELD_HEIGHT):
                 if drng.random() >= cfg.dropout_line_fraction:
@@ -309,8 +313,36 @@ def video_parameters_json(nfields: int) -> dict:
     }
 
 
-def write_tbc(path: str, cap: SynthCapture) -> str:
-    """Write an ld-decode style .tbc and its .tbc.json sidecar; returns the json path."""
+def _bcd(v: int) -> int:
+    out, shift = 0, 0
+    while True:
+        out |= (v % 10) << shift
+        v //= 10
+        shift += 4
+        if v == 0:
+            return out
+
+
+def cav_vbi(picture: int):
+    """VBI lines 16-18 of a field carrying CAV picture number `picture`
+    (IEC 60857-1986 10.1.3: 0xF00000 | BCD on lines 17 and 18)."""
+    code = 0xF00000 | _bcd(picture)
+    return [0, code, code]
+
+
+def clv_vbi(hours: int, minutes: int, seconds: int, picture: int):
+    """VBI lines 16-18 carrying a CLV time code (IEC 60857-1986 10.1.6 on
+    line 17: 0xF0DD00 | BCD hour << 16 | BCD minutes; 10.1.10 on line 16:
+    0x80E000 | (0xA + tens of seconds) << 16 | units << 8 | BCD picture)."""
+    l17 = 0xF0DD00 | (_bcd(hours) << 16) | _bcd(minutes)
+    l16 = 0x80E000 | ((0xA + seconds // 10) << 16) | ((seconds % 10) << 8) | _bcd(picture)
+    return [l16, l17, 0]
+
+
+def write_tbc(path: str, cap: SynthCapture, vbi=None, bpsnr=None) -> str:
+    """Write an ld-decode style .tbc and its .tbc.json sidecar; returns the
+    json path. vbi: per field [line16, line17, line18] or None; bpsnr: per
+    field VITS bPSNR or None."""
     nfields = cap.fields.shape[0]
     with open(path, "wb") as fp:
         fp.write(np.ascontiguousarray(cap.fields).tobytes())
@@ -320,7 +352,7 @@ def write_tbc(path: str, cap: SynthCapture) -> str:
     }
     for i in range(nfields):
         spans = cap.dropouts[i]
-        meta["fields"].append({
+        fm = {
             "seqNo": i + 1,
             "isFirstField": (i % 2) == 0,
             "syncConf": 100,
@@ -329,7 +361,12 @@ def write_tbc(path: str, cap: SynthCapture) -> str:
                 "endx": [s[1] for s in spans],
                 "fieldLine": [s[2] for s in spans],
             },
-        })
+        }
+        if vbi is not None and vbi[i] is not None:
+            fm["vbi"] = {"vbiData": [int(v) for v in vbi[i]]}
+        if bpsnr is not None:
+            fm["vitsMetrics"] = {"bPSNR": float(bpsnr[i]), "wSNR": 0.0}
+        meta["fields"].append(fm)
     jpath = path + ".json"
     with open(jpath, "w") as fp:
         json.dump(meta, fp)

@@ -54,6 +54,16 @@ class Stats(C.Structure):
     _fields_ = [("corrected", C.c_int64), ("failed", C.c_int64), ("total_distance", C.c_int64)]
 
 
+class Extra(C.Structure):
+    _fields_ = [("fields", C.c_void_p), ("nfields", C.c_int32), ("dropouts", C.POINTER(Dropout)),
+                ("ndropouts", C.c_int32), ("bpsnr", C.POINTER(C.c_double)), ("frame_map", C.POINTER(C.c_int32)),
+                ("nframe_map", C.c_int32)]
+
+
+class Sources(C.Structure):
+    _fields_ = [("bpsnr", C.POINTER(C.c_double)), ("extras", C.POINTER(Extra)), ("nextras", C.c_int32)]
+
+
 class Span(C.Structure):
     _fields_ = [("y", C.c_int32), ("x_start", C.c_int32), ("x_end", C.c_int32), ("origin", C.c_int32)]
 
@@ -95,6 +105,12 @@ def lib():
         L.tpo_dropout_correct_frame.argtypes = [C.POINTER(Params), C.c_void_p, C.c_int32, C.POINTER(Dropout),
                                                 C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
                                                 C.POINTER(Stats)]
+        L.tpo_decode_frames_ms.argtypes = [C.POINTER(Params), C.c_void_p, C.c_int32, C.POINTER(Dropout), C.c_int32,
+                                           C.POINTER(Sources), C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                           C.c_void_p, C.c_int32, C.POINTER(Stats)]
+        L.tpo_dropout_correct_frame_ms.argtypes = [C.POINTER(Params), C.c_void_p, C.c_int32, C.POINTER(Dropout),
+                                                   C.c_int32, C.POINTER(Sources), C.c_int32, C.c_int32, C.c_int32,
+                                                   C.c_void_p, C.POINTER(Stats)]
         L.tpo_dropout_spans.argtypes = [C.POINTER(Params), C.POINTER(Dropout), C.c_int32, C.c_int32, C.c_int32,
                                         C.POINTER(Span), C.c_int32]
         L.tpo_dropout_spans.restype = C.c_int32
@@ -165,18 +181,59 @@ def flatten_dropouts(per_field) -> List[Tuple[int, int, int, int]]:
     return out
 
 
+def _sources(bpsnr, extras):
+    """ctypes Sources for the primary's per-field bPSNR and extra captures
+    [dict(fields=(n, h, w) uint16, dropouts=[(field, startx, endx, fieldLine)],
+    bpsnr=[per field] or None, frame_map=[per primary frame] or None)];
+    returns (Sources or None, keep-alive list)."""
+    if bpsnr is None and not extras:
+        return None, []
+    keep = []
+    src = Sources()
+    if bpsnr is not None:
+        b = np.ascontiguousarray(bpsnr, dtype=np.float64)
+        keep.append(b)
+        src.bpsnr = b.ctypes.data_as(C.POINTER(C.c_double))
+    ex = (Extra * max(1, len(extras or [])))()
+    for i, e in enumerate(extras or []):
+        f = np.ascontiguousarray(e["fields"], dtype=np.uint16)
+        keep.append(f)
+        ex[i].fields = f.ctypes.data
+        ex[i].nfields = f.shape[0]
+        arr, nd = _dropout_array(e.get("dropouts"))
+        keep.append(arr)
+        ex[i].dropouts = arr if arr is not None else None
+        ex[i].ndropouts = nd
+        if e.get("bpsnr") is not None:
+            b = np.ascontiguousarray(e["bpsnr"], dtype=np.float64)
+            keep.append(b)
+            ex[i].bpsnr = b.ctypes.data_as(C.POINTER(C.c_double))
+        if e.get("frame_map") is not None:
+            m = np.ascontiguousarray(e["frame_map"], dtype=np.int32)
+            keep.append(m)
+            ex[i].frame_map = m.ctypes.data_as(C.POINTER(C.c_int32))
+            ex[i].nframe_map = m.shape[0]
+    keep.append(ex)
+    src.extras = ex
+    src.nextras = len(extras or [])
+    return src, keep
+
+
 def decode_frames(p: Params, fields: np.ndarray, first: int, count: int, dropouts=None,
-                  overcorrect: bool = False, intra: bool = False, threads: int = 1):
+                  overcorrect: bool = False, intra: bool = False, threads: int = 1, bpsnr=None, extras=None):
     """Decoded frames as an array (count, 3, h, w) of uint16 (p16) or float32 (ps),
-    plus the summed dropout stats of the decoded frames."""
+    plus the summed dropout stats of the decoded frames. bpsnr / extras: the
+    multi-source concealment inputs (see _sources)."""
     fields = np.ascontiguousarray(fields, dtype=np.uint16)
     nfields = fields.shape[0]
     w, h, _, _ = output_geometry(p)
     out = np.empty(frame_shape(p, count, w, h), dtype=frame_dtype(p))
     arr, nd = _dropout_array(dropouts)
     st = Stats()
-    rc = lib().tpo_decode_frames(C.byref(p), fields.ctypes.data, nfields, arr, nd, int(overcorrect), int(intra),
-                                 first, count, out.ctypes.data, threads, C.byref(st))
+    src, _keep = _sources(bpsnr, extras)
+    rc = lib().tpo_decode_frames_ms(C.byref(p), fields.ctypes.data, nfields, arr, nd,
+                                    C.byref(src) if src is not None else None, int(overcorrect), int(intra),
+                                    first, count, out.ctypes.data, threads, C.byref(st))
     if rc != 0:
         raise RuntimeError("tpo_decode_frames failed")
     return out, (st.corrected, st.failed, st.total_distance)
@@ -191,13 +248,16 @@ def transform_chroma(p: Params, fields: np.ndarray, first: int, count: int) -> n
     return out
 
 
-def dropout_correct_frame(p: Params, fields: np.ndarray, frame: int, dropouts, overcorrect=False, intra=False):
+def dropout_correct_frame(p: Params, fields: np.ndarray, frame: int, dropouts, overcorrect=False, intra=False,
+                          bpsnr=None, extras=None):
     fields = np.ascontiguousarray(fields, dtype=np.uint16)
     out = np.empty((2, p.field_height, p.field_width), dtype=np.uint16)
     arr, nd = _dropout_array(dropouts)
     st = Stats()
-    if lib().tpo_dropout_correct_frame(C.byref(p), fields.ctypes.data, fields.shape[0], arr, nd, int(overcorrect),
-                                       int(intra), frame, out.ctypes.data, C.byref(st)) != 0:
+    src, _keep = _sources(bpsnr, extras)
+    if lib().tpo_dropout_correct_frame_ms(C.byref(p), fields.ctypes.data, fields.shape[0], arr, nd,
+                                          C.byref(src) if src is not None else None, int(overcorrect), int(intra),
+                                          frame, out.ctypes.data, C.byref(st)) != 0:
         raise RuntimeError("tpo_dropout_correct_frame failed")
     return out, (st.corrected, st.failed, st.total_distance)
 
@@ -208,3 +268,128 @@ def dropout_spans(p: Params, dropouts, frame: int, mode: int = 0):
     spans = (Span * cap)()
     n = lib().tpo_dropout_spans(C.byref(p), arr, nd, frame, mode, spans, cap)
     return [(spans[i].y, spans[i].x_start, spans[i].x_end, spans[i].origin) for i in range(min(n, cap))]
+
+
+# ---------------------------------------------------------------------------
+# Multi-source alignment: LaserDisc VBI codes and MultiSourceAlignment,
+# restated for the tests (src/metadata/vbi_decoder.cpp,
+# src/dropout/multi_source_alignment.cpp, src/metadata/core.cpp).
+# ---------------------------------------------------------------------------
+
+def _bcd(v: int):
+    """VbiDecoder::decodeBCD (vbi_decoder.cpp:650-668); None when a nibble is not a digit."""
+    value, place = 0, 1
+    while v:
+        d = v & 0xF
+        if d > 9:
+            return None
+        value += d * place
+        place *= 10
+        v >>= 4
+    return value
+
+
+def vbi_decode_field(l16: int, l17: int, l18: int) -> dict:
+    """VbiDecoder::decode's CAV picture number and CLV time code
+    (vbi_decoder.cpp:131-232, 575-604)."""
+    r = dict(picNo=-1, clvHr=-1, clvMin=-1, clvSec=-1, clvPicNo=-1)
+    if l16 == -1 and l17 == -1 and l18 == -1:
+        return r
+    for line in (l17, l18):
+        line &= 0xFFFFFFFF
+        if line & 0xF00000 == 0xF00000:
+            v = _bcd(line & 0x07FFFF)
+            if v is not None:
+                r["picNo"] = v
+    for line in (l17, l18):
+        line &= 0xFFFFFFFF
+        if line & 0xF0FF00 == 0xF0DD00:
+            h = _bcd((line & 0x0F0000) >> 16)
+            m = _bcd(line & 0xFF) if h is not None else None
+            if m is not None:
+                r["clvMin"], r["clvHr"] = m, h
+    line = l16 & 0xFFFFFFFF
+    if line & 0xF0F000 == 0x80E000:
+        x1 = (line & 0x0F0000) >> 16
+        if x1 >= 0xA:
+            sec = _bcd((line & 0xF00) >> 8)
+            pic = _bcd(line & 0xFF) if sec is not None else None
+            if pic is not None:
+                r["clvPicNo"], r["clvSec"], r["picNo"] = pic, 10 * (x1 - 0xA) + sec, -1
+    return r
+
+
+def vbi_decode_frame(first, second) -> dict:
+    """VbiDecoder::decodeFrame (vbi_decoder.cpp:49-80): first field's code, else the second's."""
+    a, b = vbi_decode_field(*first), vbi_decode_field(*second)
+    return {k: (a[k] if a[k] != -1 else b[k]) for k in a}
+
+
+def num_frames(is_first, first_field_first: bool) -> int:
+    """LdDecodeMetaData::getNumberOfFrames (core.cpp:1092-1110)."""
+    f1 = bool(is_first[0]) if is_first else False
+    off = (0 if f1 else 1) if first_field_first else (1 if f1 else 0)
+    return len(is_first) // 2 - off
+
+
+def field_number(is_first, frame: int, which: int, first_field_first: bool) -> int:
+    """getFirstFieldNumber / getSecondFieldNumber (core.cpp:1112-1190), 1-based; -1 when none."""
+    if frame < 1:
+        return -1
+    if first_field_first:
+        first = frame * 2 - 1
+        second = first + 1
+    else:
+        second = frame * 2 - 1
+        first = second + 1
+    n = len(is_first)
+
+    def isf(k):
+        return 1 <= k <= n and bool(is_first[k - 1])
+
+    while not isf(first):
+        first += 1
+        second += 1
+        if first > n or second > n:
+            return -1
+    if first > n or second > n:
+        return -1
+    return first if which == 1 else second
+
+
+def align_sources(sources):
+    """MultiSourceAlignment over sources [(is_first per field, vbi per field
+    [l16, l17, l18], first_field_first, is_pal)], source 0 the primary.
+    Returns frame_for(primary_frame_1based, s) -> 1-based frame or -1
+    (setMinAndMaxVbiFrames / sourceFrameForPrimaryFrame,
+    multi_source_alignment.cpp:54-177)."""
+    info = []
+    for is_first, vbi, ffF, is_pal in sources:
+        cav = []
+        clv = []
+        for f in range(1, num_frames(is_first, ffF) + 1):
+            a, b = field_number(is_first, f, 1, ffF), field_number(is_first, f, 2, ffF)
+            va = vbi[a - 1] if 1 <= a <= len(vbi) else (0, 0, 0)
+            vb = vbi[b - 1] if 1 <= b <= len(vbi) else (0, 0, 0)
+            v = vbi_decode_frame(va, vb)
+            if v["picNo"] > 0:
+                cav.append(v["picNo"])
+            if -1 not in (v["clvHr"], v["clvMin"], v["clvSec"], v["clvPicNo"]):
+                fps = 25 if is_pal else 30
+                clv.append(v["clvHr"] * 3600 * fps + v["clvMin"] * 60 * fps + v["clvSec"] * fps + v["clvPicNo"])
+        if not cav and not clv:
+            info.append(None)
+        elif len(cav) > len(clv):
+            info.append((min(cav), max(cav)))
+        else:
+            info.append((min(clv), max(clv)))
+
+    def frame_for(frame: int, s: int) -> int:
+        if s == 0 or info[0] is None or info[s] is None:
+            return frame
+        v = info[0][0] - 1 + frame
+        if info[s][0] <= v <= info[s][1]:
+            return v - info[s][0] + 1
+        return -1
+
+    return frame_for

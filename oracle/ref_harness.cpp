@@ -21,6 +21,13 @@
 //   ynr=<luma_nr_level> sff=1 (window slot 0 holds second fields: the
 //   reversed pairing) sclocked=1 (subcarrier-locked: slot-1 fields shifted)
 //   cdp=classic|modern bsp=classic|modern|scientific
+//   extra1=<fields>:<nfields>:<dropout file or ->:<frame offset> (up to
+//   extra8): extra captures for multi-source concealment; window frame f
+//   takes frame f + offset of the extra, positionally as the reference's
+//   MultiSourceAlignment does without VBI codes
+//   (src/dropout/multi_source_alignment.cpp:54-71), skipped when the extra
+//   does not hold it (src/abi/c_api_decoder.cpp:252-262)
+//   bpsnr=<file>: lines "source field bPSNR" (source 0 = primary)
 // The field file holds N fields of 1135x313 uint16, first field first.
 // The dropout file holds lines "field_index startx endx fieldLine".
 
@@ -90,7 +97,31 @@ struct Capture {
     int nfields = 0;
     size_t fieldLen = 0;
     std::vector<chd::metadata::DropOuts> dropouts;  // per field
+    std::vector<double> bpsnr;                       // per field
+    int frameOffset = 0;                             // extras: window frame f is this capture's f + offset
 };
+
+bool readFields(const std::string &path, Capture &cap)
+{
+    cap.samples.resize(cap.fieldLen * cap.nfields);
+    FILE *fp = std::fopen(path.c_str(), "rb");
+    if (!fp) return false;
+    const bool ok = std::fread(cap.samples.data(), 2, cap.samples.size(), fp) == cap.samples.size();
+    std::fclose(fp);
+    return ok;
+}
+
+void readDropouts(const std::string &path, Capture &cap)
+{
+    cap.dropouts.assign(cap.nfields, chd::metadata::DropOuts());
+    cap.bpsnr.assign(cap.nfields, 0.0);
+    if (path.empty() || path == "-") return;
+    std::ifstream in(path);
+    int fi, sx, ex, fl;
+    while (in >> fi >> sx >> ex >> fl) {
+        if (fi >= 0 && fi < cap.nfields) cap.dropouts[fi].append(sx, ex, fl);
+    }
+}
 
 // Field window for frames [firstFrame - lookBehind, firstFrame + 1 + lookAhead),
 // black padding outside the capture (source_field.cpp:88-170).
@@ -112,6 +143,7 @@ void loadWindow(const Capture &cap, const LdDecodeMetaData::VideoParameters &vp,
             const int srcField = pad ? j : 2 * f + j;
             sf.fieldNumber = srcField + 1;
             sf.field.dropOuts = cap.dropouts[srcField];
+            sf.field.vitsMetrics.bPSNR = cap.bpsnr[srcField];
             if (pad) {
                 sf.data.assign(cap.fieldLen, static_cast<uint16_t>(vp.black16bIre));
             } else {
@@ -149,22 +181,47 @@ int main(int argc, char **argv)
     Capture cap;
     cap.nfields = std::atoi(a["nfields"].c_str());
     cap.fieldLen = static_cast<size_t>(vp.fieldWidth) * vp.fieldHeight;
-    cap.samples.resize(cap.fieldLen * cap.nfields);
-    {
-        FILE *fp = std::fopen(a["in"].c_str(), "rb");
-        if (!fp || std::fread(cap.samples.data(), 2, cap.samples.size(), fp) != cap.samples.size()) {
-            std::fprintf(stderr, "ref_harness: cannot read %s\n", a["in"].c_str());
+    if (!readFields(a["in"], cap)) {
+        std::fprintf(stderr, "ref_harness: cannot read %s\n", a["in"].c_str());
+        return 2;
+    }
+    const bool correcting = a.count("dropouts") != 0;
+    readDropouts(correcting ? a["dropouts"] : std::string(), cap);
+    std::vector<Capture> extras;
+    for (int e = 1; e <= 8; e++) {
+        const std::string key = "extra" + std::to_string(e);
+        if (!a.count(key)) break;
+        // <fields>:<nfields>:<dropouts>:<offset>
+        std::vector<std::string> parts;
+        std::string cur;
+        for (char ch : a[key]) {
+            if (ch == ':') {
+                parts.push_back(cur);
+                cur.clear();
+            } else {
+                cur += ch;
+            }
+        }
+        parts.push_back(cur);
+        if (parts.size() != 4) return 2;
+        Capture x;
+        x.nfields = std::atoi(parts[1].c_str());
+        x.fieldLen = cap.fieldLen;
+        if (!readFields(parts[0], x)) {
+            std::fprintf(stderr, "ref_harness: cannot read %s\n", parts[0].c_str());
             return 2;
         }
-        std::fclose(fp);
+        readDropouts(parts[2], x);
+        x.frameOffset = std::atoi(parts[3].c_str());
+        extras.push_back(std::move(x));
     }
-    cap.dropouts.assign(cap.nfields, chd::metadata::DropOuts());
-    const bool correcting = a.count("dropouts") != 0;
-    if (correcting) {
-        std::ifstream in(a["dropouts"]);
-        int fi, sx, ex, fl;
-        while (in >> fi >> sx >> ex >> fl) {
-            if (fi >= 0 && fi < cap.nfields) cap.dropouts[fi].append(sx, ex, fl);
+    if (a.count("bpsnr")) {
+        std::ifstream in(a["bpsnr"]);
+        int src, fi;
+        double v;
+        while (in >> src >> fi >> v) {
+            Capture &c = (src == 0) ? cap : extras.at(src - 1);
+            if (fi >= 0 && fi < c.nfields) c.bpsnr[fi] = v;
         }
     }
 
@@ -229,8 +286,36 @@ int main(int argc, char **argv)
                 if (fields[i].field.dropOuts.empty() && fields[i + 1].field.dropOuts.empty()) continue;
                 chd::dropout::DropoutCorrector corrector(vp);
                 chd::dropout::DropoutCorrectionStats stats;
+                // The extras that hold this window frame, read the way
+                // decodeSourceFrame does (src/abi/c_api_decoder.cpp:245-282):
+                // slot 0 as "first", slot 1 (shifted when subcarrier-locked)
+                // as "second", quality the fields' average bPSNR.
+                const int f = frame - lb + static_cast<int>(i / 2);
+                std::vector<chd::dropout::ExtraSourceFrame> ex;
+                for (const Capture &x : extras) {
+                    const int k = f + x.frameOffset;
+                    if (k < 0 || k >= x.nfields / 2) continue;
+                    chd::dropout::ExtraSourceFrame esf;
+                    esf.firstFieldData.assign(x.samples.begin() + x.fieldLen * (2 * k),
+                                              x.samples.begin() + x.fieldLen * (2 * k + 1));
+                    esf.secondFieldData.assign(x.samples.begin() + x.fieldLen * (2 * k + 1),
+                                               x.samples.begin() + x.fieldLen * (2 * k + 2));
+                    esf.firstFieldMeta.dropOuts = x.dropouts[2 * k];
+                    esf.secondFieldMeta.dropOuts = x.dropouts[2 * k + 1];
+                    esf.firstFieldMeta.vitsMetrics.bPSNR = x.bpsnr[2 * k];
+                    esf.secondFieldMeta.vitsMetrics.bPSNR = x.bpsnr[2 * k + 1];
+                    esf.videoParams = vp;
+                    if (chd::decoders::SourceField::secondFieldIsShifted(esf.videoParams))
+                        chd::decoders::SourceField::shiftSecondField(esf.secondFieldData, esf.secondFieldMeta.dropOuts,
+                                                                     static_cast<uint16_t>(vp.black16bIre));
+                    esf.quality = (esf.firstFieldMeta.vitsMetrics.bPSNR + esf.secondFieldMeta.vitsMetrics.bPSNR) / 2.0;
+                    ex.push_back(std::move(esf));
+                }
                 // correctFrame orders the pair by isFirstField itself
-                corrector.correctFrame(fields[i], fields[i + 1], overcorrect, intra, &stats);
+                if (ex.empty())
+                    corrector.correctFrame(fields[i], fields[i + 1], overcorrect, intra, &stats);
+                else
+                    corrector.correctFrame(fields[i], fields[i + 1], ex, overcorrect, intra, &stats);
                 if (static_cast<int>(i) == startIndex) {
                     totalCorrected += stats.corrected;
                     totalFailed += stats.failed;

@@ -852,7 +852,7 @@ static void set_locations(const tpo_params *p, do_list *d)
 }
 
 typedef struct replacement {
-    int32_t isSameField, fieldLine, distance;
+    int32_t isSameField, fieldLine, distance, sourceNumber;
     double quality;
 } replacement;
 
@@ -862,14 +862,27 @@ static replacement no_replacement(void)
     r.isSameField = 1;
     r.fieldLine = -1;
     r.distance = 0;
+    r.sourceNumber = 0;
     r.quality = -1.0;
     return r;
 }
 
+/* The captures one frame is concealed from: source 0 is the primary (its
+ * broadcast-first and second fields, corrected in place), sources 1.. are
+ * the extra captures that hold the frame (DropoutCorrector::correctFrame's
+ * multi-source form, dropout_corrector.cpp:50-114). */
+#define MAX_SOURCES 9
+typedef struct frame_sources {
+    int32_t n;
+    const uint16_t *first[MAX_SOURCES], *second[MAX_SOURCES];
+    do_list fd[MAX_SOURCES], sd[MAX_SOURCES];   /* located dropouts per source */
+    double quality[MAX_SOURCES];                /* average VITS bPSNR of the frame's two fields */
+} frame_sources;
+
 /* findPotentialReplacementLine, dropout_corrector.cpp:417-466 */
 static void find_potential(const tpo_params *p, const do_list *target, int32_t targetIndex, const do_list *source,
-                           int32_t isSameField, int32_t sourceOffset, int32_t stepAmount, replacement *cands,
-                           int32_t *ncand)
+                           int32_t isSameField, int32_t sourceOffset, int32_t stepAmount, int32_t sourceNo,
+                           double quality, replacement *cands, int32_t *ncand)
 {
     const int32_t firstField = (p->first_active_frame_line + 1) / 2; /* core.h firstActiveFieldLine() */
     const int32_t lastField = p->last_active_frame_line / 2;         /* lastActiveFieldLine() */
@@ -889,7 +902,8 @@ static void find_potential(const tpo_params *p, const do_list *target, int32_t t
             replacement r;
             r.isSameField = isSameField;
             r.fieldLine = sourceLine;
-            r.quality = 0.0; /* no VITS metrics: (bPSNR + bPSNR) / 2 = 0 */
+            r.sourceNumber = sourceNo;
+            r.quality = quality;
             r.distance = 0;
             cands[(*ncand)++] = r;
             return;
@@ -897,10 +911,11 @@ static void find_potential(const tpo_params *p, const do_list *target, int32_t t
     }
 }
 
-/* findReplacementLine, dropout_corrector.cpp:248-414 (single source) */
-static replacement find_replacement(const tpo_params *p, const do_list *thisD, const do_list *otherD,
-                                    int32_t idx, int32_t thisFieldIsFirst, int32_t matchChromaPhase,
-                                    int32_t isColourBurst, int32_t intraField)
+/* findReplacementLine, dropout_corrector.cpp:248-414. thisD / otherD hold
+ * every source's located dropouts; the target is source 0's entry idx. */
+static replacement find_replacement(const tpo_params *p, const do_list *thisD, const do_list *otherD, int32_t nsrc,
+                                    const double *quality, int32_t idx, int32_t thisFieldIsFirst,
+                                    int32_t matchChromaPhase, int32_t isColourBurst, int32_t intraField)
 {
     int32_t stepAmount, otherFieldOffset;
     if (!matchChromaPhase) {
@@ -911,20 +926,24 @@ static replacement find_replacement(const tpo_params *p, const do_list *thisD, c
         stepAmount = 4;
         otherFieldOffset = thisFieldIsFirst ? -3 : -1;
     }
-    replacement cands[4];
+    replacement cands[4 * MAX_SOURCES];
     int32_t nc = 0;
-    find_potential(p, thisD, idx, thisD, 1, 0, -stepAmount, cands, &nc);
-    find_potential(p, thisD, idx, thisD, 1, stepAmount, stepAmount, cands, &nc);
-    if (!isColourBurst && !intraField) {
-        find_potential(p, thisD, idx, otherD, 0, otherFieldOffset, -stepAmount, cands, &nc);
-        find_potential(p, thisD, idx, otherD, 0, otherFieldOffset + stepAmount, stepAmount, cands, &nc);
+    for (int32_t s = 0; s < nsrc; s++) {
+        find_potential(p, &thisD[0], idx, &thisD[s], 1, 0, -stepAmount, s, quality[s], cands, &nc);
+        find_potential(p, &thisD[0], idx, &thisD[s], 1, stepAmount, stepAmount, s, quality[s], cands, &nc);
+        if (!isColourBurst && !intraField) {
+            find_potential(p, &thisD[0], idx, &otherD[s], 0, otherFieldOffset, -stepAmount, s, quality[s], cands,
+                           &nc);
+            find_potential(p, &thisD[0], idx, &otherD[s], 0, otherFieldOffset + stepAmount, stepAmount, s,
+                           quality[s], cands, &nc);
+        }
     }
     replacement rep = no_replacement();
     if (nc > 0) {
         rep.distance = 1000000;
         rep.quality = -1;
         for (int32_t i = 0; i < nc; i++) {
-            const int32_t dropoutFrameLine = (2 * thisD->v[idx].fieldLine) + (thisFieldIsFirst ? 0 : 1);
+            const int32_t dropoutFrameLine = (2 * thisD[0].v[idx].fieldLine) + (thisFieldIsFirst ? 0 : 1);
             const int32_t sourceFrameLine =
                 (2 * cands[i].fieldLine) + (cands[i].isSameField ? (thisFieldIsFirst ? 0 : 1) : (thisFieldIsFirst ? 1 : 0));
             const int32_t distance = abs(dropoutFrameLine - sourceFrameLine);
@@ -956,21 +975,25 @@ static void pal_luma_fir(uint16_t *data, int32_t n, uint16_t *tmp)
     memcpy(data, tmp, sizeof(uint16_t) * (size_t)n);
 }
 
-/* correctDropOut, dropout_corrector.cpp:469-530 */
+/* correctDropOut, dropout_corrector.cpp:469-530. thisData[0] is the target
+ * field; thisData[s] / otherData[s] are source s's fields. */
 static void correct_dropout(const tpo_params *p, const do_loc *d, const replacement *rep, const replacement *crep,
-                            uint16_t *thisData, const uint16_t *otherData, uint16_t *lineBuf, uint16_t *tmp)
+                            uint16_t *target, const uint16_t *const *thisData, const uint16_t *const *otherData,
+                            uint16_t *lineBuf, uint16_t *tmp)
 {
     const int32_t fw = p->field_width;
     if (rep->fieldLine == -1) return;
-    const uint16_t *sourceLine = (rep->isSameField ? thisData : otherData) + ((rep->fieldLine - 1) * fw);
-    uint16_t *targetLine = thisData + ((d->fieldLine - 1) * fw);
+    const uint16_t *sourceLine =
+        (rep->isSameField ? thisData[rep->sourceNumber] : otherData[rep->sourceNumber]) + ((rep->fieldLine - 1) * fw);
+    uint16_t *targetLine = target + ((d->fieldLine - 1) * fw);
     if ((crep->fieldLine == -1) || ((d->fieldLine == rep->fieldLine) && (d->fieldLine == crep->fieldLine))) {
         for (int32_t px = d->startx; px < d->endx; px++) targetLine[px] = sourceLine[px];
     } else {
         memcpy(lineBuf, sourceLine, sizeof(uint16_t) * (size_t)fw);
         pal_luma_fir(lineBuf, fw, tmp);
         for (int32_t px = d->startx; px < d->endx; px++) targetLine[px] = lineBuf[px];
-        const uint16_t *chromaLine = (crep->isSameField ? thisData : otherData) + ((crep->fieldLine - 1) * fw);
+        const uint16_t *chromaLine = (crep->isSameField ? thisData[crep->sourceNumber] : otherData[crep->sourceNumber]) +
+                                     ((crep->fieldLine - 1) * fw);
         memcpy(lineBuf, chromaLine, sizeof(uint16_t) * (size_t)fw);
         pal_luma_fir(lineBuf, fw, tmp);
         for (int32_t px = d->startx; px < d->endx; px++)
@@ -979,18 +1002,20 @@ static void correct_dropout(const tpo_params *p, const do_loc *d, const replacem
 }
 
 /* correctField, dropout_corrector.cpp:117-157 */
-static void correct_field(const tpo_params *p, const do_list *thisD, const do_list *otherD, uint16_t *thisData,
-                          const uint16_t *otherData, int32_t thisFieldIsFirst, int32_t intraField, tpo_stats *stats)
+static void correct_field(const tpo_params *p, const do_list *thisD, const do_list *otherD, int32_t nsrc,
+                          const double *quality, uint16_t *target, const uint16_t *const *thisData,
+                          const uint16_t *const *otherData, int32_t thisFieldIsFirst, int32_t intraField,
+                          tpo_stats *stats)
 {
     uint16_t *lineBuf = (uint16_t *)malloc(sizeof(uint16_t) * 2 * (size_t)p->field_width);
     uint16_t *tmp = lineBuf + p->field_width;
-    for (int32_t i = 0; i < thisD->n; i++) {
+    for (int32_t i = 0; i < thisD[0].n; i++) {
         replacement rep = no_replacement(), crep = no_replacement();
-        if (thisD->v[i].location == LOC_BURST)
-            rep = find_replacement(p, thisD, otherD, i, thisFieldIsFirst, 1, 1, intraField);
-        if (thisD->v[i].location == LOC_VISIBLE) {
-            rep = find_replacement(p, thisD, otherD, i, thisFieldIsFirst, 0, 0, intraField);
-            crep = find_replacement(p, thisD, otherD, i, thisFieldIsFirst, 1, 0, intraField);
+        if (thisD[0].v[i].location == LOC_BURST)
+            rep = find_replacement(p, thisD, otherD, nsrc, quality, i, thisFieldIsFirst, 1, 1, intraField);
+        if (thisD[0].v[i].location == LOC_VISIBLE) {
+            rep = find_replacement(p, thisD, otherD, nsrc, quality, i, thisFieldIsFirst, 0, 0, intraField);
+            crep = find_replacement(p, thisD, otherD, nsrc, quality, i, thisFieldIsFirst, 1, 0, intraField);
         }
         if (stats) {
             if (rep.fieldLine == -1) {
@@ -1000,36 +1025,75 @@ static void correct_field(const tpo_params *p, const do_list *thisD, const do_li
                 stats->total_distance += rep.distance;
             }
         }
-        correct_dropout(p, &thisD->v[i], &rep, &crep, thisData, otherData, lineBuf, tmp);
+        correct_dropout(p, &thisD[0].v[i], &rep, &crep, target, thisData, otherData, lineBuf, tmp);
     }
     free(lineBuf);
 }
 
-/* DropoutCorrector::correctFrame (single source), dropout_corrector.cpp:40-114.
- * The two fields are taken in broadcast order: `first` is the field whose
- * metadata says isFirstField (capture field index fi_first), `second` the
- * other one. d holds the frame's dropouts as loaded (shifted for a
- * subcarrier-locked second field). */
+static int32_t frame_dropouts(const tpo_params *p, const tpo_dropout *d, int32_t nd, int32_t frame,
+                              tpo_dropout **out);
+static void shift_field(const tpo_params *p, const uint16_t *src, uint16_t *dst);
+
+/* DropoutCorrector::correctFrame, dropout_corrector.cpp:40-114, with the
+ * extra sources decodeSourceFrame passes (c_api_decoder.cpp:245-297). The
+ * primary's two fields are taken in broadcast order: `first` is the field
+ * whose metadata says isFirstField (capture field index fi_first), `second`
+ * the other one. d holds the frame's dropouts as loaded (shifted for a
+ * subcarrier-locked second field). An extra source contributes the frame
+ * its frame_map gives for primary frame `frame`, its slot-0 field as
+ * "first" and slot-1 field (shifted when subcarrier-locked) as "second",
+ * the way decodeSourceFrame reads getFirstFieldNumber / getSecondFieldNumber;
+ * extras without the frame are left out. */
 static void correct_frame(const tpo_params *p, const tpo_dropout *d, int32_t nd, int32_t fi_first,
                           int32_t fi_second, uint16_t *first, uint16_t *second, int32_t overCorrect,
-                          int32_t intraField, tpo_stats *stats)
+                          int32_t intraField, tpo_stats *stats, const tpo_sources *src, int32_t frame)
 {
-    do_list fd = {0}, sd = {0};
-    populate(p, d, nd, fi_first, overCorrect, &fd);
-    populate(p, d, nd, fi_second, overCorrect, &sd);
     /* "Skip if no dropouts in primary fields" tests the metadata lists, which
      * also hold entries populate() drops for being off the field. */
     int32_t any = 0;
     for (int32_t i = 0; i < nd; i++)
         if (d[i].field == fi_first || d[i].field == fi_second) any = 1;
-    if (any) {
-        if (fd.n) set_locations(p, &fd);
-        if (sd.n) set_locations(p, &sd);
-        correct_field(p, &fd, &sd, first, second, 1, intraField, stats);
-        correct_field(p, &sd, &fd, second, first, 0, intraField, stats);
+    if (!any) return;
+    const size_t fl = (size_t)p->field_width * p->field_height;
+    frame_sources fs;
+    memset(&fs, 0, sizeof(fs));
+    uint16_t *shifted[MAX_SOURCES] = {0};
+    fs.n = 1;
+    fs.first[0] = first;
+    fs.second[0] = second;
+    fs.quality[0] = (src && src->bpsnr) ? (src->bpsnr[fi_first] + src->bpsnr[fi_second]) / 2.0 : 0.0;
+    populate(p, d, nd, fi_first, overCorrect, &fs.fd[0]);
+    populate(p, d, nd, fi_second, overCorrect, &fs.sd[0]);
+    for (int32_t e = 0; src && e < src->nextras && fs.n < MAX_SOURCES; e++) {
+        const tpo_extra *x = &src->extras[e];
+        const int32_t k = x->frame_map ? (frame < x->nframe_map ? x->frame_map[frame] : -1) : frame;
+        if (k < 0 || k >= x->nfields / 2) continue;
+        const int32_t s = fs.n++;
+        fs.first[s] = x->fields + fl * (size_t)(2 * k);
+        fs.second[s] = x->fields + fl * (size_t)(2 * k + 1);
+        if (p->sc_locked) {
+            shifted[s] = (uint16_t *)malloc(sizeof(uint16_t) * fl);
+            shift_field(p, fs.second[s], shifted[s]);
+            fs.second[s] = shifted[s];
+        }
+        fs.quality[s] = x->bpsnr ? (x->bpsnr[2 * k] + x->bpsnr[2 * k + 1]) / 2.0 : 0.0;
+        tpo_dropout *xd = NULL;
+        const int32_t nxd = x->dropouts ? frame_dropouts(p, x->dropouts, x->ndropouts, k, &xd) : 0;
+        populate(p, xd, nxd, 2 * k, overCorrect, &fs.fd[s]);
+        populate(p, xd, nxd, 2 * k + 1, overCorrect, &fs.sd[s]);
+        free(xd);
     }
-    free(fd.v);
-    free(sd.v);
+    for (int32_t s = 0; s < fs.n; s++) {
+        if (fs.fd[s].n) set_locations(p, &fs.fd[s]);
+        if (fs.sd[s].n) set_locations(p, &fs.sd[s]);
+    }
+    correct_field(p, fs.fd, fs.sd, fs.n, fs.quality, first, fs.first, fs.second, 1, intraField, stats);
+    correct_field(p, fs.sd, fs.fd, fs.n, fs.quality, second, fs.second, fs.first, 0, intraField, stats);
+    for (int32_t s = 0; s < fs.n; s++) {
+        free(fs.fd[s].v);
+        free(fs.sd[s].v);
+        free(shifted[s]);
+    }
 }
 
 /* The dropouts of frame `frame` as SourceField::loadFields leaves them: a
@@ -1072,12 +1136,12 @@ static void shift_field(const tpo_params *p, const uint16_t *src, uint16_t *dst)
 
 /* Correct frame f's fields c0 (slot 0) and c1 (slot 1) in place; stats of the correction. */
 static void correct_slots(const tpo_params *p, const tpo_dropout *fd, int32_t nfd, int32_t f, uint16_t *c0,
-                          uint16_t *c1, int32_t overcorrect, int32_t intra, tpo_stats *st)
+                          uint16_t *c1, int32_t overcorrect, int32_t intra, tpo_stats *st, const tpo_sources *src)
 {
     if (p->first_field_offset == 0)
-        correct_frame(p, fd, nfd, 2 * f, 2 * f + 1, c0, c1, overcorrect, intra, st);
+        correct_frame(p, fd, nfd, 2 * f, 2 * f + 1, c0, c1, overcorrect, intra, st, src, f);
     else
-        correct_frame(p, fd, nfd, 2 * f + 1, 2 * f, c1, c0, overcorrect, intra, st);
+        correct_frame(p, fd, nfd, 2 * f + 1, 2 * f, c1, c0, overcorrect, intra, st, src, f);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1131,7 +1195,7 @@ static int32_t look_ahead(const tpo_params *p) { return p->kind == 3 ? (8 - 1 + 
  * non-padding window frame that has dropouts (c_api_decoder.cpp:300-321). */
 static int32_t load_window(decoder *d, const uint16_t *fields, int32_t nfields, const tpo_dropout *drops,
                            int32_t nd, int32_t overcorrect, int32_t intra, int32_t frame, int32_t lb, int32_t la,
-                           src_field *win, tpo_stats *stats)
+                           src_field *win, tpo_stats *stats, const tpo_sources *src)
 {
     const tpo_params *p = &d->p;
     const size_t fl = (size_t)p->field_width * p->field_height;
@@ -1160,7 +1224,7 @@ static int32_t load_window(decoder *d, const uint16_t *fields, int32_t nfields, 
             if (win[i].data != c0) memcpy(c0, win[i].data, sizeof(uint16_t) * fl);
             if (win[i + 1].data != c1) memcpy(c1, win[i + 1].data, sizeof(uint16_t) * fl);
             tpo_stats st = {0, 0, 0};
-            correct_slots(p, fd, nfd, f, c0, c1, overcorrect, intra, &st);
+            correct_slots(p, fd, nfd, f, c0, c1, overcorrect, intra, &st, src);
             if (f == frame && stats) {
                 stats->corrected += st.corrected;
                 stats->failed += st.failed;
@@ -1175,14 +1239,15 @@ static int32_t load_window(decoder *d, const uint16_t *fields, int32_t nfields, 
 }
 
 static int decode_one(decoder *d, const uint16_t *fields, int32_t nfields, const tpo_dropout *drops, int32_t nd,
-                      int32_t overcorrect, int32_t intra, int32_t frame, void *out, tpo_stats *stats)
+                      int32_t overcorrect, int32_t intra, int32_t frame, void *out, tpo_stats *stats,
+                      const tpo_sources *src)
 {
     const tpo_params *p = &d->p;
     const size_t fl = (size_t)p->field_width * p->field_height;
     src_field win[16];
     const int32_t lb = look_behind(p), la = look_ahead(p);
     const int32_t startIndex =
-        load_window(d, fields, nfields, drops, nd, overcorrect, intra, frame, lb, la, win, stats);
+        load_window(d, fields, nfields, drops, nd, overcorrect, intra, frame, lb, la, win, stats, src);
     double *chroma[2];
     for (int j = 0; j < 2; j++) {
         if (d->tp.nchroma <= j) {
@@ -1218,6 +1283,7 @@ typedef struct job {
     atomic_int err;
     tpo_stats *stats;
     pthread_mutex_t statsMu;
+    const tpo_sources *src;
 } job;
 
 static void *worker(void *arg)
@@ -1234,7 +1300,7 @@ static void *worker(void *arg)
         if (i >= j->count) break;
         tpo_stats st = {0, 0, 0};
         decode_one(&d, j->fields, j->nfields, j->drops, j->nd, j->overcorrect, j->intra, j->first + i,
-                   j->out + (size_t)i * j->frameBytes, &st);
+                   j->out + (size_t)i * j->frameBytes, &st, j->src);
         if (j->stats) {
             pthread_mutex_lock(&j->statsMu);
             j->stats->corrected += st.corrected;
@@ -1251,6 +1317,15 @@ int tpo_decode_frames(const tpo_params *p, const uint16_t *fields, int32_t nfiel
                       int32_t ndropouts, int32_t overcorrect, int32_t intra_field, int32_t first, int32_t count,
                       void *out, int32_t nthreads, tpo_stats *stats)
 {
+    return tpo_decode_frames_ms(p, fields, nfields, dropouts, ndropouts, NULL, overcorrect, intra_field, first, count,
+                                out, nthreads, stats);
+}
+
+int tpo_decode_frames_ms(const tpo_params *p, const uint16_t *fields, int32_t nfields, const tpo_dropout *dropouts,
+                         int32_t ndropouts, const tpo_sources *sources, int32_t overcorrect, int32_t intra_field,
+                         int32_t first, int32_t count, void *out, int32_t nthreads, tpo_stats *stats)
+{
+    if (sources && (sources->nextras < 0 || sources->nextras > MAX_SOURCES - 1)) return -1;
     if (!p || !fields || !out || count < 0 || (p->kind != 1 && p->kind != 2 && p->kind != 3)) return -1;
     if (p->output_format < TPO_FMT_P16 || p->output_format > TPO_FMT_GRAYS) return -1;
     if (p->thresholds && p->n_thresholds != (p->kind == 2 ? 80 : 768)) return -1;
@@ -1269,6 +1344,7 @@ int tpo_decode_frames(const tpo_params *p, const uint16_t *fields, int32_t nfiel
     atomic_init(&j.next, 0);
     atomic_init(&j.err, 0);
     j.stats = stats;
+    j.src = sources;
     if (stats) memset(stats, 0, sizeof(*stats));
     pthread_mutex_init(&j.statsMu, NULL);
     if (nthreads < 1) nthreads = 1;
@@ -1297,7 +1373,7 @@ int tpo_transform_chroma(const tpo_params *p, const uint16_t *fields, int32_t nf
     for (int32_t k = 0; k < count; k++) {
         src_field win[16];
         const int32_t lb = look_behind(p), la = look_ahead(p);
-        const int32_t startIndex = load_window(&d, fields, nfields, NULL, 0, 0, 0, first + k, lb, la, win, NULL);
+        const int32_t startIndex = load_window(&d, fields, nfields, NULL, 0, 0, 0, first + k, lb, la, win, NULL, NULL);
         double *chroma[2] = {out + fl * (size_t)(2 * k), out + fl * (size_t)(2 * k + 1)};
         memset(chroma[0], 0, sizeof(double) * fl * 2);
         if (p->kind == 2) {
@@ -1315,6 +1391,16 @@ int tpo_dropout_correct_frame(const tpo_params *p, const uint16_t *fields, int32
                               const tpo_dropout *dropouts, int32_t ndropouts, int32_t overcorrect,
                               int32_t intra_field, int32_t frame, uint16_t *out, tpo_stats *stats)
 {
+    return tpo_dropout_correct_frame_ms(p, fields, nfields, dropouts, ndropouts, NULL, overcorrect, intra_field,
+                                        frame, out, stats);
+}
+
+int tpo_dropout_correct_frame_ms(const tpo_params *p, const uint16_t *fields, int32_t nfields,
+                                 const tpo_dropout *dropouts, int32_t ndropouts, const tpo_sources *sources,
+                                 int32_t overcorrect, int32_t intra_field, int32_t frame, uint16_t *out,
+                                 tpo_stats *stats)
+{
+    if (sources && (sources->nextras < 0 || sources->nextras > MAX_SOURCES - 1)) return -1;
     const size_t fl = (size_t)p->field_width * p->field_height;
     if (frame < 0 || 2 * frame + 1 >= nfields) return -1;
     memcpy(out, fields + fl * (size_t)(2 * frame), sizeof(uint16_t) * fl);
@@ -1323,7 +1409,7 @@ int tpo_dropout_correct_frame(const tpo_params *p, const uint16_t *fields, int32
     tpo_stats st = {0, 0, 0};
     tpo_dropout *fd = NULL;
     const int32_t nfd = frame_dropouts(p, dropouts, ndropouts, frame, &fd);
-    if (nfd > 0) correct_slots(p, fd, nfd, frame, out, out + fl, overcorrect, intra_field, &st);
+    if (nfd > 0) correct_slots(p, fd, nfd, frame, out, out + fl, overcorrect, intra_field, &st, sources);
     free(fd);
     if (stats) *stats = st;
     return 0;

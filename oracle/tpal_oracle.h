@@ -70,6 +70,30 @@ typedef struct tpo_dropout {
     int32_t field_line;         /* 1-based */
 } tpo_dropout;
 
+/* An extra capture of the same disc for multi-source concealment
+ * (chd_video_add_extra_source_composite): its fields in pairing order
+ * (frame k = fields 2k (slot 0) and 2k+1 (slot 1)), its dropouts, per-field
+ * VITS bPSNR (NULL = 0) and, per primary frame, the frame of this capture
+ * that holds the same picture (-1 = not held; frame_map NULL = the same
+ * frame index, the reference's positional alignment). */
+typedef struct tpo_extra {
+    const uint16_t *fields;
+    int32_t nfields;
+    const struct tpo_dropout *dropouts;
+    int32_t ndropouts;
+    const double *bpsnr;
+    const int32_t *frame_map;
+    int32_t nframe_map;
+} tpo_extra;
+
+/* The sources of a decode: the primary's per-field bPSNR (NULL = 0) and up
+ * to 8 extra captures. */
+typedef struct tpo_sources {
+    const double *bpsnr;
+    const tpo_extra *extras;
+    int32_t nextras;
+} tpo_sources;
+
 typedef struct tpo_stats {
     int64_t corrected, failed, total_distance;
 } tpo_stats;
@@ -99,6 +123,13 @@ int tpo_decode_frames(const tpo_params *p, const uint16_t *fields, int32_t nfiel
                       int32_t first, int32_t count, void *out, int32_t nthreads,
                       tpo_stats *stats);
 
+/* tpo_decode_frames with extra sources for multi-source concealment
+ * (sources NULL = single source). */
+int tpo_decode_frames_ms(const tpo_params *p, const uint16_t *fields, int32_t nfields,
+                         const tpo_dropout *dropouts, int32_t ndropouts, const tpo_sources *sources,
+                         int32_t overcorrect, int32_t intra_field, int32_t first, int32_t count, void *out,
+                         int32_t nthreads, tpo_stats *stats);
+
 /* Transform-PAL chroma (the TransformPal::filterFields output) for the two
  * fields of each frame in [first, first+count): 2*count arrays of
  * field_width*field_height doubles. */
@@ -111,6 +142,11 @@ int tpo_dropout_correct_frame(const tpo_params *p, const uint16_t *fields, int32
                               const tpo_dropout *dropouts, int32_t ndropouts,
                               int32_t overcorrect, int32_t intra_field, int32_t frame,
                               uint16_t *out, tpo_stats *stats);
+
+int tpo_dropout_correct_frame_ms(const tpo_params *p, const uint16_t *fields, int32_t nfields,
+                                 const tpo_dropout *dropouts, int32_t ndropouts, const tpo_sources *sources,
+                                 int32_t overcorrect, int32_t intra_field, int32_t frame, uint16_t *out,
+                                 tpo_stats *stats);
 
 typedef struct tpo_span {
     int32_t y, x_start, x_end, origin;

@@ -63,6 +63,27 @@ CASES = {
                          dropouts=0.02),
     "conceal_sclocked": dict(mode="dropout", kind=3, fmt="p16", nfields=12, seed=33, first=0, count=6,
                              sc_locked=1, dropouts=0.02, overcorrect=1),
+    # multi-source concealment: extra captures of the same pictures with their
+    # own noise and dropouts; `offset` frames of other content lead an extra
+    # (window frame f is its frame f + offset), `trim` frames are cut off its
+    # end; bpsnr is each source's VITS bPSNR (one value per source, or a
+    # per-field list)
+    "conceal_multi": dict(mode="dropout", kind=3, fmt="p16", nfields=12, seed=33, first=0, count=6, dropouts=0.03,
+                          bpsnr=40.5, extras=[dict(noise_seed=61, dropout_seed=71, dropouts=0.03, bpsnr=38.0),
+                                              dict(noise_seed=62, dropout_seed=72, dropouts=0.02, offset=1,
+                                                   bpsnr=42.25)]),
+    "conceal_multi_tie": dict(mode="dropout", kind=3, fmt="p16", nfields=12, seed=36, first=0, count=6,
+                              dropouts=0.04, overcorrect=1,
+                              extras=[dict(noise_seed=63, dropout_seed=73, dropouts=0.05, trim=2),
+                                      dict(noise_seed=64, dropout_seed=74, dropouts=0.05, offset=2)]),
+    "conceal_multi_intra_sclocked": dict(mode="dropout", kind=3, fmt="p16", nfields=12, seed=33, first=0, count=6,
+                                         dropouts=0.03, intra=1, sc_locked=1, bpsnr=[30.0 + 0.5 * i for i in range(12)],
+                                         extras=[dict(noise_seed=65, dropout_seed=75, dropouts=0.04, bpsnr=33.0)]),
+    "t3d_drop_multi": dict(mode="decode", kind=3, fmt="p16", nfields=12, seed=33, first=0, count=6, dropouts=0.03,
+                           bpsnr=39.0, extras=[dict(noise_seed=61, dropout_seed=71, dropouts=0.03, bpsnr=41.0),
+                                               dict(noise_seed=66, dropout_seed=76, dropouts=0.02, offset=1, trim=1)]),
+    "t2d_drop_multi_rev_ps": dict(mode="decode", kind=2, fmt="ps", nfields=9, seed=35, first=0, count=4, sff=1,
+                                  dropouts=0.03, extras=[dict(noise_seed=67, dropout_seed=77, dropouts=0.03)]),
 }
 
 # harness argument of each optional case key
@@ -90,6 +111,43 @@ def case_inputs(case: dict):
     if case.get("dropouts", 0.0) > 0:
         flat = [(f - skip, s[0], s[1], s[2]) for f, spans in enumerate(cap.dropouts) for s in spans if f >= skip]
     return np.ascontiguousarray(cap.fields[skip:]), flat
+
+
+def _per_field(v, n):
+    if v is None:
+        return None
+    if isinstance(v, (list, tuple)):
+        return np.asarray(v[:n], dtype=np.float64)
+    return np.full(n, float(v))
+
+
+def case_sources(case: dict):
+    """Multi-source inputs of a case: (primary per-field bPSNR or None,
+    [dict(fields, dropouts, bpsnr, offset)] extras) laid out like the
+    primary from case_inputs (reversed pairing drops the same first field)."""
+    if "extras" not in case:
+        return None, []
+    skip = 1 if case.get("sff") else 0
+    n = case["nfields"] - skip
+    extras = []
+    for e in case["extras"]:
+        off, trim = e.get("offset", 0), e.get("trim", 0)
+        cfg = synth.SynthConfig(seed=case["seed"], pan_x=1.5, pan_y=0.5, dropout_line_fraction=e["dropouts"],
+                                noise_seed=e["noise_seed"], dropout_seed=e["dropout_seed"])
+        rc = synth.make_capture(case["nfields"], cfg)
+        fields = np.ascontiguousarray(rc.fields[skip:])
+        drops = [(f - skip, s[0], s[1], s[2]) for f, spans in enumerate(rc.dropouts) for s in spans if f >= skip]
+        if off > 0:   # leading frames of other content
+            lead = synth.make_capture(2 * off, synth.SynthConfig(seed=case["seed"] + 1000, noise_seed=e["noise_seed"]))
+            fields = np.concatenate([lead.fields, fields])
+            drops = [(f + 2 * off, a, b, c) for f, a, b, c in drops]
+        if trim > 0:
+            keep = fields.shape[0] - 2 * trim
+            fields = np.ascontiguousarray(fields[:keep])
+            drops = [d for d in drops if d[0] < keep]
+        extras.append(dict(fields=fields, dropouts=drops, bpsnr=_per_field(e.get("bpsnr"), fields.shape[0]),
+                           offset=off))
+    return _per_field(case.get("bpsnr"), n), extras
 
 
 def thresholds_for(case: dict):

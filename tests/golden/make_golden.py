@@ -25,7 +25,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from tests.golden.cases import CASES, HARNESS_ARGS, case_inputs, thresholds_for  # noqa: E402
+from tests.golden.cases import CASES, HARNESS_ARGS, case_inputs, case_sources, thresholds_for  # noqa: E402
 from oracle import oracle  # noqa: E402
 
 
@@ -48,6 +48,25 @@ def run_case(harness: str, case: dict, tmp: str) -> dict:
                 fp.write(f"{f} {sx} {ex} {fl}\n")
         args += [f"dropouts={dpath}", f"overcorrect={int(case.get('overcorrect', 0))}",
                  f"intra={int(case.get('intra', 0))}"]
+    bpsnr, extras = case_sources(case)
+    blines = []
+    if bpsnr is not None:
+        blines += [f"0 {i} {float(v)!r}" for i, v in enumerate(bpsnr)]
+    for k, e in enumerate(extras):
+        epath = os.path.join(tmp, f"extra{k + 1}.u16")
+        e["fields"].tofile(epath)
+        edrop = os.path.join(tmp, f"extra{k + 1}_drop.txt")
+        with open(edrop, "w") as fp:
+            for f, sx, ex, fl in e["dropouts"]:
+                fp.write(f"{f} {sx} {ex} {fl}\n")
+        args.append(f"extra{k + 1}={epath}:{e['fields'].shape[0]}:{edrop}:{e['offset']}")
+        if e["bpsnr"] is not None:
+            blines += [f"{k + 1} {i} {float(v)!r}" for i, v in enumerate(e["bpsnr"])]
+    if blines:
+        bpath = os.path.join(tmp, "bpsnr.txt")
+        with open(bpath, "w") as fp:
+            fp.write("\n".join(blines) + "\n")
+        args.append(f"bpsnr={bpath}")
     thr = thresholds_for(case)
     if thr is not None:
         tpath = os.path.join(tmp, "thr.txt")
@@ -61,8 +80,11 @@ def run_case(harness: str, case: dict, tmp: str) -> dict:
     stats = json.loads(r.stdout.strip().splitlines()[-1])
     with open(out, "rb") as fp:
         data = fp.read()
-    return {"input_sha256": sha(fields.tobytes()), "output_sha256": sha(data), "output_bytes": len(data),
-            "stats": [stats["corrected"], stats["failed"], stats["total_distance"]]}
+    res = {"input_sha256": sha(fields.tobytes()), "output_sha256": sha(data), "output_bytes": len(data),
+           "stats": [stats["corrected"], stats["failed"], stats["total_distance"]]}
+    if extras:
+        res["extras_sha256"] = [sha(e["fields"].tobytes()) for e in extras]
+    return res
 
 
 def main() -> None:

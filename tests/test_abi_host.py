@@ -139,7 +139,6 @@ def test_video_info_and_conversions(pal_tbc):
     assert L.chd_video_standard_sample_to_row_sample(v._h, 1000, C.byref(o)) == 0 and o.value == 42
     assert L.chd_video_row_sample_to_standard_sample(v._h, 42, C.byref(o)) == 0 and o.value == 1000
     assert L.chd_video_row_sample_to_standard_sample(v._h, 1135, C.byref(o)) == abi.E_OUT_OF_RANGE
-    assert L.chd_video_add_extra_source_composite(v._h, path.encode(), None) == abi.E_UNSUPPORTED
 
 
 def test_option_applicability(pal_tbc):
@@ -230,6 +229,140 @@ def _write_ntsc_capture(tmp_path, dropouts, nfields=4):
     with open(path + ".json", "w") as fp:
         json.dump(meta, fp)
     return path
+
+
+def _write_vbi_capture(tmp_path, name, nframes, vbi_of_frame, nfields=None, first_is_first=True):
+    """A small PAL .tbc whose fields carry VBI lines from vbi_of_frame(k)
+    (frame k = fields 2k, 2k+1; both fields carry the frame's code, as in the
+    reference's test_multi_source_alignment.cpp), or none when it returns None."""
+    n = nfields if nfields is not None else 2 * nframes
+    cap = synth.SynthCapture(fields=np.full((n, 313, 1135), 0x4000, dtype=np.uint16), dropouts=[[] for _ in range(n)])
+    vbi = [vbi_of_frame(i // 2) for i in range(n)]
+    path = str(tmp_path / name)
+    synth.write_tbc(path, cap, vbi=vbi)
+    if not first_is_first:
+        meta = json.load(open(path + ".json"))
+        for i, f in enumerate(meta["fields"]):
+            f["isFirstField"] = (i % 2) == 1
+        json.dump(meta, open(path + ".json", "w"))
+    return path
+
+
+def test_extra_source_statuses(tmp_path, pal_tbc):
+    """chd_video_add_extra_source_* (src/abi/c_api_video.cpp:631-897): null
+    arguments, missing files, the Y/C pair checks, and this library's own
+    rule that an extra shares the primary's field geometry."""
+    path, _ = pal_tbc
+    v = abi.Video(path)
+    L = abi.lib()
+    assert L.chd_video_add_extra_source_composite(None, path.encode(), None) == abi.E_INVALID_ARG
+    assert L.chd_video_add_extra_source_composite(v._h, None, None) == abi.E_INVALID_ARG
+    assert L.chd_video_add_extra_source_composite(v._h, str(tmp_path / "none.tbc").encode(), None) == \
+        abi.E_FILE_NOT_FOUND
+    ntsc = _write_ntsc_capture(tmp_path, [])
+    assert L.chd_video_add_extra_source_composite(v._h, ntsc.encode(), None) == abi.E_FORMAT_UNSUPPORTED
+    assert b"geometry" in L.chd_last_error()
+    assert L.chd_video_add_extra_source_composite(v._h, path.encode(), None) == 0
+    # Y/C: luma sidecar shared by the chroma plane
+    luma = _write_vbi_capture(tmp_path, "yc.tbc", 2, lambda k: None)
+    chroma = str(tmp_path / "yc_chroma.tbc")
+    np.full((4, 313, 1135), 0x4000, dtype=np.uint16).tofile(chroma)
+    assert L.chd_video_add_extra_source_yc(v._h, luma.encode(), None, None) == abi.E_INVALID_ARG
+    assert L.chd_video_add_extra_source_yc(v._h, luma.encode(), str(tmp_path / "x").encode(), None) == \
+        abi.E_FILE_NOT_FOUND
+    short = str(tmp_path / "short_chroma.tbc")
+    np.full((2, 313, 1135), 0x4000, dtype=np.uint16).tofile(short)
+    meta = json.load(open(luma + ".json"))
+    meta["fields"] = meta["fields"][:2]
+    json.dump(meta, open(short + ".json", "w"))
+    assert L.chd_video_add_extra_source_yc(v._h, luma.encode(), short.encode(), None) == abi.E_FORMAT_UNSUPPORTED
+    assert L.chd_video_add_extra_source_yc(v._h, luma.encode(), chroma.encode(), None) == 0
+    o = C.c_int32()
+    assert L.chdg_video_source_frame(v._h, 0, 3, 0, C.byref(o)) == abi.E_OUT_OF_RANGE
+    assert L.chdg_video_source_frame(v._h, 0, 2, 1, C.byref(o)) == 0 and o.value == 1   # no VBI: positional
+
+
+def _cav(pic):
+    return None if pic is None else [0, 0xF00000 | int(str(pic), 16), 0]
+
+
+def test_multi_source_alignment_known_answers(tmp_path):
+    """The reference's own alignment test (tests/unit/test_multi_source_alignment.cpp)
+    through chdg_video_source_frame: a primary holding CAV pictures 100..109,
+    extra A 105..114, extra B without VBI; then the reversed pairing."""
+    L = abi.lib()
+    prim = _write_vbi_capture(tmp_path, "p.tbc", 10, lambda k: _cav(100 + k))
+    a = _write_vbi_capture(tmp_path, "a.tbc", 10, lambda k: _cav(105 + k))
+    b = _write_vbi_capture(tmp_path, "b.tbc", 10, lambda k: None)
+    v = abi.Video(prim)
+    assert L.chd_video_add_extra_source_composite(v._h, a.encode(), None) == 0
+    assert L.chd_video_add_extra_source_composite(v._h, b.encode(), None) == 0
+    o = C.c_int32()
+
+    def fr(rev, s, f):
+        assert L.chdg_video_source_frame(v._h, rev, s, f, C.byref(o)) == 0
+        return o.value
+
+    # 0-based here: the reference's sequential frame 6 is frame 5
+    assert fr(0, 1, 5) == 0          # disc 105 is extra A's first frame
+    assert fr(0, 1, 0) == -1         # disc 100 precedes extra A
+    assert fr(0, 0, 5) == 5          # the primary maps to itself
+    assert fr(0, 2, 5) == 5          # no VBI: positional
+    assert fr(0, 1, 9) == 4
+    # reversed pairing: sequential frame 1 is fields (3, 2), disc 101
+    assert fr(1, 1, 5) == 0          # disc 106: the reversed primary's frame 6, extra A's frame 1
+    assert fr(1, 1, 4) == -1
+
+
+def test_multi_source_alignment_matches_oracle(tmp_path):
+    """CAV and CLV codes, invalid BCD digits, codes on only one field, a
+    CLV picture number on line 16 cancelling a CAV one, sources with no
+    codes, and both pairings: the library's alignment against the oracle's
+    restatement of VbiDecoder / MultiSourceAlignment."""
+    L = abi.lib()
+    rng = np.random.default_rng(17)
+
+    def clv(fn):
+        s_, p_ = divmod(fn, 25)
+        m_, s_ = divmod(s_, 60)
+        h_, m_ = divmod(m_, 60)
+        return synth.clv_vbi(h_, m_, s_, p_)
+
+    layouts = {
+        "cav": lambda base: (lambda k: _cav(base + k)),
+        "clv": lambda base: (lambda k: clv(base + k)),
+        "noisy": lambda base: (lambda k: [int(rng.integers(0, 1 << 24)) for _ in range(3)] if k % 3 == 0
+                               else _cav(base + k)),
+        "none": lambda base: (lambda k: None),
+        "cav_then_clv16": lambda base: (lambda k: [clv(base + k)[0], 0xF00000 | int(str(base + k), 16), 0]),
+    }
+    names = list(layouts)
+    for trial in range(6):
+        srcs = []
+        paths = []
+        for s in range(3):
+            kind = names[int(rng.integers(0, len(names)))] if s or trial % 2 else "cav"
+            base = int(rng.integers(1, 200))
+            nfr = int(rng.integers(4, 9))
+            fn = layouts[kind](base)
+            p = _write_vbi_capture(tmp_path, f"t{trial}_{s}.tbc", nfr, fn)
+            meta = json.load(open(p + ".json"))
+            srcs.append(([f["isFirstField"] for f in meta["fields"]],
+                         [tuple(f.get("vbi", {}).get("vbiData", [0, 0, 0])) for f in meta["fields"]], nfr))
+            paths.append(p)
+        v = abi.Video(paths[0])
+        for p in paths[1:]:
+            assert L.chd_video_add_extra_source_composite(v._h, p.encode(), None) == 0
+        for rev in (0, 1):
+            frame_for = oracle.align_sources([(f, vb, not rev, True) for f, vb, _ in srcs])
+            for s in range(3):
+                nfr_s = oracle.num_frames(srcs[s][0], not rev)
+                for f in range(oracle.num_frames(srcs[0][0], not rev)):
+                    want = frame_for(f + 1, s)
+                    want = want - 1 if 1 <= want <= nfr_s else -1
+                    o = C.c_int32()
+                    assert L.chdg_video_source_frame(v._h, rev, s, f, C.byref(o)) == 0
+                    assert o.value == want, (trial, rev, s, f)
 
 
 def test_dropout_spans_known_answers(tmp_path):

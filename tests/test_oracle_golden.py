@@ -15,7 +15,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
-from tests.golden.cases import CASES, case_inputs, thresholds_for
+from tests.golden.cases import CASES, case_inputs, case_sources, thresholds_for
 
 GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "golden.json")))["cases"]
 
@@ -44,9 +44,16 @@ def test_restatement_matches_reference_golden(name):
     assert hashlib.sha256(fields.tobytes()).hexdigest() == gold["input_sha256"], "synthetic input changed"
     p = _params(case)
     oc, intra = bool(case.get("overcorrect", 0)), bool(case.get("intra", 0))
+    bpsnr, extras = case_sources(case)
+    if extras:
+        assert [hashlib.sha256(e["fields"].tobytes()).hexdigest() for e in extras] == gold["extras_sha256"]
+    nframes = fields.shape[0] // 2
+    # positional alignment with each extra's leading frames: window frame f is the extra's f + offset
+    ex = [dict(fields=e["fields"], dropouts=e["dropouts"], bpsnr=e["bpsnr"],
+               frame_map=[f + e["offset"] for f in range(nframes)]) for e in extras]
     if case["mode"] == "decode":
         out, st = O.decode_frames(p, fields, case["first"], case["count"], dropouts=drops, overcorrect=oc,
-                                  intra=intra, threads=8)
+                                  intra=intra, threads=8, bpsnr=bpsnr, extras=ex)
         data = out.tobytes()
     elif case["mode"] == "chroma":
         data = O.transform_chroma(p, fields, case["first"], case["count"]).tobytes()
@@ -54,7 +61,7 @@ def test_restatement_matches_reference_golden(name):
     else:
         parts, tot = [], np.zeros(3, dtype=np.int64)
         for k in range(case["first"], case["first"] + case["count"]):
-            f2, s = O.dropout_correct_frame(p, fields, k, drops, oc, intra)
+            f2, s = O.dropout_correct_frame(p, fields, k, drops, oc, intra, bpsnr=bpsnr, extras=ex)
             parts.append(f2.tobytes())
             tot += s
         data, st = b"".join(parts), tuple(int(x) for x in tot)
