@@ -109,10 +109,11 @@ int chdg_chroma_device(chdg_engine *e, const uint16_t *d_fields, int64_t field_s
  * allocate device memory while decoding: hosts whose device memory belongs to
  * their own allocator or budget, and latency-critical loops where cudaMalloc's
  * implicit device synchronisation would stall other work. The chroma scratch
- * is a fixed array compiled into the library (69.9 MB: 8 frames of the
- * 948x576 active picture), which every GPU that loads the library holds until
- * the process exits; calls asking for more than 8 frames, or a larger active
- * picture, fail with CHDG_E_INVALID_ARG. No cudaMalloc/cudaFree or other
+ * and the guard-band decision records are fixed arrays compiled into the
+ * library (85.3 MB: 8 frames of the 948x576 active picture), which every GPU
+ * that loads the library holds until the process exits; calls asking for
+ * more than 8 frames, or a larger active picture, fail with
+ * CHDG_E_INVALID_ARG. No cudaMalloc/cudaFree or other
  * allocating call is made. All calls on a device share the one scratch array
  * (it keeps the last call's contents), so calls whose work overlaps on the GPU
  * race: serialise them on one stream. The first call on a device resolves the

@@ -63,6 +63,9 @@ Engine::~Engine()
     if (partial_) cudaFree(partial_);
     if (thr_dev_) cudaFree(thr_dev_);
     if (stats_dev_) cudaFree(stats_dev_);
+    if (unc_rec_) cudaFree(unc_rec_);
+    if (rerun_) cudaFree(rerun_);
+    if (counters_) cudaFree(counters_);
     for (int i = 0; i < 2; i++) {
         if (hp_fields_[i]) cudaFree(hp_fields_[i]);
         if (hp_out_[i]) cudaFree(hp_out_[i]);
@@ -143,6 +146,7 @@ int Engine::init_static(const chdg_geometry &g, const chdg_config &c, float *thr
 {
     g_ = g;
     c_ = c;
+    static_ = true;
     if (c.kind != 8) return arg_fail("the allocation-free decode supports CHD_DEC_TRANSFORM_3D (8) only");
     if (g.field_width <= 0 || g.field_height <= 0 || g.active_start < 0 || g.active_end > g.field_width ||
         g.active_end <= g.active_start || g.first_active_frame_line < 0 ||
@@ -238,6 +242,35 @@ int Engine::ensure_partial(int nout_fields)
     return 0;
 }
 
+int Engine::ensure_deferred(int frames, int nchunks)
+{
+    const int ntiles = ((g_.active_end - (g_.active_start - 8) + 7) / 8) *
+                       ((g_.last_active_frame_line - (g_.first_active_frame_line - 16)) / 16 + 1);
+    const unsigned long long need = tpal::tp3_unc_capacity(ntiles, frames, nchunks);
+    cudaError_t e;
+    if (counters_ == nullptr && (e = cudaMalloc(&counters_, 2 * sizeof(unsigned))) != cudaSuccess) {
+        counters_ = nullptr;
+        return cuda_fail("decision counters", e);
+    }
+    if (need <= unc_cap_) return 0;
+    if (unc_rec_) cudaFree(unc_rec_);
+    if (rerun_) cudaFree(rerun_);
+    unc_rec_ = nullptr;
+    rerun_ = nullptr;
+    unc_cap_ = 0;
+    // every kx group of every step can hold a record, and each record lists
+    // at most one work item
+    if ((e = cudaMalloc(&unc_rec_, need * sizeof(tpal::UncRecord))) != cudaSuccess ||
+        (e = cudaMalloc(&rerun_, 2 * need * sizeof(unsigned))) != cudaSuccess) {
+        if (unc_rec_) cudaFree(unc_rec_);
+        unc_rec_ = nullptr;
+        rerun_ = nullptr;
+        return cuda_fail("decision records", e);
+    }
+    unc_cap_ = need;
+    return 0;
+}
+
 int Engine::run_transform(const uint16_t *fields, long long stride, int field_base, int nfields, int fb, int fe,
                           float *partial, cudaStream_t s)
 {
@@ -277,7 +310,23 @@ int Engine::run_transform(const uint16_t *fields, long long stride, int field_ba
         P.thr_table = thr_dev_;
         P.frame_t2 = frame_t2_;
         P.stats = stats_dev_;
+        // guard-band decisions: recorded by the walk, decided by the resolve
+        // pass, work items with a wrong FP32 decision walked again exactly
+        if (static_) {
+            const int ntiles = P.ntx * P.nty;
+            if (unc_rec_ == nullptr || tpal::tp3_unc_capacity(ntiles, fe - fb, P.nchunks) > unc_cap_)
+                return arg_fail("decode: the static decision records are too small for this picture");
+        } else if (const int rc = ensure_deferred(fe - fb, P.nchunks); rc != 0) {
+            return rc;
+        }
+        P.unc_rec = static_cast<tpal::UncRecord *>(unc_rec_);
+        P.rerun = rerun_;
+        P.counters = counters_;
+        P.unc_cap = (unsigned)std::min<unsigned long long>(unc_cap_, 0xFFFFFFFFull);
+        if (cudaError_t e = cudaMemsetAsync(counters_, 0, 2 * sizeof(unsigned), s); e != cudaSuccess)
+            return cuda_fail("decision counters", e);
         if (tpal::tp3_launch(P, s, max_blocks3_) != 0) return cuda_fail("tpal3d launch", cudaGetLastError());
+        if (tpal::tp3_resolve_launch(P, s) != 0) return cuda_fail("tpal3d resolve", cudaGetLastError());
     } else {
         tpal::T2Params P{};
         P.fields = fields;
@@ -463,7 +512,9 @@ int Engine::decode(const uint16_t *fields, long long stride, int field_base, int
             cudaEventRecord(ev.c, s);
             pending_.push_back(ev);
         }
-        launches_ += 2;
+        // transform (+ resolve and apply when deferred) and demodulator;
+        // PALcolour runs the demodulator alone
+        launches_ += (c_.kind == 6) ? 1 : (c_.kind == 8) ? 4 : 2;
         o += frame_bytes() * (size_t)(be - b);
     }
     return 0;

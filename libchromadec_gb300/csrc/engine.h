@@ -28,8 +28,24 @@ public:
     int decode_scratch(const uint16_t *fields, long long stride, int nfields, int fb, int fe, void *out,
                        float *scratch, size_t scratch_floats, cudaStream_t s);
     static size_t scratch_floats_for(const chdg_geometry &g, int nframes);
-    // Drop the borrowed threshold table before destruction (it is not ours to free).
-    void forget_static() { thr_dev_ = nullptr; }
+    // Caller-provided buffers of the guard-band decision passes for the
+    // allocation-free decode: records, a list of as many (work item, step)
+    // pairs, two counters.
+    void set_static_decisions(void *records, unsigned *items, unsigned long long cap, unsigned *counters)
+    {
+        unc_rec_ = records;
+        rerun_ = items;
+        unc_cap_ = cap;
+        counters_ = counters;
+    }
+    // Drop the borrowed buffers before destruction (they are not ours to free).
+    void forget_static()
+    {
+        thr_dev_ = nullptr;
+        unc_rec_ = nullptr;
+        rerun_ = nullptr;
+        counters_ = nullptr;
+    }
     // fields: device buffer holding capture fields [field_base, ...)
     int decode(const uint16_t *fields, long long stride, int field_base, int nfields, int fb, int fe, void *out,
                cudaStream_t s);
@@ -75,6 +91,9 @@ private:
     bool padded() const { return left_pad_ || top_pad_ || out_w_ != (g_.active_end - g_.active_start) ||
                                  out_h_ != (g_.last_active_frame_line - g_.first_active_frame_line + 1); }
     int ensure_partial(int nout_fields);
+    // deferred 3D decisions: record and work-item buffers for a launch of
+    // `frames` frames in `nchunks` chunks
+    int ensure_deferred(int frames, int nchunks);
     int run_transform(const uint16_t *fields, long long stride, int field_base, int nfields, int fb, int fe,
                       float *partial, cudaStream_t s);
     int run_demod(const uint16_t *fields, long long stride, int field_base, int fb, int fe, const float *partial,
@@ -91,6 +110,10 @@ private:
     unsigned *stats_dev_ = nullptr;
     float *partial_ = nullptr;
     size_t partial_elems_ = 0;
+    bool static_ = false;          // init_static: caller-provided buffers, no allocation
+    void *unc_rec_ = nullptr;
+    unsigned *rerun_ = nullptr, *counters_ = nullptr;
+    unsigned long long unc_cap_ = 0;
     int fl_lo_ = 0, fl_hi_ = 0, rows_ = 0, cols_ = 0;
     int out_w_ = 0, out_h_ = 0, left_pad_ = 0, top_pad_ = 0;
     int max_batch_frames_ = 256;

@@ -21,6 +21,7 @@
 #include "../../include/chromadec_gb300.h"
 #include "engine.h"
 #include "error_state.h"
+#include "tpal_kernels.h"
 
 namespace {
 
@@ -28,12 +29,21 @@ constexpr int kStaticMaxFrames = 8;
 constexpr size_t kStaticScratchFloats = (size_t)4 * 2 * kStaticMaxFrames * 288 * 948;
 
 // Shared by every call on a device; holds the previous call's chroma planes.
+// guard-band decision records of an 8-frame call (every kx group of the
+// default 4,440 tile positions, with room to spare) and the work-item list
+constexpr unsigned long long kStaticRecords = 160000;
+
 static __device__ __align__(256) float g_static_scratch[kStaticScratchFloats];
 static __device__ __align__(256) float g_static_thresholds[3 * 768];
+static __device__ __align__(256) tpal::UncRecord g_static_records[kStaticRecords];
+static __device__ __align__(256) unsigned g_static_items[2 * kStaticRecords];
+static __device__ __align__(256) unsigned g_static_counters[2];
 
 struct DeviceSymbols {
     float *scratch = nullptr;
     float *thresholds = nullptr;
+    void *records = nullptr;
+    unsigned *items = nullptr, *counters = nullptr;
 };
 constexpr int kMaxDevices = 64;
 static DeviceSymbols g_symbols[kMaxDevices];
@@ -48,15 +58,21 @@ int resolve_symbols(int device, DeviceSymbols &out)
     }
     DeviceSymbols &d = g_symbols[device];
     if (d.scratch == nullptr) {
-        void *p = nullptr, *q = nullptr;
+        void *p = nullptr, *q = nullptr, *r = nullptr, *f = nullptr, *c = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
         if (e == cudaSuccess) e = cudaGetSymbolAddress(&q, g_static_thresholds);
+        if (e == cudaSuccess) e = cudaGetSymbolAddress(&r, g_static_records);
+        if (e == cudaSuccess) e = cudaGetSymbolAddress(&f, g_static_items);
+        if (e == cudaSuccess) e = cudaGetSymbolAddress(&c, g_static_counters);
         if (e != cudaSuccess) {
             chd::detail::set_last_error(std::string("chdg_decode_device_static: cudaGetSymbolAddress: ") +
                                         cudaGetErrorString(e));
             return CHDG_E_CUDA;
         }
         d.thresholds = static_cast<float *>(q);
+        d.records = r;
+        d.items = static_cast<unsigned *>(f);
+        d.counters = static_cast<unsigned *>(c);
         d.scratch = static_cast<float *>(p);
     }
     out = d;
@@ -95,6 +111,7 @@ extern "C" int chdg_decode_device_static(const chdg_geometry *g, const chdg_conf
     if (const int rc = resolve_symbols(device, sym); rc != 0) return rc;
     chdg::Engine eng;
     int rc = eng.init_static(*g, *c, sym.thresholds);
+    eng.set_static_decisions(sym.records, sym.items, kStaticRecords, sym.counters);
     // Every chroma sample the demodulator reads is written by the transform
     // in the same call, so the scratch needs no clearing.
     if (rc == 0)

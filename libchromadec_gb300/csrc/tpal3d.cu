@@ -209,7 +209,7 @@ __device__ __forceinline__ void forward_pair(const T3Params &P, int q, int tileX
         for (int h = 8; h >= 1; h >>= 1, st++) {
             const bool upper = (LC.i & h) != 0;
             const float2 o = shfl_xor2(X, h);
-            X = upper ? cmul(make_float2(o.x - X.x, o.y - X.y), LC.ftw[st]) : make_float2(X.x + o.x, X.y + o.y);
+            X = upper ? cmul(sub2(o, X), LC.ftw[st]) : add2(X, o);
         }
         // parity twiddle: S[kk] = exp(-2 pi i kk y0/32) A[kk], S[kk+16] = (-1)^y0 S[kk];
         // swap halves so lane l holds both fields at ky = kappa(l)
@@ -338,6 +338,9 @@ __device__ __forceinline__ void dft8_fwd(const float2 (&in)[8], float2 (&out)[8]
 constexpr int kWarps3 = 4;
 constexpr float kBoundFactor = 2.0f;   // guard band, in units of the per-bin error estimate
 constexpr float kEps32 = 5.9604645e-8f;
+// a + b + E^2 + rE^2 below this (with a margin for the FP32 magnitudes)
+// keeps the effect of a decision under 1/4 sample unit: (4/4096) * 256 = 1/4
+constexpr float kTinyPair = 65000.0f;
 constexpr int kWarpSmemF2 = 8 * 5 * 32 + 2 * 2 * 5 * 32 + 32;   // float2 units per warp
 
 struct Col {
@@ -398,10 +401,10 @@ __device__ __forceinline__ bool funcertain(float a, float b, float t, float pa, 
     return (fabsf(__fmaf_rn(-b, t, a)) <= pa + t * pb) || (fabsf(__fmaf_rn(-a, t, b)) <= pb + t * pa);
 }
 
-// Exact resolution of the guard-band decisions of one kx group, one pair at
-// a time, all lanes cooperating (kept out of line: it runs rarely).
-__device__ __noinline__ void resolve_uncertain(const T3Params &P, int m, int tileX, int tileY, int g, int kxa, int lane,
-                                               unsigned &keep, unsigned &unc, unsigned &n_exact, unsigned &n_flip)
+// Exact resolution of the guard-band decisions of one kx group inside the
+// exact walk, one pair at a time, all lanes cooperating.
+__device__ __forceinline__ unsigned resolve_uncertain(const T3Params &P, int m, int tileX, int tileY, int g,
+                                                      int kxa, int lane, unsigned keep, unsigned unc)
 {
     unsigned any = __ballot_sync(0xffffffffu, unc != 0);
     while (any) {
@@ -415,8 +418,6 @@ __device__ __noinline__ void resolve_uncertain(const T3Params &P, int m, int til
         bool sim = df_sim(mb, mr, thr_of(P, m, kz, kyb, kxa).d);
         if (kxa == 4) sim |= df_sim(mb, mr, thr_of(P, m, kzr, kybr, 4).d);
         if (lane == src) {
-            n_exact++;
-            if ((((keep >> kz) & 1u) != 0) != sim) n_flip++;
             keep = sim ? (keep | (1u << kz)) : (keep & ~(1u << kz));
             unc &= ~(1u << kz);
         }
@@ -426,28 +427,42 @@ __device__ __noinline__ void resolve_uncertain(const T3Params &P, int m, int til
         }
         any = __ballot_sync(0xffffffffu, unc != 0);
     }
+    return keep;
 }
 
 // TMODE: 0 = one uniform threshold, 1 = per-bin table, 2 = per-frame
-// thresholds (batches of captures).
-template <int TMODE>
+// thresholds (batches of captures). EXACT = false: the walk over every work
+// item, guard-band decisions taken in FP32 and recorded for
+// tp3_resolve_kernel (an exact path inside this loop, however rarely taken,
+// slows the whole walk by a third). EXACT = true: the walk again over the
+// items tp3_resolve_kernel listed, deciding those bins exactly; it writes
+// the same output locations, so its result replaces the FP32 one.
+template <int TMODE, bool EXACT>
 __global__ void __launch_bounds__(32 * kWarps3, 3) tpal3d_kernel(T3Params P)
 {
     constexpr bool PER_BIN = (TMODE == 1);
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int ntiles = P.ntx * P.nty;
-    unsigned int n_exact = 0, n_flip = 0;
     // Work items (tile position, chunk of frames); a grid smaller than the
     // item count walks them persistently.
-    for (int item = blockIdx.x * kWarps3 + warp; item < ntiles * P.nchunks; item += gridDim.x * kWarps3) {
+    const unsigned nitems = EXACT ? min(P.counters[1], P.unc_cap) : (unsigned)(ntiles * P.nchunks);
+    for (unsigned w = blockIdx.x * kWarps3 + warp; w < nitems; w += gridDim.x * kWarps3) {
+    const int item = EXACT ? (int)P.rerun[2 * w] : (int)w;
     const int tile = item % ntiles;
     const int chunk = item / ntiles;
     const int tx = tile % P.ntx, ty = tile / P.ntx;
     const int tileX = P.tileX0 + 8 * tx;
     const int tileY = P.tileY0 + 16 * ty;
-    const int m0 = P.frame_begin + chunk * P.chunk_frames;
-    const int m1 = min(m0 + P.chunk_frames, P.frame_end);
+    int m0 = P.frame_begin + chunk * P.chunk_frames;
+    int m1 = min(m0 + P.chunk_frames, P.frame_end);
+    if (EXACT) {
+        // only the steps a wrong decision at step mf reached: its own output
+        // (fields 2mf, 2mf+1) and the one its carries feed (step mf + 2)
+        const int mf = (int)P.rerun[2 * w + 1];
+        m0 = max(m0, mf);
+        m1 = min(m1, mf + 3);
+    }
     const int cls = ((ty & 1) << 1) | (tx & 1);
 
     // Per-warp shared state (dynamic): window of field spectra, Z carries,
@@ -519,6 +534,13 @@ __global__ void __launch_bounds__(32 * kWarps3, 3) tpal3d_kernel(T3Params P)
             // The mirror of my column-A bin kz is bin kzr of the mirror lane's
             // column B (its column A when g = 2).
             unsigned keep = 0, unc = 0;
+            // A pair too small to matter is left to FP32: toggling bins of
+            // magnitudes |Y_b|, |Y_r| moves any output sample by at most
+            // (2/4096)(|Y_b| + |Y_r|) <= (4/4096) sqrt(a + b + E^2 + rE^2)
+            // (true magnitudes within E of the computed ones), so under
+            // kTinyPair the change is below 1/4 of a composite sample unit
+            // (0.38 LSB of yuv444p16, 7e-6 of yuv444ps).
+            const float tiny_lim = kTinyPair - __fmaf_rn(A.E, A.E, rE * rE);
 #pragma unroll
             for (int kz = 0; kz < 8; kz++) {
                 const int kzr = (10 - kz) & 7;
@@ -537,14 +559,30 @@ __global__ void __launch_bounds__(32 * kWarps3, 3) tpal3d_kernel(T3Params P)
                 // a carrier (its own mirror) is always kept
                 const bool self = (g == 2) && (kz == kzr) && (my_ky == kyr);
                 if (sim || self) keep |= 1u << kz;
-                if (u && !self) unc |= 1u << kz;
+                if (u && !self && !(a + b < tiny_lim)) unc |= 1u << kz;
             }
-            // A zero error bound on both columns means a flat or black tile:
-            // every visited bin is exactly zero, and so is either decision's output.
-            if (A.E == 0.f && rE == 0.f) unc = 0;
-            // Resolve decisions inside the guard band exactly (rare).
-            if (__any_sync(0xffffffffu, unc != 0))
-                resolve_uncertain(P, m, tileX, tileY, g, kxa, lane, keep, unc, n_exact, n_flip);
+            // Record decisions inside the guard band for the exact passes
+            // (a flat or black tile, whose bound is zero, never has any).
+            if (__any_sync(0xffffffffu, unc != 0)) {
+                if (EXACT) {
+                    keep = resolve_uncertain(P, m, tileX, tileY, g, kxa, lane, keep, unc);
+                } else {
+                    unsigned slot = 0;
+                    if (lane == 0) slot = atomicAdd(P.counters, 1u);
+                    slot = __shfl_sync(0xffffffffu, slot, 0);
+                    if (slot < P.unc_cap) {   // sized for every kx group of the launch
+                        UncRecord &rec = P.unc_rec[slot];
+                        if (lane == 0) {
+                            rec.item = item;
+                            rec.tile = tile;
+                            rec.m = m;
+                            rec.g = g;
+                        }
+                        rec.unc[lane] = (uint8_t)unc;
+                        rec.keep[lane] = (uint8_t)keep;
+                    }
+                }
+            }
             z_inverse(A.Y, keep, carry, RA, RB, ka, lane);
             if (g < 2) {
                 // Column B bins are kept exactly when their mirror visit kept them.
@@ -570,8 +608,7 @@ __global__ void __launch_bounds__(32 * kWarps3, 3) tpal3d_kernel(T3Params P)
         for (int k = 0; k < 5; k++) {
             const float2 lo_v = Rj[k * 32 + LC.i];        // R[kk]   (lane kappa^-1(kk) = i)
             const float2 hi_v = Rj[k * 32 + LC.i + 16];   // R[kk+16]
-            float2 G = LC.y0 ? make_float2(lo_v.x - hi_v.x, lo_v.y - hi_v.y)
-                             : make_float2(lo_v.x + hi_v.x, lo_v.y + hi_v.y);
+            float2 G = LC.y0 ? sub2(lo_v, hi_v) : add2(lo_v, hi_v);
             G = cmul(G, make_float2(LC.ptw.x, -LC.ptw.y));   // exp(+i pi kk y0 / 16)
             // 16-point inverse DFT, bit-reversed input -> natural order (DIT)
             int st = 3;
@@ -581,7 +618,7 @@ __global__ void __launch_bounds__(32 * kWarps3, 3) tpal3d_kernel(T3Params P)
                 const float2 w = make_float2(LC.ftw[st].x, -LC.ftw[st].y);   // exp(+2 pi i r/(2h))
                 const float2 o = shfl_xor2(G, h);
                 const float2 t = cmul(upper ? G : o, w);
-                G = upper ? make_float2(o.x - t.x, o.y - t.y) : make_float2(G.x + t.x, G.y + t.y);
+                G = upper ? sub2(o, t) : add2(G, t);
             }
 #pragma unroll
             for (int x = 0; x < 8; x++) CS[x] = __ffma2_rn(G, c3_xi[k][x], CS[x]);
@@ -601,6 +638,112 @@ __global__ void __launch_bounds__(32 * kWarps3, 3) tpal3d_kernel(T3Params P)
         }
     }
     __syncwarp();   // the next item reuses this warp's shared window
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Deferred exact decisions
+// ---------------------------------------------------------------------------
+// One warp per record: decide its guard-band bins exactly in double-float
+// (the arithmetic of exact_pair, with the X stage of the record's two kx
+// columns computed once for all its bins) and, where an exact decision
+// differs from the FP32 one the walk used, list the record's work item and
+// step for the exact walk.
+__global__ void __launch_bounds__(32 * kWarps3) tp3_resolve_kernel(T3Params P)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned n = min(P.counters[0], P.unc_cap);
+    unsigned n_exact = 0, n_flip = 0;
+    const int z = lane >> 2, part = lane & 3;
+    for (unsigned rec = blockIdx.x * kWarps3 + warp; rec < n; rec += gridDim.x * kWarps3) {
+        const UncRecord &R = P.unc_rec[rec];
+        const int item = R.item, tile = R.tile, m = R.m, g = R.g;
+        const int tileX = P.tileX0 + 8 * (tile % P.ntx), tileY = P.tileY0 + 16 * (tile / P.ntx);
+        const int kxa = 2 + g, kxb = 8 - kxa;
+        const unsigned keep = R.keep[lane];
+        unsigned unc = R.unc[lane];
+        // X stage of this lane's four rows of field 2m + z, both columns
+        const int f = 2 * m + z;
+        const int p = (f & 1) ^ P.swap;
+        const int y0 = (p - tileY) & 1;
+        dfc xa[4], xb[4];
+        const uint16_t *fp = (f >= 0 && f < P.nfields) ? field_at(P, f) : nullptr;
+#pragma unroll
+        for (int r4 = 0; r4 < 4; r4++) {
+            xa[r4] = xb[r4] = {{0.f, 0.f}, {0.f, 0.f}};
+            const int L = tileY + y0 + 2 * (part * 4 + r4);
+            if (fp == nullptr || L < P.fafl || L > P.lafl) continue;
+            const long long base = (long long)(L >> 1) * P.fw + tileX;
+            for (int x = 0; x < 16; x++) {
+                long long idx = base + x;
+                idx = idx < 0 ? 0 : idx;
+                const float a = (float)((int)__ldg(fp + idx) - P.black);
+                const float *ca = c3_dfx[kxa - 2][x];
+                const float *cb = c3_dfx[kxb - 2][x];
+                xa[r4].re = df_add(xa[r4].re, df_mul_f({ca[0], ca[1]}, a));
+                xa[r4].im = df_add(xa[r4].im, df_mul_f({ca[2], ca[3]}, a));
+                xb[r4].re = df_add(xb[r4].re, df_mul_f({cb[0], cb[1]}, a));
+                xb[r4].im = df_add(xb[r4].im, df_mul_f({cb[2], cb[3]}, a));
+            }
+        }
+        const df wz = {c3_dfwz[z][0], c3_dfwz[z][1]};
+        bool flipped = false;
+        unsigned any = __ballot_sync(0xffffffffu, unc != 0);
+        while (any) {
+            const int src = __ffs(any) - 1;
+            const unsigned su = __shfl_sync(0xffffffffu, unc, src);
+            const int kz = __ffs(su) - 1;
+            const int kyb = kappa(src);
+            const int kzr = (10 - kz) & 7, kybr = (40 - kyb) & 31;
+            // Y stage over this lane's rows, then the 4 row groups, then Z
+            dfc accb = {{0.f, 0.f}, {0.f, 0.f}}, accr = accb;
+#pragma unroll
+            for (int r4 = 0; r4 < 4; r4++) {
+                const int y = y0 + 2 * (part * 4 + r4);
+                const df wy = {c3_dfwy[y][0], c3_dfwy[y][1]};
+                dfc cb = dfc_tw32(kyb * y), cr = dfc_tw32(kybr * y);
+                cb.re = df_mul(cb.re, wy); cb.im = df_mul(cb.im, wy);
+                cr.re = df_mul(cr.re, wy); cr.im = df_mul(cr.im, wy);
+                accb = dfc_add(accb, dfc_mul(xa[r4], cb));
+                accr = dfc_add(accr, dfc_mul(xb[r4], cr));
+            }
+            accb = dfc_add(accb, dfc_shfl_xor(accb, 1));
+            accb = dfc_add(accb, dfc_shfl_xor(accb, 2));
+            accr = dfc_add(accr, dfc_shfl_xor(accr, 1));
+            accr = dfc_add(accr, dfc_shfl_xor(accr, 2));
+            {
+                dfc tb = dfc_tw32(4 * ((kz * z) & 7)), tr = dfc_tw32(4 * ((kzr * z) & 7));
+                tb.re = df_mul(tb.re, wz); tb.im = df_mul(tb.im, wz);
+                tr.re = df_mul(tr.re, wz); tr.im = df_mul(tr.im, wz);
+                accb = dfc_mul(accb, tb);
+                accr = dfc_mul(accr, tr);
+            }
+            accb = dfc_add(accb, dfc_shfl_xor(accb, 4));
+            accb = dfc_add(accb, dfc_shfl_xor(accb, 8));
+            accb = dfc_add(accb, dfc_shfl_xor(accb, 16));
+            accr = dfc_add(accr, dfc_shfl_xor(accr, 4));
+            accr = dfc_add(accr, dfc_shfl_xor(accr, 8));
+            accr = dfc_add(accr, dfc_shfl_xor(accr, 16));
+            const df mb = dfc_abs2(accb), mr = dfc_abs2(accr);
+            bool sim = df_sim(mb, mr, thr_of(P, m, kz, kyb, kxa).d);
+            if (kxa == 4) sim |= df_sim(mb, mr, thr_of(P, m, kzr, kybr, 4).d);
+            const bool old = ((__shfl_sync(0xffffffffu, keep, src) >> kz) & 1u) != 0;
+            flipped |= (old != sim);
+            if (lane == src) {
+                n_exact++;
+                if (old != sim) n_flip++;
+                unc &= ~(1u << kz);
+            }
+            if (g == 2 && lane == kappa(kybr)) unc &= ~(1u << kzr);   // kx = 4: the same pair
+            any = __ballot_sync(0xffffffffu, unc != 0);
+        }
+        if (flipped && lane == 0) {
+            const unsigned at = atomicAdd(P.counters + 1, 1u);
+            if (at < P.unc_cap) {   // at most one entry per record
+                P.rerun[2 * at] = (unsigned)item;
+                P.rerun[2 * at + 1] = (unsigned)m;
+            }
+        }
     }
     if (P.stats != nullptr) {
         if (n_exact) atomicAdd(P.stats + 0, n_exact);
@@ -693,18 +836,39 @@ int tp3_launch(const T3Params &P, cudaStream_t stream, int max_blocks)
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64) return -1;
     if (!attr_set[dev]) {
-        if (cudaFuncSetAttribute(tpal3d_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-                cudaSuccess ||
-            cudaFuncSetAttribute(tpal3d_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-                cudaSuccess ||
-            cudaFuncSetAttribute(tpal3d_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-                cudaSuccess)
+        const int b = (int)smem;
+        const auto a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+        if (cudaFuncSetAttribute(tpal3d_kernel<0, false>, a, b) != cudaSuccess ||
+            cudaFuncSetAttribute(tpal3d_kernel<1, false>, a, b) != cudaSuccess ||
+            cudaFuncSetAttribute(tpal3d_kernel<2, false>, a, b) != cudaSuccess ||
+            cudaFuncSetAttribute(tpal3d_kernel<0, true>, a, b) != cudaSuccess ||
+            cudaFuncSetAttribute(tpal3d_kernel<1, true>, a, b) != cudaSuccess ||
+            cudaFuncSetAttribute(tpal3d_kernel<2, true>, a, b) != cudaSuccess)
             return -1;
         attr_set[dev] = true;
     }
-    if (P.thr_table != nullptr) tpal3d_kernel<1><<<blocks, 32 * kWarps3, smem, stream>>>(P);
-    else if (P.frame_t2 != nullptr) tpal3d_kernel<2><<<blocks, 32 * kWarps3, smem, stream>>>(P);
-    else tpal3d_kernel<0><<<blocks, 32 * kWarps3, smem, stream>>>(P);
+    if (P.unc_rec == nullptr || P.counters == nullptr || P.rerun == nullptr) return -1;
+    const unsigned t = 32 * kWarps3;
+    if (P.thr_table != nullptr) tpal3d_kernel<1, false><<<blocks, t, smem, stream>>>(P);
+    else if (P.frame_t2 != nullptr) tpal3d_kernel<2, false><<<blocks, t, smem, stream>>>(P);
+    else tpal3d_kernel<0, false><<<blocks, t, smem, stream>>>(P);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int tp3_resolve_launch(const T3Params &P, cudaStream_t stream)
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+    // the record and item counts are only known on the device: fixed grids
+    // walk them
+    tp3_resolve_kernel<<<4 * sms, 32 * kWarps3, 0, stream>>>(P);
+    const size_t smem = sizeof(float2) * (size_t)kWarpSmemF2 * kWarps3;
+    const unsigned t = 32 * kWarps3, blocks = 3u * (unsigned)sms;
+    if (P.thr_table != nullptr) tpal3d_kernel<1, true><<<blocks, t, smem, stream>>>(P);
+    else if (P.frame_t2 != nullptr) tpal3d_kernel<2, true><<<blocks, t, smem, stream>>>(P);
+    else tpal3d_kernel<0, true><<<blocks, t, smem, stream>>>(P);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

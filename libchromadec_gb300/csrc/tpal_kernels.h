@@ -24,6 +24,20 @@ __device__ __forceinline__ const uint16_t *field_at(const Params &P, int f)
     return P.fields + (long long)(f - P.field_base) * P.field_stride;
 }
 
+// Deferred exact decisions of the 3D transform. The walk decides every bin
+// in FP32 and, for each kx group with a bin inside the guard band, appends
+// one record; the resolve pass decides those bins exactly and lists the work
+// items where FP32 got one wrong, which the exact walk then runs again with
+// every guard-band decision taken exactly, overwriting their output.
+struct UncRecord {
+    int item;            // work item (tile + ntiles * chunk)
+    int tile;            // tile position, tx + ntx * ty
+    int m;               // the Z tile T(2m)
+    int g;               // kx group: column A is kx = 2 + g
+    uint8_t unc[32];     // per lane (ky = kappa(lane)): kz bits inside the guard band
+    uint8_t keep[32];    // per lane: the FP32 decisions the walk used
+};
+
 struct T3Params {
     const uint16_t *fields;      // buffer holding fields [field_base, ...)
     const uint16_t *const *field_ptrs;   // or (batches) each field's first sample by index, null = black
@@ -43,6 +57,11 @@ struct T3Params {
     const float *thr_table;      // per-bin squared thresholds [8][32][3] x (f, hi, lo), or null
     const float *frame_t2;       // per-frame squared threshold (f, hi, lo) by frame index, or null (batches)
     unsigned int *stats;         // [0] exact decisions taken, [1] of which FP32 was wrong
+    // deferred exact decisions (required)
+    UncRecord *unc_rec;
+    unsigned int *rerun;         // (work item, step) pairs to walk again exactly (unc_cap pairs)
+    unsigned int *counters;      // [0] records, [1] items listed in rerun
+    unsigned int unc_cap;
 };
 
 struct T2Params {
@@ -98,6 +117,14 @@ struct DemodParams {
 int tp3_init_constants(int device);
 // max_blocks > 0 caps the grid; the blocks then walk the work items persistently.
 int tp3_launch(const T3Params &p, cudaStream_t stream, int max_blocks = 0);
+// The resolve pass and the exact walk of the listed items (after
+// tp3_launch; the counters are zeroed before it).
+int tp3_resolve_launch(const T3Params &p, cudaStream_t stream);
+// Records one launch can write at most: every kx group of every step.
+inline unsigned long long tp3_unc_capacity(int ntiles, int frames, int nchunks)
+{
+    return (unsigned long long)ntiles * (unsigned long long)(frames + 2 * nchunks) * 3ull;
+}
 int tp2_init_constants(int device);
 int tp2_launch(const T2Params &p, cudaStream_t stream);
 int demod_init_constants(int device, double sample_rate, int field_width);
