@@ -34,6 +34,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "tpal_common.cuh"
 #include "tpal_kernels.h"
 
 namespace tpal {
@@ -164,6 +165,38 @@ __device__ __forceinline__ void pack_sample(const DemodParams &P, void *out, lon
     }
 }
 
+// Double-float pieces of the burst normalisation (FP64 is scarce on this
+// GPU and one lane per line waiting on it stalls the block).
+__device__ __forceinline__ df two_prod(float a, float b)
+{
+    const float p = __fmul_rn(a, b);
+    return {p, __fmaf_rn(a, b, -p)};
+}
+
+// max(sqrt(pn^2 + qn^2), floor), the square root refined by one Newton step
+__device__ __forceinline__ df burst_norm(float pn, float qn, float floor_v)
+{
+    const df s = df_add(two_prod(pn, pn), two_prod(qn, qn));
+    df r = df_make(0.f);
+    if (s.hi > 0.f) {
+        const float x = __fsqrt_rn(s.hi);
+        const df d = df_sub(s, two_prod(x, x));
+        r = quick_two_sum(x, __fdiv_rn(d.hi, 2.0f * x));
+    }
+    if (r.hi > floor_v || (r.hi == floor_v && r.lo > 0.f)) return r;
+    return df_make(floor_v);
+}
+
+// a / d for an exact float a
+__device__ __forceinline__ df df_div_f(float a, df d)
+{
+    const float q1 = __fdiv_rn(a, d.hi);
+    const df r = df_sub(df_sub(df_make(a), two_prod(q1, d.hi)), df_make(q1 * d.lo));
+    return quick_two_sum(q1, __fdiv_rn(r.hi, d.hi));
+}
+
+__device__ __forceinline__ float df_round(df v) { return __fadd_rn(v.hi, v.lo); }
+
 template <bool COMPOSITE, bool YNR>
 __global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
 {
@@ -281,16 +314,19 @@ __global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
             QOs += __shfl_xor_sync(0xffffffffu, QOs, h);
         }
         if (lane == 0) {
-            const double len = (double)(P.burst_end - P.burst_start);
             // bp = P/(4 len), bpo = PO/(2 len): the V-switch test scaled by (4 len)^2
             const long long a = Ps - 2 * POs, b = Qs - 2 * QOs;
             const bool vpos = (a * a + b * b) < 2 * (Ps * Ps + Qs * Qs);
-            const double bp = (double)(Ps - 2 * QOs) / (8.0 * len);
-            const double bq = (double)(Qs + 2 * POs) / (8.0 * len);
-            const double n = fmax(sqrt(bp * bp + bq * bq), 130000.0 / 128);
-            const double nbp = bp / n, nbq = bq / n;
-            s_bp[ln] = (float)(nbp * P.gain_cos - nbq * P.gain_sin);
-            s_bq[ln] = (float)(nbp * P.gain_sin + nbq * P.gain_cos);
+            // bp / max(|(bp, bq)|, 130000/128) with bp = pn / (8 len): the
+            // 8 len cancels, leaving pn / max(|(pn, qn)|, 8 len 130000/128).
+            // pn, qn are integers below 2^23 (exact in FP32); the rest runs
+            // in double-float (about 2^-46), so the rounded results are the
+            // double computation's.
+            const float pn = (float)(Ps - 2 * QOs), qn = (float)(Qs + 2 * POs);
+            const df n = burst_norm(pn, qn, 8.0f * (float)(P.burst_end - P.burst_start) * (130000.0f / 128.0f));
+            const df nbp = df_div_f(pn, n), nbq = df_div_f(qn, n);
+            s_bp[ln] = df_round(df_sub(df_mul_f(nbp, P.gain_cos), df_mul_f(nbq, P.gain_sin)));
+            s_bq[ln] = df_round(df_add(df_mul_f(nbp, P.gain_sin), df_mul_f(nbq, P.gain_cos)));
             s_vsw[ln] = vpos ? 1.f : -1.f;
         }
     }
