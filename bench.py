@@ -451,7 +451,7 @@ def main():
     # (a smaller capture of the same kernel; traffic grows with the fields)
     traffic = None
     try:
-        with open(os.path.join(ROOT, "profiles", "tpal3d_traffic_250fields.md")) as fp:
+        with open(os.path.join(ROOT, "profiles", "tpal3d_traffic_200fields.md")) as fp:
             for ln in fp:
                 if ln.startswith("traffic_bytes_per_field:"):
                     traffic = int(ln.split(":")[1]) * fields_per_launch
