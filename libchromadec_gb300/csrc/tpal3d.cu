@@ -222,6 +222,34 @@ __device__ __forceinline__ void forward_pair(const T3Params &P, int q, int tileX
 }
 
 // ---------------------------------------------------------------------------
+// Double-float X stage of one row for columns kx and 8 - kx. The second
+// column's coefficients are the first's conjugated with sign (-1)^x
+// (w(x) exp(-2 pi i (8-k) x / 16) = (-1)^x conj(w(x) exp(-2 pi i k x / 16))),
+// so the products are formed once and summed twice.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void x_row_pair(const uint16_t *field, long long base, int black, int kx, dfc &xa,
+                                           dfc &xb)
+{
+    xa = {{0.f, 0.f}, {0.f, 0.f}};
+    xb = xa;
+    for (int x = 0; x < 16; x++) {
+        const long long idx = base + x < 0 ? 0 : base + x;   // never before the field start
+        const float a = (float)((int)__ldg(field + idx) - black);
+        const float *c = c3_dfx[kx - 2][x];
+        const df pr = df_mul_f({c[0], c[1]}, a), pi = df_mul_f({c[2], c[3]}, a);
+        xa.re = df_add(xa.re, pr);
+        xa.im = df_add(xa.im, pi);
+        if (x & 1) {
+            xb.re = df_sub(xb.re, pr);
+            xb.im = df_add(xb.im, pi);
+        } else {
+            xb.re = df_add(xb.re, pr);
+            xb.im = df_sub(xb.im, pi);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Exact (double-float) magnitudes of bin b = (kzb, kyb, kxb) and its mirror
 // r of Z tile T(2m). All 32 lanes cooperate; every lane returns the result.
 // ---------------------------------------------------------------------------
@@ -244,18 +272,8 @@ __device__ __noinline__ void exact_pair(const T3Params &P, int m, int tileX, int
             const int L = tileY + y;
             if (L < P.fafl || L > P.lafl) continue;
             const long long base = (long long)(L >> 1) * P.fw + tileX;   // within the field
-            dfc xb = {{0.f, 0.f}, {0.f, 0.f}}, xr = xb;
-            for (int x = 0; x < 16; x++) {
-                long long idx = base + x;
-                idx = idx < 0 ? 0 : idx;
-                const float a = (float)((int)__ldg(fp + idx) - P.black);
-                const float *cb = c3_dfx[kxb - 2][x];
-                const float *cr = c3_dfx[kxr - 2][x];
-                xb.re = df_add(xb.re, df_mul_f({cb[0], cb[1]}, a));
-                xb.im = df_add(xb.im, df_mul_f({cb[2], cb[3]}, a));
-                xr.re = df_add(xr.re, df_mul_f({cr[0], cr[1]}, a));
-                xr.im = df_add(xr.im, df_mul_f({cr[2], cr[3]}, a));
-            }
+            dfc xb, xr;
+            x_row_pair(fp, base, P.black, kxb, xb, xr);
             const df wy = {c3_dfwy[y][0], c3_dfwy[y][1]};
             dfc cb = dfc_tw32(kyb * y), cr = dfc_tw32(kyr * y);
             cb.re = df_mul(cb.re, wy); cb.im = df_mul(cb.im, wy);
@@ -673,18 +691,8 @@ __global__ void __launch_bounds__(32 * kWarps3) tp3_resolve_kernel(T3Params P)
             xa[r4] = xb[r4] = {{0.f, 0.f}, {0.f, 0.f}};
             const int L = tileY + y0 + 2 * (part * 4 + r4);
             if (fp == nullptr || L < P.fafl || L > P.lafl) continue;
-            const long long base = (long long)(L >> 1) * P.fw + tileX;
-            for (int x = 0; x < 16; x++) {
-                long long idx = base + x;
-                idx = idx < 0 ? 0 : idx;
-                const float a = (float)((int)__ldg(fp + idx) - P.black);
-                const float *ca = c3_dfx[kxa - 2][x];
-                const float *cb = c3_dfx[kxb - 2][x];
-                xa[r4].re = df_add(xa[r4].re, df_mul_f({ca[0], ca[1]}, a));
-                xa[r4].im = df_add(xa[r4].im, df_mul_f({ca[2], ca[3]}, a));
-                xb[r4].re = df_add(xb[r4].re, df_mul_f({cb[0], cb[1]}, a));
-                xb[r4].im = df_add(xb[r4].im, df_mul_f({cb[2], cb[3]}, a));
-            }
+            const long long base = (long long)(L >> 1) * P.fw + tileX;   // within the field
+            x_row_pair(fp, base, P.black, kxa, xa[r4], xb[r4]);
         }
         const df wz = {c3_dfwz[z][0], c3_dfwz[z][1]};
         bool flipped = false;
