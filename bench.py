@@ -174,10 +174,12 @@ def reference_arm(a):
         return
     fields = make_capture(a)
     threads = cpu_threads()
-    # each step: a bounded sample of frames, ~10 s on all host threads
+    # each step: a bounded sample of frames on all host threads, sized so
+    # the timed steps take about 90 s in all (at most 10 s each)
+    budget = max(1.0, min(10.0, 90.0 / max(1, a.steps)))
     t1 = run_cpu(a, fields, max(1, threads), threads)
     per_frame = t1 / max(1, threads)
-    n = int(max(threads, min(fields.shape[0] // 2, 10.0 / max(per_frame, 1e-6))))
+    n = int(max(threads, min(fields.shape[0] // 2, budget / max(per_frame, 1e-6))))
     n = min(n, fields.shape[0] // 2)
     for _ in range(a.warmup):
         run_cpu(a, fields, min(n, threads), threads)
