@@ -377,6 +377,15 @@ __global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
         const int fl = fl0 + t;
         if (fl >= fl_last) continue;
         const int xl0 = seg * 8;   // local index of the first sample (absolute base4 + xl0, a multiple of 4)
+        // the composite samples luma needs, loaded before the FIR so their
+        // latency hides behind it
+        const uint16_t *comp = field + (long long)fl * P.fw;
+        float cv[8];
+#pragma unroll
+        for (int s = 0; s < 8; s++) {
+            const int x = base4 + xl0 + s;
+            cv[s] = (float)comp[x < P.fw ? x : P.fw - 1];
+        }
         float v[4][22];
         item_window(ch + t * SW + kPad + xl0 - 7, SW, v);
         float PU[8], QU[8], PV[8], QV[8], PY[8], QY[8];
@@ -385,7 +394,6 @@ __global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
         const float bp = s_bp[t], bq = s_bq[t], vsw = s_vsw[t];
         const int orow = P.top_pad + 2 * fl + off - P.fafl;
         const long long rowpix = (long long)orow * P.out_w + P.left_pad;
-        const uint16_t *comp = field + (long long)fl * P.fw;
 #pragma unroll
         for (int s = 0; s < 8; s++) {
             const int x = base4 + xl0 + s;
@@ -400,9 +408,9 @@ __global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
                 a = fminf(fmaxf(a, -P.nr_y), P.nr_y);
                 Y = yl[0] - a;
             } else if (COMPOSITE) {
-                Y = (float)comp[x] - 2.0f * __fmaf_rn(PY[s], carrier_sin(x), QY[s] * carrier_cos(x));
+                Y = cv[s] - 2.0f * __fmaf_rn(PY[s], carrier_sin(x), QY[s] * carrier_cos(x));
             } else {
-                Y = (float)comp[x] - v[0][s + 7];
+                Y = cv[s] - v[0][s + 7];
             }
             const float U = -(PU[s] * bp + QU[s] * bq) * 2.0f;
             const float V = vsw * -(QV[s] * bp - PV[s] * bq) * 2.0f;
