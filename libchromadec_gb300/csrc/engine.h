@@ -117,7 +117,7 @@ private:
     int fl_lo_ = 0, fl_hi_ = 0, rows_ = 0, cols_ = 0;
     int out_w_ = 0, out_h_ = 0, left_pad_ = 0, top_pad_ = 0;
     int max_batch_frames_ = 256;
-    int chunk_frames_ = 32;
+    int chunk_frames_ = 48;
     int max_blocks3_ = 0;
     const uint16_t *const *field_ptrs_ = nullptr;
     const float *frame_t2_ = nullptr;

@@ -216,12 +216,11 @@ int FramePipeline::decode(int64_t a, int64_t b, const Deliver &deliver, const st
         int count = 0;
         int slot = 0;
     };
-    Pending prev;
+    Pending prev, pendingOut;
     bool havePrev = false;
     const size_t fb = eng_.frame_bytes();
     std::vector<ExtraField> extFields;   // this batch's extra-source fields, in buffer order
     cudaError_t e;
-    int i = 0;
     // Batch boundaries: full batches in the middle, short ones at both ends,
     // so the first upload and the last download -- the parts no kernel
     // overlaps -- stay small.
@@ -245,18 +244,23 @@ int FramePipeline::decode(int64_t a, int64_t b, const Deliver &deliver, const st
             batches.emplace_back(c, b);
         }
     }
-    for (const auto &bt : batches) {
-        if (cancelled && cancelled()) break;
-        const int64_t c = bt.first, ce = bt.second;
-        const int slot = i & 1;
+    // Two stages per batch on two window slots: the upload (window fields,
+    // dropout plans, extra-source fields) on copy_, and the kernels plus the
+    // download on comp_ / d2h_. The next batch's upload is issued before the
+    // host waits for the previous batch's frames, so the host's time in the
+    // (blocking, pageable) field copies overlaps the GPU's work.
+    std::vector<int> nplans(batches.size(), 0);
+    auto stage_upload = [&](size_t bi) -> int {
+        const int64_t c = batches[bi].first, ce = batches[bi].second;
+        const int slot = (int)(bi & 1);
         const int64_t w0 = std::max<int64_t>(0, c - lb_);
         const int64_t w1 = std::min<int64_t>(nframes_, ce + la_);
         // bound the plan cache; plans behind the window are not needed again
         // by this run (references into the map stay valid: only others go)
         if (plans_.size() > 4096) plans_.erase(plans_.begin(), plans_.lower_bound(w0));
-        if (i >= 2) {
-            // the window of this slot was last read by batch i-2's kernels, and
-            // its plan buffers were last uploaded for batch i-2
+        if (bi >= 2) {
+            // the window of this slot was last read by batch bi-2's kernels,
+            // and its plan buffers were last uploaded for batch bi-2
             cudaStreamWaitEvent(copy_, ev_comp_[slot], 0);
             if ((e = cudaEventSynchronize(ev_h2d_[slot])) != cudaSuccess) return cuda_status("sync", e);
         }
@@ -361,8 +365,16 @@ int FramePipeline::decode(int64_t a, int64_t b, const Deliver &deliver, const st
             cudaMemcpyAsync(d_idx_[slot], h_idx_[slot], (2 * nplan + 1) * sizeof(int), cudaMemcpyHostToDevice, copy_);
         }
         cudaEventRecord(ev_h2d_[slot], copy_);
+        nplans[bi] = nplan;
+        return CHD_OK;
+    };
+    auto stage_compute = [&](size_t bi) -> int {
+        const int64_t c = batches[bi].first, ce = batches[bi].second;
+        const int slot = (int)(bi & 1);
+        const int64_t w0 = std::max<int64_t>(0, c - lb_);
+        const int nplan = nplans[bi];
         cudaStreamWaitEvent(comp_, ev_h2d_[slot], 0);
-        if (i >= 2) cudaStreamWaitEvent(comp_, ev_d2h_[slot], 0);   // output slot drained
+        if (bi >= 2) cudaStreamWaitEvent(comp_, ev_d2h_[slot], 0);   // output slot drained
         if (nplan > 0 &&
             dropout_apply(dwin_[slot], dstride_, cap_->vp().fieldWidth, d_idx_[slot], d_ops_[slot],
                           d_idx_[slot] + nplan, nplan, dext_[slot], comp_) != 0)
@@ -379,13 +391,6 @@ int FramePipeline::decode(int64_t a, int64_t b, const Deliver &deliver, const st
             cudaSuccess)
             return cuda_status("D2H", e);
         cudaEventRecord(ev_d2h_[slot], d2h_);
-        i++;
-        if (havePrev) {
-            if ((e = cudaEventSynchronize(ev_d2h_[prev.slot])) != cudaSuccess) return cuda_status("sync", e);
-            deliver(prev.out, prev.first, prev.count);
-        }
-        prev = {chunk, c, (int)(ce - c), slot};
-        havePrev = true;
         if (stats != nullptr && drop_.enabled) {
             for (int64_t k = c; k < ce; k++) {
                 const FramePlan &p = plan_for(k);
@@ -394,6 +399,24 @@ int FramePipeline::decode(int64_t a, int64_t b, const Deliver &deliver, const st
                 stats->totalDistance += p.totalDistance;
             }
         }
+        pendingOut = {chunk, c, (int)(ce - c), slot};
+        return CHD_OK;
+    };
+    if (!batches.empty() && !(cancelled && cancelled())) {
+        if (const int rc = stage_upload(0); rc != CHD_OK) return rc;
+    }
+    for (size_t bi = 0; bi < batches.size(); bi++) {
+        if (cancelled && cancelled()) break;
+        if (const int rc = stage_compute(bi); rc != CHD_OK) return rc;
+        // the next batch's fields go up while this batch computes
+        if (bi + 1 < batches.size() && !(cancelled && cancelled()))
+            if (const int rc = stage_upload(bi + 1); rc != CHD_OK) return rc;
+        if (havePrev) {
+            if ((e = cudaEventSynchronize(ev_d2h_[prev.slot])) != cudaSuccess) return cuda_status("sync", e);
+            deliver(prev.out, prev.first, prev.count);
+        }
+        prev = pendingOut;
+        havePrev = true;
     }
     if (havePrev) {
         if ((e = cudaEventSynchronize(ev_d2h_[prev.slot])) != cudaSuccess) return cuda_status("sync", e);
