@@ -190,7 +190,7 @@ __device__ __forceinline__ void forward_pair(const T3Params &P, int q, int tileX
     if (LC.i == 0) bnd[8 * fslot + 5] = rowl1;
     const int f0slot = (2 * q) & 7;
 
-#pragma unroll 1
+#pragma unroll
     for (int k = 0; k < 5; k++) {
         // column DFT bin kx = k+2 of this row (window and centre phase folded)
         float2 X = make_float2(0.f, 0.f);
@@ -622,7 +622,7 @@ __global__ void __launch_bounds__(32 * kWarps3, 3) tpal3d_kernel(T3Params P)
 #pragma unroll
         for (int x = 0; x < 8; x++) CS[x] = make_float2(0.f, 0.f);
         const float2 *Rj = LC.j ? RB : RA;
-#pragma unroll 1
+#pragma unroll
         for (int k = 0; k < 5; k++) {
             const float2 lo_v = Rj[k * 32 + LC.i];        // R[kk]   (lane kappa^-1(kk) = i)
             const float2 hi_v = Rj[k * 32 + LC.i + 16];   // R[kk+16]
