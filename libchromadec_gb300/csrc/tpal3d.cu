@@ -57,7 +57,9 @@ __constant__ float c3_wz[8];       // w_z(z)
 __constant__ float2 c3_tw16[16];   // exp(-2 pi i r / 16)
 __constant__ float2 c3_tw32[32];   // exp(-2 pi i r / 32)
 // double-float tables for the exact decision path
-__constant__ float c3_dfx[5][16][4];   // w_x(x) exp(-2 pi i kx x/16): re.hi, re.lo, im.hi, im.lo
+// w_x(x) exp(-2 pi i kx x/16) as 60-bit fixed point, c * 2^60 = hi * 2^30 + lo
+// (lo in [0, 2^30)): re.hi, re.lo, im.hi, im.lo
+__constant__ int c3_qx[5][16][4];
 __constant__ float c3_dfwy[32][2];     // w_y(y)
 __constant__ float c3_dfwz[8][2];      // w_z(z)
 __constant__ float c3_dftw32[32][4];   // exp(-2 pi i r/32)
@@ -227,26 +229,41 @@ __device__ __forceinline__ void forward_pair(const T3Params &P, int q, int tileX
 // (w(x) exp(-2 pi i (8-k) x / 16) = (-1)^x conj(w(x) exp(-2 pi i k x / 16))),
 // so the products are formed once and summed twice.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ df df_from_fixed60(long long hi_acc, long long lo_acc)
+{
+    // v = hi_acc * 2^-30 + lo_acc * 2^-60; hi_acc and lo_acc are below 2^51
+    const float h = (float)hi_acc;
+    const long long r = hi_acc - (long long)h;   // exact, below 2^27
+    df v = quick_two_sum(h, (float)r);
+    v = df_add(v, df_make((float)lo_acc * 9.3132257461547852e-10f));   // 2^-30
+    return {v.hi * 9.3132257461547852e-10f, v.lo * 9.3132257461547852e-10f};
+}
+
+// The X stage in 60-bit fixed point: each sample times each coefficient
+// word is an exact 64-bit integer product, so the sums are exact and the one
+// rounding is the conversion to double-float (about 2^-47 of the sum).
 __device__ __forceinline__ void x_row_pair(const uint16_t *field, long long base, int black, int kx, dfc &xa,
                                            dfc &xb)
 {
-    xa = {{0.f, 0.f}, {0.f, 0.f}};
-    xb = xa;
+    long long ar_h = 0, ar_l = 0, ai_h = 0, ai_l = 0, br_h = 0, br_l = 0, bi_h = 0, bi_l = 0;
+#pragma unroll
     for (int x = 0; x < 16; x++) {
         const long long idx = base + x < 0 ? 0 : base + x;   // never before the field start
-        const float a = (float)((int)__ldg(field + idx) - black);
-        const float *c = c3_dfx[kx - 2][x];
-        const df pr = df_mul_f({c[0], c[1]}, a), pi = df_mul_f({c[2], c[3]}, a);
-        xa.re = df_add(xa.re, pr);
-        xa.im = df_add(xa.im, pi);
-        if (x & 1) {
-            xb.re = df_sub(xb.re, pr);
-            xb.im = df_add(xb.im, pi);
-        } else {
-            xb.re = df_add(xb.re, pr);
-            xb.im = df_sub(xb.im, pi);
-        }
+        const long long a = (long long)((int)__ldg(field + idx) - black);
+        const int *c = c3_qx[kx - 2][x];
+        ar_h += a * c[0];
+        ar_l += a * c[1];
+        ai_h += a * c[2];
+        ai_l += a * c[3];
+        // column 8 - kx: (-1)^x times the conjugate
+        const long long sa = (x & 1) ? -a : a;
+        br_h += sa * c[0];
+        br_l += sa * c[1];
+        bi_h -= sa * c[2];
+        bi_l -= sa * c[3];
     }
+    xa = {df_from_fixed60(ar_h, ar_l), df_from_fixed60(ai_h, ai_l)};
+    xb = {df_from_fixed60(br_h, br_l), df_from_fixed60(bi_h, bi_l)};
 }
 
 // ---------------------------------------------------------------------------
@@ -257,7 +274,7 @@ __device__ __noinline__ void exact_pair(const T3Params &P, int m, int tileX, int
                                         df &mb, df &mr)
 {
     const int lane = threadIdx.x & 31;
-    const int kzr = (10 - kzb) & 7, kyr = (40 - kyb) & 31, kxr = 8 - kxb;
+    const int kzr = (10 - kzb) & 7, kyr = (40 - kyb) & 31;
     const int z = lane >> 2;
     const int part = lane & 3;
     const int f = 2 * m + z;
@@ -677,7 +694,7 @@ __global__ void __launch_bounds__(32 * kWarps3) tp3_resolve_kernel(T3Params P)
         const UncRecord &R = P.unc_rec[rec];
         const int item = R.item, tile = R.tile, m = R.m, g = R.g;
         const int tileX = P.tileX0 + 8 * (tile % P.ntx), tileY = P.tileY0 + 16 * (tile / P.ntx);
-        const int kxa = 2 + g, kxb = 8 - kxa;
+        const int kxa = 2 + g;
         const unsigned keep = R.keep[lane];
         unsigned unc = R.unc[lane];
         // X stage of this lane's four rows of field 2m + z, both columns
@@ -793,13 +810,18 @@ int tp3_init_constants(int device)
     float2 tw16[16], tw32[32];
     for (int r = 0; r < 16; r++) tw16[r] = make_float2((float)cos(-2 * M_PI * r / 16), (float)sin(-2 * M_PI * r / 16));
     for (int r = 0; r < 32; r++) tw32[r] = make_float2((float)cos(-2 * M_PI * r / 32), (float)sin(-2 * M_PI * r / 32));
-    float dfx[5][16][4], dfwy[32][2], dfwz[8][2], dftw32[32][4];
+    float dfwy[32][2], dfwz[8][2], dftw32[32][4];
+    int qx[5][16][4];
     for (int k = 0; k < 5; k++)
         for (int x = 0; x < 16; x++) {
             const double w = rc_window(x, 16);
             const double a = -2.0 * M_PI * (k + 2) * x / 16.0;
-            split_df(w * cos(a), dfx[k][x][0], dfx[k][x][1]);
-            split_df(w * sin(a), dfx[k][x][2], dfx[k][x][3]);
+            const double parts[2] = {w * cos(a), w * sin(a)};
+            for (int c = 0; c < 2; c++) {
+                const long long q = llround(parts[c] * 1152921504606846976.0);   // 2^60
+                qx[k][x][2 * c] = (int)(q >> 30);                               // floor(q / 2^30)
+                qx[k][x][2 * c + 1] = (int)(q & ((1LL << 30) - 1));
+            }
         }
     for (int y = 0; y < 32; y++) split_df(rc_window(y, 32), dfwy[y][0], dfwy[y][1]);
     for (int z = 0; z < 8; z++) split_df(rc_window(z, 8), dfwz[z][0], dfwz[z][1]);
@@ -822,7 +844,7 @@ int tp3_init_constants(int device)
     TPAL_CPY(c3_wz, wz);
     TPAL_CPY(c3_tw16, tw16);
     TPAL_CPY(c3_tw32, tw32);
-    TPAL_CPY(c3_dfx, dfx);
+    TPAL_CPY(c3_qx, qx);
     TPAL_CPY(c3_dfwy, dfwy);
     TPAL_CPY(c3_dfwz, dfwz);
     TPAL_CPY(c3_dftw32, dftw32);
