@@ -104,12 +104,16 @@ FramePlan FramePipeline::frame_stats(int64_t frame)
 
 std::shared_ptr<HostChunk> FramePipeline::take_chunk(size_t bytes)
 {
+    // Every chunk holds a full batch, so any free chunk serves any batch and
+    // the pool settles after the first call (a pinned allocation costs
+    // milliseconds; one made mid-run would stall the pipeline).
+    bytes = std::max(bytes, eng_.frame_bytes() * (size_t)batch_);
     // A chunk only this pool still references is free for reuse.
     for (auto &c : chunks_)
         if (c.use_count() == 1 && c->bytes >= bytes) return c;
     size_t idle = 0;
     for (auto it = chunks_.begin(); it != chunks_.end();) {
-        if (it->use_count() == 1 && ++idle > 2) it = chunks_.erase(it);
+        if (it->use_count() == 1 && ++idle > 4) it = chunks_.erase(it);
         else ++it;
     }
     auto c = std::make_shared<HostChunk>();

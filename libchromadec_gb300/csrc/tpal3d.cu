@@ -229,14 +229,23 @@ __device__ __forceinline__ void forward_pair(const T3Params &P, int q, int tileX
 // (w(x) exp(-2 pi i (8-k) x / 16) = (-1)^x conj(w(x) exp(-2 pi i k x / 16))),
 // so the products are formed once and summed twice.
 // ---------------------------------------------------------------------------
+// An integer below 2^51 in magnitude as double-float, through 32-bit
+// conversions (the 64-bit ones run on the FP64 pipe, which this GPU has
+// little of): v = hi * 2^32 + mid * 2^16 + low, each part exact in FP32.
+__device__ __forceinline__ df df_from_i51(long long v)
+{
+    const float fh = (float)(int)(v >> 32) * 4294967296.0f;   // |v >> 32| < 2^19: exact
+    const unsigned lo = (unsigned)v;
+    const float fm = (float)(lo >> 16) * 65536.0f, fl = (float)(lo & 0xFFFFu);
+    return df_add(two_sum(fh, fm), df_make(fl));
+}
+
 __device__ __forceinline__ df df_from_fixed60(long long hi_acc, long long lo_acc)
 {
     // v = hi_acc * 2^-30 + lo_acc * 2^-60; hi_acc and lo_acc are below 2^51
-    const float h = (float)hi_acc;
-    const long long r = hi_acc - (long long)h;   // exact, below 2^27
-    df v = quick_two_sum(h, (float)r);
-    v = df_add(v, df_make((float)lo_acc * 9.3132257461547852e-10f));   // 2^-30
-    return {v.hi * 9.3132257461547852e-10f, v.lo * 9.3132257461547852e-10f};
+    const df v = df_add(df_from_i51(hi_acc), df_make((float)(int)(lo_acc >> 30) + (float)(int)(lo_acc & 0x3FFFFFFF) *
+                                                                                    9.3132257461547852e-10f));
+    return {v.hi * 9.3132257461547852e-10f, v.lo * 9.3132257461547852e-10f};   // 2^-30
 }
 
 // The X stage in 60-bit fixed point: each sample times each coefficient
