@@ -33,6 +33,9 @@ __constant__ float c2_cwx[9][16];   // w32(x) cos(theta), theta = 2 pi kx (x - 1
 __constant__ float c2_swx[9][16];   // w32(x) sin(theta)
 __constant__ float c2_cix[9][16];   // (2/512) cos(theta)
 __constant__ float c2_six[9][16];   // (2/512) sin(theta)
+// the same as pairs for the f32x2 instructions: (cwx, -swx) and (cix, six)
+__constant__ float2 c2_xf[9][16];
+__constant__ float2 c2_xi[9][16];
 __constant__ float c2_wx[16];       // w32(x), x < 16
 __constant__ float c2_wy[16];       // w16(i)
 __constant__ float2 c2_tw16[16];    // exp(-2 pi i r/16)
@@ -164,7 +167,7 @@ __global__ void __launch_bounds__(32 * kWarps2) tpal2d_kernel(T2Params P)
     const int fl = tileY + i;
     const uint16_t *fp = (f >= 0 && f < P.nfields) ? field_at(P, f) : nullptr;
     const bool valid = (fp != nullptr) && (fl >= fl_first) && (fl < fl_last);
-    float sx[16], dx[16];
+    float2 sd[16];   // (s_x, d_x)
     float rowl1 = 0.f;
     if (valid) {
         const uint16_t *row = fp + (long long)fl * P.fw;
@@ -179,13 +182,13 @@ __global__ void __launch_bounds__(32 * kWarps2) tpal2d_kernel(T2Params P)
         const float m32 = (float)sum * 0.03125f;
 #pragma unroll
         for (int x = 0; x < 16; x++) {
-            sx[x] = (float)(16 * (a[x] + a[31 - x]) - sum) * 0.0625f;   // a_x + a_31-x - 2 mean (exact)
-            dx[x] = (float)(a[x] - a[31 - x]);
+            sd[x] = make_float2((float)(16 * (a[x] + a[31 - x]) - sum) * 0.0625f,   // a_x + a_31-x - 2 mean (exact)
+                                (float)(a[x] - a[31 - x]));
             rowl1 = __fmaf_rn(c2_wx[x], fabsf((float)a[x] - m32) + fabsf((float)a[31 - x] - m32), rowl1);
         }
     } else {
 #pragma unroll
-        for (int x = 0; x < 16; x++) sx[x] = dx[x] = 0.f;
+        for (int x = 0; x < 16; x++) sd[x] = make_float2(0.f, 0.f);
     }
     const float wy = c2_wy[i];
     rowl1 *= wy;
@@ -211,8 +214,7 @@ __global__ void __launch_bounds__(32 * kWarps2) tpal2d_kernel(T2Params P)
         float2 X = make_float2(0.f, 0.f);
 #pragma unroll
         for (int x = 0; x < 16; x++) {
-            X.x = __fmaf_rn(c2_cwx[row][x], sx[x], X.x);
-            X.y = __fmaf_rn(-c2_swx[row][x], dx[x], X.y);
+            X = __ffma2_rn(c2_xf[row][x], sd[x], X);   // (cwx sx + .., -swx dx + ..)
         }
         const float wk = real ? wy : 0.f;
         X.x *= wk;
@@ -227,7 +229,7 @@ __global__ void __launch_bounds__(32 * kWarps2) tpal2d_kernel(T2Params P)
         for (int hh = 8; hh >= 1; hh >>= 1, s++) {
             const bool upper = (i & hh) != 0;
             const float2 ov = shx(X, hh);
-            X = upper ? cmul2(make_float2(ov.x - X.x, ov.y - X.y), tw[s]) : make_float2(X.x + ov.x, X.y + ov.y);
+            X = upper ? cmul2(sub2(ov, X), tw[s]) : add2(X, ov);
         }
         Y[k] = X;
     }
@@ -315,9 +317,9 @@ __global__ void __launch_bounds__(32 * kWarps2) tpal2d_kernel(T2Params P)
     }
 
     // --- inverse Y (DIT, bit-reversed in -> natural rows out) and X partial sums
-    float C[16], S[16];
+    float2 CS[16];   // (cosine sum, sine sum)
 #pragma unroll
-    for (int x = 0; x < 16; x++) C[x] = S[x] = 0.f;
+    for (int x = 0; x < 16; x++) CS[x] = make_float2(0.f, 0.f);
 #pragma unroll
     for (int k = 0; k < 5; k++) {   // all lanes, all five bins (shuffles); half 1's fifth is zero
         const int row = (k < nk) ? kbase + k : 8;
@@ -329,26 +331,20 @@ __global__ void __launch_bounds__(32 * kWarps2) tpal2d_kernel(T2Params P)
             const float2 w = make_float2(tw[s].x, -tw[s].y);
             const float2 ov = shx(G, hh);
             const float2 tt = cmul2(upper ? G : ov, w);
-            G = upper ? make_float2(ov.x - tt.x, ov.y - tt.y) : make_float2(G.x + tt.x, G.y + tt.y);
+            G = upper ? sub2(ov, tt) : add2(G, tt);
         }
 #pragma unroll
-        for (int x = 0; x < 16; x++) {
-            C[x] = __fmaf_rn(G.x, c2_cix[row][x], C[x]);
-            S[x] = __fmaf_rn(G.y, c2_six[row][x], S[x]);
-        }
+        for (int x = 0; x < 16; x++) CS[x] = __ffma2_rn(G, c2_xi[row][x], CS[x]);
     }
 #pragma unroll
-    for (int x = 0; x < 16; x++) {
-        C[x] += __shfl_xor_sync(0xffffffffu, C[x], 16);
-        S[x] += __shfl_xor_sync(0xffffffffu, S[x], 16);
-    }
+    for (int x = 0; x < 16; x++) CS[x] = add2(CS[x], shx(CS[x], 16));
     if (fl >= fl_first && fl < fl_last) {
         float *dst = P.partial + (long long)cls * P.part_class_stride + (long long)o * P.part_field_stride +
                      (long long)(fl - P.fl_lo) * P.part_row_stride - P.avs;
 #pragma unroll
         for (int x = 0; x < 16; x++) {
             const int X = h ? tileX + 31 - x : tileX + x;
-            if (X >= P.avs && X < P.ave) dst[X] = h ? C[x] + S[x] : C[x] - S[x];
+            if (X >= P.avs && X < P.ave) dst[X] = h ? CS[x].x + CS[x].y : CS[x].x - CS[x].y;
         }
     }
     if (P.stats != nullptr) {
@@ -402,6 +398,14 @@ int tp2_init_constants(int device)
     TP2_CPY(c2_swx, swx);
     TP2_CPY(c2_cix, cix);
     TP2_CPY(c2_six, six);
+    float2 xf[9][16], xi[9][16];
+    for (int k = 0; k < 9; k++)
+        for (int x = 0; x < 16; x++) {
+            xf[k][x] = make_float2(cwx[k][x], -swx[k][x]);
+            xi[k][x] = make_float2(cix[k][x], six[k][x]);
+        }
+    TP2_CPY(c2_xf, xf);
+    TP2_CPY(c2_xi, xi);
     TP2_CPY(c2_wx, wx);
     TP2_CPY(c2_wy, wy);
     TP2_CPY(c2_tw16, tw);

@@ -77,9 +77,6 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 
 __device__ __forceinline__ float l1(float2 a) { return fabsf(a.x) + fabsf(a.y); }
 
-// Paired FP32 (sm_100+): each lane of the pair rounds exactly like the scalar op.
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
 // multiply by -i: (y, -x); by the tables' exp(-i pi/2) = (6e-17, -1), whose
 // tiny real part is below the rounding of any non-degenerate product
 __device__ __forceinline__ float2 mul_negi(float2 a) { return make_float2(a.y, -a.x); }

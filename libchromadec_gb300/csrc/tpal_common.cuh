@@ -12,6 +12,10 @@
 
 namespace tpal {
 
+// Paired FP32 (sm_100+): each lane of the pair rounds exactly like the scalar op.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+
 struct df {
     float hi, lo;
 };
