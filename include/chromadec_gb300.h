@@ -162,6 +162,32 @@ void chdg_batch_free(chdg_batch *b);
 int chdg_batch_decode(chdg_batch *b, const chdg_capture *caps, int32_t n, void *stream);
 int chdg_batch_autotune(chdg_batch *b, const chdg_capture *caps, int32_t n, void *stream, chdg_batch_tuning *out);
 
+/* Tensor-core form of the Transform-PAL 3D forward transform (no
+ * counterpart in the reference; the precision study beside the plain form,
+ * which remains the decoder). The spectra of the reference's 8x32x16 tiles
+ * (TransformPal3D::forwardFFTTile, src/decoders/palcolour/
+ * transform_pal_3d.cpp:168-202) at the bins the filter reads (kx = 2..6), with
+ * the X, Y and Z DFT stages run as tcgen05 tensor-core contractions in split
+ * precision: variant CHDG_TC_3XTF32 (TF32 hi/lo operands) or CHDG_TC_BF16X3
+ * (BF16 hi/lo), three products per contraction, FP32 accumulation.
+ *
+ * chdg_tc3d_spectra writes the Z tiles m = m_begin .. m_end-1 (Z tile m holds
+ * fields 2m .. 2m+7; fields outside the capture are black) of every spatial
+ * tile: d_spec is complex float (re, im) [m_end - m_begin][ntiles][8 kz][5 kx]
+ * [32 ky], spatial tiles row-major over tileY = first_active_frame_line - 16
+ * + 16 ty and tileX = active_start - 8 + 8 tx, kx = 2 + index. The first
+ * field of each frame is at the even index. Asynchronous on `stream`;
+ * chdg_tc3d_sync waits for it and reports a tensor-core completion wait that
+ * ran out (none is expected). chdg_tc3d_operand copies the host-built image
+ * of one coefficient operand (stage 0 = X, 1 = Y, 2 = Z; split 0 = hi,
+ * 1 = lo) in its shared-memory layout and returns its size in bytes. */
+#define CHDG_TC_3XTF32 0
+#define CHDG_TC_BF16X3 1
+int chdg_tc3d_spectra(const chdg_geometry *g, int32_t variant, const uint16_t *d_fields, int64_t field_stride,
+                      int32_t nfields, int32_t m_begin, int32_t m_end, void *d_spec, void *stream);
+int chdg_tc3d_sync(void *stream);
+int chdg_tc3d_operand(int32_t variant, int32_t stage, int32_t y0, int32_t split, void *out, size_t bytes);
+
 /* Multi-source concealment alignment (MultiSourceAlignment::
  * sourceFrameForPrimaryFrame, src/dropout/multi_source_alignment.cpp:54-71):
  * the 0-based frame of extra source `source` (1 = the first added with

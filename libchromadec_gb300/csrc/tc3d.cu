@@ -1,0 +1,760 @@
+// tc3d.cu -- tensor-core form of the Transform-PAL 3D forward transform on
+// sm_103a: the DFT stages of every tile as matrix contractions on the
+// 5th-generation tensor cores (tcgen05.mma, accumulators in tensor memory),
+// with split-precision products. A precision study beside the plain form
+// (tpal3d.cu), which stays the decoder: it answers how far tensor-core
+// spectra move from the FP64 ones and how many threshold decisions that
+// flips.
+//
+// The spectra are the reference's (TransformPal3D::forwardFFTTile,
+// src/decoders/palcolour/transform_pal_3d.cpp:168-202): 8 fields x 32 frame
+// lines x 16 samples, raised-cosine windowed in all three axes, rows of the
+// other field parity and outside the active lines black, bins kx = 2..6 --
+// the ones the filter reads (transform_pal_3d.cpp:294-331). Black is
+// subtracted first (the raised cosine's spectrum lives on kx in {0, +-1}, so
+// kx >= 2 is unchanged), leaving integer samples below 2^17 in magnitude.
+//
+// The separable DFT runs in three contractions, each a real GEMM with the
+// window folded into its coefficient matrix B (K-major, N x K):
+//
+//   X   rows (tile, row i) x 16 samples        . B_X [10 (5 kx re/im) x 16]
+//   Y   rows (tile, kx) x [re(16 rows) | im]   . B_Y [64 (32 ky re/im) x 32]  (per row parity y0)
+//   Z   rows (tile, kx, ky) x [re(8 z) | im]   . B_Z [16 (8 kz re/im) x 16]
+//
+// Split products: an operand a becomes a_hi + a_lo in the MMA's input type
+// (TF32: 10 stored mantissa bits, BF16: 7) and each contraction is three MMAs
+// accumulating in FP32 in tensor memory, small terms first:
+// a_lo.b_hi + a_hi.b_lo + a_hi.b_hi. Variant 0 is 3xTF32 (kind::tf32),
+// variant 1 is BF16x3 (kind::f16 with BF16 inputs).
+//
+// Kernels (one CTA of 128 threads; thread t owns tensor-memory lane t):
+//  * tc3_xy_kernel: a unit is 24 spatial tiles of one field. The X stage is
+//    three M = 128 MMAs (384 rows = 24 tiles x 16 own-parity rows); its
+//    results are read back with tcgen05.ld, split, and written as the Y
+//    stage's A operand (120 rows = 24 tiles x 5 kx); one M = 128, N = 64 MMA
+//    chain gives S_f[tile][kx][ky].
+//  * tc3_z_kernel: 128 rows (Z tile, spatial tile, kx, ky) per block, each
+//    gathering the 8 fields' S_f; one N = 16 MMA chain gives S[kz][kx][ky].
+// Shared-memory operands use the no-swizzle K-major canonical layout: 8-row x
+// 16-byte core matrices, K-adjacent core matrices 128 B apart (leading byte
+// offset), 8-row groups a whole row-group apart (stride byte offset). Every
+// wait on an MMA completion has an iteration limit; running out sets an error
+// flag that chdg_tc3d_sync reports, and the CTA frees its tensor memory and
+// returns.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "../../include/chromadec_gb300.h"
+#include "error_state.h"
+
+namespace tpal {
+namespace tc {
+
+constexpr int kThreads = 128;
+constexpr int kTilesPerUnit = 24;      // X rows 384 = 3 MMAs of 128; Y rows 120
+constexpr int kXRows = kTilesPerUnit * 16;
+constexpr int kYRows = kTilesPerUnit * 5;
+constexpr int kQ = 160;                // (kx, ky) per spatial tile: 5 x 32
+constexpr int kSpecPerTile = 8 * kQ;   // (kz, kx, ky)
+constexpr unsigned kWaitLimit = 1u << 22;
+
+struct Params {
+    const uint16_t *fields;
+    long long field_stride;
+    int nfields, fw, fh, fafl, lafl, black, swap;
+    int tileX0, tileY0, ntx, nty, ntiles;
+    int f_begin, nf;           // XY stage: fields [f_begin, f_begin + nf)
+    int nm;                    // Z stage: Z tiles m_begin .. m_begin + nm - 1 (fields 2m .. 2m+7)
+    const uint8_t *bx, *by, *bz;   // operand images: [split][...], by [y0][split][...]
+    float2 *sf;                // XY output: [nf][ntiles][kQ] (kx major, ky minor)
+    float2 *spec;              // Z output: [nm][ntiles][8 kz][kQ]
+    int *err;
+};
+
+// ---------------------------------------------------------------------------
+// PTX wrappers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: start address, leading byte offset 128
+// (K-adjacent core matrices), stride byte offset sbo (8-row groups), version
+// 1, no swizzle
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t sbo)
+{
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(128u >> 4) << 16) | ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) |
+           (1ull << 46);
+}
+
+// instruction descriptor: FP32 accumulator, A/B format (TF32 = 2 for
+// kind::tf32, BF16 = 1 for kind::f16), both K-major, N >> 3, M >> 4
+__host__ __device__ constexpr uint32_t idesc(int fmt, int M, int N)
+{
+    return (1u << 4) | ((uint32_t)fmt << 7) | ((uint32_t)fmt << 10) | ((uint32_t)(N >> 3) << 17) |
+           ((uint32_t)(M >> 4) << 24);
+}
+
+template <int KIND>
+__device__ __forceinline__ void mma(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t id, uint32_t acc)
+{
+    if (KIND == 0) {
+        asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                     "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+                     "l"(a), "l"(b), "r"(id), "r"(acc));
+    } else {
+        asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                     "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+                     "l"(a), "l"(b), "r"(id), "r"(acc));
+    }
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void bar_init(uint64_t *bar)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Wait for the barrier's phase `parity` to complete; false if the limit ran out.
+__device__ __forceinline__ bool bar_wait(uint64_t *bar, uint32_t parity)
+{
+    const uint32_t a = smem_addr(bar);
+    for (unsigned it = 0; it < kWaitLimit; it++) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred P1;\n\tmbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n\t"
+                     "selp.b32 %0, 1, 0, P1;\n\t}\n"
+                     : "=r"(done)
+                     : "r"(a), "r"(parity)
+                     : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t *dst, uint32_t ncols)
+{
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(dst)), "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// 16 consecutive 32-bit columns of this thread's lane (the warp reads lanes
+// 32 w .. 32 w + 31), then wait for the load
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                 "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                   "=r"(r[15])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 16; j++) v[j] = __uint_as_float(r[j]);
+}
+
+// ---------------------------------------------------------------------------
+// Operand layout and splitting
+// ---------------------------------------------------------------------------
+// Byte offset of element k of row r in a K-major no-swizzle operand whose rows
+// hold row_bytes of K.
+__host__ __device__ __forceinline__ uint32_t elem_off(int r, int k, int eb, int row_bytes)
+{
+    const int kb = k * eb;
+    return (uint32_t)((r >> 3) * (8 * row_bytes) + (kb >> 4) * 128 + (r & 7) * 16 + (kb & 15));
+}
+
+template <int KIND>
+struct Split;
+
+template <>
+struct Split<0> {   // TF32: hi = a rounded to 10 stored mantissa bits (to nearest, ties away), lo = the rest rounded
+    static constexpr int eb = 4;
+    __device__ __forceinline__ static void put(uint8_t *hi, uint8_t *lo, uint32_t off, float a)
+    {
+        uint32_t h, l;
+        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(a));
+        h &= 0xFFFFE000u;
+        const float rest = a - __uint_as_float(h);
+        asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(rest));
+        *reinterpret_cast<uint32_t *>(hi + off) = h;
+        *reinterpret_cast<uint32_t *>(lo + off) = l & 0xFFFFE000u;
+    }
+};
+
+template <>
+struct Split<1> {   // BF16: hi = bf16(a), lo = bf16(a - hi), both round to nearest even
+    static constexpr int eb = 2;
+    __device__ __forceinline__ static void put(uint8_t *hi, uint8_t *lo, uint32_t off, float a)
+    {
+        const __nv_bfloat16 h = __float2bfloat16_rn(a);
+        const __nv_bfloat16 l = __float2bfloat16_rn(a - __bfloat162float(h));
+        *reinterpret_cast<__nv_bfloat16 *>(hi + off) = h;
+        *reinterpret_cast<__nv_bfloat16 *>(lo + off) = l;
+    }
+};
+
+// Shared-memory plan of the XY kernel (bytes), every region 1024-aligned.
+template <int KIND>
+struct XYLayout {
+    static constexpr int eb = Split<KIND>::eb;
+    static constexpr int rbx = 16 * eb;   // X rows: 16 samples
+    static constexpr int rby = 32 * eb;   // Y rows: 16 re + 16 im
+    static constexpr int ax_blk = 128 * rbx;
+    static constexpr int ax = 0;                              // [split][3 blocks][128 rows]
+    static constexpr int ay = ax + 2 * 3 * ax_blk;            // [split][128 rows]
+    static constexpr int bx = ay + 2 * 128 * rby;             // [split][16 rows]
+    static constexpr int by = bx + ((2 * 16 * rbx + 1023) & ~1023);   // [y0][split][64 rows]
+    static constexpr int bar = by + 2 * 2 * 64 * rby;
+    static constexpr int bytes = bar + 64;
+    static constexpr int ksx = rbx / 32;   // MMA K steps (32 bytes each)
+    static constexpr int ksy = rby / 32;
+};
+
+template <int KIND>
+struct ZLayout {
+    static constexpr int eb = Split<KIND>::eb;
+    static constexpr int rbz = 16 * eb;
+    static constexpr int az = 0;                   // [split][128 rows]
+    static constexpr int bz = az + 2 * 128 * rbz;  // [split][16 rows]
+    static constexpr int bar = bz + ((2 * 16 * rbz + 1023) & ~1023);
+    static constexpr int bytes = bar + 64;
+    static constexpr int ksz = rbz / 32;
+};
+
+__device__ __forceinline__ void copy_image(uint8_t *dst, const uint8_t *src, int bytes)
+{
+    for (int o = threadIdx.x * 16; o < bytes; o += kThreads * 16)
+        *reinterpret_cast<uint4 *>(dst + o) = __ldg(reinterpret_cast<const uint4 *>(src + o));
+}
+
+// the three split products into one accumulator: lo.hi, hi.lo, hi.hi
+template <int KIND>
+__device__ __forceinline__ void mma3(uint32_t dtmem, uint32_t a_hi, uint32_t a_lo, uint32_t b_hi, uint32_t b_lo,
+                                     uint32_t a_sbo, uint32_t b_sbo, int ksteps, uint32_t id)
+{
+    for (int s = 0; s < ksteps; s++) {
+        const uint32_t o = 256u * s;   // two K-adjacent core matrices per step
+        mma<KIND>(dtmem, sdesc(a_lo + o, a_sbo), sdesc(b_hi + o, b_sbo), id, s > 0 ? 1u : 0u);
+        mma<KIND>(dtmem, sdesc(a_hi + o, a_sbo), sdesc(b_lo + o, b_sbo), id, 1u);
+        mma<KIND>(dtmem, sdesc(a_hi + o, a_sbo), sdesc(b_hi + o, b_sbo), id, 1u);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// X and Y stages: S_f[tile][kx][ky] of fields [f_begin, f_begin + nf)
+// ---------------------------------------------------------------------------
+template <int KIND>
+__global__ void __launch_bounds__(kThreads) tc3_xy_kernel(Params P)
+{
+    using LY = XYLayout<KIND>;
+    using SP = Split<KIND>;
+    constexpr int eb = LY::eb;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + LY::bar);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + LY::bar + 8);
+    const int t = threadIdx.x, warp = t >> 5;
+
+    // coefficient images (both row parities), zeroed Y operand (rows 120..127 stay zero)
+    copy_image(smem + LY::bx, P.bx, 2 * 16 * LY::rbx);
+    copy_image(smem + LY::by, P.by, 2 * 2 * 64 * LY::rby);
+    for (int o = t * 16; o < 2 * 128 * LY::rby; o += kThreads * 16) *reinterpret_cast<uint4 *>(smem + LY::ay + o) = uint4{0, 0, 0, 0};
+    if (t == 0) bar_init(bar);
+    if (warp == 0) tmem_alloc(tslot, 128);   // X accumulators: columns 0..47; Y: 64..127
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tslot;
+    uint32_t phase = 0;
+
+    uint8_t *ax_hi = smem + LY::ax, *ax_lo = smem + LY::ax + 3 * LY::ax_blk;
+    uint8_t *ay_hi = smem + LY::ay, *ay_lo = smem + LY::ay + 128 * LY::rby;
+    const int groups = (P.ntiles + kTilesPerUnit - 1) / kTilesPerUnit;
+    const int units = P.nf * groups;
+    for (int u = blockIdx.x; u < units; u += gridDim.x) {
+        const int fi = u / groups;
+        const int tile0 = (u % groups) * kTilesPerUnit;
+        const int f = P.f_begin + fi;
+        const bool fvalid = f >= 0 && f < P.nfields;
+        const int p = (f & 1) ^ P.swap;
+        const uint16_t *fp = fvalid ? P.fields + (long long)f * P.field_stride : nullptr;
+
+        // 1. X operand: rows (tile, i), samples minus black
+        for (int R = t; R < kXRows; R += kThreads) {
+            const int ft = R >> 4, i = R & 15;
+            const int tile = tile0 + ft;
+            float a[16];
+#pragma unroll
+            for (int x = 0; x < 16; x++) a[x] = 0.f;
+            if (fvalid && tile < P.ntiles) {
+                const int tileX = P.tileX0 + 8 * (tile % P.ntx);
+                const int tileY = P.tileY0 + 16 * (tile / P.ntx);
+                const int y0 = (p - tileY) & 1;
+                const int L = tileY + y0 + 2 * i;
+                if (L >= P.fafl && L <= P.lafl) {
+                    const long long last = (long long)P.fh * P.fw - 1;
+#pragma unroll
+                    for (int x = 0; x < 16; x++) {
+                        long long idx = (long long)(L >> 1) * P.fw + tileX + x;   // flat, as the reference reads
+                        idx = idx < 0 ? 0 : (idx > last ? last : idx);
+                        a[x] = (float)((int)__ldg(fp + idx) - P.black);
+                    }
+                }
+            }
+            const int blk = R >> 7, r = R & 127;
+#pragma unroll
+            for (int x = 0; x < 16; x++)
+                SP::put(ax_hi + blk * LY::ax_blk, ax_lo + blk * LY::ax_blk, elem_off(r, x, eb, LY::rbx), a[x]);
+        }
+        fence_async_smem();
+        __syncthreads();
+
+        // 2. X MMAs: block b -> tensor columns 16 b
+        if (t == 0) {
+            fence_after();
+            for (int b = 0; b < 3; b++)
+                mma3<KIND>(tmem + 16 * b, smem_addr(ax_hi + b * LY::ax_blk), smem_addr(ax_lo + b * LY::ax_blk),
+                           smem_addr(smem + LY::bx), smem_addr(smem + LY::bx + 16 * LY::rbx), 8 * LY::rbx,
+                           8 * LY::rbx, LY::ksx, idesc(KIND == 0 ? 2 : 1, 128, 16));
+            mma_commit(bar);
+        }
+        bool ok = bar_wait(bar, phase);
+        phase ^= 1;
+        if (__syncthreads_or(!ok)) {
+            if (t == 0) atomicExch(P.err, 1);
+            break;
+        }
+        fence_after();
+
+        // 3. X results -> Y operand rows (tile, kx), columns [re(i) | im(i)]
+        for (int b = 0; b < 3; b++) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + 16 * b, v);
+            const int R = 128 * b + t;
+            const int ft = R >> 4, i = R & 15;
+#pragma unroll
+            for (int k = 0; k < 5; k++) {
+                const int ry = ft * 5 + k;
+                SP::put(ay_hi, ay_lo, elem_off(ry, i, eb, LY::rby), v[2 * k]);
+                SP::put(ay_hi, ay_lo, elem_off(ry, 16 + i, eb, LY::rby), v[2 * k + 1]);
+            }
+        }
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+
+        // 4. Y MMAs with the coefficients of this field's row parity
+        if (t == 0) {
+            fence_after();
+            // tileY0 + 16 ty keeps the parity of tileY0 for every tile
+            const int y0 = (p - P.tileY0) & 1;
+            const uint8_t *byh = smem + LY::by + (2 * y0) * 64 * LY::rby;
+            mma3<KIND>(tmem + 64, smem_addr(ay_hi), smem_addr(ay_lo), smem_addr(byh), smem_addr(byh + 64 * LY::rby),
+                       8 * LY::rby, 8 * LY::rby, LY::ksy, idesc(KIND == 0 ? 2 : 1, 128, 64));
+            mma_commit(bar);
+        }
+        ok = bar_wait(bar, phase);
+        phase ^= 1;
+        if (__syncthreads_or(!ok)) {
+            if (t == 0) atomicExch(P.err, 1);
+            break;
+        }
+        fence_after();
+
+        // 5. row t = (tile, kx): 32 complex ky, stored contiguously
+        {
+            const int ft = t / 5, k = t % 5;
+            const int tile = tile0 + ft;
+            float2 *dst = P.sf + ((long long)fi * P.ntiles + tile) * kQ + k * 32;
+            for (int c = 0; c < 4; c++) {
+                float v[16];
+                tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + 64 + 16 * c, v);
+                if (t < kYRows && tile < P.ntiles) {
+#pragma unroll
+                    for (int j = 0; j < 8; j++) dst[8 * c + j] = make_float2(v[2 * j], v[2 * j + 1]);
+                }
+            }
+        }
+        fence_before();
+        __syncthreads();
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 0) tmem_dealloc(tmem, 128);
+}
+
+// ---------------------------------------------------------------------------
+// Z stage: S[m][tile][kz][kx][ky] from the 8 fields 2m .. 2m+7
+// ---------------------------------------------------------------------------
+template <int KIND>
+__global__ void __launch_bounds__(kThreads) tc3_z_kernel(Params P)
+{
+    using LY = ZLayout<KIND>;
+    using SP = Split<KIND>;
+    constexpr int eb = LY::eb;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + LY::bar);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + LY::bar + 8);
+    const int t = threadIdx.x, warp = t >> 5;
+
+    copy_image(smem + LY::bz, P.bz, 2 * 16 * LY::rbz);
+    if (t == 0) bar_init(bar);
+    if (warp == 0) tmem_alloc(tslot, 32);
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tslot;
+    uint32_t phase = 0;
+    uint8_t *az_hi = smem + LY::az, *az_lo = smem + LY::az + 128 * LY::rbz;
+
+    const long long rows = (long long)P.nm * P.ntiles * kQ;
+    const long long nblk = (rows + 127) / 128;
+    for (long long blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+        const long long g = blk * 128 + t;
+        const bool valid = g < rows;
+        int mi = 0, tile = 0, q = 0;
+        float re[8], im[8];
+#pragma unroll
+        for (int z = 0; z < 8; z++) re[z] = im[z] = 0.f;
+        if (valid) {
+            mi = (int)(g / ((long long)P.ntiles * kQ));
+            const long long rem = g % ((long long)P.ntiles * kQ);
+            tile = (int)(rem / kQ);
+            q = (int)(rem % kQ);
+#pragma unroll
+            for (int z = 0; z < 8; z++) {
+                const float2 s = P.sf[((long long)(2 * mi + z) * P.ntiles + tile) * kQ + q];
+                re[z] = s.x;
+                im[z] = s.y;
+            }
+        }
+#pragma unroll
+        for (int z = 0; z < 8; z++) {
+            SP::put(az_hi, az_lo, elem_off(t, z, eb, LY::rbz), re[z]);
+            SP::put(az_hi, az_lo, elem_off(t, 8 + z, eb, LY::rbz), im[z]);
+        }
+        fence_async_smem();
+        __syncthreads();
+        if (t == 0) {
+            fence_after();
+            mma3<KIND>(tmem, smem_addr(az_hi), smem_addr(az_lo), smem_addr(smem + LY::bz),
+                       smem_addr(smem + LY::bz + 16 * LY::rbz), 8 * LY::rbz, 8 * LY::rbz, LY::ksz,
+                       idesc(KIND == 0 ? 2 : 1, 128, 16));
+            mma_commit(bar);
+        }
+        const bool ok = bar_wait(bar, phase);
+        phase ^= 1;
+        if (__syncthreads_or(!ok)) {
+            if (t == 0) atomicExch(P.err, 1);
+            break;
+        }
+        fence_after();
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16), v);
+        if (valid) {
+            float2 *dst = P.spec + ((long long)mi * P.ntiles + tile) * kSpecPerTile + q;
+#pragma unroll
+            for (int kz = 0; kz < 8; kz++) dst[kz * kQ] = make_float2(v[2 * kz], v[2 * kz + 1]);
+        }
+        fence_before();
+        __syncthreads();
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 0) tmem_dealloc(tmem, 32);
+}
+
+// ---------------------------------------------------------------------------
+// Host: coefficient images
+// ---------------------------------------------------------------------------
+static double rc_window(int n, int N) { return 0.5 - (0.5 * cos((2 * M_PI * (n + 0.5)) / N)); }
+
+static float tf32_rna(float f)
+{
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    u = (u + 0x1000u) & 0xFFFFE000u;
+    memcpy(&f, &u, 4);
+    return f;
+}
+
+static uint16_t bf16_rn(float f)
+{
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+
+static float bf16_val(uint16_t h)
+{
+    const uint32_t u = (uint32_t)h << 16;
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+}
+
+// Write the (hi, lo) split of matrix M (rows x K, row-major doubles) as two
+// operand images.
+static void put_image(std::vector<uint8_t> &img, size_t off_hi, size_t off_lo, const std::vector<double> &M, int rows,
+                      int K, int variant)
+{
+    const int eb = variant == 0 ? 4 : 2;
+    const int rb = K * eb;
+    for (int r = 0; r < rows; r++)
+        for (int k = 0; k < K; k++) {
+            const double v = M[(size_t)r * K + k];
+            const uint32_t o = elem_off(r, k, eb, rb);
+            if (variant == 0) {
+                const float h = tf32_rna((float)v);
+                const float l = tf32_rna((float)(v - (double)h));
+                memcpy(&img[off_hi + o], &h, 4);
+                memcpy(&img[off_lo + o], &l, 4);
+            } else {
+                const uint16_t h = bf16_rn((float)v);
+                const uint16_t l = bf16_rn((float)(v - (double)bf16_val(h)));
+                memcpy(&img[off_hi + o], &h, 2);
+                memcpy(&img[off_lo + o], &l, 2);
+            }
+        }
+}
+
+// B_X [16 x 16]: row 2k + c (kx = k + 2), column x: w_x(x) (cos th, -sin th), th = 2 pi kx x / 16
+static std::vector<double> matrix_x()
+{
+    std::vector<double> M(16 * 16, 0.0);
+    for (int k = 0; k < 5; k++)
+        for (int x = 0; x < 16; x++) {
+            const double th = 2.0 * M_PI * (k + 2) * x / 16.0, w = rc_window(x, 16);
+            M[(2 * k) * 16 + x] = w * cos(th);
+            M[(2 * k + 1) * 16 + x] = -w * sin(th);
+        }
+    return M;
+}
+
+// B_Y [64 x 32] for row parity y0: row 2 ky + c, columns re(i), im(i);
+// frame line y = y0 + 2 i, ph = 2 pi ky y / 32
+static std::vector<double> matrix_y(int y0)
+{
+    std::vector<double> M(64 * 32, 0.0);
+    for (int ky = 0; ky < 32; ky++)
+        for (int i = 0; i < 16; i++) {
+            const int y = y0 + 2 * i;
+            const double ph = 2.0 * M_PI * ky * y / 32.0, w = rc_window(y, 32);
+            M[(2 * ky) * 32 + i] = w * cos(ph);
+            M[(2 * ky) * 32 + 16 + i] = w * sin(ph);
+            M[(2 * ky + 1) * 32 + i] = -w * sin(ph);
+            M[(2 * ky + 1) * 32 + 16 + i] = w * cos(ph);
+        }
+    return M;
+}
+
+// B_Z [16 x 16]: row 2 kz + c, columns re(z), im(z); ph = 2 pi kz z / 8
+static std::vector<double> matrix_z()
+{
+    std::vector<double> M(16 * 16, 0.0);
+    for (int kz = 0; kz < 8; kz++)
+        for (int z = 0; z < 8; z++) {
+            const double ph = 2.0 * M_PI * kz * z / 8.0, w = rc_window(z, 8);
+            M[(2 * kz) * 16 + z] = w * cos(ph);
+            M[(2 * kz) * 16 + 8 + z] = w * sin(ph);
+            M[(2 * kz + 1) * 16 + z] = -w * sin(ph);
+            M[(2 * kz + 1) * 16 + 8 + z] = w * cos(ph);
+        }
+    return M;
+}
+
+struct Images {
+    std::vector<uint8_t> bx, by, bz;   // bx/bz: [split], by: [y0][split]
+};
+
+static Images build_images(int variant)
+{
+    const int eb = variant == 0 ? 4 : 2;
+    Images im;
+    const size_t sx = 16 * 16 * eb, sy = 64 * 32 * eb, sz = 16 * 16 * eb;
+    im.bx.assign(2 * sx, 0);
+    im.by.assign(4 * sy, 0);
+    im.bz.assign(2 * sz, 0);
+    put_image(im.bx, 0, sx, matrix_x(), 16, 16, variant);
+    for (int y0 = 0; y0 < 2; y0++) put_image(im.by, (2 * y0) * sy, (2 * y0 + 1) * sy, matrix_y(y0), 64, 32, variant);
+    put_image(im.bz, 0, sz, matrix_z(), 16, 16, variant);
+    return im;
+}
+
+struct DeviceState {
+    uint8_t *img[2] = {nullptr, nullptr};   // per variant: bx | by | bz
+    size_t off_by[2] = {0, 0}, off_bz[2] = {0, 0};
+    float2 *sf = nullptr;
+    size_t sf_bytes = 0;
+    int *err = nullptr;
+    bool attrs = false;
+};
+
+static std::mutex g_mu;
+static DeviceState g_dev[64];
+
+static int fail(const std::string &what, int code)
+{
+    chd::detail::set_last_error("chromadec_gb300: " + what);
+    return code;
+}
+
+}  // namespace tc
+}  // namespace tpal
+
+using namespace tpal::tc;
+
+#pragma GCC visibility push(default)
+extern "C" {
+
+int chdg_tc3d_operand(int32_t variant, int32_t stage, int32_t y0, int32_t split, void *out, size_t bytes)
+{
+    if (variant < 0 || variant > 1 || stage < 0 || stage > 2 || y0 < 0 || y0 > 1 || split < 0 || split > 1 || !out)
+        return fail("chdg_tc3d_operand: bad argument", CHDG_E_INVALID_ARG);
+    const Images im = build_images(variant);
+    const std::vector<uint8_t> &src = stage == 0 ? im.bx : (stage == 1 ? im.by : im.bz);
+    const size_t one = src.size() / (stage == 1 ? 4 : 2);
+    const size_t off = (stage == 1 ? (size_t)(2 * y0 + split) : (size_t)split) * one;
+    if (bytes < one) return fail("chdg_tc3d_operand: buffer too small", CHDG_E_INVALID_ARG);
+    memcpy(out, src.data() + off, one);
+    return (int)one;
+}
+
+int chdg_tc3d_spectra(const chdg_geometry *g, int32_t variant, const uint16_t *d_fields, int64_t field_stride,
+                      int32_t nfields, int32_t m_begin, int32_t m_end, void *d_spec, void *stream)
+{
+    if (!g || !d_fields || !d_spec || variant < 0 || variant > 1 || m_end <= m_begin || nfields <= 0 ||
+        field_stride < (int64_t)g->field_width * g->field_height)
+        return fail("chdg_tc3d_spectra: bad argument", CHDG_E_INVALID_ARG);
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+        return fail("chdg_tc3d_spectra: no CUDA device", CHDG_E_CUDA);
+    Params P{};
+    P.fields = d_fields;
+    P.field_stride = field_stride;
+    P.nfields = nfields;
+    P.fw = g->field_width;
+    P.fh = g->field_height;
+    P.fafl = g->first_active_frame_line;
+    P.lafl = g->last_active_frame_line;
+    P.black = g->black;
+    P.swap = 0;
+    P.tileX0 = g->active_start - 8;
+    P.ntx = (g->active_end - P.tileX0 + 7) / 8;
+    P.tileY0 = g->first_active_frame_line - 16;
+    P.nty = (g->last_active_frame_line - P.tileY0) / 16 + 1;
+    P.ntiles = P.ntx * P.nty;
+    P.nm = m_end - m_begin;
+    P.f_begin = 2 * m_begin;
+    P.nf = 2 * P.nm + 6;
+    P.spec = (float2 *)d_spec;
+    cudaStream_t s = (cudaStream_t)stream;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        DeviceState &D = g_dev[dev];
+        if (!D.img[variant]) {
+            const Images im = build_images(variant);
+            const size_t total = im.bx.size() + im.by.size() + im.bz.size();
+            if (cudaMalloc(&D.img[variant], total) != cudaSuccess) return fail("chdg_tc3d_spectra: cudaMalloc", CHDG_E_OOM);
+            std::vector<uint8_t> all(im.bx);
+            all.insert(all.end(), im.by.begin(), im.by.end());
+            all.insert(all.end(), im.bz.begin(), im.bz.end());
+            if (cudaMemcpy(D.img[variant], all.data(), total, cudaMemcpyHostToDevice) != cudaSuccess)
+                return fail("chdg_tc3d_spectra: upload", CHDG_E_CUDA);
+            D.off_by[variant] = im.bx.size();
+            D.off_bz[variant] = im.bx.size() + im.by.size();
+        }
+        if (!D.err) {
+            if (cudaMalloc(&D.err, sizeof(int)) != cudaSuccess || cudaMemset(D.err, 0, sizeof(int)) != cudaSuccess)
+                return fail("chdg_tc3d_spectra: cudaMalloc", CHDG_E_OOM);
+        }
+        const size_t need = (size_t)P.nf * P.ntiles * kQ * sizeof(float2);
+        if (D.sf_bytes < need) {
+            if (D.sf) {
+                cudaDeviceSynchronize();
+                cudaFree(D.sf);
+            }
+            D.sf = nullptr;
+            D.sf_bytes = 0;
+            if (cudaMalloc(&D.sf, need) != cudaSuccess) return fail("chdg_tc3d_spectra: cudaMalloc", CHDG_E_OOM);
+            D.sf_bytes = need;
+        }
+        if (!D.attrs) {
+            cudaFuncSetAttribute(tc3_xy_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, XYLayout<0>::bytes);
+            cudaFuncSetAttribute(tc3_xy_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, XYLayout<1>::bytes);
+            cudaFuncSetAttribute(tc3_z_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, ZLayout<0>::bytes);
+            cudaFuncSetAttribute(tc3_z_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, ZLayout<1>::bytes);
+            D.attrs = true;
+        }
+        P.bx = D.img[variant];
+        P.by = D.img[variant] + D.off_by[variant];
+        P.bz = D.img[variant] + D.off_bz[variant];
+        P.sf = D.sf;
+        P.err = D.err;
+    }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int groups = (P.ntiles + kTilesPerUnit - 1) / kTilesPerUnit;
+    const long long units = (long long)P.nf * groups;
+    const long long zblocks = ((long long)P.nm * P.ntiles * kQ + 127) / 128;
+    const int gxy = (int)std::min<long long>(units, 2LL * sms);
+    const int gz = (int)std::min<long long>(zblocks, 8LL * sms);
+    if (variant == 0) {
+        tc3_xy_kernel<0><<<gxy, kThreads, XYLayout<0>::bytes, s>>>(P);
+        tc3_z_kernel<0><<<gz, kThreads, ZLayout<0>::bytes, s>>>(P);
+    } else {
+        tc3_xy_kernel<1><<<gxy, kThreads, XYLayout<1>::bytes, s>>>(P);
+        tc3_z_kernel<1><<<gz, kThreads, ZLayout<1>::bytes, s>>>(P);
+    }
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(std::string("chdg_tc3d_spectra: launch: ") + cudaGetErrorString(e), CHDG_E_CUDA);
+    return 0;
+}
+
+int chdg_tc3d_sync(void *stream)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return fail("chdg_tc3d_sync: no CUDA device", CHDG_E_CUDA);
+    const cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return fail(std::string("chdg_tc3d_sync: ") + cudaGetErrorString(e), CHDG_E_CUDA);
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_dev[dev].err) return 0;
+    int flag = 0;
+    if (cudaMemcpy(&flag, g_dev[dev].err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return fail("chdg_tc3d_sync: read flag", CHDG_E_CUDA);
+    if (flag) {
+        cudaMemset(g_dev[dev].err, 0, sizeof(int));
+        return fail("chdg_tc3d_sync: a tensor-core completion wait ran out", CHDG_E_CUDA);
+    }
+    return 0;
+}
+
+}  // extern "C"
+#pragma GCC visibility pop

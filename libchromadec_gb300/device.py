@@ -84,6 +84,10 @@ def lib(build: bool = True):
                                           C.POINTER(BatchTuning)]
         L.chdg_engine_kernel_times.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                                C.POINTER(C.c_int64)]
+        L.chdg_tc3d_spectra.argtypes = [C.POINTER(Geometry), C.c_int32, C.c_void_p, C.c_int64, C.c_int32, C.c_int32,
+                                        C.c_int32, C.c_void_p, C.c_void_p]
+        L.chdg_tc3d_sync.argtypes = [C.c_void_p]
+        L.chdg_tc3d_operand.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_size_t]
         L.chd_last_error.restype = C.c_char_p
         _lib = L
     return _lib
@@ -214,3 +218,42 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+TC_3XTF32 = 0
+TC_BF16X3 = 1
+
+
+def tc3d_spectra(fields, m_begin: int, m_end: int, spec, variant: int = TC_3XTF32, stream=None,
+                 geometry: Optional[Geometry] = None, field_stride: Optional[int] = None,
+                 nfields: Optional[int] = None):
+    """chdg_tc3d_spectra: tensor-core spectra of Z tiles [m_begin, m_end) into
+    spec, a complex64 (or float32 (..., 2)) CUDA tensor of
+    (m_end - m_begin) x ntiles x 8 x 5 x 32 bins."""
+    g = geometry or default_geometry()
+    stride = field_stride if field_stride is not None else fields[0].numel()
+    nf = nfields if nfields is not None else fields.shape[0]
+    ntx = (g.active_end - g.active_start + 8 + 7) // 8
+    nty = (g.last_active_frame_line - g.first_active_frame_line + 16) // 16 + 1
+    need = (m_end - m_begin) * ntx * nty * 8 * 5 * 32 * 8
+    if m_end <= m_begin or spec.numel() * spec.element_size() < need or not spec.is_contiguous():
+        raise ValueError(f"spec must be a contiguous buffer of at least {need} bytes")
+    rc = lib().chdg_tc3d_spectra(C.byref(g), variant, C.c_void_p(fields.data_ptr()), stride, nf, m_begin, m_end,
+                                 C.c_void_p(spec.data_ptr()), Engine._stream_ptr(stream))
+    if rc != 0:
+        raise RuntimeError(f"chdg_tc3d_spectra failed ({rc}): {last_error()}")
+
+
+def tc3d_sync(stream=None):
+    rc = lib().chdg_tc3d_sync(Engine._stream_ptr(stream))
+    if rc != 0:
+        raise RuntimeError(f"chdg_tc3d_sync failed ({rc}): {last_error()}")
+
+
+def tc3d_operand(variant: int, stage: int, y0: int = 0, split: int = 0) -> bytes:
+    """Host-built shared-memory image of one tensor-core coefficient operand."""
+    buf = (C.c_uint8 * 65536)()
+    n = lib().chdg_tc3d_operand(variant, stage, y0, split, buf, len(buf))
+    if n < 0:
+        raise RuntimeError(f"chdg_tc3d_operand failed ({n}): {last_error()}")
+    return bytes(buf[:n])
