@@ -179,14 +179,25 @@ int chdg_batch_autotune(chdg_batch *b, const chdg_capture *caps, int32_t n, void
  * field of each frame is at the even index. Asynchronous on `stream`;
  * chdg_tc3d_sync waits for it and reports a tensor-core completion wait that
  * ran out (none is expected). chdg_tc3d_operand copies the host-built image
- * of one coefficient operand (stage 0 = X, 1 = Y, 2 = Z; split 0 = hi,
- * 1 = lo) in its shared-memory layout and returns its size in bytes. */
+ * of one coefficient operand (stage 0 = X, 1 = Y, 2 = Z forward, 3 = Z,
+ * 4 = Y, 5 = X inverse; split 0 = hi, 1 = lo) in its shared-memory layout
+ * and returns its size in bytes. */
 #define CHDG_TC_3XTF32 0
 #define CHDG_TC_BF16X3 1
 int chdg_tc3d_spectra(const chdg_geometry *g, int32_t variant, const uint16_t *d_fields, int64_t field_stride,
                       int32_t nfields, int32_t m_begin, int32_t m_end, void *d_spec, void *stream);
 int chdg_tc3d_sync(void *stream);
 int chdg_tc3d_operand(int32_t variant, int32_t stage, int32_t y0, int32_t split, void *out, size_t bytes);
+
+/* Decode with the tensor-core form: a Transform 3D engine with a uniform
+ * threshold runs its transform stage as tcgen05 contractions in `variant`
+ * (CHDG_TC_3XTF32 or CHDG_TC_BF16X3) -- forward X/Y/Z, the threshold decision
+ * of each visited bin taken in FP32 on those spectra (not re-decided exactly,
+ * unlike the plain form), inverse Z/Y/X and overlap-add -- then the same
+ * demodulator; -1 restores the plain form. Its scratch is shared by the
+ * device's tensor-core calls: serialise them. Stage images 3..5 of
+ * chdg_tc3d_operand are the inverse Z, Y, X coefficients. */
+int chdg_engine_set_tc_form(chdg_engine *e, int32_t variant);
 
 /* Multi-source concealment alignment (MultiSourceAlignment::
  * sourceFrameForPrimaryFrame, src/dropout/multi_source_alignment.cpp:54-71):

@@ -310,6 +310,7 @@ int Engine::run_transform(const uint16_t *fields, long long stride, int field_ba
         P.thr_table = thr_dev_;
         P.frame_t2 = frame_t2_;
         P.stats = stats_dev_;
+        if (tc_variant_ >= 0) return tpal::tc3_transform(P, g_.field_height, tc_variant_, s);
         // guard-band decisions: recorded by the walk, decided by the resolve
         // pass, work items with a wrong FP32 decision walked again exactly
         if (static_) {
@@ -487,6 +488,15 @@ int Engine::fill_border(void *out, int nframes, cudaStream_t s)
     return e == cudaSuccess ? 0 : cuda_fail("fill", e);
 }
 
+int Engine::set_tc_form(int variant)
+{
+    if (variant < -1 || variant > 1) return arg_fail("set_tc_form: variant must be -1, 0 or 1");
+    if (variant >= 0 && (c_.kind != 8 || thr_dev_ != nullptr || static_))
+        return arg_fail("set_tc_form: the tensor-core form is Transform 3D with a uniform threshold");
+    tc_variant_ = variant;
+    return 0;
+}
+
 int Engine::decode(const uint16_t *fields, long long stride, int field_base, int nfields, int fb, int fe, void *out,
                    cudaStream_t s)
 {
@@ -514,7 +524,7 @@ int Engine::decode(const uint16_t *fields, long long stride, int field_base, int
         }
         // transform (+ resolve and apply when deferred) and demodulator;
         // PALcolour runs the demodulator alone
-        launches_ += (c_.kind == 6) ? 1 : (c_.kind == 8) ? 4 : 2;
+        launches_ += (c_.kind == 6) ? 1 : (c_.kind == 8) ? (tc_variant_ >= 0 ? tpal::tc3_launches_per_frames(be - b) + 1 : 4) : 2;
         o += frame_bytes() * (size_t)(be - b);
     }
     return 0;
@@ -779,6 +789,12 @@ int chdg_chroma_device(chdg_engine *e, const uint16_t *d_fields, int64_t field_s
 {
     if (!e) return chdg::arg_fail("chdg_chroma_device: null engine");
     return e->eng.chroma(d_fields, field_stride, nfields, frame_begin, frame_end, d_chroma, (cudaStream_t)stream);
+}
+
+int chdg_engine_set_tc_form(chdg_engine *e, int32_t variant)
+{
+    if (!e) return chdg::arg_fail("chdg_engine_set_tc_form: null engine");
+    return e->eng.set_tc_form(variant);
 }
 
 int chdg_engine_stats(chdg_engine *e, uint64_t *exact_decisions, uint64_t *fp32_flips)

@@ -75,6 +75,10 @@ public:
     // capped grid walks the items persistently.
     void set_max_blocks(int n) { max_blocks3_ = n > 0 ? n : 0; }
     int max_blocks() const { return max_blocks3_; }
+    // Tensor-core form of the 3D transform (-1: the plain form, the default;
+    // 0: 3xTF32; 1: BF16x3). Transform 3D, uniform threshold only.
+    int set_tc_form(int variant);
+    int tc_form() const { return tc_variant_; }
     // Batches of captures in one frame index space: every field's first
     // sample (null for the black gap fields between captures), every frame's
     // squared threshold (f, hi, lo) and output pointer (null for gap frames).
@@ -119,6 +123,7 @@ private:
     int max_batch_frames_ = 256;
     int chunk_frames_ = 48;
     int max_blocks3_ = 0;
+    int tc_variant_ = -1;
     const uint16_t *const *field_ptrs_ = nullptr;
     const float *frame_t2_ = nullptr;
     void *const *frame_out_ = nullptr;

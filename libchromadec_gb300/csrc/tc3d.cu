@@ -54,6 +54,7 @@
 
 #include "../../include/chromadec_gb300.h"
 #include "error_state.h"
+#include "tpal_kernels.h"
 
 namespace tpal {
 namespace tc {
@@ -67,15 +68,25 @@ constexpr int kSpecPerTile = 8 * kQ;   // (kz, kx, ky)
 constexpr unsigned kWaitLimit = 1u << 22;
 
 struct Params {
-    const uint16_t *fields;
+    const uint16_t *fields;              // buffer holding fields [field_base, ...)
+    const uint16_t *const *field_ptrs;   // unused (null): the tensor-core form reads one buffer
     long long field_stride;
+    int field_base;
     int nfields, fw, fh, fafl, lafl, black, swap;
     int tileX0, tileY0, ntx, nty, ntiles;
     int f_begin, nf;           // XY stage: fields [f_begin, f_begin + nf)
     int nm;                    // Z stage: Z tiles m_begin .. m_begin + nm - 1 (fields 2m .. 2m+7)
-    const uint8_t *bx, *by, *bz;   // operand images: [split][...], by [y0][split][...]
+    const uint8_t *bx, *by, *bz;   // forward operand images: [split][...], by [y0][split][...]
+    const uint8_t *bzi, *byi, *bxi;   // inverse operand images: bzi [split], byi [y0][split], bxi [split]
     float2 *sf;                // XY output: [nf][ntiles][kQ] (kx major, ky minor)
     float2 *spec;              // Z output: [nm][ntiles][8 kz][kQ]
+    // decode (Z forward + decisions + Z inverse, then Y/X inverse and overlap-add)
+    float t2f;                 // squared threshold
+    float2 *rz;                // [nm][ntiles][4 slices z = 0, 1, 4, 5][kQ]
+    int frame0, nout;          // output fields 2 frame0 .. 2 frame0 + nout - 1
+    float *partial;            // overlap-class planes, output field (out_field0 + o)
+    long long part_class_stride, part_field_stride;
+    int part_row_stride, fl_lo, avs, ave, out_field0;
     int *err;
 };
 
@@ -300,7 +311,7 @@ __global__ void __launch_bounds__(kThreads) tc3_xy_kernel(Params P)
         const int f = P.f_begin + fi;
         const bool fvalid = f >= 0 && f < P.nfields;
         const int p = (f & 1) ^ P.swap;
-        const uint16_t *fp = fvalid ? P.fields + (long long)f * P.field_stride : nullptr;
+        const uint16_t *fp = fvalid ? P.fields + (long long)(f - P.field_base) * P.field_stride : nullptr;
 
         // 1. X operand: rows (tile, i), samples minus black
         for (int R = t; R < kXRows; R += kThreads) {
@@ -491,6 +502,333 @@ __global__ void __launch_bounds__(kThreads) tc3_z_kernel(Params P)
 }
 
 // ---------------------------------------------------------------------------
+// Decode: Z forward, threshold decisions and Z inverse of one Z tile of one
+// spatial tile per CTA iteration (160 rows (kx, ky) as two M = 128 blocks).
+// The decision is the plain form's FP32 rule on the tensor-core spectrum:
+// keep a bin when |bin|^2 and |mirror|^2 are within t^2 of each other, the
+// mirror about the carrier being ((10 - kz) & 7, 8 - kx, (40 - ky) & 31)
+// (transform_pal_3d.cpp:294-331; the carrier, its own mirror, is kept). The
+// inverse Z DFT is evaluated only at the four slices an output field takes:
+// z = 0, 1 (fields 2m, 2m+1) and z = 4, 5 (fields 2m+4, 2m+5,
+// transform_pal_3d.cpp:214-215).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool keep_pair(float a, float b, float t2)
+{
+    return (__fmaf_rn(-b, t2, a) >= 0.f) && (__fmaf_rn(-a, t2, b) >= 0.f);
+}
+
+template <int KIND>
+struct ZDLayout {
+    static constexpr int eb = Split<KIND>::eb;
+    static constexpr int rb = 16 * eb;
+    static constexpr int blk = 128 * rb;
+    static constexpr int af = 0;                     // [split][2 blocks][128 rows]
+    static constexpr int ai = af + 4 * blk;          // [split][2 blocks][128 rows]
+    static constexpr int bf = ai + 4 * blk;          // [split][16 rows]
+    static constexpr int bi = bf + 2 * 16 * rb;      // [split][16 rows]
+    static constexpr int mag = bi + 2 * 16 * rb;     // [160][8] floats
+    static constexpr int bar = mag + kQ * 8 * 4;
+    static constexpr int bytes = bar + 64;
+    static constexpr int ks = rb / 32;
+};
+
+template <int KIND>
+__global__ void __launch_bounds__(kThreads) tc3_zd_kernel(Params P)
+{
+    using LY = ZDLayout<KIND>;
+    using SP = Split<KIND>;
+    constexpr int eb = LY::eb;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + LY::bar);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + LY::bar + 8);
+    float *mag = reinterpret_cast<float *>(smem + LY::mag);
+    const int t = threadIdx.x, warp = t >> 5;
+
+    copy_image(smem + LY::bf, P.bz, 2 * 16 * LY::rb);
+    copy_image(smem + LY::bi, P.bzi, 2 * 16 * LY::rb);
+    for (int o = t * 16; o < 8 * LY::blk; o += kThreads * 16) *reinterpret_cast<uint4 *>(smem + LY::af + o) = uint4{0, 0, 0, 0};
+    if (t == 0) bar_init(bar);
+    if (warp == 0) tmem_alloc(tslot, 64);   // forward: columns 0..31, inverse: 32..63
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tslot;
+    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    uint32_t phase = 0;
+    uint8_t *af_hi = smem + LY::af, *af_lo = smem + LY::af + 2 * LY::blk;
+    uint8_t *ai_hi = smem + LY::ai, *ai_lo = smem + LY::ai + 2 * LY::blk;
+    const uint32_t id = idesc(KIND == 0 ? 2 : 1, 128, 16);
+
+    const long long units = (long long)P.nm * P.ntiles;
+    for (long long u = blockIdx.x; u < units; u += gridDim.x) {
+        const int mi = (int)(u / P.ntiles), tile = (int)(u % P.ntiles);
+        // 1. rows q = t, 128 + t: the 8 fields' S_f (rows 160..255 stay zero)
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int q = 128 * h + t;
+            if (q < kQ) {
+#pragma unroll
+                for (int z = 0; z < 8; z++) {
+                    const float2 v = P.sf[((long long)(2 * mi + z) * P.ntiles + tile) * kQ + q];
+                    SP::put(af_hi + h * LY::blk, af_lo + h * LY::blk, elem_off(t, z, eb, LY::rb), v.x);
+                    SP::put(af_hi + h * LY::blk, af_lo + h * LY::blk, elem_off(t, 8 + z, eb, LY::rb), v.y);
+                }
+            }
+        }
+        fence_async_smem();
+        __syncthreads();
+        if (t == 0) {
+            fence_after();
+            for (int h = 0; h < 2; h++)
+                mma3<KIND>(tmem + 16 * h, smem_addr(af_hi + h * LY::blk), smem_addr(af_lo + h * LY::blk),
+                           smem_addr(smem + LY::bf), smem_addr(smem + LY::bf + 16 * LY::rb), 8 * LY::rb, 8 * LY::rb,
+                           LY::ks, id);
+            mma_commit(bar);
+        }
+        bool ok = bar_wait(bar, phase);
+        phase ^= 1;
+        if (__syncthreads_or(!ok)) {
+            if (t == 0) atomicExch(P.err, 1);
+            break;
+        }
+        fence_after();
+
+        // 2. spectra of this thread's rows; their squared magnitudes for the mirrors
+        float v[2][16];
+        tmem_ld16(tmem + lane_base, v[0]);
+        tmem_ld16(tmem + lane_base + 16, v[1]);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int q = 128 * h + t;
+            if (q < kQ)
+#pragma unroll
+                for (int kz = 0; kz < 8; kz++) mag[q * 8 + kz] = __fmaf_rn(v[h][2 * kz], v[h][2 * kz], v[h][2 * kz + 1] * v[h][2 * kz + 1]);
+        }
+        __syncthreads();
+
+        // 3. decisions; the kept bins are the inverse's operand
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int q = 128 * h + t;
+            if (q < kQ) {
+                const int kxi = q >> 5, ky = q & 31, kyr = (40 - ky) & 31;
+                const int qm = (4 - kxi) * 32 + kyr;
+#pragma unroll
+                for (int kz = 0; kz < 8; kz++) {
+                    const int kzr = (10 - kz) & 7;
+                    const bool keep = keep_pair(mag[q * 8 + kz], mag[qm * 8 + kzr], P.t2f) ||
+                                      (kxi == 2 && kz == kzr && ky == kyr);
+                    SP::put(ai_hi + h * LY::blk, ai_lo + h * LY::blk, elem_off(t, kz, eb, LY::rb),
+                            keep ? v[h][2 * kz] : 0.f);
+                    SP::put(ai_hi + h * LY::blk, ai_lo + h * LY::blk, elem_off(t, 8 + kz, eb, LY::rb),
+                            keep ? v[h][2 * kz + 1] : 0.f);
+                }
+            }
+        }
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+        if (t == 0) {
+            fence_after();
+            for (int h = 0; h < 2; h++)
+                mma3<KIND>(tmem + 32 + 16 * h, smem_addr(ai_hi + h * LY::blk), smem_addr(ai_lo + h * LY::blk),
+                           smem_addr(smem + LY::bi), smem_addr(smem + LY::bi + 16 * LY::rb), 8 * LY::rb, 8 * LY::rb,
+                           LY::ks, id);
+            mma_commit(bar);
+        }
+        ok = bar_wait(bar, phase);
+        phase ^= 1;
+        if (__syncthreads_or(!ok)) {
+            if (t == 0) atomicExch(P.err, 1);
+            break;
+        }
+        fence_after();
+
+        // 4. the four slices of each row
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            float w[16];
+            tmem_ld16(tmem + lane_base + 32 + 16 * h, w);
+            const int q = 128 * h + t;
+            if (q < kQ) {
+                float2 *dst = P.rz + ((long long)mi * P.ntiles + tile) * 4 * kQ + q;
+#pragma unroll
+                for (int sl = 0; sl < 4; sl++) dst[sl * kQ] = make_float2(w[2 * sl], w[2 * sl + 1]);
+            }
+        }
+        fence_before();
+        __syncthreads();
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 0) tmem_dealloc(tmem, 64);
+}
+
+// ---------------------------------------------------------------------------
+// Decode: Y and X inverse and overlap-add of 24 spatial tiles of one output
+// field per CTA iteration. Output field 2k + j sums slice j of Z tile k and
+// slice 4 + j of Z tile k - 2 (transform_pal_3d.cpp:214-215); the Y inverse
+// gives its own-parity rows (y = y0 + 2 i), the X inverse its 16 samples,
+// (2/4096) Re(sum over kx = 2..6), the conjugate bins kx = 10..14 of the
+// reference's c2r folded into the factor 2 (transform_pal_3d.cpp:205-240).
+// Each (tileY, tileX) parity class writes its own plane, as in the plain
+// form.
+// ---------------------------------------------------------------------------
+template <int KIND>
+struct YXLayout {
+    static constexpr int eb = Split<KIND>::eb;
+    static constexpr int rby = 64 * eb;     // Y inverse rows: 32 re + 32 im
+    static constexpr int rbx = 16 * eb;     // X inverse rows: 5 kx re/im (+6 zero)
+    static constexpr int ax_blk = 128 * rbx;
+    static constexpr int ay = 0;                        // [split][128 rows]
+    static constexpr int by = ay + 2 * 128 * rby;       // [y0][split][32 rows]
+    static constexpr int ax = by + 2 * 2 * 32 * rby;    // [split][3 blocks][128 rows]
+    static constexpr int bx = ax + 2 * 3 * ax_blk;      // [split][16 rows]
+    static constexpr int bar = bx + ((2 * 16 * rbx + 1023) & ~1023);
+    static constexpr int bytes = bar + 64;
+    static constexpr int ksy = rby / 32;
+    static constexpr int ksx = rbx / 32;
+};
+
+template <int KIND>
+__global__ void __launch_bounds__(kThreads) tc3_yx_kernel(Params P)
+{
+    using LY = YXLayout<KIND>;
+    using SP = Split<KIND>;
+    constexpr int eb = LY::eb;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + LY::bar);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + LY::bar + 8);
+    const int t = threadIdx.x, warp = t >> 5;
+
+    copy_image(smem + LY::by, P.byi, 2 * 2 * 32 * LY::rby);
+    copy_image(smem + LY::bx, P.bxi, 2 * 16 * LY::rbx);
+    for (int o = t * 16; o < 2 * 128 * LY::rby; o += kThreads * 16) *reinterpret_cast<uint4 *>(smem + LY::ay + o) = uint4{0, 0, 0, 0};
+    for (int o = t * 16; o < 2 * 3 * LY::ax_blk; o += kThreads * 16) *reinterpret_cast<uint4 *>(smem + LY::ax + o) = uint4{0, 0, 0, 0};
+    if (t == 0) bar_init(bar);
+    if (warp == 0) tmem_alloc(tslot, 128);   // Y inverse: columns 0..31, X inverse: 32..79
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tslot;
+    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    uint32_t phase = 0;
+    uint8_t *ay_hi = smem + LY::ay, *ay_lo = smem + LY::ay + 128 * LY::rby;
+    uint8_t *ax_hi = smem + LY::ax, *ax_lo = smem + LY::ax + 3 * LY::ax_blk;
+
+    const int groups = (P.ntiles + kTilesPerUnit - 1) / kTilesPerUnit;
+    const int units = P.nout * groups;
+    for (int u = blockIdx.x; u < units; u += gridDim.x) {
+        const int fo = u / groups;
+        const int tile0 = (u % groups) * kTilesPerUnit;
+        const int k = fo >> 1, j = fo & 1;
+        const int f = 2 * (P.frame0 + k) + j;
+        const int y0 = (((f & 1) ^ P.swap) - P.tileY0) & 1;   // every tileY has tileY0's parity
+
+        // 1. Y inverse operand, row t = (tile, kx): R = slice j of Z tile k + slice 4 + j of Z tile k - 2
+        if (t < kYRows) {
+            const int ft = t / 5, kxi = t % 5;
+            const int tile = tile0 + ft;
+            if (tile < P.ntiles) {
+                const float2 *ra = P.rz + (((long long)(k + 2) * P.ntiles + tile) * 4 + j) * kQ + kxi * 32;
+                const float2 *rb = P.rz + (((long long)k * P.ntiles + tile) * 4 + 2 + j) * kQ + kxi * 32;
+                for (int ky = 0; ky < 32; ky++) {
+                    const float2 a = ra[ky], b = rb[ky];
+                    SP::put(ay_hi, ay_lo, elem_off(t, ky, eb, LY::rby), a.x + b.x);
+                    SP::put(ay_hi, ay_lo, elem_off(t, 32 + ky, eb, LY::rby), a.y + b.y);
+                }
+            }
+        }
+        fence_async_smem();
+        __syncthreads();
+        if (t == 0) {
+            fence_after();
+            const uint8_t *byh = smem + LY::by + (2 * y0) * 32 * LY::rby;
+            mma3<KIND>(tmem, smem_addr(ay_hi), smem_addr(ay_lo), smem_addr(byh), smem_addr(byh + 32 * LY::rby),
+                       8 * LY::rby, 8 * LY::rby, LY::ksy, idesc(KIND == 0 ? 2 : 1, 128, 32));
+            mma_commit(bar);
+        }
+        bool ok = bar_wait(bar, phase);
+        phase ^= 1;
+        if (__syncthreads_or(!ok)) {
+            if (t == 0) atomicExch(P.err, 1);
+            break;
+        }
+        fence_after();
+
+        // 2. rows i of (tile, kx) -> X inverse operand rows (tile, i), columns kx re/im
+        {
+            float g0[16], g1[16];
+            tmem_ld16(tmem + lane_base, g0);
+            tmem_ld16(tmem + lane_base + 16, g1);
+            if (t < kYRows) {
+                const int ft = t / 5, kxi = t % 5;
+#pragma unroll
+                for (int i = 0; i < 16; i++) {
+                    const int R = ft * 16 + i;
+                    const float re = i < 8 ? g0[2 * i] : g1[2 * i - 16];
+                    const float im = i < 8 ? g0[2 * i + 1] : g1[2 * i - 15];
+                    uint8_t *h = ax_hi + (R >> 7) * LY::ax_blk, *l = ax_lo + (R >> 7) * LY::ax_blk;
+                    SP::put(h, l, elem_off(R & 127, 2 * kxi, eb, LY::rbx), re);
+                    SP::put(h, l, elem_off(R & 127, 2 * kxi + 1, eb, LY::rbx), im);
+                }
+            }
+        }
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+        if (t == 0) {
+            fence_after();
+            for (int b = 0; b < 3; b++)
+                mma3<KIND>(tmem + 32 + 16 * b, smem_addr(ax_hi + b * LY::ax_blk), smem_addr(ax_lo + b * LY::ax_blk),
+                           smem_addr(smem + LY::bx), smem_addr(smem + LY::bx + 16 * LY::rbx), 8 * LY::rbx,
+                           8 * LY::rbx, LY::ksx, idesc(KIND == 0 ? 2 : 1, 128, 16));
+            mma_commit(bar);
+        }
+        ok = bar_wait(bar, phase);
+        phase ^= 1;
+        if (__syncthreads_or(!ok)) {
+            if (t == 0) atomicExch(P.err, 1);
+            break;
+        }
+        fence_after();
+
+        // 3. 16 samples of row (tile, i) into the tile's parity-class plane
+        for (int b = 0; b < 3; b++) {
+            float o[16];
+            tmem_ld16(tmem + lane_base + 32 + 16 * b, o);
+            const int R = 128 * b + t;
+            const int tile = tile0 + (R >> 4), i = R & 15;
+            if (tile < P.ntiles) {
+                const int tx = tile % P.ntx, ty = tile / P.ntx;
+                const int tileX = P.tileX0 + 8 * tx, tileY = P.tileY0 + 16 * ty;
+                const int L = tileY + y0 + 2 * i;
+                if (L >= P.fafl && L <= P.lafl) {
+                    const int cls = ((ty & 1) << 1) | (tx & 1);
+                    float *dst = P.partial + (long long)cls * P.part_class_stride +
+                                 (long long)(P.out_field0 + fo) * P.part_field_stride +
+                                 (long long)((L >> 1) - P.fl_lo) * P.part_row_stride - P.avs;
+#pragma unroll
+                    for (int x = 0; x < 16; x++) {
+                        const int X = tileX + x;
+                        if (X >= P.avs && X < P.ave) dst[X] = o[x];
+                    }
+                }
+            }
+        }
+        fence_before();
+        __syncthreads();
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 0) tmem_dealloc(tmem, 128);
+}
+
+// ---------------------------------------------------------------------------
 // Host: coefficient images
 // ---------------------------------------------------------------------------
 static double rc_window(int n, int N) { return 0.5 - (0.5 * cos((2 * M_PI * (n + 0.5)) / N)); }
@@ -590,29 +928,80 @@ static std::vector<double> matrix_z()
     return M;
 }
 
+// B_Zi [16 x 16]: rows 2 s + c for the slices z_s = 0, 1, 4, 5 (rows 8..15
+// zero), columns re(kz), im(kz); exp(+i ph), ph = 2 pi kz z_s / 8
+static std::vector<double> matrix_zi()
+{
+    static const int zs[4] = {0, 1, 4, 5};
+    std::vector<double> M(16 * 16, 0.0);
+    for (int sl = 0; sl < 4; sl++)
+        for (int kz = 0; kz < 8; kz++) {
+            const double ph = 2.0 * M_PI * kz * zs[sl] / 8.0;
+            M[(2 * sl) * 16 + kz] = cos(ph);
+            M[(2 * sl) * 16 + 8 + kz] = -sin(ph);
+            M[(2 * sl + 1) * 16 + kz] = sin(ph);
+            M[(2 * sl + 1) * 16 + 8 + kz] = cos(ph);
+        }
+    return M;
+}
+
+// B_Yi [32 x 64] for row parity y0: rows 2 i + c (frame line y = y0 + 2 i),
+// columns re(ky), im(ky); exp(+i ph), ph = 2 pi ky y / 32
+static std::vector<double> matrix_yi(int y0)
+{
+    std::vector<double> M(32 * 64, 0.0);
+    for (int i = 0; i < 16; i++)
+        for (int ky = 0; ky < 32; ky++) {
+            const double ph = 2.0 * M_PI * ky * (y0 + 2 * i) / 32.0;
+            M[(2 * i) * 64 + ky] = cos(ph);
+            M[(2 * i) * 64 + 32 + ky] = -sin(ph);
+            M[(2 * i + 1) * 64 + ky] = sin(ph);
+            M[(2 * i + 1) * 64 + 32 + ky] = cos(ph);
+        }
+    return M;
+}
+
+// B_Xi [16 x 16]: row x, columns kx re/im (10..15 zero): (2/4096) (cos th, -sin th), th = 2 pi kx x / 16
+static std::vector<double> matrix_xi()
+{
+    std::vector<double> M(16 * 16, 0.0);
+    for (int x = 0; x < 16; x++)
+        for (int k = 0; k < 5; k++) {
+            const double th = 2.0 * M_PI * (k + 2) * x / 16.0;
+            M[x * 16 + 2 * k] = (2.0 / 4096.0) * cos(th);
+            M[x * 16 + 2 * k + 1] = -(2.0 / 4096.0) * sin(th);
+        }
+    return M;
+}
+
+// Operand images of one variant: per stage [split] (the Y stages [y0][split]).
 struct Images {
-    std::vector<uint8_t> bx, by, bz;   // bx/bz: [split], by: [y0][split]
+    std::vector<uint8_t> stage[6];   // 0 X, 1 Y, 2 Z forward; 3 Z, 4 Y, 5 X inverse
 };
 
 static Images build_images(int variant)
 {
     const int eb = variant == 0 ? 4 : 2;
     Images im;
-    const size_t sx = 16 * 16 * eb, sy = 64 * 32 * eb, sz = 16 * 16 * eb;
-    im.bx.assign(2 * sx, 0);
-    im.by.assign(4 * sy, 0);
-    im.bz.assign(2 * sz, 0);
-    put_image(im.bx, 0, sx, matrix_x(), 16, 16, variant);
-    for (int y0 = 0; y0 < 2; y0++) put_image(im.by, (2 * y0) * sy, (2 * y0 + 1) * sy, matrix_y(y0), 64, 32, variant);
-    put_image(im.bz, 0, sz, matrix_z(), 16, 16, variant);
+    const int rows[6] = {16, 64, 16, 16, 32, 16}, K[6] = {16, 32, 16, 16, 64, 16};
+    for (int st = 0; st < 6; st++) {
+        const size_t one = (size_t)rows[st] * K[st] * eb;
+        const bool per_y0 = (st == 1 || st == 4);
+        im.stage[st].assign((per_y0 ? 4 : 2) * one, 0);
+        for (int y0 = 0; y0 < (per_y0 ? 2 : 1); y0++) {
+            const std::vector<double> M = st == 0 ? matrix_x() : st == 1 ? matrix_y(y0) : st == 2 ? matrix_z()
+                                        : st == 3 ? matrix_zi() : st == 4 ? matrix_yi(y0) : matrix_xi();
+            put_image(im.stage[st], (2 * y0) * one, (2 * y0 + 1) * one, M, rows[st], K[st], variant);
+        }
+    }
     return im;
 }
 
 struct DeviceState {
-    uint8_t *img[2] = {nullptr, nullptr};   // per variant: bx | by | bz
-    size_t off_by[2] = {0, 0}, off_bz[2] = {0, 0};
-    float2 *sf = nullptr;
-    size_t sf_bytes = 0;
+    uint8_t *img[2] = {nullptr, nullptr};   // per variant: the six stages back to back
+    size_t off[2][6] = {};
+    float2 *sf = nullptr, *rz = nullptr;
+    size_t sf_bytes = 0, rz_bytes = 0;
     int *err = nullptr;
     bool attrs = false;
 };
@@ -626,7 +1015,166 @@ static int fail(const std::string &what, int code)
     return code;
 }
 
+static int grow(float2 *&buf, size_t &have, size_t need)
+{
+    if (have >= need) return 0;
+    if (buf) {
+        cudaDeviceSynchronize();
+        cudaFree(buf);
+    }
+    buf = nullptr;
+    have = 0;
+    if (cudaMalloc(&buf, need) != cudaSuccess) return fail("tensor-core form: cudaMalloc", CHDG_E_OOM);
+    have = need;
+    return 0;
+}
+
+// Images, error flag, kernel attributes and scratch of the calling thread's
+// device (under g_mu); fills the operand pointers of P.
+static int prepare(int variant, size_t sf_need, size_t rz_need, Params &P, int &dev)
+{
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return fail("tensor-core form: no CUDA device", CHDG_E_CUDA);
+    DeviceState &D = g_dev[dev];
+    if (!D.img[variant]) {
+        const Images im = build_images(variant);
+        std::vector<uint8_t> all;
+        for (int st = 0; st < 6; st++) {
+            D.off[variant][st] = all.size();
+            all.insert(all.end(), im.stage[st].begin(), im.stage[st].end());
+        }
+        if (cudaMalloc(&D.img[variant], all.size()) != cudaSuccess) return fail("tensor-core form: cudaMalloc", CHDG_E_OOM);
+        if (cudaMemcpy(D.img[variant], all.data(), all.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+            return fail("tensor-core form: upload", CHDG_E_CUDA);
+    }
+    if (!D.err) {
+        if (cudaMalloc(&D.err, sizeof(int)) != cudaSuccess || cudaMemset(D.err, 0, sizeof(int)) != cudaSuccess)
+            return fail("tensor-core form: cudaMalloc", CHDG_E_OOM);
+    }
+    if (const int rc = grow(D.sf, D.sf_bytes, sf_need); rc != 0) return rc;
+    if (rz_need)
+        if (const int rc = grow(D.rz, D.rz_bytes, rz_need); rc != 0) return rc;
+    if (!D.attrs) {
+        cudaFuncSetAttribute(tc3_xy_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, XYLayout<0>::bytes);
+        cudaFuncSetAttribute(tc3_xy_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, XYLayout<1>::bytes);
+        cudaFuncSetAttribute(tc3_z_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, ZLayout<0>::bytes);
+        cudaFuncSetAttribute(tc3_z_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, ZLayout<1>::bytes);
+        cudaFuncSetAttribute(tc3_zd_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, ZDLayout<0>::bytes);
+        cudaFuncSetAttribute(tc3_zd_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, ZDLayout<1>::bytes);
+        cudaFuncSetAttribute(tc3_yx_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, YXLayout<0>::bytes);
+        cudaFuncSetAttribute(tc3_yx_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, YXLayout<1>::bytes);
+        D.attrs = true;
+    }
+    const uint8_t *b = D.img[variant];
+    P.bx = b + D.off[variant][0];
+    P.by = b + D.off[variant][1];
+    P.bz = b + D.off[variant][2];
+    P.bzi = b + D.off[variant][3];
+    P.byi = b + D.off[variant][4];
+    P.bxi = b + D.off[variant][5];
+    P.sf = D.sf;
+    P.rz = D.rz;
+    P.err = D.err;
+    return 0;
+}
+
+static void tile_grid(Params &P, int avs, int ave, int fafl, int lafl)
+{
+    // transform_pal_3d.cpp:151-153
+    P.tileX0 = avs - 8;
+    P.ntx = (ave - P.tileX0 + 7) / 8;
+    P.tileY0 = fafl - 16;
+    P.nty = (lafl - P.tileY0) / 16 + 1;
+    P.ntiles = P.ntx * P.nty;
+}
+
+static int sm_count(int dev)
+{
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms > 0 ? sms : 1;
+}
+
+template <typename K>
+static void launch(K kernel, long long work, int per_sm, int sms, int smem, cudaStream_t s, const Params &P)
+{
+    const int grid = (int)std::min<long long>(work, (long long)per_sm * sms);
+    if (grid > 0) kernel<<<grid, kThreads, smem, s>>>(P);
+}
+
+static void launch_xy(int variant, const Params &P, int sms, cudaStream_t s)
+{
+    const long long units = (long long)P.nf * ((P.ntiles + kTilesPerUnit - 1) / kTilesPerUnit);
+    if (variant == 0) launch(tc3_xy_kernel<0>, units, 1, sms, XYLayout<0>::bytes, s, P);
+    else launch(tc3_xy_kernel<1>, units, 3, sms, XYLayout<1>::bytes, s, P);
+}
+
 }  // namespace tc
+
+// The tensor-core form's transform stage of an engine decode: frames
+// [frame_begin, frame_end) of T into its overlap-class planes, in chunks of
+// up to 64 frames (each with its 2-frame look-behind of Z tiles and the
+// fields they span). Uniform threshold only.
+int tc3_transform(const T3Params &T, int field_height, int variant, cudaStream_t s)
+{
+    using namespace tc;
+    if (variant < 0 || variant > 1 || T.thr_table != nullptr || T.frame_t2 != nullptr || T.field_ptrs != nullptr)
+        return fail("tensor-core form: uniform threshold on one capture buffer only", CHDG_E_UNSUPPORTED);
+    constexpr int kChunk = 64;
+    Params P{};
+    P.fields = T.fields;
+    P.field_stride = T.field_stride;
+    P.field_base = T.field_base;
+    P.nfields = T.nfields;
+    P.fw = T.fw;
+    P.fh = field_height;
+    P.fafl = T.fafl;
+    P.lafl = T.lafl;
+    P.black = T.black;
+    P.swap = T.swap;
+    tile_grid(P, T.avs, T.ave, T.fafl, T.lafl);
+    P.t2f = T.t2f;
+    P.partial = T.partial;
+    P.part_class_stride = T.part_class_stride;
+    P.part_field_stride = T.part_field_stride;
+    P.part_row_stride = T.part_row_stride;
+    P.fl_lo = T.fl_lo;
+    P.avs = T.avs;
+    P.ave = T.ave;
+    const int maxc = std::min(kChunk, T.frame_end - T.frame_begin);
+    const size_t sf_need = (size_t)(2 * (maxc + 2) + 6) * P.ntiles * kQ * sizeof(float2);
+    const size_t rz_need = (size_t)(maxc + 2) * P.ntiles * 4 * kQ * sizeof(float2);
+    int dev = 0;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        if (const int rc = prepare(variant, sf_need, rz_need, P, dev); rc != 0) return rc;
+    }
+    const int sms = sm_count(dev);
+    for (int c0 = T.frame_begin; c0 < T.frame_end; c0 += kChunk) {
+        const int c1 = std::min(T.frame_end, c0 + kChunk);
+        P.nm = (c1 - c0) + 2;         // Z tiles c0 - 2 .. c1 - 1
+        P.f_begin = 2 * (c0 - 2);
+        P.nf = 2 * P.nm + 6;
+        P.frame0 = c0;
+        P.nout = 2 * (c1 - c0);
+        P.out_field0 = 2 * (c0 - T.frame_begin);
+        launch_xy(variant, P, sms, s);
+        const long long zd_units = (long long)P.nm * P.ntiles;
+        const long long yx_units = (long long)P.nout * ((P.ntiles + kTilesPerUnit - 1) / kTilesPerUnit);
+        if (variant == 0) {
+            launch(tc3_zd_kernel<0>, zd_units, 3, sms, ZDLayout<0>::bytes, s, P);
+            launch(tc3_yx_kernel<0>, yx_units, 1, sms, YXLayout<0>::bytes, s, P);
+        } else {
+            launch(tc3_zd_kernel<1>, zd_units, 5, sms, ZDLayout<1>::bytes, s, P);
+            launch(tc3_yx_kernel<1>, yx_units, 3, sms, YXLayout<1>::bytes, s, P);
+        }
+    }
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(std::string("tensor-core form: launch: ") + cudaGetErrorString(e), CHDG_E_CUDA);
+    return 0;
+}
+
+int tc3_launches_per_frames(int frames) { return 3 * ((frames + 63) / 64); }
+
 }  // namespace tpal
 
 using namespace tpal::tc;
@@ -636,12 +1184,13 @@ extern "C" {
 
 int chdg_tc3d_operand(int32_t variant, int32_t stage, int32_t y0, int32_t split, void *out, size_t bytes)
 {
-    if (variant < 0 || variant > 1 || stage < 0 || stage > 2 || y0 < 0 || y0 > 1 || split < 0 || split > 1 || !out)
+    if (variant < 0 || variant > 1 || stage < 0 || stage > 5 || y0 < 0 || y0 > 1 || split < 0 || split > 1 || !out)
         return fail("chdg_tc3d_operand: bad argument", CHDG_E_INVALID_ARG);
     const Images im = build_images(variant);
-    const std::vector<uint8_t> &src = stage == 0 ? im.bx : (stage == 1 ? im.by : im.bz);
-    const size_t one = src.size() / (stage == 1 ? 4 : 2);
-    const size_t off = (stage == 1 ? (size_t)(2 * y0 + split) : (size_t)split) * one;
+    const std::vector<uint8_t> &src = im.stage[stage];
+    const bool per_y0 = (stage == 1 || stage == 4);
+    const size_t one = src.size() / (per_y0 ? 4 : 2);
+    const size_t off = (per_y0 ? (size_t)(2 * y0 + split) : (size_t)split) * one;
     if (bytes < one) return fail("chdg_tc3d_operand: buffer too small", CHDG_E_INVALID_ARG);
     memcpy(out, src.data() + off, one);
     return (int)one;
@@ -653,12 +1202,10 @@ int chdg_tc3d_spectra(const chdg_geometry *g, int32_t variant, const uint16_t *d
     if (!g || !d_fields || !d_spec || variant < 0 || variant > 1 || m_end <= m_begin || nfields <= 0 ||
         field_stride < (int64_t)g->field_width * g->field_height)
         return fail("chdg_tc3d_spectra: bad argument", CHDG_E_INVALID_ARG);
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
-        return fail("chdg_tc3d_spectra: no CUDA device", CHDG_E_CUDA);
     Params P{};
     P.fields = d_fields;
     P.field_stride = field_stride;
+    P.field_base = 0;
     P.nfields = nfields;
     P.fw = g->field_width;
     P.fh = g->field_height;
@@ -666,73 +1213,23 @@ int chdg_tc3d_spectra(const chdg_geometry *g, int32_t variant, const uint16_t *d
     P.lafl = g->last_active_frame_line;
     P.black = g->black;
     P.swap = 0;
-    P.tileX0 = g->active_start - 8;
-    P.ntx = (g->active_end - P.tileX0 + 7) / 8;
-    P.tileY0 = g->first_active_frame_line - 16;
-    P.nty = (g->last_active_frame_line - P.tileY0) / 16 + 1;
-    P.ntiles = P.ntx * P.nty;
+    tile_grid(P, g->active_start, g->active_end, g->first_active_frame_line, g->last_active_frame_line);
     P.nm = m_end - m_begin;
     P.f_begin = 2 * m_begin;
     P.nf = 2 * P.nm + 6;
     P.spec = (float2 *)d_spec;
     cudaStream_t s = (cudaStream_t)stream;
+    int dev = 0;
     {
         std::lock_guard<std::mutex> lk(g_mu);
-        DeviceState &D = g_dev[dev];
-        if (!D.img[variant]) {
-            const Images im = build_images(variant);
-            const size_t total = im.bx.size() + im.by.size() + im.bz.size();
-            if (cudaMalloc(&D.img[variant], total) != cudaSuccess) return fail("chdg_tc3d_spectra: cudaMalloc", CHDG_E_OOM);
-            std::vector<uint8_t> all(im.bx);
-            all.insert(all.end(), im.by.begin(), im.by.end());
-            all.insert(all.end(), im.bz.begin(), im.bz.end());
-            if (cudaMemcpy(D.img[variant], all.data(), total, cudaMemcpyHostToDevice) != cudaSuccess)
-                return fail("chdg_tc3d_spectra: upload", CHDG_E_CUDA);
-            D.off_by[variant] = im.bx.size();
-            D.off_bz[variant] = im.bx.size() + im.by.size();
-        }
-        if (!D.err) {
-            if (cudaMalloc(&D.err, sizeof(int)) != cudaSuccess || cudaMemset(D.err, 0, sizeof(int)) != cudaSuccess)
-                return fail("chdg_tc3d_spectra: cudaMalloc", CHDG_E_OOM);
-        }
-        const size_t need = (size_t)P.nf * P.ntiles * kQ * sizeof(float2);
-        if (D.sf_bytes < need) {
-            if (D.sf) {
-                cudaDeviceSynchronize();
-                cudaFree(D.sf);
-            }
-            D.sf = nullptr;
-            D.sf_bytes = 0;
-            if (cudaMalloc(&D.sf, need) != cudaSuccess) return fail("chdg_tc3d_spectra: cudaMalloc", CHDG_E_OOM);
-            D.sf_bytes = need;
-        }
-        if (!D.attrs) {
-            cudaFuncSetAttribute(tc3_xy_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, XYLayout<0>::bytes);
-            cudaFuncSetAttribute(tc3_xy_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, XYLayout<1>::bytes);
-            cudaFuncSetAttribute(tc3_z_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, ZLayout<0>::bytes);
-            cudaFuncSetAttribute(tc3_z_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, ZLayout<1>::bytes);
-            D.attrs = true;
-        }
-        P.bx = D.img[variant];
-        P.by = D.img[variant] + D.off_by[variant];
-        P.bz = D.img[variant] + D.off_bz[variant];
-        P.sf = D.sf;
-        P.err = D.err;
+        const size_t sf_need = (size_t)P.nf * P.ntiles * kQ * sizeof(float2);
+        if (const int rc = prepare(variant, sf_need, 0, P, dev); rc != 0) return rc;
     }
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int groups = (P.ntiles + kTilesPerUnit - 1) / kTilesPerUnit;
-    const long long units = (long long)P.nf * groups;
+    const int sms = sm_count(dev);
+    launch_xy(variant, P, sms, s);
     const long long zblocks = ((long long)P.nm * P.ntiles * kQ + 127) / 128;
-    const int gxy = (int)std::min<long long>(units, 2LL * sms);
-    const int gz = (int)std::min<long long>(zblocks, 8LL * sms);
-    if (variant == 0) {
-        tc3_xy_kernel<0><<<gxy, kThreads, XYLayout<0>::bytes, s>>>(P);
-        tc3_z_kernel<0><<<gz, kThreads, ZLayout<0>::bytes, s>>>(P);
-    } else {
-        tc3_xy_kernel<1><<<gxy, kThreads, XYLayout<1>::bytes, s>>>(P);
-        tc3_z_kernel<1><<<gz, kThreads, ZLayout<1>::bytes, s>>>(P);
-    }
+    if (variant == 0) launch(tc3_z_kernel<0>, zblocks, 8, sms, ZLayout<0>::bytes, s, P);
+    else launch(tc3_z_kernel<1>, zblocks, 8, sms, ZLayout<1>::bytes, s, P);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(std::string("chdg_tc3d_spectra: launch: ") + cudaGetErrorString(e), CHDG_E_CUDA);
     return 0;

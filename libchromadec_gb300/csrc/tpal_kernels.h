@@ -127,6 +127,12 @@ inline unsigned long long tp3_unc_capacity(int ntiles, int frames, int nchunks)
 }
 int tp2_init_constants(int device);
 int tp2_launch(const T2Params &p, cudaStream_t stream);
+// Tensor-core form of the 3D transform stage (tc3d.cu): the same overlap-class
+// planes as tp3_launch, with the DFT stages as split-precision tcgen05
+// contractions (variant 0 = 3xTF32, 1 = BF16x3) and FP32 decisions on their
+// spectra. Uniform threshold, one capture buffer.
+int tc3_transform(const T3Params &p, int field_height, int variant, cudaStream_t stream);
+int tc3_launches_per_frames(int frames);
 int demod_init_constants(int device, double sample_rate, int field_width);
 int demod_launch(const DemodParams &p, cudaStream_t stream);
 

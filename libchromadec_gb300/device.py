@@ -87,6 +87,7 @@ def lib(build: bool = True):
         L.chdg_tc3d_spectra.argtypes = [C.POINTER(Geometry), C.c_int32, C.c_void_p, C.c_int64, C.c_int32, C.c_int32,
                                         C.c_int32, C.c_void_p, C.c_void_p]
         L.chdg_tc3d_sync.argtypes = [C.c_void_p]
+        L.chdg_engine_set_tc_form.argtypes = [C.c_void_p, C.c_int32]
         L.chdg_tc3d_operand.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_size_t]
         L.chd_last_error.restype = C.c_char_p
         _lib = L
@@ -168,6 +169,12 @@ class Engine:
                                       C.c_void_p(out.data_ptr()), self._stream_ptr(stream))
         if rc != 0:
             raise RuntimeError(f"chdg_chroma_device failed ({rc}): {last_error()}")
+
+    def set_tc_form(self, variant: int):
+        """-1: the plain form; TC_3XTF32 / TC_BF16X3: the tensor-core form."""
+        rc = lib().chdg_engine_set_tc_form(self._h, variant)
+        if rc != 0:
+            raise RuntimeError(f"chdg_engine_set_tc_form failed ({rc}): {last_error()}")
 
     def stats(self):
         a, b = C.c_uint64(), C.c_uint64()

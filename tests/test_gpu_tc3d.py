@@ -60,3 +60,63 @@ def test_tc_black_window_is_zero(spectra):
     cap, g, ntiles, m_begin, m_end, out = spectra
     for variant in out:
         assert np.all(out[variant][0] == 0)   # Z tile -5: fields -10 .. -3
+
+
+def _psnr(x, ref, peak):
+    mse = float(np.mean((x.astype(np.float64) - ref) ** 2))
+    return 10.0 * np.log10(peak * peak / mse)
+
+
+@pytest.fixture(scope="module")
+def decoded(cuda):
+    """The 16-field capture decoded by the plain form and both tensor-core
+    variants: chroma planes and yuv444ps frames, with the FP64 oracle's and
+    the encoder's ground truth."""
+    torch = cuda
+    from libchromadec_gb300 import synth
+    from oracle import oracle as O
+    cfg = synth.SynthConfig(seed=13, pan_x=1.5, pan_y=0.5)
+    cap = synth.make_capture(16, cfg, truth=True)
+    fields = torch.from_numpy(cap.fields.reshape(16, -1).view(np.int16)).cuda()
+    res = {}
+    for form in (-1, D.TC_3XTF32, D.TC_BF16X3):
+        eng = D.Engine(D.default_geometry(), D.default_config(kind=8, fmt=D.FMT_PS))
+        eng.set_tc_form(form)
+        chroma = torch.empty((16, 288, 948), dtype=torch.float32, device="cuda")
+        eng.chroma(fields, 0, 8, chroma)
+        frames = torch.empty((8, 3, eng.out_height, eng.out_width), dtype=torch.float32, device="cuda")
+        eng.decode(fields, 0, 8, frames)
+        torch.cuda.synchronize()
+        D.tc3d_sync()
+        res[form] = (chroma.cpu().numpy(), frames.cpu().numpy())
+    ref_frames, _ = O.decode_frames(O.params(3, O.FMT_PS), cap.fields, 0, 8, threads=8)
+    truth = cap.chroma[:, 22:310, 177:1125]
+    return cap, res, ref_frames, truth
+
+
+@pytest.mark.parametrize("form,rms_tol,max_tol", [(D.TC_3XTF32, 2e-5, 2e-2), (D.TC_BF16X3, 2e-4, 5e-2)])
+def test_tc_decode_error_per_plane(decoded, form, rms_tol, max_tol):
+    """yuv444ps of the tensor-core form against the FP64 oracle, per plane;
+    the plain form is within the parity tolerance everywhere."""
+    cap, res, ref, truth = decoded
+    plain = res[-1][1]
+    assert np.abs(plain - ref).max() <= 1e-4
+    got = res[form][1]
+    assert np.isfinite(got).all()
+    for pl, name in enumerate("Y Cb Cr".split()):
+        d = np.abs(got[:, pl] - ref[:, pl])
+        print(f"form {form} {name}: max {d.max():.3e} rms {np.sqrt(np.mean(d * d)):.3e}")
+        assert np.sqrt(np.mean(d * d)) < rms_tol
+        assert d.max() < max_tol
+
+
+def test_tc_chroma_psnr_matches_plain(decoded):
+    """Chroma separated by each form against the encoder's true chroma: the
+    tensor-core forms reach the plain form's PSNR (within 0.05 dB)."""
+    cap, res, ref, truth = decoded
+    peak = 54016.0 - 16384.0
+    ps = {form: _psnr(res[form][0][4:12], truth[4:12], peak) for form in res}
+    print("chroma PSNR dB:", ps)
+    assert ps[-1] > 25.0
+    for form in (D.TC_3XTF32, D.TC_BF16X3):
+        assert abs(ps[form] - ps[-1]) < 0.05
