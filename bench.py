@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the tensor-core forms and chroma PSNR report")
     ap.add_argument("--workload", default="stream", choices=["stream", "batched"],
                     help="stream: the 500-field 3D capture (the headline line); batched: 48 captures of "
                          "6-300 fields, 40%% 2D / 60%% 3D, one threshold each, through chdg_batch_*")
@@ -374,6 +375,89 @@ def run_batched(a):
     b.close()
 
 
+def forms_report(a, dfields, nfields, plain_value, stream):
+    """The metric's comparison of forms, outside the timed region: the plain
+    form and the tensor-core forms (3xTF32, BF16x3 split products on tcgen05)
+    on the same 500-field workload -- device-resident fields/s of each, chroma
+    PSNR against the encoder's true chroma on the first 48 fields (same seed
+    and content), each tensor-core form's yuv444ps planes against the plain
+    form's (which the parity tests hold within 1e-4 of the FP64 oracle), and
+    its spectra against numpy's FP64 FFT of the same tiles with the share of
+    threshold decisions that flip."""
+    import numpy as np
+    import torch
+    from libchromadec_gb300 import device as D, synth, tc_study as T
+
+    g = D.default_geometry()
+    nframes = nfields // 2
+    forms = {-1: "plain", D.TC_3XTF32: "tc_3xtf32", D.TC_BF16X3: "tc_bf16x3"}
+    out = {name: {} for name in forms.values()}
+    out["plain"]["fields_per_s"] = plain_value
+    # throughput of the tensor-core forms on the bench workload
+    for form in (D.TC_3XTF32, D.TC_BF16X3):
+        eng = D.Engine(g, D.default_config(kind=D.KIND_TRANSFORM_3D, fmt=D.FMT_P16))
+        eng.set_tc_form(form)
+        dout = torch.empty((nframes, 3, eng.out_height, eng.out_width), dtype=torch.int16, device="cuda")
+        for _ in range(max(3, a.warmup)):
+            eng.decode(dfields, 0, nframes, dout, stream)
+        D.tc3d_sync(stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        steps = max(3, a.steps // 4)
+        e0.record(stream)
+        for _ in range(steps):
+            eng.decode(dfields, 0, nframes, dout, stream)
+        e1.record(stream)
+        D.tc3d_sync(stream)
+        ms = e0.elapsed_time(e1) / steps
+        out[forms[form]].update({"fields_per_s": nfields / (ms / 1000.0), "ms_per_step": ms})
+        del dout, eng
+    # chroma PSNR against the true chroma, and planes against the plain form
+    cap = synth.make_capture(48, synth.SynthConfig(seed=a.seed, pan_x=1.5, pan_y=0.5), truth=True)
+    tf = torch.from_numpy(cap.fields.reshape(48, -1).view(np.int16)).cuda()
+    truth = cap.chroma[8:40, 22:310, 177:1125].astype(np.float64)
+    peak = float(g.white - g.black)
+    frames = {}
+    for form, name in forms.items():
+        eng = D.Engine(g, D.default_config(kind=D.KIND_TRANSFORM_3D, fmt=D.FMT_PS))
+        eng.set_tc_form(form)
+        ch = torch.empty((32, 288, 948), dtype=torch.float32, device="cuda")
+        eng.chroma(tf, 4, 20, ch, stream)
+        fr = torch.empty((16, 3, eng.out_height, eng.out_width), dtype=torch.float32, device="cuda")
+        eng.decode(tf, 4, 20, fr, stream)
+        D.tc3d_sync(stream)
+        mse = float(np.mean((ch.cpu().numpy().astype(np.float64) - truth) ** 2))
+        out[name]["chroma_psnr_db"] = 10.0 * np.log10(peak * peak / mse)
+        frames[form] = fr.cpu().numpy()
+    for form in (D.TC_3XTF32, D.TC_BF16X3):
+        d = np.abs(frames[form].astype(np.float64) - frames[-1])
+        out[forms[form]]["planes_vs_plain_ps"] = {
+            pl: {"max": float(d[:, i].max()), "rms": float(np.sqrt(np.mean(d[:, i] ** 2)))}
+            for i, pl in enumerate(("Y", "Cb", "Cr"))}
+    # spectra against FP64 on a sample of tiles of 4 Z tiles mid-capture
+    tx0, ty0, ntx, nty = T.tile_grid(g)
+    ntiles = ntx * nty
+    fields_np = dfields.cpu().numpy().view(np.uint16).reshape(nfields, g.field_height, g.field_width)
+    m0 = min(100, max(0, nframes // 2))
+    tiles = np.random.default_rng(a.seed).choice(ntiles, 300, replace=False)
+    spec = torch.empty((4, ntiles, 8, 5, 32), dtype=torch.complex64, device="cuda")
+    refs = [T.fp64_spectra(fields_np, m0 + i, tiles, g) for i in range(4)]
+    for form in (D.TC_3XTF32, D.TC_BF16X3):
+        D.tc3d_spectra(dfields, m0, m0 + 4, spec, form, stream=stream)
+        D.tc3d_sync(stream)
+        S = spec.cpu().numpy()
+        rs = [T.report(S[i][tiles], refs[i], 0.4) for i in range(4)]
+        out[forms[form]]["spectra_vs_fp64"] = {
+            "rms_rel_err": max(r["rms_rel_err"] for r in rs), "max_rel_err": max(r["max_rel_err"] for r in rs),
+            "flip_fraction": sum(r["flips"] for r in rs) / sum(r["bins"] for r in rs),
+            "bins": sum(r["bins"] for r in rs)}
+    out["learned_nn"] = "not built: the per-bin learned chroma mask of the brief has no kernels in this library"
+    out["note"] = ("plain: FP32 CUDA cores with every threshold decision taken exactly (the value above); "
+                   "tc_*: tcgen05 split-precision DFT stages (3 MMAs per contraction, FP32 accumulation in "
+                   "tensor memory) with FP32 decisions on their spectra; chroma PSNR over fields 8-39 of the "
+                   "same seeded content against the encoder's chroma, peak = white - black")
+    return out
+
+
 def main():
     a = parse()
     if a.impl == "reference":
@@ -515,6 +599,8 @@ def main():
             "value": nfields * a.steps / (e0.elapsed_time(e1) / 1000.0), "unit": "fields/s",
             "path": "chdg_decode_host: pinned host fields -> pinned host frames, one call per step"}
 
+    if rank == 0 and not a.no_forms and a.format == "p16":
+        line["forms"] = forms_report(a, dfields, nfields, value, stream)
     if rank == 0 and not a.no_cpu:
         line["cpu_baseline"] = cpu_baseline(a, fields_np)
     if rank == 0:
