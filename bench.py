@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the tensor-core forms and chroma PSNR report")
+    ap.add_argument("--form", default="plain", choices=["plain", "tc_3xtf32", "tc_bf16x3"],
+                    help="transform form of the timed decode (the tensor-core forms for profiling them)")
     ap.add_argument("--workload", default="stream", choices=["stream", "batched"],
                     help="stream: the 500-field 3D capture (the headline line); batched: 48 captures of "
                          "6-300 fields, 40%% 2D / 60%% 3D, one threshold each, through chdg_batch_*")
@@ -485,6 +487,8 @@ def main():
     nframes = nfields // 2
     fmt = D.FMT_P16 if a.format == "p16" else D.FMT_PS
     eng = D.Engine(D.default_geometry(), D.default_config(kind=D.KIND_TRANSFORM_3D, fmt=fmt))
+    tc_form = {"plain": -1, "tc_3xtf32": D.TC_3XTF32, "tc_bf16x3": D.TC_BF16X3}[a.form]
+    eng.set_tc_form(tc_form)
     lib = D.lib()
     dfields = torch.from_numpy(fields_np.reshape(nfields, -1).view(np.int16)).cuda()
     out_dtype = torch.int16 if fmt == D.FMT_P16 else torch.float32
@@ -521,7 +525,7 @@ def main():
     # roofline of the dominant kernel (the transform): launches per step
     # one engine batch = 4 launches: the transform walk, the resolve pass,
     # the exact re-walk of the items it lists, the demodulator
-    launches_transform = nl.value // 4
+    launches_transform = nl.value // 4 if tc_form < 0 else a.steps * ((nframes + 255) // 256)
     per_launch_ms = mt.value / max(1, launches_transform)
     fields_per_launch = nfields * a.steps / max(1, launches_transform)
     bytes_per_field = FIELD_BYTES_IN + OUT_BYTES[a.format]
@@ -537,6 +541,8 @@ def main():
     # (a smaller capture of the same kernel; traffic grows with the fields)
     traffic = None
     try:
+        if tc_form >= 0:
+            raise FileNotFoundError("the committed traffic figure is the plain form's")
         with open(os.path.join(ROOT, "profiles", "tpal3d_traffic_200fields.md")) as fp:
             for ln in fp:
                 if ln.startswith("traffic_bytes_per_field:"):
@@ -551,11 +557,12 @@ def main():
         "metric": METRIC, "value": value, "unit": "fields/s", "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": ms_max / a.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
-        "config": {"workload": workload_desc(a), "fields_per_step": nfields, "frames_per_step": nframes,
+        "config": {"workload": workload_desc(a), "form": a.form, "fields_per_step": nfields, "frames_per_step": nframes,
                    "format": "yuv444" + a.format, "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
                    "l2": f"inputs {nfields * FIELD_BYTES_IN / 1e6:.0f} MB > 129 MB L2 (no flush)"},
         "roofline": {
-            "bound": "hbm", "kernel": "tpal3d transform stage (walk, resolve, exact re-walk)", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+            "bound": "hbm", "kernel": "tpal3d transform stage (walk, resolve, exact re-walk)" if tc_form < 0
+            else "tensor-core transform stage (tc3_xy, tc3_zd, tc3_yx)", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
             "frac": achieved_gbs / hbm_peak, "traffic": traffic,
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback 6.8 TB/s",
             "algorithmic_bytes_per_field": bytes_per_field,
@@ -599,7 +606,7 @@ def main():
             "value": nfields * a.steps / (e0.elapsed_time(e1) / 1000.0), "unit": "fields/s",
             "path": "chdg_decode_host: pinned host fields -> pinned host frames, one call per step"}
 
-    if rank == 0 and not a.no_forms and a.format == "p16":
+    if rank == 0 and not a.no_forms and a.format == "p16" and tc_form < 0:
         line["forms"] = forms_report(a, dfields, nfields, value, stream)
     if rank == 0 and not a.no_cpu:
         line["cpu_baseline"] = cpu_baseline(a, fields_np)

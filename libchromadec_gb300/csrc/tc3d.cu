@@ -200,24 +200,39 @@ __host__ __device__ __forceinline__ uint32_t elem_off(int r, int k, int eb, int 
 template <int KIND>
 struct Split;
 
+// put: one element; put_chunk: the ce elements of one 16-byte core-matrix
+// row (offset 16-byte aligned) with one vector store per split.
 template <>
 struct Split<0> {   // TF32: hi = a rounded to 10 stored mantissa bits (to nearest, ties away), lo = the rest rounded
-    static constexpr int eb = 4;
-    __device__ __forceinline__ static void put(uint8_t *hi, uint8_t *lo, uint32_t off, float a)
+    static constexpr int eb = 4, ce = 4;
+    __device__ __forceinline__ static void split(float a, uint32_t &h, uint32_t &l)
     {
-        uint32_t h, l;
         asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(a));
         h &= 0xFFFFE000u;
         const float rest = a - __uint_as_float(h);
         asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(rest));
+        l &= 0xFFFFE000u;
+    }
+    __device__ __forceinline__ static void put(uint8_t *hi, uint8_t *lo, uint32_t off, float a)
+    {
+        uint32_t h, l;
+        split(a, h, l);
         *reinterpret_cast<uint32_t *>(hi + off) = h;
-        *reinterpret_cast<uint32_t *>(lo + off) = l & 0xFFFFE000u;
+        *reinterpret_cast<uint32_t *>(lo + off) = l;
+    }
+    __device__ __forceinline__ static void put_chunk(uint8_t *hi, uint8_t *lo, uint32_t off, const float *v)
+    {
+        uint32_t h[4], l[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) split(v[j], h[j], l[j]);
+        *reinterpret_cast<uint4 *>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<uint4 *>(lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
     }
 };
 
 template <>
 struct Split<1> {   // BF16: hi = bf16(a), lo = bf16(a - hi), both round to nearest even
-    static constexpr int eb = 2;
+    static constexpr int eb = 2, ce = 8;
     __device__ __forceinline__ static void put(uint8_t *hi, uint8_t *lo, uint32_t off, float a)
     {
         const __nv_bfloat16 h = __float2bfloat16_rn(a);
@@ -225,7 +240,31 @@ struct Split<1> {   // BF16: hi = bf16(a), lo = bf16(a - hi), both round to near
         *reinterpret_cast<__nv_bfloat16 *>(hi + off) = h;
         *reinterpret_cast<__nv_bfloat16 *>(lo + off) = l;
     }
+    __device__ __forceinline__ static void put_chunk(uint8_t *hi, uint8_t *lo, uint32_t off, const float *v)
+    {
+        uint32_t h[4], l[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const __nv_bfloat162 hh = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+            const float2 hf = __bfloat1622float2(hh);
+            const __nv_bfloat162 ll = __floats2bfloat162_rn(v[2 * j] - hf.x, v[2 * j + 1] - hf.y);
+            h[j] = *reinterpret_cast<const uint32_t *>(&hh);
+            l[j] = *reinterpret_cast<const uint32_t *>(&ll);
+        }
+        *reinterpret_cast<uint4 *>(hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<uint4 *>(lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
+    }
 };
+
+// All n elements of row r (n a multiple of the chunk) with vector stores.
+template <int KIND>
+__device__ __forceinline__ void put_row(uint8_t *hi, uint8_t *lo, int r, int row_bytes, const float *v, int n)
+{
+    using SP = Split<KIND>;
+#pragma unroll
+    for (int c = 0; c < n / SP::ce; c++)
+        SP::put_chunk(hi, lo, elem_off(r, c * SP::ce, SP::eb, row_bytes), v + c * SP::ce);
+}
 
 // Shared-memory plan of the XY kernel (bytes), every region 1024-aligned.
 template <int KIND>
@@ -235,8 +274,11 @@ struct XYLayout {
     static constexpr int rby = 32 * eb;   // Y rows: 16 re + 16 im
     static constexpr int ax_blk = 128 * rbx;
     static constexpr int ax = 0;                              // [split][3 blocks][128 rows]
-    static constexpr int ay = ax + 2 * 3 * ax_blk;            // [split][128 rows]
-    static constexpr int bx = ay + 2 * 128 * rby;             // [split][16 rows]
+    // the Y operand reuses the X operand's space: it is written once the X
+    // MMAs are complete, and the next X operand once the Y MMAs are
+    static constexpr int ay = ax;                             // [split][128 rows]
+    static_assert(2 * 128 * rby <= 2 * 3 * ax_blk, "Y operand fits the X operand's space");
+    static constexpr int bx = ax + 2 * 3 * ax_blk;            // [split][16 rows]
     static constexpr int by = bx + ((2 * 16 * rbx + 1023) & ~1023);   // [y0][split][64 rows]
     static constexpr int bar = by + 2 * 2 * 64 * rby;
     static constexpr int bytes = bar + 64;
@@ -288,10 +330,10 @@ __global__ void __launch_bounds__(kThreads) tc3_xy_kernel(Params P)
     uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + LY::bar + 8);
     const int t = threadIdx.x, warp = t >> 5;
 
-    // coefficient images (both row parities), zeroed Y operand (rows 120..127 stay zero)
+    // coefficient images (both row parities); the Y operand's rows 120..127
+    // hold X-operand data, and their outputs are never stored
     copy_image(smem + LY::bx, P.bx, 2 * 16 * LY::rbx);
     copy_image(smem + LY::by, P.by, 2 * 2 * 64 * LY::rby);
-    for (int o = t * 16; o < 2 * 128 * LY::rby; o += kThreads * 16) *reinterpret_cast<uint4 *>(smem + LY::ay + o) = uint4{0, 0, 0, 0};
     if (t == 0) bar_init(bar);
     if (warp == 0) tmem_alloc(tslot, 128);   // X accumulators: columns 0..47; Y: 64..127
     fence_async_smem();
@@ -336,9 +378,7 @@ __global__ void __launch_bounds__(kThreads) tc3_xy_kernel(Params P)
                 }
             }
             const int blk = R >> 7, r = R & 127;
-#pragma unroll
-            for (int x = 0; x < 16; x++)
-                SP::put(ax_hi + blk * LY::ax_blk, ax_lo + blk * LY::ax_blk, elem_off(r, x, eb, LY::rbx), a[x]);
+            put_row<KIND>(ax_hi + blk * LY::ax_blk, ax_lo + blk * LY::ax_blk, r, LY::rbx, a, 16);
         }
         fence_async_smem();
         __syncthreads();
@@ -523,8 +563,10 @@ struct ZDLayout {
     static constexpr int rb = 16 * eb;
     static constexpr int blk = 128 * rb;
     static constexpr int af = 0;                     // [split][2 blocks][128 rows]
-    static constexpr int ai = af + 4 * blk;          // [split][2 blocks][128 rows]
-    static constexpr int bf = ai + 4 * blk;          // [split][16 rows]
+    // the inverse operand reuses the forward one's space (written once the
+    // forward MMAs are complete; rows 160..255 stay zero in both)
+    static constexpr int ai = af;
+    static constexpr int bf = af + 4 * blk;          // [split][16 rows]
     static constexpr int bi = bf + 2 * 16 * rb;      // [split][16 rows]
     static constexpr int mag = bi + 2 * 16 * rb;     // [160][8] floats
     static constexpr int bar = mag + kQ * 8 * 4;
@@ -546,7 +588,7 @@ __global__ void __launch_bounds__(kThreads) tc3_zd_kernel(Params P)
 
     copy_image(smem + LY::bf, P.bz, 2 * 16 * LY::rb);
     copy_image(smem + LY::bi, P.bzi, 2 * 16 * LY::rb);
-    for (int o = t * 16; o < 8 * LY::blk; o += kThreads * 16) *reinterpret_cast<uint4 *>(smem + LY::af + o) = uint4{0, 0, 0, 0};
+    for (int o = t * 16; o < 4 * LY::blk; o += kThreads * 16) *reinterpret_cast<uint4 *>(smem + LY::af + o) = uint4{0, 0, 0, 0};
     if (t == 0) bar_init(bar);
     if (warp == 0) tmem_alloc(tslot, 64);   // forward: columns 0..31, inverse: 32..63
     fence_async_smem();
@@ -568,12 +610,14 @@ __global__ void __launch_bounds__(kThreads) tc3_zd_kernel(Params P)
         for (int h = 0; h < 2; h++) {
             const int q = 128 * h + t;
             if (q < kQ) {
+                float row[16];
 #pragma unroll
                 for (int z = 0; z < 8; z++) {
                     const float2 v = P.sf[((long long)(2 * mi + z) * P.ntiles + tile) * kQ + q];
-                    SP::put(af_hi + h * LY::blk, af_lo + h * LY::blk, elem_off(t, z, eb, LY::rb), v.x);
-                    SP::put(af_hi + h * LY::blk, af_lo + h * LY::blk, elem_off(t, 8 + z, eb, LY::rb), v.y);
+                    row[z] = v.x;
+                    row[8 + z] = v.y;
                 }
+                put_row<KIND>(af_hi + h * LY::blk, af_lo + h * LY::blk, t, LY::rb, row, 16);
             }
         }
         fence_async_smem();
@@ -614,16 +658,16 @@ __global__ void __launch_bounds__(kThreads) tc3_zd_kernel(Params P)
             if (q < kQ) {
                 const int kxi = q >> 5, ky = q & 31, kyr = (40 - ky) & 31;
                 const int qm = (4 - kxi) * 32 + kyr;
+                float row[16];
 #pragma unroll
                 for (int kz = 0; kz < 8; kz++) {
                     const int kzr = (10 - kz) & 7;
                     const bool keep = keep_pair(mag[q * 8 + kz], mag[qm * 8 + kzr], P.t2f) ||
                                       (kxi == 2 && kz == kzr && ky == kyr);
-                    SP::put(ai_hi + h * LY::blk, ai_lo + h * LY::blk, elem_off(t, kz, eb, LY::rb),
-                            keep ? v[h][2 * kz] : 0.f);
-                    SP::put(ai_hi + h * LY::blk, ai_lo + h * LY::blk, elem_off(t, 8 + kz, eb, LY::rb),
-                            keep ? v[h][2 * kz + 1] : 0.f);
+                    row[kz] = keep ? v[h][2 * kz] : 0.f;
+                    row[8 + kz] = keep ? v[h][2 * kz + 1] : 0.f;
                 }
+                put_row<KIND>(ai_hi + h * LY::blk, ai_lo + h * LY::blk, t, LY::rb, row, 16);
             }
         }
         fence_async_smem();
@@ -683,9 +727,12 @@ struct YXLayout {
     static constexpr int rbx = 16 * eb;     // X inverse rows: 5 kx re/im (+6 zero)
     static constexpr int ax_blk = 128 * rbx;
     static constexpr int ay = 0;                        // [split][128 rows]
+    // the X operand reuses the Y operand's space (written once the Y MMAs are
+    // complete; its pad columns 10..15 are zeroed with every write)
+    static constexpr int ax = ay;                       // [split][3 blocks][128 rows]
+    static_assert(2 * 3 * ax_blk <= 2 * 128 * rby, "X operand fits the Y operand's space");
     static constexpr int by = ay + 2 * 128 * rby;       // [y0][split][32 rows]
-    static constexpr int ax = by + 2 * 2 * 32 * rby;    // [split][3 blocks][128 rows]
-    static constexpr int bx = ax + 2 * 3 * ax_blk;      // [split][16 rows]
+    static constexpr int bx = by + 2 * 2 * 32 * rby;    // [split][16 rows]
     static constexpr int bar = bx + ((2 * 16 * rbx + 1023) & ~1023);
     static constexpr int bytes = bar + 64;
     static constexpr int ksy = rby / 32;
@@ -706,7 +753,6 @@ __global__ void __launch_bounds__(kThreads) tc3_yx_kernel(Params P)
     copy_image(smem + LY::by, P.byi, 2 * 2 * 32 * LY::rby);
     copy_image(smem + LY::bx, P.bxi, 2 * 16 * LY::rbx);
     for (int o = t * 16; o < 2 * 128 * LY::rby; o += kThreads * 16) *reinterpret_cast<uint4 *>(smem + LY::ay + o) = uint4{0, 0, 0, 0};
-    for (int o = t * 16; o < 2 * 3 * LY::ax_blk; o += kThreads * 16) *reinterpret_cast<uint4 *>(smem + LY::ax + o) = uint4{0, 0, 0, 0};
     if (t == 0) bar_init(bar);
     if (warp == 0) tmem_alloc(tslot, 128);   // Y inverse: columns 0..31, X inverse: 32..79
     fence_async_smem();
@@ -733,13 +779,20 @@ __global__ void __launch_bounds__(kThreads) tc3_yx_kernel(Params P)
             const int ft = t / 5, kxi = t % 5;
             const int tile = tile0 + ft;
             if (tile < P.ntiles) {
-                const float2 *ra = P.rz + (((long long)(k + 2) * P.ntiles + tile) * 4 + j) * kQ + kxi * 32;
-                const float2 *rb = P.rz + (((long long)k * P.ntiles + tile) * 4 + 2 + j) * kQ + kxi * 32;
-                for (int ky = 0; ky < 32; ky++) {
-                    const float2 a = ra[ky], b = rb[ky];
-                    SP::put(ay_hi, ay_lo, elem_off(t, ky, eb, LY::rby), a.x + b.x);
-                    SP::put(ay_hi, ay_lo, elem_off(t, 32 + ky, eb, LY::rby), a.y + b.y);
+                const float4 *ra = reinterpret_cast<const float4 *>(
+                    P.rz + (((long long)(k + 2) * P.ntiles + tile) * 4 + j) * kQ + kxi * 32);
+                const float4 *rb = reinterpret_cast<const float4 *>(
+                    P.rz + (((long long)k * P.ntiles + tile) * 4 + 2 + j) * kQ + kxi * 32);
+                float row[64];
+#pragma unroll
+                for (int c = 0; c < 16; c++) {   // two ky per float4
+                    const float4 a = ra[c], b = rb[c];
+                    row[2 * c] = a.x + b.x;
+                    row[32 + 2 * c] = a.y + b.y;
+                    row[2 * c + 1] = a.z + b.z;
+                    row[33 + 2 * c] = a.w + b.w;
                 }
+                put_row<KIND>(ay_hi, ay_lo, t, LY::rby, row, 64);
             }
         }
         fence_async_smem();
@@ -774,6 +827,9 @@ __global__ void __launch_bounds__(kThreads) tc3_yx_kernel(Params P)
                     uint8_t *h = ax_hi + (R >> 7) * LY::ax_blk, *l = ax_lo + (R >> 7) * LY::ax_blk;
                     SP::put(h, l, elem_off(R & 127, 2 * kxi, eb, LY::rbx), re);
                     SP::put(h, l, elem_off(R & 127, 2 * kxi + 1, eb, LY::rbx), im);
+                    if (kxi == 0)   // pad columns 10..15 (this space held the Y operand)
+#pragma unroll
+                        for (int c = 10; c < 16; c++) SP::put(h, l, elem_off(R & 127, c, eb, LY::rbx), 0.f);
                 }
             }
         }
@@ -1104,8 +1160,8 @@ static void launch(K kernel, long long work, int per_sm, int sms, int smem, cuda
 static void launch_xy(int variant, const Params &P, int sms, cudaStream_t s)
 {
     const long long units = (long long)P.nf * ((P.ntiles + kTilesPerUnit - 1) / kTilesPerUnit);
-    if (variant == 0) launch(tc3_xy_kernel<0>, units, 1, sms, XYLayout<0>::bytes, s, P);
-    else launch(tc3_xy_kernel<1>, units, 3, sms, XYLayout<1>::bytes, s, P);
+    if (variant == 0) launch(tc3_xy_kernel<0>, units, 2, sms, XYLayout<0>::bytes, s, P);
+    else launch(tc3_xy_kernel<1>, units, 4, sms, XYLayout<1>::bytes, s, P);
 }
 
 }  // namespace tc
@@ -1160,12 +1216,13 @@ int tc3_transform(const T3Params &T, int field_height, int variant, cudaStream_t
         launch_xy(variant, P, sms, s);
         const long long zd_units = (long long)P.nm * P.ntiles;
         const long long yx_units = (long long)P.nout * ((P.ntiles + kTilesPerUnit - 1) / kTilesPerUnit);
+        // CTAs per SM: shared memory and tensor memory (512 columns) allow
         if (variant == 0) {
-            launch(tc3_zd_kernel<0>, zd_units, 3, sms, ZDLayout<0>::bytes, s, P);
-            launch(tc3_yx_kernel<0>, yx_units, 1, sms, YXLayout<0>::bytes, s, P);
+            launch(tc3_zd_kernel<0>, zd_units, 5, sms, ZDLayout<0>::bytes, s, P);
+            launch(tc3_yx_kernel<0>, yx_units, 2, sms, YXLayout<0>::bytes, s, P);
         } else {
-            launch(tc3_zd_kernel<1>, zd_units, 5, sms, ZDLayout<1>::bytes, s, P);
-            launch(tc3_yx_kernel<1>, yx_units, 3, sms, YXLayout<1>::bytes, s, P);
+            launch(tc3_zd_kernel<1>, zd_units, 8, sms, ZDLayout<1>::bytes, s, P);
+            launch(tc3_yx_kernel<1>, yx_units, 4, sms, YXLayout<1>::bytes, s, P);
         }
     }
     const cudaError_t e = cudaGetLastError();
