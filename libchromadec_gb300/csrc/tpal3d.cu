@@ -251,25 +251,21 @@ __device__ __forceinline__ df df_from_fixed60(long long hi_acc, long long lo_acc
 __device__ __forceinline__ void x_row_pair(const uint16_t *field, long long base, int black, int kx, dfc &xa,
                                            dfc &xb)
 {
-    long long ar_h = 0, ar_l = 0, ai_h = 0, ai_l = 0, br_h = 0, br_l = 0, bi_h = 0, bi_l = 0;
+    // even and odd samples summed apart: column kx is even + odd, column
+    // 8 - kx ((-1)^x times the conjugate) is the conjugate of even - odd --
+    // the same integers as summing each column's products directly
+    long long e[4] = {0, 0, 0, 0}, o[4] = {0, 0, 0, 0};   // re.hi, re.lo, im.hi, im.lo
 #pragma unroll
     for (int x = 0; x < 16; x++) {
         const long long idx = base + x < 0 ? 0 : base + x;   // never before the field start
-        const long long a = (long long)((int)__ldg(field + idx) - black);
+        const int a = (int)__ldg(field + idx) - black;
         const int *c = c3_qx[kx - 2][x];
-        ar_h += a * c[0];
-        ar_l += a * c[1];
-        ai_h += a * c[2];
-        ai_l += a * c[3];
-        // column 8 - kx: (-1)^x times the conjugate
-        const long long sa = (x & 1) ? -a : a;
-        br_h += sa * c[0];
-        br_l += sa * c[1];
-        bi_h -= sa * c[2];
-        bi_l -= sa * c[3];
+        long long *acc = (x & 1) ? o : e;
+#pragma unroll
+        for (int k = 0; k < 4; k++) acc[k] += (long long)a * c[k];
     }
-    xa = {df_from_fixed60(ar_h, ar_l), df_from_fixed60(ai_h, ai_l)};
-    xb = {df_from_fixed60(br_h, br_l), df_from_fixed60(bi_h, bi_l)};
+    xa = {df_from_fixed60(e[0] + o[0], e[1] + o[1]), df_from_fixed60(e[2] + o[2], e[3] + o[3])};
+    xb = {df_from_fixed60(e[0] - o[0], e[1] - o[1]), df_from_fixed60(o[2] - e[2], o[3] - e[3])};
 }
 
 // ---------------------------------------------------------------------------
@@ -696,6 +692,18 @@ __global__ void __launch_bounds__(32 * kWarps3) tp3_resolve_kernel(T3Params P)
     const unsigned n = min(P.counters[0], P.unc_cap);
     unsigned n_exact = 0, n_flip = 0;
     const int z = lane >> 2, part = lane & 3;
+    // The double-float twiddles and windows are read with 8 distinct indices
+    // per warp (one per field row set): from shared memory, not the constant
+    // cache, which serialises distinct addresses. Same values.
+    __shared__ float s_tw[32][4], s_wy[32][2], s_wz[8][2];
+    for (int i = threadIdx.x; i < 128; i += blockDim.x) s_tw[i >> 2][i & 3] = c3_dftw32[i >> 2][i & 3];
+    for (int i = threadIdx.x; i < 64; i += blockDim.x) s_wy[i >> 1][i & 1] = c3_dfwy[i >> 1][i & 1];
+    for (int i = threadIdx.x; i < 16; i += blockDim.x) s_wz[i >> 1][i & 1] = c3_dfwz[i >> 1][i & 1];
+    __syncthreads();
+    auto tw = [&](int r) -> dfc {
+        r &= 31;
+        return {{s_tw[r][0], s_tw[r][1]}, {s_tw[r][2], s_tw[r][3]}};
+    };
     for (unsigned rec = blockIdx.x * kWarps3 + warp; rec < n; rec += gridDim.x * kWarps3) {
         const UncRecord &R = P.unc_rec[rec];
         const int item = R.item, tile = R.tile, m = R.m, g = R.g;
@@ -717,7 +725,7 @@ __global__ void __launch_bounds__(32 * kWarps3) tp3_resolve_kernel(T3Params P)
             const long long base = (long long)(L >> 1) * P.fw + tileX;   // within the field
             x_row_pair(fp, base, P.black, kxa, xa[r4], xb[r4]);
         }
-        const df wz = {c3_dfwz[z][0], c3_dfwz[z][1]};
+        const df wz = {s_wz[z][0], s_wz[z][1]};
         bool flipped = false;
         unsigned any = __ballot_sync(0xffffffffu, unc != 0);
         while (any) {
@@ -731,8 +739,8 @@ __global__ void __launch_bounds__(32 * kWarps3) tp3_resolve_kernel(T3Params P)
 #pragma unroll
             for (int r4 = 0; r4 < 4; r4++) {
                 const int y = y0 + 2 * (part * 4 + r4);
-                const df wy = {c3_dfwy[y][0], c3_dfwy[y][1]};
-                dfc cb = dfc_tw32(kyb * y), cr = dfc_tw32(kybr * y);
+                const df wy = {s_wy[y][0], s_wy[y][1]};
+                dfc cb = tw(kyb * y), cr = tw(kybr * y);
                 cb.re = df_mul(cb.re, wy); cb.im = df_mul(cb.im, wy);
                 cr.re = df_mul(cr.re, wy); cr.im = df_mul(cr.im, wy);
                 accb = dfc_add(accb, dfc_mul(xa[r4], cb));
@@ -743,7 +751,7 @@ __global__ void __launch_bounds__(32 * kWarps3) tp3_resolve_kernel(T3Params P)
             accr = dfc_add(accr, dfc_shfl_xor(accr, 1));
             accr = dfc_add(accr, dfc_shfl_xor(accr, 2));
             {
-                dfc tb = dfc_tw32(4 * ((kz * z) & 7)), tr = dfc_tw32(4 * ((kzr * z) & 7));
+                dfc tb = tw(4 * ((kz * z) & 7)), tr = tw(4 * ((kzr * z) & 7));
                 tb.re = df_mul(tb.re, wz); tb.im = df_mul(tb.im, wz);
                 tr.re = df_mul(tr.re, wz); tr.im = df_mul(tr.im, wz);
                 accb = dfc_mul(accb, tb);
