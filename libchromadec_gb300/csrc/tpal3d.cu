@@ -692,18 +692,27 @@ __global__ void __launch_bounds__(32 * kWarps3) tp3_resolve_kernel(T3Params P)
     const unsigned n = min(P.counters[0], P.unc_cap);
     unsigned n_exact = 0, n_flip = 0;
     const int z = lane >> 2, part = lane & 3;
-    // The double-float twiddles and windows are read with 8 distinct indices
-    // per warp (one per field row set): from shared memory, not the constant
-    // cache, which serialises distinct addresses. Same values.
-    __shared__ float s_tw[32][4], s_wy[32][2], s_wz[8][2];
-    for (int i = threadIdx.x; i < 128; i += blockDim.x) s_tw[i >> 2][i & 3] = c3_dftw32[i >> 2][i & 3];
-    for (int i = threadIdx.x; i < 64; i += blockDim.x) s_wy[i >> 1][i & 1] = c3_dfwy[i >> 1][i & 1];
-    for (int i = threadIdx.x; i < 16; i += blockDim.x) s_wz[i >> 1][i & 1] = c3_dfwz[i >> 1][i & 1];
+    // Window-scaled double-float twiddles, w_y(y) exp(-2 pi i r/32) for every
+    // (y, r) and w_z(z) exp(-2 pi i 4 r/32) for every (z, r), formed once per
+    // block with the same df_mul the products would use (the same values),
+    // read from shared memory: a warp reads them with 8 distinct indices,
+    // which the constant cache would serialise. Rows padded by one entry.
+    __shared__ float4 s_yw[32][33], s_zw[8][8];
+    for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) {
+        const int y = i >> 5, r = i & 31;
+        const df w = {c3_dfwy[y][0], c3_dfwy[y][1]};
+        const df re = df_mul({c3_dftw32[r][0], c3_dftw32[r][1]}, w), im = df_mul({c3_dftw32[r][2], c3_dftw32[r][3]}, w);
+        s_yw[y][r] = make_float4(re.hi, re.lo, im.hi, im.lo);
+    }
+    for (int i = threadIdx.x; i < 8 * 8; i += blockDim.x) {
+        const int zz = i >> 3, r = i & 7;
+        const df w = {c3_dfwz[zz][0], c3_dfwz[zz][1]};
+        const df re = df_mul({c3_dftw32[4 * r][0], c3_dftw32[4 * r][1]}, w);
+        const df im = df_mul({c3_dftw32[4 * r][2], c3_dftw32[4 * r][3]}, w);
+        s_zw[zz][r] = make_float4(re.hi, re.lo, im.hi, im.lo);
+    }
     __syncthreads();
-    auto tw = [&](int r) -> dfc {
-        r &= 31;
-        return {{s_tw[r][0], s_tw[r][1]}, {s_tw[r][2], s_tw[r][3]}};
-    };
+    auto as_dfc = [](float4 v) -> dfc { return {{v.x, v.y}, {v.z, v.w}}; };
     for (unsigned rec = blockIdx.x * kWarps3 + warp; rec < n; rec += gridDim.x * kWarps3) {
         const UncRecord &R = P.unc_rec[rec];
         const int item = R.item, tile = R.tile, m = R.m, g = R.g;
@@ -725,7 +734,6 @@ __global__ void __launch_bounds__(32 * kWarps3) tp3_resolve_kernel(T3Params P)
             const long long base = (long long)(L >> 1) * P.fw + tileX;   // within the field
             x_row_pair(fp, base, P.black, kxa, xa[r4], xb[r4]);
         }
-        const df wz = {s_wz[z][0], s_wz[z][1]};
         bool flipped = false;
         unsigned any = __ballot_sync(0xffffffffu, unc != 0);
         while (any) {
@@ -739,10 +747,7 @@ __global__ void __launch_bounds__(32 * kWarps3) tp3_resolve_kernel(T3Params P)
 #pragma unroll
             for (int r4 = 0; r4 < 4; r4++) {
                 const int y = y0 + 2 * (part * 4 + r4);
-                const df wy = {s_wy[y][0], s_wy[y][1]};
-                dfc cb = tw(kyb * y), cr = tw(kybr * y);
-                cb.re = df_mul(cb.re, wy); cb.im = df_mul(cb.im, wy);
-                cr.re = df_mul(cr.re, wy); cr.im = df_mul(cr.im, wy);
+                const dfc cb = as_dfc(s_yw[y][(kyb * y) & 31]), cr = as_dfc(s_yw[y][(kybr * y) & 31]);
                 accb = dfc_add(accb, dfc_mul(xa[r4], cb));
                 accr = dfc_add(accr, dfc_mul(xb[r4], cr));
             }
@@ -751,9 +756,7 @@ __global__ void __launch_bounds__(32 * kWarps3) tp3_resolve_kernel(T3Params P)
             accr = dfc_add(accr, dfc_shfl_xor(accr, 1));
             accr = dfc_add(accr, dfc_shfl_xor(accr, 2));
             {
-                dfc tb = tw(4 * ((kz * z) & 7)), tr = tw(4 * ((kzr * z) & 7));
-                tb.re = df_mul(tb.re, wz); tb.im = df_mul(tb.im, wz);
-                tr.re = df_mul(tr.re, wz); tr.im = df_mul(tr.im, wz);
+                const dfc tb = as_dfc(s_zw[z][(kz * z) & 7]), tr = as_dfc(s_zw[z][(kzr * z) & 7]);
                 accb = dfc_mul(accb, tb);
                 accr = dfc_mul(accr, tr);
             }
