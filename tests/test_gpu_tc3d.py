@@ -120,3 +120,25 @@ def test_tc_chroma_psnr_matches_plain(decoded):
     assert ps[-1] > 25.0
     for form in (D.TC_3XTF32, D.TC_BF16X3):
         assert abs(ps[form] - ps[-1]) < 0.05
+
+
+def test_tc_form_through_host_buffers(cuda):
+    """The tensor-core form through chdg_decode_host (double-buffered field
+    windows that start mid-capture) equals its device-resident decode."""
+    import ctypes as C
+    torch = cuda
+    cap = capture(NF, seed=17)
+    eng = D.Engine(D.default_geometry(), D.default_config(kind=8, fmt=D.FMT_P16))
+    eng.set_tc_form(D.TC_3XTF32)
+    nfr = NF // 2
+    dev_fields = torch.from_numpy(cap.fields.reshape(NF, -1).view(np.int16)).cuda()
+    dev_out = torch.empty((nfr, 3, eng.out_height, eng.out_width), dtype=torch.int16, device="cuda")
+    eng.decode(dev_fields, 0, nfr, dev_out)
+    host_fields = torch.from_numpy(cap.fields.reshape(NF, -1).view(np.int16)).pin_memory()
+    host_out = torch.empty((nfr, 3, eng.out_height, eng.out_width), dtype=torch.int16).pin_memory()
+    rc = D.lib().chdg_decode_host(eng._h, C.c_void_p(host_fields.data_ptr()), host_fields[0].numel(), NF, 0, nfr,
+                                  C.c_void_p(host_out.data_ptr()), None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    D.tc3d_sync()
+    assert np.array_equal(host_out.numpy(), dev_out.cpu().numpy())
