@@ -341,10 +341,29 @@ __global__ void __launch_bounds__(32 * kWarps2) tpal2d_kernel(T2Params P)
     if (fl >= fl_first && fl < fl_last) {
         float *dst = P.partial + (long long)cls * P.part_class_stride + (long long)o * P.part_field_stride +
                      (long long)(fl - P.fl_lo) * P.part_row_stride - P.avs;
+        // this lane's 16 samples [tileX + 16 h, +16): tileX - avs is a multiple
+        // of 16, so inside the active window they start on a 64-byte boundary
+        // whenever the planes' strides are multiples of 4 floats and their
+        // base is 16-byte aligned: four vector stores
+        const int x0 = tileX + 16 * h;
+        const bool vec = ((P.part_row_stride | P.part_field_stride | P.part_class_stride) & 3) == 0 &&
+                         (reinterpret_cast<uintptr_t>(P.partial) & 15) == 0 && x0 >= P.avs && x0 + 16 <= P.ave;
+        if (vec) {
+            float v[16];
 #pragma unroll
-        for (int x = 0; x < 16; x++) {
-            const int X = h ? tileX + 31 - x : tileX + x;
-            if (X >= P.avs && X < P.ave) dst[X] = h ? CS[x].x + CS[x].y : CS[x].x - CS[x].y;
+            for (int x = 0; x < 16; x++) {
+                if (h) v[15 - x] = CS[x].x + CS[x].y;
+                else v[x] = CS[x].x - CS[x].y;
+            }
+            float4 *d4 = reinterpret_cast<float4 *>(dst + x0);
+#pragma unroll
+            for (int q = 0; q < 4; q++) d4[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        } else {
+#pragma unroll
+            for (int x = 0; x < 16; x++) {
+                const int X = h ? tileX + 31 - x : tileX + x;
+                if (X >= P.avs && X < P.ave) dst[X] = h ? CS[x].x + CS[x].y : CS[x].x - CS[x].y;
+            }
         }
     }
     if (P.stats != nullptr) {

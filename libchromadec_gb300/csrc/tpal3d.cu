@@ -666,11 +666,29 @@ __global__ void __launch_bounds__(32 * kWarps3, 3) tpal3d_kernel(T3Params P)
             const int ofield = 2 * (m - P.frame_begin) + LC.j;
             float *dst = P.partial + (long long)cls * P.part_class_stride + (long long)ofield * P.part_field_stride +
                          (long long)((L >> 1) - P.fl_lo) * P.part_row_stride - P.avs;
+            // tileX - avs is a multiple of 8, so an interior tile's row starts
+            // on a 32-byte boundary whenever the planes' strides are multiples
+            // of 4 floats and their base is 16-byte aligned: four vector stores
+            const bool vec = ((P.part_row_stride | P.part_field_stride | P.part_class_stride) & 3) == 0 &&
+                             (reinterpret_cast<uintptr_t>(P.partial) & 15) == 0 && tileX >= P.avs &&
+                             tileX + 16 <= P.ave;
+            if (vec) {
+                float o[16];
 #pragma unroll
-            for (int x = 0; x < 8; x++) {
-                const int X0 = tileX + x, X1 = tileX + 15 - x;
-                if (X0 >= P.avs && X0 < P.ave) dst[X0] = CS[x].x - CS[x].y;
-                if (X1 >= P.avs && X1 < P.ave) dst[X1] = CS[x].x + CS[x].y;
+                for (int x = 0; x < 8; x++) {
+                    o[x] = CS[x].x - CS[x].y;
+                    o[15 - x] = CS[x].x + CS[x].y;
+                }
+                float4 *d4 = reinterpret_cast<float4 *>(dst + tileX);
+#pragma unroll
+                for (int q = 0; q < 4; q++) d4[q] = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
+            } else {
+#pragma unroll
+                for (int x = 0; x < 8; x++) {
+                    const int X0 = tileX + x, X1 = tileX + 15 - x;
+                    if (X0 >= P.avs && X0 < P.ave) dst[X0] = CS[x].x - CS[x].y;
+                    if (X1 >= P.avs && X1 < P.ave) dst[X1] = CS[x].x + CS[x].y;
+                }
             }
         }
     }
