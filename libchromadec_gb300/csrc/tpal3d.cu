@@ -166,11 +166,35 @@ __device__ __forceinline__ void forward_pair(const T3Params &P, int q, int tileX
         const uint16_t *row = fp + (long long)(L >> 1) * P.fw;
         int a[16];
         int sum = 0;
+        if (tileX >= 0 && (L >> 1) >= 1) {
+            // Rows start on any 2-byte boundary (odd line and field
+            // lengths): nine aligned 32-bit words cover the 16 samples, and a
+            // funnel shift by 0 or 16 bits lines each pair up -- 9 loads
+            // instead of 16, each warp load touching 32 rows either way. The
+            // words span at most the sample before and two after the 16
+            // (inside the field: the row is not its first, and a row past
+            // the last active line is never read).
+            const uintptr_t pa = reinterpret_cast<uintptr_t>(row + tileX);
+            const uint32_t *w = reinterpret_cast<const uint32_t *>(pa & ~(uintptr_t)3);
+            const unsigned sh = (unsigned)(pa & 2) * 8u;
+            uint32_t wd[9];
 #pragma unroll
-        for (int x = 0; x < 16; x++) {
-            const int xx = max(tileX + x, -(L >> 1) * P.fw);   // never before the field start
-            a[x] = (int)__ldg(row + xx) - P.black;
-            sum += a[x];
+            for (int k = 0; k < 9; k++) wd[k] = __ldg(w + k);
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                const uint32_t v = __funnelshift_r(wd[k], wd[k + 1], sh);
+                a[2 * k] = (int)(v & 0xFFFFu) - P.black;
+                a[2 * k + 1] = (int)(v >> 16) - P.black;
+            }
+#pragma unroll
+            for (int x = 0; x < 16; x++) sum += a[x];
+        } else {
+#pragma unroll
+            for (int x = 0; x < 16; x++) {
+                const int xx = max(tileX + x, -(L >> 1) * P.fw);   // never before the field start
+                a[x] = (int)__ldg(row + xx) - P.black;
+                sum += a[x];
+            }
         }
         const float m16 = (float)sum * 0.0625f;
 #pragma unroll
