@@ -279,14 +279,34 @@ __device__ __forceinline__ void x_row_pair(const uint16_t *field, long long base
     // 8 - kx ((-1)^x times the conjugate) is the conjugate of even - odd --
     // the same integers as summing each column's products directly
     long long e[4] = {0, 0, 0, 0}, o[4] = {0, 0, 0, 0};   // re.hi, re.lo, im.hi, im.lo
+    int a[16];
+    if (base >= 1) {
+        // nine aligned 32-bit words and a funnel shift, as in forward_pair
+        const uintptr_t pa = reinterpret_cast<uintptr_t>(field + base);
+        const uint32_t *w = reinterpret_cast<const uint32_t *>(pa & ~(uintptr_t)3);
+        const unsigned sh = (unsigned)(pa & 2) * 8u;
+        uint32_t wd[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) wd[k] = __ldg(w + k);
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const uint32_t v = __funnelshift_r(wd[k], wd[k + 1], sh);
+            a[2 * k] = (int)(v & 0xFFFFu) - black;
+            a[2 * k + 1] = (int)(v >> 16) - black;
+        }
+    } else {
+#pragma unroll
+        for (int x = 0; x < 16; x++) {
+            const long long idx = base + x < 0 ? 0 : base + x;   // never before the field start
+            a[x] = (int)__ldg(field + idx) - black;
+        }
+    }
 #pragma unroll
     for (int x = 0; x < 16; x++) {
-        const long long idx = base + x < 0 ? 0 : base + x;   // never before the field start
-        const int a = (int)__ldg(field + idx) - black;
         const int *c = c3_qx[kx - 2][x];
         long long *acc = (x & 1) ? o : e;
 #pragma unroll
-        for (int k = 0; k < 4; k++) acc[k] += (long long)a * c[k];
+        for (int k = 0; k < 4; k++) acc[k] += (long long)a[x] * c[k];
     }
     xa = {df_from_fixed60(e[0] + o[0], e[1] + o[1]), df_from_fixed60(e[2] + o[2], e[3] + o[3])};
     xb = {df_from_fixed60(e[0] - o[0], e[1] - o[1]), df_from_fixed60(o[2] - e[2], o[3] - e[3])};
