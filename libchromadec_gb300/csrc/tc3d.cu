@@ -256,13 +256,13 @@ struct Split<1> {   // BF16: hi = bf16(a), lo = bf16(a - hi), both round to near
     }
 };
 
-// All n elements of row r (n a multiple of the chunk) with vector stores.
-template <int KIND>
-__device__ __forceinline__ void put_row(uint8_t *hi, uint8_t *lo, int r, int row_bytes, const float *v, int n)
+// All N elements of row r (N a multiple of the chunk) with vector stores.
+template <int KIND, int N>
+__device__ __forceinline__ void put_row(uint8_t *hi, uint8_t *lo, int r, int row_bytes, const float (&v)[N])
 {
     using SP = Split<KIND>;
 #pragma unroll
-    for (int c = 0; c < n / SP::ce; c++)
+    for (int c = 0; c < N / SP::ce; c++)
         SP::put_chunk(hi, lo, elem_off(r, c * SP::ce, SP::eb, row_bytes), v + c * SP::ce);
 }
 
@@ -369,16 +369,34 @@ __global__ void __launch_bounds__(kThreads) tc3_xy_kernel(Params P)
                 const int L = tileY + y0 + 2 * i;
                 if (L >= P.fafl && L <= P.lafl) {
                     const long long last = (long long)P.fh * P.fw - 1;
+                    const long long first = (long long)(L >> 1) * P.fw + tileX;   // flat, as the reference reads
+                    if (first >= 1 && first + 18 <= last) {
+                        // nine aligned 32-bit words lined up by a funnel shift
+                        // (rows start on any 2-byte boundary)
+                        const uintptr_t pa = reinterpret_cast<uintptr_t>(fp + first);
+                        const uint32_t *w = reinterpret_cast<const uint32_t *>(pa & ~(uintptr_t)3);
+                        const unsigned sh = (unsigned)(pa & 2) * 8u;
+                        uint32_t wd[9];
 #pragma unroll
-                    for (int x = 0; x < 16; x++) {
-                        long long idx = (long long)(L >> 1) * P.fw + tileX + x;   // flat, as the reference reads
-                        idx = idx < 0 ? 0 : (idx > last ? last : idx);
-                        a[x] = (float)((int)__ldg(fp + idx) - P.black);
+                        for (int k = 0; k < 9; k++) wd[k] = __ldg(w + k);
+#pragma unroll
+                        for (int k = 0; k < 8; k++) {
+                            const uint32_t v = __funnelshift_r(wd[k], wd[k + 1], sh);
+                            a[2 * k] = (float)((int)(v & 0xFFFFu) - P.black);
+                            a[2 * k + 1] = (float)((int)(v >> 16) - P.black);
+                        }
+                    } else {
+#pragma unroll
+                        for (int x = 0; x < 16; x++) {
+                            long long idx = first + x;
+                            idx = idx < 0 ? 0 : (idx > last ? last : idx);
+                            a[x] = (float)((int)__ldg(fp + idx) - P.black);
+                        }
                     }
                 }
             }
             const int blk = R >> 7, r = R & 127;
-            put_row<KIND>(ax_hi + blk * LY::ax_blk, ax_lo + blk * LY::ax_blk, r, LY::rbx, a, 16);
+            put_row<KIND, 16>(ax_hi + blk * LY::ax_blk, ax_lo + blk * LY::ax_blk, r, LY::rbx, a);
         }
         fence_async_smem();
         __syncthreads();
@@ -617,7 +635,7 @@ __global__ void __launch_bounds__(kThreads) tc3_zd_kernel(Params P)
                     row[z] = v.x;
                     row[8 + z] = v.y;
                 }
-                put_row<KIND>(af_hi + h * LY::blk, af_lo + h * LY::blk, t, LY::rb, row, 16);
+                put_row<KIND, 16>(af_hi + h * LY::blk, af_lo + h * LY::blk, t, LY::rb, row);
             }
         }
         fence_async_smem();
@@ -667,7 +685,7 @@ __global__ void __launch_bounds__(kThreads) tc3_zd_kernel(Params P)
                     row[kz] = keep ? v[h][2 * kz] : 0.f;
                     row[8 + kz] = keep ? v[h][2 * kz + 1] : 0.f;
                 }
-                put_row<KIND>(ai_hi + h * LY::blk, ai_lo + h * LY::blk, t, LY::rb, row, 16);
+                put_row<KIND, 16>(ai_hi + h * LY::blk, ai_lo + h * LY::blk, t, LY::rb, row);
             }
         }
         fence_async_smem();
@@ -792,7 +810,7 @@ __global__ void __launch_bounds__(kThreads) tc3_yx_kernel(Params P)
                     row[2 * c + 1] = a.z + b.z;
                     row[33 + 2 * c] = a.w + b.w;
                 }
-                put_row<KIND>(ay_hi, ay_lo, t, LY::rby, row, 64);
+                put_row<KIND, 64>(ay_hi, ay_lo, t, LY::rby, row);
             }
         }
         fence_async_smem();
@@ -867,10 +885,21 @@ __global__ void __launch_bounds__(kThreads) tc3_yx_kernel(Params P)
                     float *dst = P.partial + (long long)cls * P.part_class_stride +
                                  (long long)(P.out_field0 + fo) * P.part_field_stride +
                                  (long long)((L >> 1) - P.fl_lo) * P.part_row_stride - P.avs;
+                    // interior tiles: tileX - avs is a multiple of 8, so with
+                    // 4-float strides and a 16-byte base the row is 32-byte aligned
+                    const bool vec = ((P.part_row_stride | P.part_field_stride | P.part_class_stride) & 3) == 0 &&
+                                     (reinterpret_cast<uintptr_t>(P.partial) & 15) == 0 && tileX >= P.avs &&
+                                     tileX + 16 <= P.ave;
+                    if (vec) {
+                        float4 *d4 = reinterpret_cast<float4 *>(dst + tileX);
 #pragma unroll
-                    for (int x = 0; x < 16; x++) {
-                        const int X = tileX + x;
-                        if (X >= P.avs && X < P.ave) dst[X] = o[x];
+                        for (int q = 0; q < 4; q++) d4[q] = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
+                    } else {
+#pragma unroll
+                        for (int x = 0; x < 16; x++) {
+                            const int X = tileX + x;
+                            if (X >= P.avs && X < P.ave) dst[X] = o[x];
+                        }
                     }
                 }
             }
