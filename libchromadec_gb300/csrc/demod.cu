@@ -165,6 +165,55 @@ __device__ __forceinline__ void pack_sample(const DemodParams &P, void *out, lon
     }
 }
 
+// The three outputs of one sample in the units yuv444p16 (the quantised
+// code, exact in FP32) or yuv444ps (E'Y, E'Cb, E'Cr) stores -- the
+// arithmetic of pack_sample's cases 0 and 1.
+__device__ __forceinline__ void yuv_values(const DemodParams &P, float Y, float U, float V, float &o0, float &o1,
+                                           float &o2)
+{
+    const float ey = (Y - (float)P.black) * P.ey_scale;
+    if (P.format == 0) {
+        o0 = (float)h273q(__fmaf_rn(219.0f * 256.0f, ey, 16.0f * 256.0f), P.y_lo, P.y_hi);
+        o1 = (float)h273q(__fmaf_rn(224.0f * 256.0f, U * P.ecb_scale, 128.0f * 256.0f), P.c_lo, P.c_hi);
+        o2 = (float)h273q(__fmaf_rn(224.0f * 256.0f, V * P.ecr_scale, 128.0f * 256.0f), P.c_lo, P.c_hi);
+    } else {
+        o0 = fminf(fmaxf(ey, P.y_lo), P.y_hi);
+        o1 = fminf(fmaxf(U * P.ecb_scale, P.c_lo), P.c_hi);
+        o2 = fminf(fmaxf(V * P.ecr_scale, P.c_lo), P.c_hi);
+    }
+}
+
+__device__ __forceinline__ void store_yuv(const DemodParams &P, void *out, long long e, long long plane, float o0,
+                                          float o1, float o2)
+{
+    if (P.format == 0) {
+        uint16_t *o = (uint16_t *)out;
+        o[e] = (uint16_t)o0;
+        o[e + plane] = (uint16_t)o1;
+        o[e + 2 * plane] = (uint16_t)o2;
+    } else {
+        float *o = (float *)out;
+        o[e] = o0;
+        o[e + plane] = o1;
+        o[e + 2 * plane] = o2;
+    }
+}
+
+// 8 consecutive outputs of one plane at element e (a multiple of 4): two
+// 8-byte stores (yuv444p16) or two 16-byte stores (yuv444ps)
+__device__ __forceinline__ void store8(const DemodParams &P, void *out, long long e, const float (&a)[8])
+{
+    if (P.format == 0) {
+        uint2 *o = reinterpret_cast<uint2 *>((uint16_t *)out + e);
+        o[0] = make_uint2((uint32_t)a[0] | ((uint32_t)a[1] << 16), (uint32_t)a[2] | ((uint32_t)a[3] << 16));
+        o[1] = make_uint2((uint32_t)a[4] | ((uint32_t)a[5] << 16), (uint32_t)a[6] | ((uint32_t)a[7] << 16));
+    } else {
+        float4 *o = reinterpret_cast<float4 *>((float *)out + e);
+        o[0] = make_float4(a[0], a[1], a[2], a[3]);
+        o[1] = make_float4(a[4], a[5], a[6], a[7]);
+    }
+}
+
 // Double-float pieces of the burst normalisation (FP64 is scarce on this
 // GPU and one lane per line waiting on it stalls the block).
 __device__ __forceinline__ df two_prod(float a, float b)
@@ -370,51 +419,104 @@ __global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
         __syncthreads();
     }
 
-    // 4. 2D FIR + rotation + pack; work item = (line, 8-sample segment)
-    for (int item = threadIdx.x; item < kDemodLines * per_line; item += blockDim.x) {
+    // 4. 2D FIR + rotation + pack; work item = (line, 8-sample segment).
+    // Sample s of an item is output pixel 8 seg + s - xoff. For yuv444p16 /
+    // yuv444ps with 4-element-aligned rows, planes and frames, a lane stores
+    // pixels 8 seg .. 8 seg + 7 with vector stores: its samples xoff..7 and
+    // (xoff = 1) the next lane's sample 0, passed by a shuffle; edges and the
+    // other formats store per sample. Every lane runs every round, so the
+    // shuffles see the whole warp.
+    const int total = kDemodLines * per_line;
+    const int xoff = P.avs - base4;
+    const int aw = P.ave - P.avs;
+    const long long plane = (long long)P.out_w * P.out_h;
+    const bool vout = (P.format == 0 || P.format == 1) && xoff <= 1 && ((P.out_w | P.left_pad) & 3) == 0 &&
+                      (P.out_frame_stride & 3) == 0 && (reinterpret_cast<uintptr_t>(out_base) & 15) == 0;
+    for (int ib = 0; ib < total; ib += blockDim.x) {
+        const int item = ib + threadIdx.x;
         const int t = item / per_line;
         const int seg = item % per_line;
         const int fl = fl0 + t;
-        if (fl >= fl_last) continue;
-        const int xl0 = seg * 8;   // local index of the first sample (absolute base4 + xl0, a multiple of 4)
-        // the composite samples luma needs, loaded before the FIR so their
-        // latency hides behind it
-        const uint16_t *comp = field + (long long)fl * P.fw;
-        float cv[8];
+        const bool live = item < total && fl < fl_last;
+        float o0[8], o1[8], o2[8];
+        long long rowpix = 0;
+        if (live) {
+            const int xl0 = seg * 8;   // local index of the first sample (absolute base4 + xl0, a multiple of 4)
+            // the composite samples luma needs, loaded before the FIR so their
+            // latency hides behind it
+            const uint16_t *comp = field + (long long)fl * P.fw;
+            float cv[8];
 #pragma unroll
-        for (int s = 0; s < 8; s++) {
-            const int x = base4 + xl0 + s;
-            cv[s] = (float)comp[x < P.fw ? x : P.fw - 1];
-        }
-        float v[4][22];
-        item_window(ch + t * SW + kPad + xl0 - 7, SW, v);
-        float PU[8], QU[8], PV[8], QV[8], PY[8], QY[8];
-        item_fir<COMPOSITE && !YNR>(v, PU, QU, PV, QV, PY, QY);
-
-        const float bp = s_bp[t], bq = s_bq[t], vsw = s_vsw[t];
-        const int orow = P.top_pad + 2 * fl + off - P.fafl;
-        const long long rowpix = (long long)orow * P.out_w + P.left_pad;
-#pragma unroll
-        for (int s = 0; s < 8; s++) {
-            const int x = base4 + xl0 + s;
-            if (x < P.avs || x >= P.ave) continue;
-            float Y;
-            if (YNR) {
-                // doYNR: a = sum_i b_i Y[x + 12 - i], cored to +-nr_y, subtracted
-                const float *yl = ys + t * YW + kNrHalf + xl0 + s;
-                float a = 0.f;
-#pragma unroll
-                for (int i = 0; i < 25; i++) a = __fmaf_rn(cd_nrpal[i], yl[kNrHalf - i], a);
-                a = fminf(fmaxf(a, -P.nr_y), P.nr_y);
-                Y = yl[0] - a;
-            } else if (COMPOSITE) {
-                Y = cv[s] - 2.0f * __fmaf_rn(PY[s], carrier_sin(x), QY[s] * carrier_cos(x));
-            } else {
-                Y = cv[s] - v[0][s + 7];
+            for (int s = 0; s < 8; s++) {
+                const int x = base4 + xl0 + s;
+                cv[s] = (float)comp[x < P.fw ? x : P.fw - 1];
             }
-            const float U = -(PU[s] * bp + QU[s] * bq) * 2.0f;
-            const float V = vsw * -(QV[s] * bp - PV[s] * bq) * 2.0f;
-            pack_sample(P, out_base, frame_slot, rowpix + (x - P.avs), Y, U, V);
+            float v[4][22];
+            item_window(ch + t * SW + kPad + xl0 - 7, SW, v);
+            float PU[8], QU[8], PV[8], QV[8], PY[8], QY[8];
+            item_fir<COMPOSITE && !YNR>(v, PU, QU, PV, QV, PY, QY);
+
+            const float bp = s_bp[t], bq = s_bq[t], vsw = s_vsw[t];
+            const int orow = P.top_pad + 2 * fl + off - P.fafl;
+            rowpix = (long long)orow * P.out_w + P.left_pad;
+#pragma unroll
+            for (int s = 0; s < 8; s++) {
+                const int x = base4 + xl0 + s;
+                float Y;
+                if (YNR) {
+                    // doYNR: a = sum_i b_i Y[x + 12 - i], cored to +-nr_y, subtracted
+                    const float *yl = ys + t * YW + kNrHalf + xl0 + s;
+                    float a = 0.f;
+#pragma unroll
+                    for (int i = 0; i < 25; i++) a = __fmaf_rn(cd_nrpal[i], yl[kNrHalf - i], a);
+                    a = fminf(fmaxf(a, -P.nr_y), P.nr_y);
+                    Y = yl[0] - a;
+                } else if (COMPOSITE) {
+                    Y = cv[s] - 2.0f * __fmaf_rn(PY[s], carrier_sin(x), QY[s] * carrier_cos(x));
+                } else {
+                    Y = cv[s] - v[0][s + 7];
+                }
+                const float U = -(PU[s] * bp + QU[s] * bq) * 2.0f;
+                const float V = vsw * -(QV[s] * bp - PV[s] * bq) * 2.0f;
+                if (vout) {
+                    yuv_values(P, Y, U, V, o0[s], o1[s], o2[s]);
+                } else if (x >= P.avs && x < P.ave) {
+                    pack_sample(P, out_base, frame_slot, rowpix + (x - P.avs), Y, U, V);
+                }
+            }
+        }
+        if (!vout) continue;
+        const float n0 = __shfl_down_sync(0xffffffffu, o0[0], 1);
+        const float n1 = __shfl_down_sync(0xffffffffu, o1[0], 1);
+        const float n2 = __shfl_down_sync(0xffffffffu, o2[0], 1);
+        const int nitem = __shfl_down_sync(0xffffffffu, live ? item : -1, 1);
+        const bool full = live && 8 * seg + 8 <= aw &&
+                          (xoff == 0 || (lane < 31 && nitem == item + 1 && seg + 1 < per_line));
+        const bool prev_full = (__shfl_up_sync(0xffffffffu, full ? 1 : 0, 1) != 0) && lane > 0;
+        if (!live) continue;
+        const long long e0 = frame_slot * P.out_frame_stride + rowpix;
+        if (full) {
+            float a0[8], a1[8], a2[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {   // xoff is 0 or 1 here; constant indices keep o* in registers
+                a0[j] = xoff == 0 ? o0[j] : (j < 7 ? o0[j < 7 ? j + 1 : 7] : n0);
+                a1[j] = xoff == 0 ? o1[j] : (j < 7 ? o1[j < 7 ? j + 1 : 7] : n1);
+                a2[j] = xoff == 0 ? o2[j] : (j < 7 ? o2[j < 7 ? j + 1 : 7] : n2);
+            }
+            const long long e = e0 + 8 * seg;
+            store8(P, out_base, e, a0);
+            store8(P, out_base, e + plane, a1);
+            store8(P, out_base, e + 2 * plane, a2);
+        }
+        // samples no vector store covered: edges, and sample 0 unless the
+        // previous lane stored it
+#pragma unroll
+        for (int s = 0; s < 8; s++) {
+            const int p = 8 * seg + s - xoff;
+            if (p < 0 || p >= aw) continue;
+            if (full && s >= xoff) continue;
+            if (xoff == 1 && s == 0 && prev_full) continue;
+            store_yuv(P, out_base, e0 + p, plane, o0[s], o1[s], o2[s]);
         }
     }
 }
