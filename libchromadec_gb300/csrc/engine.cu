@@ -284,6 +284,7 @@ int Engine::run_transform(const uint16_t *fields, long long stride, int field_ba
         P.field_base = field_base;
         P.nfields = nfields;
         P.fw = g_.field_width;
+        P.fh = g_.field_height;
         P.avs = g_.active_start;
         P.ave = g_.active_end;
         P.fafl = g_.first_active_frame_line;

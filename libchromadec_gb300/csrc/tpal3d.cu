@@ -166,14 +166,14 @@ __device__ __forceinline__ void forward_pair(const T3Params &P, int q, int tileX
         const uint16_t *row = fp + (long long)(L >> 1) * P.fw;
         int a[16];
         int sum = 0;
-        if (tileX >= 0 && (L >> 1) >= 1) {
+        if (tileX >= 0 && (L >> 1) >= 1 && ((L >> 1) + 1 < P.fh || tileX + 18 <= P.fw)) {
             // Rows start on any 2-byte boundary (odd line and field
             // lengths): nine aligned 32-bit words cover the 16 samples, and a
             // funnel shift by 0 or 16 bits lines each pair up -- 9 loads
             // instead of 16, each warp load touching 32 rows either way. The
-            // words span at most the sample before and two after the 16
-            // (inside the field: the row is not its first, and a row past
-            // the last active line is never read).
+            // words span at most the sample before and two after the 16,
+            // inside the field: the row is not its first, and it is not the
+            // last unless the words end inside it.
             const uintptr_t pa = reinterpret_cast<uintptr_t>(row + tileX);
             const uint32_t *w = reinterpret_cast<const uint32_t *>(pa & ~(uintptr_t)3);
             const unsigned sh = (unsigned)(pa & 2) * 8u;
@@ -272,15 +272,15 @@ __device__ __forceinline__ df df_from_fixed60(long long hi_acc, long long lo_acc
 // The X stage in 60-bit fixed point: each sample times each coefficient
 // word is an exact 64-bit integer product, so the sums are exact and the one
 // rounding is the conversion to double-float (about 2^-47 of the sum).
-__device__ __forceinline__ void x_row_pair(const uint16_t *field, long long base, int black, int kx, dfc &xa,
-                                           dfc &xb)
+__device__ __forceinline__ void x_row_pair(const uint16_t *field, long long base, long long field_len, int black,
+                                           int kx, dfc &xa, dfc &xb)
 {
     // even and odd samples summed apart: column kx is even + odd, column
     // 8 - kx ((-1)^x times the conjugate) is the conjugate of even - odd --
     // the same integers as summing each column's products directly
     long long e[4] = {0, 0, 0, 0}, o[4] = {0, 0, 0, 0};   // re.hi, re.lo, im.hi, im.lo
     int a[16];
-    if (base >= 1) {
+    if (base >= 1 && base + 18 <= field_len) {
         // nine aligned 32-bit words and a funnel shift, as in forward_pair
         const uintptr_t pa = reinterpret_cast<uintptr_t>(field + base);
         const uint32_t *w = reinterpret_cast<const uint32_t *>(pa & ~(uintptr_t)3);
@@ -336,7 +336,7 @@ __device__ __noinline__ void exact_pair(const T3Params &P, int m, int tileX, int
             if (L < P.fafl || L > P.lafl) continue;
             const long long base = (long long)(L >> 1) * P.fw + tileX;   // within the field
             dfc xb, xr;
-            x_row_pair(fp, base, P.black, kxb, xb, xr);
+            x_row_pair(fp, base, (long long)P.fh * P.fw, P.black, kxb, xb, xr);
             const df wy = {c3_dfwy[y][0], c3_dfwy[y][1]};
             dfc cb = dfc_tw32(kyb * y), cr = dfc_tw32(kyr * y);
             cb.re = df_mul(cb.re, wy); cb.im = df_mul(cb.im, wy);
@@ -794,7 +794,7 @@ __global__ void __launch_bounds__(32 * kWarps3) tp3_resolve_kernel(T3Params P)
             const int L = tileY + y0 + 2 * (part * 4 + r4);
             if (fp == nullptr || L < P.fafl || L > P.lafl) continue;
             const long long base = (long long)(L >> 1) * P.fw + tileX;   // within the field
-            x_row_pair(fp, base, P.black, kxa, xa[r4], xb[r4]);
+            x_row_pair(fp, base, (long long)P.fh * P.fw, P.black, kxa, xa[r4], xb[r4]);
         }
         bool flipped = false;
         unsigned any = __ballot_sync(0xffffffffu, unc != 0);

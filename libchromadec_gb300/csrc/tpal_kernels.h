@@ -44,7 +44,7 @@ struct T3Params {
     long long field_stride;
     int field_base;
     int nfields;
-    int fw;
+    int fw, fh;                  // samples per line, lines per field
     int avs, ave, fafl, lafl;   // active samples [avs, ave), frame lines [fafl, lafl]
     int black;
     int swap;                    // 1: even fields are second fields (reversed pairing)
