@@ -121,3 +121,43 @@ def test_keep_mask_is_the_mirror_threshold_rule():
                 assert keep[kz, k, ky] == want
     r = T.report(S.astype(np.complex64), S, 0.4)
     assert r["bins"] == 768 and r["flips"] == 0 and r["max_rel_err"] < 1e-6
+
+
+def test_tc_entry_points_reject_bad_arguments():
+    """chdg_tc3d_* and chdg_engine_set_tc_form validate before any CUDA call."""
+    import ctypes as C
+    L = D.lib()
+    g = D.default_geometry()
+    buf = (C.c_uint8 * 16)()
+    # spectra: bad variant, empty Z range, null buffers, a stride shorter than a field
+    assert L.chdg_tc3d_spectra(C.byref(g), 2, C.c_void_p(16), 355255, 8, 0, 1, C.c_void_p(16), None) == -1
+    assert L.chdg_tc3d_spectra(C.byref(g), 0, C.c_void_p(16), 355255, 8, 3, 3, C.c_void_p(16), None) == -1
+    assert L.chdg_tc3d_spectra(C.byref(g), 0, None, 355255, 8, 0, 1, C.c_void_p(16), None) == -1
+    assert L.chdg_tc3d_spectra(C.byref(g), 0, C.c_void_p(16), 1000, 8, 0, 1, C.c_void_p(16), None) == -1
+    assert b"bad argument" in L.chd_last_error()
+    # operand images: stage, split and buffer size
+    assert L.chdg_tc3d_operand(0, 6, 0, 0, buf, 16) == -1
+    assert L.chdg_tc3d_operand(0, 0, 0, 2, buf, 16) == -1
+    assert L.chdg_tc3d_operand(0, 0, 0, 0, buf, 16) == -1   # 2 KB image, 16-byte buffer
+    assert b"too small" in L.chd_last_error()
+    assert L.chdg_engine_set_tc_form(None, 0) == -1
+
+
+def test_tc_operand_sizes():
+    """Image sizes: rows x K x element bytes (TF32 4, BF16 2)."""
+    for variant, eb in ((D.TC_3XTF32, 4), (D.TC_BF16X3, 2)):
+        for stage, (rows, K) in enumerate([(16, 16), (64, 32), (16, 16), (16, 16), (32, 64), (16, 16)]):
+            assert len(D.tc3d_operand(variant, stage, 0, 0)) == rows * K * eb
+
+
+def test_report_counts_flips():
+    """A bin pushed across the threshold is one flip per visited bin it decides."""
+    rng = np.random.default_rng(4)
+    S = rng.normal(size=(8, 5, 32)) + 1j * rng.normal(size=(8, 5, 32))
+    # bin (kz 1, kx 2, ky 3) and its mirror (kz 1, kx 6, ky 5): equal magnitudes, then one scaled
+    S[1, 0, 3] = 1.0
+    S[1, 4, 5] = 1.0
+    T_ = S.copy()
+    T_[1, 0, 3] = 10.0   # |a|^2 = 100 against 1: dissimilar at t = 0.4
+    r = T.report(T_.astype(np.complex64), S, 0.4)
+    assert r["flips"] == 1 and r["bins"] == 768
