@@ -461,9 +461,10 @@ __global__ void __launch_bounds__(kThreads) tc3_xy_kernel(Params P)
             for (int c = 0; c < 4; c++) {
                 float v[16];
                 tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + 64 + 16 * c, v);
-                if (t < kYRows && tile < P.ntiles) {
+                if (t < kYRows && tile < P.ntiles) {   // rows start on 256-byte boundaries: pairs of bins per store
+                    float4 *d4 = reinterpret_cast<float4 *>(dst + 8 * c);
 #pragma unroll
-                    for (int j = 0; j < 8; j++) dst[8 * c + j] = make_float2(v[2 * j], v[2 * j + 1]);
+                    for (int j = 0; j < 4; j++) d4[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
                 }
             }
         }
