@@ -43,6 +43,9 @@ FLOP_PER_FIELD_3D = 692_311_680
 # the transform's share of it (2,220 tiles x 259,584 FLOP), for the
 # transform kernel's FP32 roofline
 FLOP_PER_FIELD_3D_TRANSFORM = 576_276_480
+# Transform-PAL 2D by the same convention: 2,257 tiles of 16 x 32 per field,
+# 2 (2.5 x 512 x 9) + 512 + 10 x 80 + 2 x 512 = 25,376 FLOP each
+FLOP_PER_FIELD_2D_TRANSFORM = 57_273_632
 
 
 def parse():
@@ -57,6 +60,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the tensor-core forms and chroma PSNR report")
+    ap.add_argument("--kind", default="3d", choices=["3d", "2d"],
+                    help="Transform-PAL 3D (the metric) or 2D (for profiling the 2D kernel)")
     ap.add_argument("--form", default="plain", choices=["plain", "tc_3xtf32", "tc_bf16x3"],
                     help="transform form of the timed decode (the tensor-core forms for profiling them)")
     ap.add_argument("--workload", default="stream", choices=["stream", "batched"],
@@ -66,8 +71,10 @@ def parse():
 
 
 def workload_desc(a):
-    return (f"Transform-PAL 3D, {a.fields} PAL fields 1135x313 uint16 (seed {a.seed}, pan 1.5 px/field + "
-            f"0.5 line/field, static 75% bars, AWGN 0.5%), 8x32x16 tiles, threshold 0.4, "
+    two = getattr(a, "kind", "3d") == "2d"
+    return (f"Transform-PAL {'2D' if two else '3D'}, {a.fields} PAL fields 1135x313 uint16 (seed {a.seed}, "
+            f"pan 1.5 px/field + 0.5 line/field, static 75% bars, AWGN 0.5%), "
+            f"{'16x32' if two else '8x32x16'} tiles, threshold 0.4, "
             f"yuv444{'p16' if a.format == 'p16' else 'ps'} out")
 
 
@@ -486,8 +493,14 @@ def main():
     nfields = fields_np.shape[0]
     nframes = nfields // 2
     fmt = D.FMT_P16 if a.format == "p16" else D.FMT_PS
-    eng = D.Engine(D.default_geometry(), D.default_config(kind=D.KIND_TRANSFORM_3D, fmt=fmt))
+    two = a.kind == "2d"
+    if two:   # the end-to-end, CPU and forms legs are the 3D metric's
+        a.no_e2e = a.no_cpu = a.no_forms = True
+    eng = D.Engine(D.default_geometry(),
+                   D.default_config(kind=D.KIND_TRANSFORM_2D if two else D.KIND_TRANSFORM_3D, fmt=fmt))
     tc_form = {"plain": -1, "tc_3xtf32": D.TC_3XTF32, "tc_bf16x3": D.TC_BF16X3}[a.form]
+    if two and tc_form >= 0:
+        raise SystemExit("the tensor-core form is Transform 3D only")
     eng.set_tc_form(tc_form)
     lib = D.lib()
     dfields = torch.from_numpy(fields_np.reshape(nfields, -1).view(np.int16)).cuda()
@@ -525,7 +538,7 @@ def main():
     # roofline of the dominant kernel (the transform): launches per step
     # one engine batch = 4 launches: the transform walk, the resolve pass,
     # the exact re-walk of the items it lists, the demodulator
-    launches_transform = nl.value // 4 if tc_form < 0 else a.steps * ((nframes + 255) // 256)
+    launches_transform = (nl.value // 2 if two else nl.value // 4) if tc_form < 0 else a.steps * ((nframes + 255) // 256)
     per_launch_ms = mt.value / max(1, launches_transform)
     fields_per_launch = nfields * a.steps / max(1, launches_transform)
     bytes_per_field = FIELD_BYTES_IN + OUT_BYTES[a.format]
@@ -541,8 +554,8 @@ def main():
     # (a smaller capture of the same kernel; traffic grows with the fields)
     traffic = None
     try:
-        if tc_form >= 0:
-            raise FileNotFoundError("the committed traffic figure is the plain form's")
+        if tc_form >= 0 or two:
+            raise FileNotFoundError("the committed traffic figure is the plain 3D form's")
         with open(os.path.join(ROOT, "profiles", "tpal3d_traffic_200fields.md")) as fp:
             for ln in fp:
                 if ln.startswith("traffic_bytes_per_field:"):
@@ -551,7 +564,8 @@ def main():
         pass
     clocks = clk.summary()
     fp32_peak = 152 * 128 * 2 * (clocks["sm_mhz"] or 2070.0) * 1e6 / 1e12
-    tr_tflops = fields_per_launch * FLOP_PER_FIELD_3D_TRANSFORM / (per_launch_ms / 1000.0) / 1e12
+    flop_field = FLOP_PER_FIELD_2D_TRANSFORM if two else FLOP_PER_FIELD_3D_TRANSFORM
+    tr_tflops = fields_per_launch * flop_field / (per_launch_ms / 1000.0) / 1e12
 
     line = {
         "metric": METRIC, "value": value, "unit": "fields/s", "n_gpus": world, "steps": a.steps,
@@ -561,8 +575,8 @@ def main():
                    "format": "yuv444" + a.format, "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
                    "l2": f"inputs {nfields * FIELD_BYTES_IN / 1e6:.0f} MB > 129 MB L2 (no flush)"},
         "roofline": {
-            "bound": "hbm", "kernel": "tpal3d transform stage (walk, resolve, exact re-walk)" if tc_form < 0
-            else "tensor-core transform stage (tc3_xy, tc3_zd, tc3_yx)", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+            "bound": "hbm", "kernel": ("tpal2d_kernel" if two else "tpal3d transform stage (walk, resolve, exact re-walk)")
+            if tc_form < 0 else "tensor-core transform stage (tc3_xy, tc3_zd, tc3_yx)", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
             "frac": achieved_gbs / hbm_peak, "traffic": traffic,
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback 6.8 TB/s",
             "algorithmic_bytes_per_field": bytes_per_field,
@@ -571,10 +585,12 @@ def main():
             "fp32": {"bound": "fp32", "achieved": tr_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": tr_tflops / fp32_peak,
                      "peak_source": "nominal: 152 SMs x 128 FP32 lanes x 2 FLOP x the sampled SM clock",
-                     "algorithmic_flop_per_field": FLOP_PER_FIELD_3D_TRANSFORM,
-                     "note": "the transform's convention FLOP count (2.5 N log2 N per real FFT each way, window, "
-                             "threshold, overlap-add; 2,220 distinct tiles per field); the kernel shares the X/Y "
-                             "stages across Z tiles, so it executes fewer FLOPs than counted"},
+                     "algorithmic_flop_per_field": flop_field,
+                     "note": ("the transform's convention FLOP count (2.5 N log2 N per real FFT each way, window, "
+                              "threshold, overlap-add; 2,257 16x32 tiles per field)") if two else
+                             ("the transform's convention FLOP count (2.5 N log2 N per real FFT each way, window, "
+                              "threshold, overlap-add; 2,220 distinct tiles per field); the kernel shares the X/Y "
+                              "stages across Z tiles, so it executes fewer FLOPs than counted")},
         },
         "clocks": clocks,
         "gpu_launches": int(nl.value),
@@ -606,7 +622,7 @@ def main():
             "value": nfields * a.steps / (e0.elapsed_time(e1) / 1000.0), "unit": "fields/s",
             "path": "chdg_decode_host: pinned host fields -> pinned host frames, one call per step"}
 
-    if rank == 0 and not a.no_forms and a.format == "p16" and tc_form < 0:
+    if rank == 0 and not a.no_forms and a.format == "p16" and tc_form < 0 and not two:
         line["forms"] = forms_report(a, dfields, nfields, value, stream)
     if rank == 0 and not a.no_cpu:
         line["cpu_baseline"] = cpu_baseline(a, fields_np)
