@@ -149,6 +149,37 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def fp32_sgemm_peak(device: int):
+    """FP32 CUDA-core throughput as cuBLAS reaches it on this GPU: an 8192^3
+    SGEMM with TF32 off, best of 5 (CUDA events), in TFLOP/s -- the FP32
+    counterpart of the driver's measured bf16 peak. None if it cannot run."""
+    try:
+        import torch
+        prev = torch.backends.cuda.matmul.allow_tf32
+        torch.backends.cuda.matmul.allow_tf32 = False
+        try:
+            n = 8192
+            x = torch.randn(n, n, device=f"cuda:{device}", dtype=torch.float32)
+            y = torch.randn(n, n, device=f"cuda:{device}", dtype=torch.float32)
+            for _ in range(2):
+                torch.matmul(x, y)
+            best = None
+            for _ in range(5):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                torch.matmul(x, y)
+                e1.record()
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1)
+                best = ms if best is None else min(best, ms)
+            del x, y
+            return 2.0 * n ** 3 / (best / 1000.0) / 1e12
+        finally:
+            torch.backends.cuda.matmul.allow_tf32 = prev
+    except Exception:
+        return None
+
+
 def cpu_threads():
     try:
         return len(os.sched_getaffinity(0))
@@ -156,26 +187,52 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
-def run_cpu(a, fields, nframes_sample, threads):
+def run_cpu(a, fields, nframes_sample, threads, kind=3, first=0):
     """Oracle (the reference's algorithm restated in C) on the host cores."""
     from oracle import oracle as O
-    p = O.params(kind=3, fmt=O.FMT_P16 if a.format == "p16" else O.FMT_PS)
+    p = O.params(kind=kind, fmt=O.FMT_P16 if a.format == "p16" else O.FMT_PS)
     t0 = time.perf_counter()
-    O.decode_frames(p, fields, 0, nframes_sample, threads=threads)
+    O.decode_frames(p, fields, first, nframes_sample, threads=threads)
     return time.perf_counter() - t0
 
 
-def cpu_baseline(a, fields, budget_s=12.0):
+def _median_rate(a, fields, nframes, threads, reps=3, kind=3):
+    times = [run_cpu(a, fields, nframes, threads, kind=kind) for _ in range(reps)]
+    return 2 * nframes / statistics.median(times), times
+
+
+def cpu_baseline(a, fields, budget_s=6.0):
+    """The CPU path on the host cores, a reported baseline: the median of 3
+    repetitions on all host threads and on one thread, for the 3D workload
+    (a bounded sample of the same capture) and for the 16-field Transform-PAL
+    2D capture (whole)."""
+    import numpy as np
+    from libchromadec_gb300 import synth
     threads = cpu_threads()
-    # calibrate on a few frames, then time a sample sized to the budget
+    nfr = fields.shape[0] // 2
+    # calibrate on a few frames, then size the sample to the budget
     t1 = run_cpu(a, fields, max(1, min(threads, 4)), threads)
     per_frame = t1 / max(1, min(threads, 4)) * min(threads, 4) / threads
-    n = int(max(threads, min(fields.shape[0] // 2, budget_s / max(per_frame, 1e-6))))
-    n = min(n, fields.shape[0] // 2)
-    dt = run_cpu(a, fields, n, threads)
-    return {"value": 2 * n / dt, "unit": "fields/s", "cores": threads, "kind": "port",
-            "sample": f"frames 0..{n - 1} ({2 * n} fields) of the same capture, all {threads} host threads, "
-                      f"one decoder instance per thread (chd_decode_frames_async's model), FP64 CPU oracle"}
+    n = int(max(threads, min(nfr, budget_s / max(per_frame, 1e-6))))
+    n = min(n, nfr)
+    v_all, t_all = _median_rate(a, fields, n, threads)
+    n1 = 2
+    v_one, t_one = _median_rate(a, fields, n1, 1)
+    cap2 = synth.make_capture(16, synth.SynthConfig(seed=a.seed, pan_x=0.0, pan_y=0.0)).fields
+    v2_all, _ = _median_rate(a, cap2, 8, threads, kind=2)
+    v2_one, _ = _median_rate(a, cap2, 8, 1, kind=2)
+    return {"value": v_all, "unit": "fields/s", "cores": threads, "kind": "port",
+            "sample": f"frames 0..{n - 1} ({2 * n} fields) of the same capture, all {threads} host threads, one "
+                      f"decoder instance per thread (chd_decode_frames_async's model), FP64 CPU oracle (radix-2 "
+                      f"FP64 FFT; FFTW is not installed on these hosts); median of 3 repetitions "
+                      f"({', '.join(f'{t:.2f}' for t in t_all)} s)",
+            "one_thread": {"value": v_one, "unit": "fields/s", "cores": 1,
+                           "sample": f"frames 0..{n1 - 1} ({2 * n1} fields), median of 3 "
+                                     f"({', '.join(f'{t:.2f}' for t in t_one)} s)"},
+            "transform_2d_16_fields": {
+                "all_threads": v2_all, "one_thread": v2_one, "unit": "fields/s",
+                "sample": "the whole 16-field capture (seeded, static content), Transform-PAL 2D 16x32 tiles, "
+                          "threshold 0.4, median of 3"}}
 
 
 def reference_arm(a):
@@ -395,7 +452,8 @@ def forms_report(a, dfields, nfields, plain_value, stream):
     threshold decisions that flip."""
     import numpy as np
     import torch
-    from libchromadec_gb300 import device as D, synth, tc_study as T
+    from libchromadec_gb300 import device as D, synth
+    from tests import tc_study as T
 
     g = D.default_geometry()
     nframes = nfields // 2
@@ -563,7 +621,11 @@ def main():
     except Exception:
         pass
     clocks = clk.summary()
-    fp32_peak = 152 * 128 * 2 * (clocks["sm_mhz"] or 2070.0) * 1e6 / 1e12
+    props = torch.cuda.get_device_properties(local)
+    sms = props.multi_processor_count
+    fp32_nominal = sms * 128 * 2 * (clocks["sm_mhz"] or 2070.0) * 1e6 / 1e12
+    fp32_meas = fp32_sgemm_peak(local)
+    fp32_peak = fp32_meas if fp32_meas else fp32_nominal
     flop_field = FLOP_PER_FIELD_2D_TRANSFORM if two else FLOP_PER_FIELD_3D_TRANSFORM
     tr_tflops = fields_per_launch * flop_field / (per_launch_ms / 1000.0) / 1e12
 
@@ -575,22 +637,26 @@ def main():
                    "format": "yuv444" + a.format, "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
                    "l2": f"inputs {nfields * FIELD_BYTES_IN / 1e6:.0f} MB > 129 MB L2 (no flush)"},
         "roofline": {
-            "bound": "hbm", "kernel": ("tpal2d_kernel" if two else "tpal3d transform stage (walk, resolve, exact re-walk)")
-            if tc_form < 0 else "tensor-core transform stage (tc3_xy, tc3_zd, tc3_yx)", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-            "frac": achieved_gbs / hbm_peak, "traffic": traffic,
-            "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback 6.8 TB/s",
-            "algorithmic_bytes_per_field": bytes_per_field,
+            "bound": "fp32", "kernel": ("tpal2d_kernel" if two else "tpal3d transform stage (walk, resolve, exact re-walk)")
+            if tc_form < 0 else "tensor-core transform stage (tc3_xy, tc3_zd, tc3_yx)",
+            "achieved": tr_tflops, "peak": fp32_peak, "unit": "TFLOP/s", "frac": tr_tflops / fp32_peak,
+            "traffic": traffic,
+            "peak_source": (f"measured: cuBLAS SGEMM 8192^3 with TF32 off, best of 5 on this GPU ({fp32_meas:.1f}; "
+                            f"nominal {sms} SMs x 128 lanes x 2 FLOP x {clocks['sm_mhz'] or 2070.0:.0f} MHz = "
+                            f"{fp32_nominal:.1f})") if fp32_meas else
+                           f"nominal: {sms} SMs x 128 FP32 lanes x 2 FLOP x the sampled SM clock",
+            "algorithmic_flop_per_field": flop_field,
             "per_launch_ms": per_launch_ms, "fields_per_launch": fields_per_launch,
             "demod_ms_per_launch": md.value / max(1, launches_transform),
-            "fp32": {"bound": "fp32", "achieved": tr_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": tr_tflops / fp32_peak,
-                     "peak_source": "nominal: 152 SMs x 128 FP32 lanes x 2 FLOP x the sampled SM clock",
-                     "algorithmic_flop_per_field": flop_field,
-                     "note": ("the transform's convention FLOP count (2.5 N log2 N per real FFT each way, window, "
-                              "threshold, overlap-add; 2,257 16x32 tiles per field)") if two else
-                             ("the transform's convention FLOP count (2.5 N log2 N per real FFT each way, window, "
-                              "threshold, overlap-add; 2,220 distinct tiles per field); the kernel shares the X/Y "
-                              "stages across Z tiles, so it executes fewer FLOPs than counted")},
+            "note": ("the transform's convention FLOP count (2.5 N log2 N per real FFT each way, window, "
+                     "threshold, overlap-add; 2,257 16x32 tiles per field)") if two else
+                    ("the transform's convention FLOP count (2.5 N log2 N per real FFT each way, window, "
+                     "threshold, overlap-add; 2,220 distinct tiles per field); the kernel shares the X/Y "
+                     "stages across Z tiles, so it executes fewer FLOPs than counted"),
+            "hbm": {"achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": achieved_gbs / hbm_peak,
+                    "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks
+                    else "fallback 6.8 TB/s",
+                    "algorithmic_bytes_per_field": bytes_per_field, "traffic": traffic},
         },
         "clocks": clocks,
         "gpu_launches": int(nl.value),

@@ -110,16 +110,17 @@ int chdg_chroma_device(chdg_engine *e, const uint16_t *d_fields, int64_t field_s
  * their own allocator or budget, and latency-critical loops where cudaMalloc's
  * implicit device synchronisation would stall other work. The chroma scratch
  * and the guard-band decision records are fixed arrays compiled into the
- * library (85.3 MB: 8 frames of the 948x576 active picture), which every GPU
+ * library (81.6 MB: 8 frames of the 948x576 active picture), which every GPU
  * that loads the library holds until the process exits; calls asking for
- * more than 8 frames, or a larger active picture, fail with
- * CHDG_E_INVALID_ARG. No cudaMalloc/cudaFree or other
+ * more than 8 frames, a negative or reversed frame range, or a larger active
+ * picture fail with CHDG_E_INVALID_ARG. No cudaMalloc/cudaFree or other
  * allocating call is made. All calls on a device share the one scratch array
  * (it keeps the last call's contents), so calls whose work overlaps on the GPU
  * race: serialise them on one stream. The first call on a device resolves the
  * array's device address and uploads constant tables; make that first call
  * before starting any stream capture. Per-bin thresholds, when given, are
- * copied into a second static array shared the same way. */
+ * copied from pageable host memory into a second static array on `stream`
+ * at every call, ordered after the decodes already queued on that stream. */
 int chdg_decode_device_static(const chdg_geometry *g, const chdg_config *c, const uint16_t *d_fields,
                               int64_t field_stride, int32_t nfields, int32_t frame_begin, int32_t frame_end,
                               void *d_out, void *stream);
@@ -211,6 +212,17 @@ int chdg_engine_set_tc_form(chdg_engine *e, int32_t variant);
 struct chd_video;
 int chdg_video_source_frame(const struct chd_video *v, int32_t reverse_field_order, int32_t source,
                             int32_t primary_frame, int32_t *out_frame);
+
+/* Dropout concealment as the decoder applies it (no counterpart in the
+ * reference ABI, whose DropoutCorrector::correctFrame,
+ * src/dropout/dropout_corrector.cpp:50-157, works on the decoder's private
+ * field copies): the two fields of frame `frame_index` of a committed
+ * decoder, in the decoder's field order (first field first unless
+ * reverse_field_order), after the GPU concealment kernel has run that
+ * frame's plan with the decoder's current chd_decoder_set_dropout settings
+ * and extra sources -- the composite the transform reads. out holds
+ * 2 * field_width * field_height uint16 samples. Returns a chd_status_t. */
+int chdg_decoder_concealed_fields(struct chd_decoder *d, int64_t frame_index, uint16_t *out);
 
 /* Threshold decisions whose FP32 margin was inside the error bound and were
  * re-evaluated in double-float, and how many of those FP32 had wrong. */

@@ -119,6 +119,7 @@ _SIGS = {
     "chd_video_add_extra_source_composite": ([_P, C.c_char_p, C.c_char_p], C.c_int),
     "chd_video_add_extra_source_yc": ([_P, C.c_char_p, C.c_char_p, C.c_char_p], C.c_int),
     "chdg_video_source_frame": ([_P, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
+    "chdg_decoder_concealed_fields": ([_P, C.c_int64, _P], C.c_int),
     "chd_decoder_create": ([_P, C.c_int, _PP], C.c_int), "chd_decoder_free": ([_P], None),
     "chd_decoder_set_option_f64": ([_P, C.c_char_p, C.c_double], C.c_int),
     "chd_decoder_set_option_i32": ([_P, C.c_char_p, C.c_int32], C.c_int),
@@ -351,6 +352,14 @@ class Decoder:
             return f.plane(PLANE_Y)
         finally:
             f.close()
+
+    def concealed_fields(self, index: int) -> np.ndarray:
+        """Frame `index`'s two fields after the GPU concealment (device-level
+        chdg_decoder_concealed_fields), shape (2, field_height, field_width)."""
+        vi = self.video.info()
+        out = np.empty((2, vi.field_height, vi.field_width), dtype=np.uint16)
+        check(lib().chdg_decoder_concealed_fields(self._h, index, out.ctypes.data), "chdg_decoder_concealed_fields")
+        return out
 
     def close(self) -> None:
         if self._h:

@@ -683,3 +683,24 @@ CHD_API chd_status_t chd_decode_frames_async(chd_decoder_t *d, const int64_t *in
     }
     return CHD_OK;
 }
+
+// ---- concealed fields (no counterpart in the reference ABI) ---------------
+
+CHD_API int chdg_decoder_concealed_fields(chd_decoder_t *d, int64_t frame_index, uint16_t *out)
+{
+    if (d == nullptr || out == nullptr) return fail(CHD_E_INVALID_ARG, "chdg_decoder_concealed_fields: null argument");
+    if (const chd_status_t s = check_decodable(d, "chdg_decoder_concealed_fields"); s != CHD_OK) return s;
+    std::lock_guard<std::mutex> lock(d->syncMutex);
+    if (frame_index < 0 || frame_index >= d->numFrames)
+        return fail(CHD_E_OUT_OF_RANGE, "chdg_decoder_concealed_fields: frame_index out of range");
+    cudaSetDevice(d->device);
+    FramePipeline &p = *d->syncPipe;
+    p.set_dropout(decode_dropout_settings(d));
+    const int rc = p.conceal_frame(frame_index, out);
+    if (rc != CHD_OK) {
+        if (rc != CHD_E_OUT_OF_RANGE)
+            chd::detail::set_last_error("chdg_decoder_concealed_fields: " + chd::detail::get_last_error());
+        return rc;
+    }
+    return CHD_OK;
+}

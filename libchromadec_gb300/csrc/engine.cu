@@ -142,7 +142,7 @@ int Engine::init(const chdg_geometry &g, const chdg_config &c)
     return 0;
 }
 
-int Engine::init_static(const chdg_geometry &g, const chdg_config &c, float *thr_table_dev)
+int Engine::init_static(const chdg_geometry &g, const chdg_config &c, float *thr_table_dev, cudaStream_t s)
 {
     g_ = g;
     c_ = c;
@@ -183,8 +183,12 @@ int Engine::init_static(const chdg_geometry &g, const chdg_config &c, float *thr
             tab[3 * i + 1] = (float)v;
             tab[3 * i + 2] = (float)(v - (double)(float)v);
         }
-        if ((e = cudaMemcpy(thr_table_dev, tab, sizeof(tab), cudaMemcpyHostToDevice)) != cudaSuccess)
-            return cuda_fail("cudaMemcpy", e);
+        // On the caller's stream: a decode still queued there reads the table
+        // of its own call before this copy replaces it. The source is
+        // pageable, so the call returns once it has been staged and the stack
+        // array may go.
+        if ((e = cudaMemcpyAsync(thr_table_dev, tab, sizeof(tab), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+            return cuda_fail("cudaMemcpyAsync", e);
         thr_dev_ = thr_table_dev;
     }
     stats_dev_ = nullptr;

@@ -23,8 +23,9 @@ public:
     int init(const chdg_geometry &g, const chdg_config &c);
     // Allocation-free set-up and decode (used by chdg_decode_device_static):
     // the per-bin threshold table and the chroma scratch are caller-provided
-    // device memory; nothing is allocated and no counters are kept.
-    int init_static(const chdg_geometry &g, const chdg_config &c, float *thr_table_dev);
+    // device memory; nothing is allocated and no counters are kept. A per-bin
+    // table is uploaded on `s`, ordered with that stream's earlier decodes.
+    int init_static(const chdg_geometry &g, const chdg_config &c, float *thr_table_dev, cudaStream_t s);
     int decode_scratch(const uint16_t *fields, long long stride, int nfields, int fb, int fe, void *out,
                        float *scratch, size_t scratch_floats, cudaStream_t s);
     static size_t scratch_floats_for(const chdg_geometry &g, int nframes);

@@ -211,6 +211,137 @@ int FramePipeline::upload_window(int slot, int64_t w0, int64_t w1)
     return CHD_OK;
 }
 
+// The window fields of frames [w0, w1) into slot `slot`, with the dropout
+// plans of those frames and the extra-source fields they read, all on copy_.
+// The slot's plan buffers must be idle (their last upload complete).
+int FramePipeline::upload_batch(int slot, int64_t w0, int64_t w1, int &nplan)
+{
+    cudaError_t e;
+    nplan = 0;
+    std::vector<ExtraField> extFields;   // the batch's extra-source fields, in buffer order
+    size_t nops = 0;
+    std::vector<const FramePlan *> plans;
+    std::vector<int> planFrames;
+    if (drop_.enabled) {
+        for (int64_t w = w0; w < w1; w++) {
+            const FramePlan &p = plan_for(w);
+            if (!p.ops.empty()) {
+                plans.push_back(&p);
+                planFrames.push_back((int)(2 * (w - w0)));
+                nops += p.ops.size();
+            }
+        }
+        nplan = (int)plans.size();
+        if (nops > ops_cap_ || (size_t)(2 * nplan + 1) > idx_cap_) {
+            cudaStreamSynchronize(comp_);
+            cudaStreamSynchronize(copy_);
+            cudaStreamSynchronize(d2h_);
+            for (int s = 0; s < 2; s++) {
+                if (h_ops_[s]) cudaFreeHost(h_ops_[s]);
+                if (d_ops_[s]) cudaFree(d_ops_[s]);
+                if (h_idx_[s]) cudaFreeHost(h_idx_[s]);
+                if (d_idx_[s]) cudaFree(d_idx_[s]);
+                h_ops_[s] = d_ops_[s] = nullptr;
+                h_idx_[s] = d_idx_[s] = nullptr;
+            }
+            ops_cap_ = std::max<size_t>(nops * 2, 1024);
+            idx_cap_ = std::max<size_t>((size_t)(2 * nplan + 1) * 2, 256);
+            for (int s = 0; s < 2; s++) {
+                if (cudaMallocHost(&h_ops_[s], ops_cap_ * sizeof(DropOp)) != cudaSuccess ||
+                    cudaMalloc(&d_ops_[s], ops_cap_ * sizeof(DropOp)) != cudaSuccess ||
+                    cudaMallocHost(&h_idx_[s], idx_cap_ * sizeof(int)) != cudaSuccess ||
+                    cudaMalloc(&d_idx_[s], idx_cap_ * sizeof(int)) != cudaSuccess)
+                    return cuda_status("dropout plan buffers", cudaErrorMemoryAllocation);
+            }
+        }
+        size_t o = 0;
+        extFields.clear();
+        std::map<std::pair<const Capture *, int32_t>, int32_t> extIndex;
+        auto ext_slot = [&](const FramePlan &pl, int32_t k) -> int32_t {
+            if (k < 0) return -1;
+            const ExtraField &xf = pl.extras[(size_t)k];
+            auto it = extIndex.find({xf.cap, xf.seq});
+            if (it != extIndex.end()) return it->second;
+            const int32_t idx = (int32_t)extFields.size();
+            extFields.push_back(xf);
+            extIndex.emplace(std::make_pair(xf.cap, xf.seq), idx);
+            return idx;
+        };
+        for (int p = 0; p < nplan; p++) {
+            h_idx_[slot][p] = planFrames[p];
+            h_idx_[slot][nplan + p] = (int)o;
+            for (const DropOp &op : plans[p]->ops) {
+                DropOp d = op;
+                d.srcExtra = ext_slot(*plans[p], op.srcExtra);
+                d.chrExtra = (op.mode == 2) ? ext_slot(*plans[p], op.chrExtra) : -1;
+                h_ops_[slot][o++] = d;
+            }
+        }
+        h_idx_[slot][2 * nplan] = (int)o;
+    }
+    if (const int rc = upload_window(slot, w0, w1); rc != CHD_OK) return rc;
+    if (!extFields.empty()) {
+        if (extFields.size() > ext_cap_) {
+            cudaStreamSynchronize(comp_);
+            cudaStreamSynchronize(copy_);
+            for (int s = 0; s < 2; s++) {
+                if (dext_[s]) cudaFree(dext_[s]);
+                dext_[s] = nullptr;
+            }
+            ext_cap_ = std::max<size_t>(extFields.size() * 2, 8);
+            for (int s = 0; s < 2; s++)
+                if ((e = cudaMalloc(&dext_[s], ext_cap_ * (size_t)dstride_ * 2)) != cudaSuccess)
+                    return cuda_status("extra source fields", e);
+        }
+        const size_t fbytes = flen_ * 2;
+        for (size_t k = 0; k < extFields.size(); k++) {
+            const ExtraField &xf = extFields[k];
+            const uint16_t *src = xf.cap->fieldData(xf.seq);
+            if (src == nullptr) {
+                chd::detail::set_last_error("chromadec_gb300: extra source field " + std::to_string(xf.seq) +
+                                            " is outside its .tbc file");
+                return CHD_E_INTERNAL;
+            }
+            uint16_t *dst = dext_[slot] + k * (size_t)dstride_;
+            if (xf.shifted) {   // shiftSecondField (src/decoders/source_field.cpp:51-57)
+                if ((e = cudaMemcpyAsync(dst, src + 2, fbytes - 4, cudaMemcpyHostToDevice, copy_)) != cudaSuccess)
+                    return cuda_status("H2D", e);
+                if (fill_samples(dst + flen_ - 2, 2, xf.black, copy_) != 0)
+                    return cuda_status("black tail", cudaGetLastError());
+            } else if ((e = cudaMemcpyAsync(dst, src, fbytes, cudaMemcpyHostToDevice, copy_)) != cudaSuccess) {
+                return cuda_status("H2D", e);
+            }
+        }
+    }
+    if (nplan > 0) {
+        cudaMemcpyAsync(d_ops_[slot], h_ops_[slot], nops * sizeof(DropOp), cudaMemcpyHostToDevice, copy_);
+        cudaMemcpyAsync(d_idx_[slot], h_idx_[slot], (2 * nplan + 1) * sizeof(int), cudaMemcpyHostToDevice, copy_);
+    }
+    return CHD_OK;
+}
+
+// Frame `frame`'s two window fields after concealment, exactly as the
+// decode would hand them to the transform: the window of that one frame is
+// uploaded into slot 0, its plan applied by the concealment kernel, and the
+// two fields copied back (window order: slot 0 first).
+int FramePipeline::conceal_frame(int64_t frame, uint16_t *host_out)
+{
+    if (frame < 0 || frame >= nframes_) return CHD_E_OUT_OF_RANGE;
+    cudaError_t e;
+    for (cudaStream_t s : {comp_, copy_, d2h_})
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_status("sync", e);
+    int nplan = 0;
+    if (const int rc = upload_batch(0, frame, frame + 1, nplan); rc != CHD_OK) return rc;
+    if (nplan > 0 && dropout_apply(dwin_[0], dstride_, cap_->vp().fieldWidth, d_idx_[0], d_ops_[0], d_idx_[0] + nplan,
+                                   nplan, dext_[0], copy_) != 0)
+        return cuda_status("dropout kernel", cudaGetLastError());
+    if ((e = cudaMemcpy2DAsync(host_out, flen_ * 2, dwin_[0], (size_t)dstride_ * 2, flen_ * 2, 2,
+                               cudaMemcpyDeviceToHost, copy_)) != cudaSuccess)
+        return cuda_status("D2H", e);
+    if ((e = cudaStreamSynchronize(copy_)) != cudaSuccess) return cuda_status("sync", e);
+    return CHD_OK;
+}
+
 int FramePipeline::decode(int64_t a, int64_t b, const Deliver &deliver, const std::function<bool()> &cancelled,
                           FramePlan *stats)
 {
@@ -223,7 +354,6 @@ int FramePipeline::decode(int64_t a, int64_t b, const Deliver &deliver, const st
     Pending prev, pendingOut;
     bool havePrev = false;
     const size_t fb = eng_.frame_bytes();
-    std::vector<ExtraField> extFields;   // this batch's extra-source fields, in buffer order
     cudaError_t e;
     // Batch boundaries: full batches in the middle, short ones at both ends,
     // so the first upload and the last download -- the parts no kernel
@@ -268,106 +398,8 @@ int FramePipeline::decode(int64_t a, int64_t b, const Deliver &deliver, const st
             cudaStreamWaitEvent(copy_, ev_comp_[slot], 0);
             if ((e = cudaEventSynchronize(ev_h2d_[slot])) != cudaSuccess) return cuda_status("sync", e);
         }
-        // dropout plans of the window's frames
         int nplan = 0;
-        size_t nops = 0;
-        std::vector<const FramePlan *> plans;
-        std::vector<int> planFrames;
-        if (drop_.enabled) {
-            for (int64_t w = w0; w < w1; w++) {
-                const FramePlan &p = plan_for(w);
-                if (!p.ops.empty()) {
-                    plans.push_back(&p);
-                    planFrames.push_back((int)(2 * (w - w0)));
-                    nops += p.ops.size();
-                }
-            }
-            nplan = (int)plans.size();
-            if (nops > ops_cap_ || (size_t)(2 * nplan + 1) > idx_cap_) {
-                cudaStreamSynchronize(comp_);
-                cudaStreamSynchronize(copy_);
-                cudaStreamSynchronize(d2h_);
-                for (int s = 0; s < 2; s++) {
-                    if (h_ops_[s]) cudaFreeHost(h_ops_[s]);
-                    if (d_ops_[s]) cudaFree(d_ops_[s]);
-                    if (h_idx_[s]) cudaFreeHost(h_idx_[s]);
-                    if (d_idx_[s]) cudaFree(d_idx_[s]);
-                    h_ops_[s] = d_ops_[s] = nullptr;
-                    h_idx_[s] = d_idx_[s] = nullptr;
-                }
-                ops_cap_ = std::max<size_t>(nops * 2, 1024);
-                idx_cap_ = std::max<size_t>((size_t)(2 * nplan + 1) * 2, 256);
-                for (int s = 0; s < 2; s++) {
-                    if (cudaMallocHost(&h_ops_[s], ops_cap_ * sizeof(DropOp)) != cudaSuccess ||
-                        cudaMalloc(&d_ops_[s], ops_cap_ * sizeof(DropOp)) != cudaSuccess ||
-                        cudaMallocHost(&h_idx_[s], idx_cap_ * sizeof(int)) != cudaSuccess ||
-                        cudaMalloc(&d_idx_[s], idx_cap_ * sizeof(int)) != cudaSuccess)
-                        return cuda_status("dropout plan buffers", cudaErrorMemoryAllocation);
-                }
-            }
-            size_t o = 0;
-            extFields.clear();
-            std::map<std::pair<const Capture *, int32_t>, int32_t> extIndex;
-            auto ext_slot = [&](const FramePlan &pl, int32_t k) -> int32_t {
-                if (k < 0) return -1;
-                const ExtraField &xf = pl.extras[(size_t)k];
-                auto it = extIndex.find({xf.cap, xf.seq});
-                if (it != extIndex.end()) return it->second;
-                const int32_t idx = (int32_t)extFields.size();
-                extFields.push_back(xf);
-                extIndex.emplace(std::make_pair(xf.cap, xf.seq), idx);
-                return idx;
-            };
-            for (int p = 0; p < nplan; p++) {
-                h_idx_[slot][p] = planFrames[p];
-                h_idx_[slot][nplan + p] = (int)o;
-                for (const DropOp &op : plans[p]->ops) {
-                    DropOp d = op;
-                    d.srcExtra = ext_slot(*plans[p], op.srcExtra);
-                    d.chrExtra = (op.mode == 2) ? ext_slot(*plans[p], op.chrExtra) : -1;
-                    h_ops_[slot][o++] = d;
-                }
-            }
-            h_idx_[slot][2 * nplan] = (int)o;
-        }
-        if (const int rc = upload_window(slot, w0, w1); rc != CHD_OK) return rc;
-        if (!extFields.empty()) {
-            if (extFields.size() > ext_cap_) {
-                cudaStreamSynchronize(comp_);
-                cudaStreamSynchronize(copy_);
-                for (int s = 0; s < 2; s++) {
-                    if (dext_[s]) cudaFree(dext_[s]);
-                    dext_[s] = nullptr;
-                }
-                ext_cap_ = std::max<size_t>(extFields.size() * 2, 8);
-                for (int s = 0; s < 2; s++)
-                    if ((e = cudaMalloc(&dext_[s], ext_cap_ * (size_t)dstride_ * 2)) != cudaSuccess)
-                        return cuda_status("extra source fields", e);
-            }
-            const size_t fbytes = flen_ * 2;
-            for (size_t k = 0; k < extFields.size(); k++) {
-                const ExtraField &xf = extFields[k];
-                const uint16_t *src = xf.cap->fieldData(xf.seq);
-                if (src == nullptr) {
-                    chd::detail::set_last_error("chromadec_gb300: extra source field " + std::to_string(xf.seq) +
-                                                " is outside its .tbc file");
-                    return CHD_E_INTERNAL;
-                }
-                uint16_t *dst = dext_[slot] + k * (size_t)dstride_;
-                if (xf.shifted) {   // shiftSecondField (src/decoders/source_field.cpp:51-57)
-                    if ((e = cudaMemcpyAsync(dst, src + 2, fbytes - 4, cudaMemcpyHostToDevice, copy_)) != cudaSuccess)
-                        return cuda_status("H2D", e);
-                    if (fill_samples(dst + flen_ - 2, 2, xf.black, copy_) != 0)
-                        return cuda_status("black tail", cudaGetLastError());
-                } else if ((e = cudaMemcpyAsync(dst, src, fbytes, cudaMemcpyHostToDevice, copy_)) != cudaSuccess) {
-                    return cuda_status("H2D", e);
-                }
-            }
-        }
-        if (nplan > 0) {
-            cudaMemcpyAsync(d_ops_[slot], h_ops_[slot], nops * sizeof(DropOp), cudaMemcpyHostToDevice, copy_);
-            cudaMemcpyAsync(d_idx_[slot], h_idx_[slot], (2 * nplan + 1) * sizeof(int), cudaMemcpyHostToDevice, copy_);
-        }
+        if (const int rc = upload_batch(slot, w0, w1, nplan); rc != CHD_OK) return rc;
         cudaEventRecord(ev_h2d_[slot], copy_);
         nplans[bi] = nplan;
         return CHD_OK;

@@ -68,6 +68,10 @@ public:
     int decode(int64_t a, int64_t b, const Deliver &deliver, const std::function<bool()> &cancelled,
                FramePlan *stats);
 
+    // Frame `frame`'s two fields (window order) after concealment, as the
+    // decode feeds them to the transform, into host_out (2 x field samples).
+    int conceal_frame(int64_t frame, uint16_t *host_out);
+
     size_t frame_bytes() const { return eng_.frame_bytes(); }
     Engine &engine() { return eng_; }
     int num_frames() const { return nframes_; }
@@ -75,6 +79,9 @@ public:
 private:
     // Enqueue the window fields of frames [w0, w1) into dwin_[slot] on copy_.
     int upload_window(int slot, int64_t w0, int64_t w1);
+    // upload_window plus the frames' dropout plans and the extra-source
+    // fields they read; nplan = frames with a plan.
+    int upload_batch(int slot, int64_t w0, int64_t w1, int &nplan);
     const FramePlan &plan_for(int64_t frame);   // cached, window frame (0-based)
     // A pinned chunk of at least `bytes`, reused once every frame borrowing
     // from it has been freed.

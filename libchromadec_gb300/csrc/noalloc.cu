@@ -2,18 +2,22 @@
 //
 // The regular entry points size their chroma scratch on demand with
 // cudaMalloc. This variant runs the same 3D transform and demodulator
-// kernels with their scratch in a file-scope __device__ array instead, for
+// kernels with their scratch in file-scope __device__ arrays instead, for
 // callers that cannot allocate device memory on the decode path: hosts whose
 // device memory belongs to their own allocator or budget (a framework's
 // caching allocator, a media server with a fixed pool), and latency-critical
 // playback loops where cudaMalloc's implicit device-wide synchronisation
 // would stall other streams.
 //
-// The array is a fixed 8-frame chroma scratch (4 overlap planes x 16 fields x
-// 288 x 948 FP32 at the default 948x576 active picture, 69.9 MB) that every
-// GPU loading the library holds until the process exits. Calls with more
-// frames, or with a larger active picture than fits, are rejected.
-#include <cstring>
+// Static arrays, held by every GPU that loads the library until the process
+// exits (sizes at the default 948x576 active picture, 4,440 tile positions):
+//   chroma scratch   4 overlap planes x 16 fields x 288 x 948 FP32   69.9 MB
+//   decision records 133,200 x 80 B (every kx group of an 8-frame call) 10.7 MB
+//   work-item list   2 x 133,200 x 4 B                                  1.1 MB
+//   per-bin table    768 x 3 FP32, two counters
+// in all 81.6 MB. Calls with more than 8 frames, or with a picture whose
+// planes or tile grid do not fit these arrays, are rejected.
+#include <mutex>
 #include <string>
 
 #include <cuda_runtime.h>
@@ -26,13 +30,16 @@
 namespace {
 
 constexpr int kStaticMaxFrames = 8;
+// 4 overlap planes x 2 fields per frame x 288 active field rows x 948 samples
 constexpr size_t kStaticScratchFloats = (size_t)4 * 2 * kStaticMaxFrames * 288 * 948;
+// Guard-band decision records: every kx group of every step of an 8-frame
+// call over the default picture's 4,440 tile positions (one walk chunk).
+constexpr int kStaticTiles = 120 * 37;
+constexpr unsigned long long kStaticRecords = tpal::tp3_unc_capacity(kStaticTiles, kStaticMaxFrames, 1);
+static_assert(kStaticRecords == 133200ull, "records of an 8-frame call over 4,440 tile positions");
+static_assert(sizeof(tpal::UncRecord) == 80, "decision record layout");
 
 // Shared by every call on a device; holds the previous call's chroma planes.
-// guard-band decision records of an 8-frame call (every kx group of the
-// default 4,440 tile positions, with room to spare) and the work-item list
-constexpr unsigned long long kStaticRecords = 160000;
-
 static __device__ __align__(256) float g_static_scratch[kStaticScratchFloats];
 static __device__ __align__(256) float g_static_thresholds[3 * 768];
 static __device__ __align__(256) tpal::UncRecord g_static_records[kStaticRecords];
@@ -44,36 +51,45 @@ struct DeviceSymbols {
     float *thresholds = nullptr;
     void *records = nullptr;
     unsigned *items = nullptr, *counters = nullptr;
+    cudaError_t status = cudaSuccess;
 };
 constexpr int kMaxDevices = 64;
 static DeviceSymbols g_symbols[kMaxDevices];
+static std::once_flag g_symbols_once[kMaxDevices];
 
 // Once per device, with that device current: the device addresses of the
-// static arrays (host code cannot take them from the symbols directly).
+// static arrays (in host code the symbols name host-side stand-ins, not
+// device memory). std::call_once makes concurrent first calls on one device
+// wait for a single resolution and see all of its results.
 int resolve_symbols(int device, DeviceSymbols &out)
 {
     if (device < 0 || device >= kMaxDevices) {
         chd::detail::set_last_error("chdg_decode_device_static: device index out of range");
         return CHDG_E_INVALID_ARG;
     }
-    DeviceSymbols &d = g_symbols[device];
-    if (d.scratch == nullptr) {
+    std::call_once(g_symbols_once[device], [device]() {
+        DeviceSymbols d;
         void *p = nullptr, *q = nullptr, *r = nullptr, *f = nullptr, *c = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
         if (e == cudaSuccess) e = cudaGetSymbolAddress(&q, g_static_thresholds);
         if (e == cudaSuccess) e = cudaGetSymbolAddress(&r, g_static_records);
         if (e == cudaSuccess) e = cudaGetSymbolAddress(&f, g_static_items);
         if (e == cudaSuccess) e = cudaGetSymbolAddress(&c, g_static_counters);
-        if (e != cudaSuccess) {
-            chd::detail::set_last_error(std::string("chdg_decode_device_static: cudaGetSymbolAddress: ") +
-                                        cudaGetErrorString(e));
-            return CHDG_E_CUDA;
+        d.status = e;
+        if (e == cudaSuccess) {
+            d.scratch = static_cast<float *>(p);
+            d.thresholds = static_cast<float *>(q);
+            d.records = r;
+            d.items = static_cast<unsigned *>(f);
+            d.counters = static_cast<unsigned *>(c);
         }
-        d.thresholds = static_cast<float *>(q);
-        d.records = r;
-        d.items = static_cast<unsigned *>(f);
-        d.counters = static_cast<unsigned *>(c);
-        d.scratch = static_cast<float *>(p);
+        g_symbols[device] = d;
+    });
+    const DeviceSymbols &d = g_symbols[device];
+    if (d.status != cudaSuccess) {
+        chd::detail::set_last_error(std::string("chdg_decode_device_static: cudaGetSymbolAddress: ") +
+                                    cudaGetErrorString(d.status));
+        return CHDG_E_CUDA;
     }
     out = d;
     return 0;
@@ -90,14 +106,18 @@ extern "C" int chdg_decode_device_static(const chdg_geometry *g, const chdg_conf
         chd::detail::set_last_error("chdg_decode_device_static: null geometry or config");
         return CHDG_E_INVALID_ARG;
     }
-    if (frame_end - frame_begin > kStaticMaxFrames) {
+    if (frame_begin < 0 || frame_end < frame_begin) {
+        chd::detail::set_last_error("chdg_decode_device_static: frame range must satisfy 0 <= frame_begin <= frame_end");
+        return CHDG_E_INVALID_ARG;
+    }
+    const int64_t nframes = (int64_t)frame_end - (int64_t)frame_begin;
+    if (nframes > kStaticMaxFrames) {
         chd::detail::set_last_error("chdg_decode_device_static: at most " + std::to_string(kStaticMaxFrames) +
                                     " frames per call (the static chroma scratch holds " +
                                     std::to_string(kStaticMaxFrames) + " frames)");
         return CHDG_E_INVALID_ARG;
     }
-    if (chdg::Engine::scratch_floats_for(*g, frame_end > frame_begin ? frame_end - frame_begin : 0) >
-        kStaticScratchFloats) {
+    if (chdg::Engine::scratch_floats_for(*g, (int)nframes) > kStaticScratchFloats) {
         chd::detail::set_last_error("chdg_decode_device_static: active picture too large for the static scratch");
         return CHDG_E_INVALID_ARG;
     }
@@ -110,10 +130,11 @@ extern "C" int chdg_decode_device_static(const chdg_geometry *g, const chdg_conf
     DeviceSymbols sym;
     if (const int rc = resolve_symbols(device, sym); rc != 0) return rc;
     chdg::Engine eng;
-    int rc = eng.init_static(*g, *c, sym.thresholds);
+    int rc = eng.init_static(*g, *c, sym.thresholds, (cudaStream_t)stream);
     eng.set_static_decisions(sym.records, sym.items, kStaticRecords, sym.counters);
     // Every chroma sample the demodulator reads is written by the transform
-    // in the same call, so the scratch needs no clearing.
+    // in the same call, so the scratch needs no clearing; the decision
+    // counters are zeroed on the stream before each transform.
     if (rc == 0)
         rc = eng.decode_scratch(d_fields, field_stride, nfields, frame_begin, frame_end, d_out, sym.scratch,
                                 kStaticScratchFloats, (cudaStream_t)stream);

@@ -121,7 +121,7 @@ int tp3_launch(const T3Params &p, cudaStream_t stream, int max_blocks = 0);
 // tp3_launch; the counters are zeroed before it).
 int tp3_resolve_launch(const T3Params &p, cudaStream_t stream);
 // Records one launch can write at most: every kx group of every step.
-inline unsigned long long tp3_unc_capacity(int ntiles, int frames, int nchunks)
+constexpr unsigned long long tp3_unc_capacity(int ntiles, int frames, int nchunks)
 {
     return (unsigned long long)ntiles * (unsigned long long)(frames + 2 * nchunks) * 3ull;
 }

@@ -77,10 +77,12 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
-def build_reference(ref_root: str = "/root/reference") -> Optional[str]:
-    """Compile the reference's own hot-path sources into oracle/_ref (only
-    where the reference checkout exists)."""
-    if not os.path.isdir(os.path.join(ref_root, "src", "decoders", "palcolour")):
+def build_reference(ref_root: Optional[str] = None) -> Optional[str]:
+    """Compile the reference's own hot-path sources into oracle/_ref from the
+    reference checkout at ``ref_root`` (default: the CHROMADEC_REFERENCE
+    environment variable); None when no checkout is given or found."""
+    ref_root = ref_root or os.environ.get("CHROMADEC_REFERENCE")
+    if not ref_root or not os.path.isdir(os.path.join(ref_root, "src", "decoders", "palcolour")):
         return None
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}"], check=True)
     return REF_HARNESS

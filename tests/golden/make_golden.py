@@ -9,7 +9,7 @@ are regenerated from their seeds by the tests, and their own SHA-256 is
 recorded too, so a changed generator is told apart from a changed oracle.
 
 Usage (needs the reference checkout, so it runs where that exists):
-    python tests/golden/make_golden.py [--ref /path/to/reference]
+    python tests/golden/make_golden.py --ref /path/to/reference
 """
 from __future__ import annotations
 
@@ -89,11 +89,12 @@ def run_case(harness: str, case: dict, tmp: str) -> dict:
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("CHROMADEC_REFERENCE"),
+                    help="reference checkout (default: $CHROMADEC_REFERENCE)")
     a = ap.parse_args()
     harness = oracle.build_reference(a.ref)
     if harness is None:
-        raise SystemExit("reference checkout not found at " + a.ref)
+        raise SystemExit(f"reference checkout not found at {a.ref!r} (pass --ref or set CHROMADEC_REFERENCE)")
     res = {}
     with tempfile.TemporaryDirectory() as tmp:
         for name, case in CASES.items():

@@ -6,7 +6,7 @@ the same spectra in FP64 (numpy's FFT over the reference's tile,
 TransformPal3D::forwardFFTTile, src/decoders/palcolour/transform_pal_3d.cpp:
 168-202) and the threshold decision of every visited bin
 (TransformPal3D::applyFilter, transform_pal_3d.cpp:249-333). It is
-measurement code: the decoder never calls it.
+measurement code for the tests and the benchmark: the decoder never calls it.
 """
 from __future__ import annotations
 

@@ -99,6 +99,30 @@ def test_dropout_correction_matches_oracle(cuda, tbc):
     assert d.last_dropout_stats() == (0, 0, 0)
 
 
+def test_concealed_fields_match_oracle_byte_for_byte(cuda, tbc):
+    """The composite the transform reads after the GPU concealment kernel,
+    compared sample for sample with the oracle's DropoutCorrector
+    (src/dropout/dropout_corrector.cpp:50-157, 469-530): every mode, every
+    frame, every sample of both fields."""
+    path, cap = tbc
+    v, d = _decoder(path)
+    flat = O.flatten_dropouts(cap.dropouts)
+    p = O.params(3, O.FMT_P16)
+    changed = 0
+    for overcorrect, intra in ((False, False), (True, False), (False, True)):
+        d.set_dropout(True, overcorrect, intra)
+        for k in range(NF // 2):
+            got = d.concealed_fields(k)
+            ref, st = O.dropout_correct_frame(p, cap.fields, k, flat, overcorrect=overcorrect, intra=intra)
+            assert got.dtype == np.uint16 and got.shape == ref.shape
+            bad = np.argwhere(got != ref)
+            assert bad.size == 0, (k, overcorrect, intra, bad[:5])
+            changed += int((got != cap.fields[2 * k:2 * k + 2]).sum())
+    assert changed > 0                                    # the kernel did conceal something
+    d.set_dropout(False)
+    assert np.array_equal(d.concealed_fields(2), cap.fields[4:6])
+
+
 def test_async_delivery_cancel_and_errors(cuda, tbc):
     path, cap = tbc
     v, d = _decoder(path)

@@ -1,10 +1,12 @@
 """The 500-field benchmark workload at full size, and capture-shape edge cases.
 
-Full size: the oracle cannot decode 250 3D frames in test time, so parity is
-checked on sampled frames (both ends of the capture, where the 3D window is
-padded, and the middle), and the rest through properties that hold at any
-size: the device path is deterministic (bit-identical on repeat), and the
-reference-facing ABI over a .tbc gives exactly the device path's frames.
+Full size: every one of the 250 frames of the seed-1 panning stream the
+benchmark decodes is compared with the oracle, in yuv444p16 (within +-1 LSB
+on every sample; the share of samples that differ at all is reported and
+bounded) and in yuv444ps (within 1e-4), and the same stream goes through
+properties that hold at any size: the device path is deterministic
+(bit-identical on repeat), and the reference-facing ABI over a .tbc gives
+exactly the device path's frames.
 
 Edge cases (as SourceField::loadFields / LdDecodeMetaData pair fields,
 src/decoders/source_field.cpp:68-171, src/metadata/core.cpp:1092-1190): a
@@ -12,6 +14,7 @@ capture that starts with a second field, an odd field count, a one-frame
 3D capture, an empty capture.
 """
 import json
+import os
 
 import numpy as np
 import pytest
@@ -34,7 +37,7 @@ def workload():
     return synth.make_capture(500, cfg)
 
 
-def test_full_workload_determinism_abi_and_sampled_parity(cuda, workload, tmp_path_factory):
+def test_full_workload_determinism_and_abi(cuda, workload, tmp_path_factory):
     torch = cuda
     from libchromadec_gb300 import device as D
     fields = workload.fields
@@ -60,9 +63,58 @@ def test_full_workload_determinism_abi_and_sampled_parity(cuda, workload, tmp_pa
     for _, i, planes in res:
         assert np.array_equal(planes, dev[i]), i           # same kernels, same frames
 
-    for k in (0, 1, 2, 124, 125, 247, 248, 249):
-        ref, _ = O.decode_frames(O.params(3, O.FMT_P16), fields, k, 1, threads=8)
-        _p16_close(dev[k], ref[0])
+
+
+# Share of yuv444p16 samples allowed to differ from the FP64 oracle by one
+# code (none may differ by more). The residue comes from FP32 rounding of
+# values that sit on a rounding boundary of the quantiser.
+P16_DIFFER_MAX = 0.0025
+
+
+def _oracle_chunks(fmt, fields, nfr, step=25):
+    threads = os.cpu_count() or 8
+    for a in range(0, nfr, step):
+        ref, _ = O.decode_frames(O.params(3, fmt), fields, a, min(step, nfr - a), threads=threads)
+        yield a, ref
+
+
+def test_full_workload_every_frame_matches_oracle(cuda, workload):
+    """All 250 frames of the 500-field stream, both output formats."""
+    torch = cuda
+    from libchromadec_gb300 import device as D
+    fields = workload.fields
+    n = fields.shape[0]
+    nfr = n // 2
+    dfields = torch.from_numpy(fields.reshape(n, -1).view(np.int16)).cuda()
+    stats = {}
+    for fmt, ofmt, dt in ((D.FMT_P16, O.FMT_P16, torch.int16), (D.FMT_PS, O.FMT_PS, torch.float32)):
+        eng = D.Engine(D.default_geometry(), D.default_config(kind=D.KIND_TRANSFORM_3D, fmt=fmt))
+        out = torch.empty((nfr, 3, 576, 948), dtype=dt, device="cuda")
+        eng.decode(dfields, 0, nfr, out)
+        torch.cuda.synchronize()
+        got = out.cpu().numpy()
+        eng.close()
+        del out
+        if fmt == D.FMT_P16:
+            got = got.view(np.uint16)
+            differ = np.zeros(3, dtype=np.int64)
+            for a, ref in _oracle_chunks(ofmt, fields, nfr):
+                d = np.abs(got[a:a + ref.shape[0]].astype(np.int32) - ref.astype(np.int32))
+                assert d.max() <= 1, (a, int(d.max()))
+                differ += (d > 0).sum(axis=(0, 2, 3))
+            total = nfr * 576 * 948
+            frac = differ / total
+            stats["p16_differ_by_plane"] = frac.tolist()
+            stats["p16_differ"] = float(differ.sum() / (3 * total))
+        else:
+            worst = 0.0
+            for a, ref in _oracle_chunks(ofmt, fields, nfr):
+                e = float(np.abs(got[a:a + ref.shape[0]].astype(np.float64) - ref.astype(np.float64)).max())
+                worst = max(worst, e)
+            stats["ps_max_abs"] = worst
+            assert worst <= 1e-4, worst
+    print("full-size parity:", json.dumps(stats))
+    assert stats["p16_differ"] <= P16_DIFFER_MAX, stats
 
 
 def _write_flags(tmp_path, fields, first_flags, name):

@@ -127,3 +127,31 @@ def test_multi_source_concealment_matches_oracle(cuda, sources, kind, overcorrec
     # the first correcting decode froze the extras
     assert L.chd_video_add_extra_source_composite(v._h, sources["b"][0].encode(), None) == abi.E_INVALID_ARG
     assert b"already run" in L.chd_last_error()
+
+
+@pytest.mark.parametrize("overcorrect,intra", [(False, False), (True, False), (False, True)])
+def test_multi_source_concealed_fields_byte_for_byte(cuda, sources, overcorrect, intra):
+    """The concealed composite itself, replacement lines drawn from the extra
+    captures, sample for sample against the oracle's multi-source corrector."""
+    names = ["a", "b", "c"]
+    ppath, pcap, _, pbp = sources["prim"]
+    v = abi.Video(ppath)
+    L = abi.lib()
+    for n in names:
+        assert L.chd_video_add_extra_source_composite(v._h, sources[n][0].encode(), None) == 0
+    extras = _oracle_extras(sources, names)
+    d = abi.Decoder(v, abi.DEC_TRANSFORM_3D)
+    d.commit()
+    d.set_dropout(True, overcorrect, intra)
+    p = O.params(3, O.FMT_P16)
+    flat = O.flatten_dropouts(pcap.dropouts)
+    from_extras = 0
+    for k in range(NF // 2):
+        got = d.concealed_fields(k)
+        ref, _ = O.dropout_correct_frame(p, pcap.fields, k, flat, overcorrect=overcorrect, intra=intra,
+                                         bpsnr=pbp, extras=extras)
+        single, _ = O.dropout_correct_frame(p, pcap.fields, k, flat, overcorrect=overcorrect, intra=intra)
+        bad = np.argwhere(got != ref)
+        assert bad.size == 0, (k, bad[:5])
+        from_extras += int((ref != single).sum())
+    assert from_extras > 0                                # some lines came from the extras

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from libchromadec_gb300 import device as D
-from libchromadec_gb300 import tc_study as T
+from tests import tc_study as T
 from tests._capture import capture
 
 pytestmark = pytest.mark.gpu
