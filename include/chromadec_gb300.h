@@ -200,6 +200,70 @@ int chdg_tc3d_operand(int32_t variant, int32_t stage, int32_t y0, int32_t split,
  * chdg_tc3d_operand are the inverse Z, Y, X coefficients. */
 int chdg_engine_set_tc_form(chdg_engine *e, int32_t variant);
 
+/* Learned form of Transform-PAL 3D (no counterpart in the reference, which
+ * decides every bin by the fixed mirror threshold of
+ * TransformPal3D::applyFilter, src/decoders/palcolour/transform_pal_3d.cpp:
+ * 249-333; its NTSC nnTransform3D decoder, src/decoders/nntransform3d/
+ * nntransform3d_pipeline_cuda.cu:160-244, is the precedent for a learned
+ * per-bin mask). A small 3D convolutional network reads each tile's
+ * log-magnitude spectrum over the bins the filter can keep -- kz 0..7,
+ * ky 0..31, kx 2..6, v = ((kx - 2) * 8 + kz) * 32 + ky, 1,280 per tile -- as
+ * two channels, f = ln(1 + |X|) / 16 at the bin and at its mirror about the
+ * carrier, and predicts the fraction p of each bin that is chroma: three
+ * 3x3x3 convolutions of 16 channels with ReLU (periodic in kz and ky, zero
+ * padded in kx), a sigmoid 1x1x1 head; BF16 weights and activations, FP32
+ * accumulation; CHDG_MASKNET_PARAMS FP32 parameters in the order W1[27][2][16],
+ * b1[16], W2[27][16][16], b2[16], W3[27][16][16], b3[16], wh[16], bh, tap
+ * t = (dz + 1) * 9 + (dy + 1) * 3 + (dkx + 1). A tile whose mean |p - 1/2|
+ * is below the confidence limit (default 0.1) takes the threshold decisions
+ * instead. Networks are trained on the GPU by these kernels: one call is a
+ * batch's forward pass, loss L = sum |p X - C|^2 / sum |X|^2 against the
+ * true chroma spectrum C, backward pass and Adam step. */
+#define CHDG_MASKNET_PARAMS 14753
+#define CHDG_MASKNET_BINS 1280
+typedef struct chdg_masknet chdg_masknet;
+int chdg_masknet_create(chdg_masknet **out);
+void chdg_masknet_free(chdg_masknet *n);
+int chdg_masknet_set_weights(chdg_masknet *n, const float *weights, int64_t count);
+int chdg_masknet_get_weights(const chdg_masknet *n, float *weights, int64_t count);
+int chdg_masknet_set_confidence(chdg_masknet *n, float limit);
+/* d_feat: ntiles x 1280 bf16 features (device); d_p: ntiles x 1280 FP32;
+ * d_fallback: ntiles bytes (1 = the tile takes the threshold) or NULL. */
+int chdg_masknet_forward(const chdg_masknet *n, const uint16_t *d_feat, int64_t ntiles, float *d_p,
+                         uint8_t *d_fallback, void *stream);
+/* One training step on a batch: d_ac holds per bin (|X|^2, Re(C conj X)) as
+ * FP32 pairs, ntiles x 1280. learning_rate 0 computes the loss and gradient
+ * only. loss (without its constant sum |C|^2 / sum |X|^2 term) and grad
+ * (CHDG_MASKNET_PARAMS floats), when not NULL, are filled after the step
+ * completes on `stream`. */
+int chdg_masknet_train_step(chdg_masknet *n, const uint16_t *d_feat, const float *d_ac, int64_t ntiles,
+                            float learning_rate, double *loss, float *grad, void *stream);
+/* Training pairs: per bin (|X|^2, Re(C conj X)) from the composite's spectrum
+ * X and the true chroma's C (FP32 complex pairs, nbins each). */
+int chdg_masknet_pairs(const float *d_spec_x, const float *d_spec_c, int64_t nbins, float *d_ac, void *stream);
+
+/* The learned form's walk passes on a device-resident capture (the engine's
+ * conventions): Z tiles T(2m) for m = frame_begin - 2 .. frame_end - 1, in
+ * that order, each over the engine's spatial tiles (chdg_tc3d_spectra's
+ * order). chdg_learned_features writes every Z tile's 1,280 features (and,
+ * when not NULL, its complex spectrum X as FP32 pairs and its FP32 threshold
+ * decisions as 0 / 1); chdg_learned_chroma decodes the separated chroma, as
+ * chdg_chroma_device does, with the given fractions (and fallback flags)
+ * applied in place of the threshold. */
+int chdg_learned_features(chdg_engine *e, const uint16_t *d_fields, int64_t field_stride, int32_t nfields,
+                          int32_t frame_begin, int32_t frame_end, uint16_t *d_feat, float *d_spec,
+                          float *d_threshold_p, void *stream);
+int chdg_learned_chroma(chdg_engine *e, const uint16_t *d_fields, int64_t field_stride, int32_t nfields,
+                        int32_t frame_begin, int32_t frame_end, const float *d_p, const uint8_t *d_fallback,
+                        float *d_chroma, void *stream);
+/* Decode with the learned form (net != NULL) or the plain form (NULL): a
+ * Transform 3D engine with a uniform threshold runs the feature pass, the
+ * network and the apply pass in place of its transform stage; the engine
+ * borrows the network. chdg_engine_learned_stats reports the tiles decoded
+ * and how many fell back to the threshold since the engine was created. */
+int chdg_engine_set_masknet(chdg_engine *e, chdg_masknet *net);
+int chdg_engine_learned_stats(chdg_engine *e, int64_t *tiles, int64_t *fallback_tiles);
+
 /* Multi-source concealment alignment (MultiSourceAlignment::
  * sourceFrameForPrimaryFrame, src/dropout/multi_source_alignment.cpp:54-71):
  * the 0-based frame of extra source `source` (1 = the first added with

@@ -108,27 +108,40 @@ __device__ __forceinline__ void item_window(const float *rw, int SW, float (&v)[
     }
 }
 
-// H.273 Round(x) = Sign(x) * Floor(Abs(x) + 0.5) then clamp (output_writer.cpp:60-76)
-__device__ __forceinline__ uint16_t h273q(float x, float lo, float hi)
+// An integer-format code (H.273 Round(x) = Sign(x) * Floor(Abs(x) + 0.5),
+// then the clamp, output_writer.cpp:52-76), zero + Round(v * (k_hi + k_lo)) for v = v_hi + v_lo,
+// without FP32 rounding at the code's magnitude: the product is formed as
+// p + e (p = v_hi k_hi rounded, e its error and the low-order terms), the
+// nearest integer n of p split off exactly, and only the remainder
+// (p - n) + e, below one in magnitude, rounded. zero is an integer, so
+// zero + n + Floor(r + 1/2) is H.273's Round of the whole sum wherever that
+// sum is non-negative; below zero both clamp to the bound lo >= 0. Returns
+// the clamped code as a float (exact).
+__device__ __forceinline__ float code_of(float zero, float v_hi, float v_lo, float k_hi, float k_lo, float lo, float hi)
 {
-    const float r = copysignf(floorf(fabsf(x) + 0.5f), x);
-    return (uint16_t)fminf(fmaxf(r, lo), hi);
+    const float p = v_hi * k_hi;
+    const float e = __fmaf_rn(v_hi, k_hi, -p) + __fmaf_rn(v_hi, k_lo, v_lo * k_hi);
+    const float n = rintf(p);
+    const float r = (p - n) + e;   // p - n is exact
+    return fminf(fmaxf(zero + n + floorf(r + 0.5f), lo), hi);
 }
 
 // Pack one sample in the output format (OutputWriter::convertLine,
 // convertToFloat, convertToFloatRGB; output_writer.cpp:402-486, 670-779).
-__device__ __forceinline__ void pack_sample(const DemodParams &P, void *out, long long frame, long long pix, float Y,
+// Luma arrives as Y - black = yb.hi + yb.lo (exact for the Transform kinds:
+// an integer composite sample minus the FP32 chroma, by two-sum).
+__device__ __forceinline__ void pack_sample(const DemodParams &P, void *out, long long frame, long long pix, df yb,
                                             float U, float V)
 {
     const long long plane = (long long)P.out_w * P.out_h;
     const long long e = frame * P.out_frame_stride + pix;
-    const float ey = (Y - (float)P.black) * P.ey_scale;
+    const float ey = (yb.hi + yb.lo) * P.ey_scale;
     switch (P.format) {
     case 0: {
         uint16_t *o = (uint16_t *)out;
-        o[e] = h273q(__fmaf_rn(219.0f * 256.0f, ey, 16.0f * 256.0f), P.y_lo, P.y_hi);
-        o[e + plane] = h273q(__fmaf_rn(224.0f * 256.0f, U * P.ecb_scale, 128.0f * 256.0f), P.c_lo, P.c_hi);
-        o[e + 2 * plane] = h273q(__fmaf_rn(224.0f * 256.0f, V * P.ecr_scale, 128.0f * 256.0f), P.c_lo, P.c_hi);
+        o[e] = (uint16_t)code_of(16.0f * 256.0f, yb.hi, yb.lo, P.qy_hi, P.qy_lo, P.y_lo, P.y_hi);
+        o[e + plane] = (uint16_t)code_of(128.0f * 256.0f, U, 0.f, P.qcb_hi, P.qcb_lo, P.c_lo, P.c_hi);
+        o[e + 2 * plane] = (uint16_t)code_of(128.0f * 256.0f, V, 0.f, P.qcr_hi, P.qcr_lo, P.c_lo, P.c_hi);
         break;
     }
     case 1: {
@@ -140,7 +153,7 @@ __device__ __forceinline__ void pack_sample(const DemodParams &P, void *out, lon
     }
     case 2: {   // interleaved R'G'B' 0..65535, truncating stores
         uint16_t *o = (uint16_t *)out + frame * P.out_frame_stride + 3 * pix;
-        const float rY = fminf(fmaxf((Y - (float)P.black) * P.rgb_y_scale, 0.f), 65535.f);
+        const float rY = fminf(fmaxf((yb.hi + yb.lo) * P.rgb_y_scale, 0.f), 65535.f);
         const float rU = U * P.rgb_uv_scale, rV = V * P.rgb_uv_scale;
         o[0] = (uint16_t)__float2uint_rz(fminf(fmaxf(__fmaf_rn(P.r_from_v, rV, rY), 0.f), 65535.f));
         o[1] = (uint16_t)__float2uint_rz(
@@ -157,7 +170,7 @@ __device__ __forceinline__ void pack_sample(const DemodParams &P, void *out, lon
         break;
     }
     case 4:
-        ((uint16_t *)out)[e] = h273q(__fmaf_rn(219.0f * 256.0f, ey, 16.0f * 256.0f), P.y_lo, P.y_hi);
+        ((uint16_t *)out)[e] = (uint16_t)code_of(16.0f * 256.0f, yb.hi, yb.lo, P.qy_hi, P.qy_lo, P.y_lo, P.y_hi);
         break;
     default:
         ((float *)out)[e] = fminf(fmaxf(ey, P.y_lo), P.y_hi);
@@ -168,16 +181,15 @@ __device__ __forceinline__ void pack_sample(const DemodParams &P, void *out, lon
 // The three outputs of one sample in the units yuv444p16 (the quantised
 // code, exact in FP32) or yuv444ps (E'Y, E'Cb, E'Cr) stores -- the
 // arithmetic of pack_sample's cases 0 and 1.
-__device__ __forceinline__ void yuv_values(const DemodParams &P, float Y, float U, float V, float &o0, float &o1,
+__device__ __forceinline__ void yuv_values(const DemodParams &P, df yb, float U, float V, float &o0, float &o1,
                                            float &o2)
 {
-    const float ey = (Y - (float)P.black) * P.ey_scale;
     if (P.format == 0) {
-        o0 = (float)h273q(__fmaf_rn(219.0f * 256.0f, ey, 16.0f * 256.0f), P.y_lo, P.y_hi);
-        o1 = (float)h273q(__fmaf_rn(224.0f * 256.0f, U * P.ecb_scale, 128.0f * 256.0f), P.c_lo, P.c_hi);
-        o2 = (float)h273q(__fmaf_rn(224.0f * 256.0f, V * P.ecr_scale, 128.0f * 256.0f), P.c_lo, P.c_hi);
+        o0 = code_of(16.0f * 256.0f, yb.hi, yb.lo, P.qy_hi, P.qy_lo, P.y_lo, P.y_hi);
+        o1 = code_of(128.0f * 256.0f, U, 0.f, P.qcb_hi, P.qcb_lo, P.c_lo, P.c_hi);
+        o2 = code_of(128.0f * 256.0f, V, 0.f, P.qcr_hi, P.qcr_lo, P.c_lo, P.c_hi);
     } else {
-        o0 = fminf(fmaxf(ey, P.y_lo), P.y_hi);
+        o0 = fminf(fmaxf((yb.hi + yb.lo) * P.ey_scale, P.y_lo), P.y_hi);
         o1 = fminf(fmaxf(U * P.ecb_scale, P.c_lo), P.c_hi);
         o2 = fminf(fmaxf(V * P.ecr_scale, P.c_lo), P.c_hi);
     }
@@ -462,7 +474,8 @@ __global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
 #pragma unroll
             for (int s = 0; s < 8; s++) {
                 const int x = base4 + xl0 + s;
-                float Y;
+                df yb;   // Y - black
+                const float cb = cv[s] - (float)P.black;   // exact: an integer sample
                 if (YNR) {
                     // doYNR: a = sum_i b_i Y[x + 12 - i], cored to +-nr_y, subtracted
                     const float *yl = ys + t * YW + kNrHalf + xl0 + s;
@@ -470,18 +483,18 @@ __global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
 #pragma unroll
                     for (int i = 0; i < 25; i++) a = __fmaf_rn(cd_nrpal[i], yl[kNrHalf - i], a);
                     a = fminf(fmaxf(a, -P.nr_y), P.nr_y);
-                    Y = yl[0] - a;
+                    yb = two_sum(yl[0] - (float)P.black, -a);
                 } else if (COMPOSITE) {
-                    Y = cv[s] - 2.0f * __fmaf_rn(PY[s], carrier_sin(x), QY[s] * carrier_cos(x));
+                    yb = two_sum(cb, -2.0f * __fmaf_rn(PY[s], carrier_sin(x), QY[s] * carrier_cos(x)));
                 } else {
-                    Y = cv[s] - v[0][s + 7];
+                    yb = two_sum(cb, -v[0][s + 7]);
                 }
                 const float U = -(PU[s] * bp + QU[s] * bq) * 2.0f;
                 const float V = vsw * -(QV[s] * bp - PV[s] * bq) * 2.0f;
                 if (vout) {
-                    yuv_values(P, Y, U, V, o0[s], o1[s], o2[s]);
+                    yuv_values(P, yb, U, V, o0[s], o1[s], o2[s]);
                 } else if (x >= P.avs && x < P.ave) {
-                    pack_sample(P, out_base, frame_slot, rowpix + (x - P.avs), Y, U, V);
+                    pack_sample(P, out_base, frame_slot, rowpix + (x - P.avs), yb, U, V);
                 }
             }
         }

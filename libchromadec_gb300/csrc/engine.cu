@@ -66,6 +66,10 @@ Engine::~Engine()
     if (unc_rec_) cudaFree(unc_rec_);
     if (rerun_) cudaFree(rerun_);
     if (counters_) cudaFree(counters_);
+    if (lfeat_) cudaFree(lfeat_);
+    if (lp_) cudaFree(lp_);
+    if (lfb_) cudaFree(lfb_);
+    if (lcount_) cudaFree(lcount_);
     for (int i = 0; i < 2; i++) {
         if (hp_fields_[i]) cudaFree(hp_fields_[i]);
         if (hp_out_[i]) cudaFree(hp_out_[i]);
@@ -275,6 +279,45 @@ int Engine::ensure_deferred(int frames, int nchunks)
     return 0;
 }
 
+void Engine::t3_params(tpal::T3Params &P, const uint16_t *fields, long long stride, int field_base, int nfields,
+                       int fb, int fe, float *partial) const
+{
+    const long long cls_stride = (long long)(fe - fb) * 2 * rows_ * cols_;
+    P.fields = fields;
+    P.field_ptrs = field_ptrs_;
+    P.field_stride = stride;
+    P.field_base = field_base;
+    P.nfields = nfields;
+    P.fw = g_.field_width;
+    P.fh = g_.field_height;
+    P.avs = g_.active_start;
+    P.ave = g_.active_end;
+    P.fafl = g_.first_active_frame_line;
+    P.lafl = g_.last_active_frame_line;
+    P.black = g_.black;
+    P.swap = c_.first_field_offset;
+    // transform_pal_3d.cpp:151-153 tile grid
+    P.tileX0 = g_.active_start - 8;
+    P.ntx = (g_.active_end - P.tileX0 + 7) / 8;
+    P.tileY0 = g_.first_active_frame_line - 16;
+    P.nty = (g_.last_active_frame_line - P.tileY0) / 16 + 1;
+    P.frame_begin = fb;
+    P.frame_end = fe;
+    P.chunk_frames = chunk_frames_;
+    P.nchunks = (fe - fb + chunk_frames_ - 1) / chunk_frames_;
+    P.partial = partial;
+    P.part_class_stride = cls_stride;
+    P.part_field_stride = (long long)rows_ * cols_;
+    P.part_row_stride = cols_;
+    P.fl_lo = fl_lo_;
+    P.t2f = t2f_;
+    P.t2hi = t2hi_;
+    P.t2lo = t2lo_;
+    P.thr_table = thr_dev_;
+    P.frame_t2 = frame_t2_;
+    P.stats = stats_dev_;
+}
+
 int Engine::run_transform(const uint16_t *fields, long long stride, int field_base, int nfields, int fb, int fe,
                           float *partial, cudaStream_t s)
 {
@@ -282,40 +325,9 @@ int Engine::run_transform(const uint16_t *fields, long long stride, int field_ba
     if (c_.kind == 6) return 0;   // the PALcolour filter demodulates the composite directly
     if (c_.kind == 8) {
         tpal::T3Params P{};
-        P.fields = fields;
-        P.field_ptrs = field_ptrs_;
-        P.field_stride = stride;
-        P.field_base = field_base;
-        P.nfields = nfields;
-        P.fw = g_.field_width;
-        P.fh = g_.field_height;
-        P.avs = g_.active_start;
-        P.ave = g_.active_end;
-        P.fafl = g_.first_active_frame_line;
-        P.lafl = g_.last_active_frame_line;
-        P.black = g_.black;
-        P.swap = c_.first_field_offset;
-        // transform_pal_3d.cpp:151-153 tile grid
-        P.tileX0 = g_.active_start - 8;
-        P.ntx = (g_.active_end - P.tileX0 + 7) / 8;
-        P.tileY0 = g_.first_active_frame_line - 16;
-        P.nty = (g_.last_active_frame_line - P.tileY0) / 16 + 1;
-        P.frame_begin = fb;
-        P.frame_end = fe;
-        P.chunk_frames = chunk_frames_;
-        P.nchunks = (fe - fb + chunk_frames_ - 1) / chunk_frames_;
-        P.partial = partial;
-        P.part_class_stride = cls_stride;
-        P.part_field_stride = (long long)rows_ * cols_;
-        P.part_row_stride = cols_;
-        P.fl_lo = fl_lo_;
-        P.t2f = t2f_;
-        P.t2hi = t2hi_;
-        P.t2lo = t2lo_;
-        P.thr_table = thr_dev_;
-        P.frame_t2 = frame_t2_;
-        P.stats = stats_dev_;
+        t3_params(P, fields, stride, field_base, nfields, fb, fe, partial);
         if (tc_variant_ >= 0) return tpal::tc3_transform(P, g_.field_height, tc_variant_, s);
+        if (net_ != nullptr) return run_learned(P, s);
         // guard-band decisions: recorded by the walk, decided by the resolve
         // pass, work items with a wrong FP32 decision walked again exactly
         if (static_) {
@@ -411,6 +423,13 @@ int Engine::run_demod(const uint16_t *fields, long long stride, int field_base, 
     D.ey_scale = (float)(1.0 / range);
     D.ecb_scale = (float)(c_.ecb_from_u / range);
     D.ecr_scale = (float)(c_.ecr_from_v / range);
+    auto split = [](double v, float &hi, float &lo) {
+        hi = (float)v;
+        lo = (float)(v - (double)hi);
+    };
+    split(219.0 * 256.0 / range, D.qy_hi, D.qy_lo);
+    split(224.0 * 256.0 * c_.ecb_from_u / range, D.qcb_hi, D.qcb_lo);
+    split(224.0 * 256.0 * c_.ecr_from_v / range, D.qcr_hi, D.qcr_lo);
     // output_writer.cpp:84-143 Y'CbCr clamp bounds
     if (fmt == 1 || fmt == 5) {
         switch (c_.clamp_mode) {
@@ -493,10 +512,126 @@ int Engine::fill_border(void *out, int nframes, cudaStream_t s)
     return e == cudaSuccess ? 0 : cuda_fail("fill", e);
 }
 
+int Engine::set_masknet(MaskNet *net)
+{
+    if (net != nullptr && (c_.kind != 8 || thr_dev_ != nullptr || static_ || tc_variant_ >= 0))
+        return arg_fail("set_masknet: the learned form is Transform 3D, plain FP32 form, uniform threshold");
+    net_ = net;
+    return 0;
+}
+
+int Engine::ensure_learned(long long ntiles)
+{
+    cudaError_t e;
+    if (lcount_ == nullptr) {
+        if ((e = cudaMalloc(&lcount_, 2 * sizeof(unsigned long long))) != cudaSuccess) {
+            lcount_ = nullptr;
+            return cuda_fail("learned counters", e);
+        }
+        cudaMemset(lcount_, 0, 2 * sizeof(unsigned long long));
+    }
+    if (ntiles <= lcap_) return 0;
+    if (lfeat_) cudaFree(lfeat_);
+    if (lp_) cudaFree(lp_);
+    if (lfb_) cudaFree(lfb_);
+    lfeat_ = nullptr;
+    lp_ = nullptr;
+    lfb_ = nullptr;
+    lcap_ = 0;
+    if ((e = cudaMalloc(&lfeat_, sizeof(uint16_t) * CHDG_MASKNET_BINS * (size_t)ntiles)) != cudaSuccess ||
+        (e = cudaMalloc(&lp_, sizeof(float) * CHDG_MASKNET_BINS * (size_t)ntiles)) != cudaSuccess ||
+        (e = cudaMalloc(&lfb_, (size_t)ntiles)) != cudaSuccess) {
+        chd::detail::set_last_error("chromadec_gb300: out of device memory for the learned form's tile buffers");
+        return CHDG_E_OOM;
+    }
+    lcap_ = ntiles;
+    return 0;
+}
+
+__global__ void sum_classes_kernel(const float *part, long long cls_stride, long long n, float *out);
+
+__global__ void count_fallback_kernel(const uint8_t *fb, long long n, unsigned long long *count)
+{
+    unsigned long long c = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        c += fb[i];
+#pragma unroll
+    for (int h = 16; h >= 1; h >>= 1) c += __shfl_xor_sync(0xffffffffu, c, h);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(count + 1, c);
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(count, (unsigned long long)n);
+}
+
+// Feature pass, network, apply pass over the Z tiles of frames [fb, fe).
+int Engine::run_learned(const tpal::T3Params &P, cudaStream_t s)
+{
+    const long long ntiles = (long long)P.ntx * P.nty * (long long)(P.frame_end - P.frame_begin + 2);
+    if (const int rc = ensure_learned(ntiles); rc != 0) return rc;
+    tpal::T3Learn L{};
+    L.feat = lfeat_;
+    L.z0 = P.frame_begin - 2;
+    if (tpal::tp3_learned_launch(P, L, 0, s) != 0) return cuda_fail("learned features", cudaGetLastError());
+    if (const int rc = net_->forward(lfeat_, ntiles, lp_, lfb_, s); rc != 0) return rc;
+    count_fallback_kernel<<<64, 256, 0, s>>>(lfb_, ntiles, lcount_);
+    L.p = lp_;
+    L.fallback = lfb_;
+    if (tpal::tp3_learned_launch(P, L, 1, s) != 0) return cuda_fail("learned apply", cudaGetLastError());
+    return 0;
+}
+
+int Engine::learned_features(const uint16_t *fields, long long stride, int nfields, int fb, int fe, uint16_t *feat,
+                             float2 *spec, float *thr_p, cudaStream_t s)
+{
+    if (c_.kind != 8) return arg_fail("learned_features: Transform 3D only");
+    if (fields == nullptr || feat == nullptr || fe < fb || stride < (long long)g_.field_width * g_.field_height)
+        return arg_fail("learned_features: bad arguments");
+    if (fe == fb) return 0;
+    tpal::T3Params P{};
+    t3_params(P, fields, stride, 0, nfields, fb, fe, nullptr);
+    tpal::T3Learn L{};
+    L.feat = feat;
+    L.spec = spec;
+    L.plain_p = thr_p;
+    L.z0 = fb - 2;
+    return tpal::tp3_learned_launch(P, L, 0, s) == 0 ? 0 : cuda_fail("learned features", cudaGetLastError());
+}
+
+int Engine::learned_chroma(const uint16_t *fields, long long stride, int nfields, int fb, int fe, const float *p,
+                           const uint8_t *fallback, float *out, cudaStream_t s)
+{
+    if (c_.kind != 8) return arg_fail("learned_chroma: Transform 3D only");
+    if (fields == nullptr || p == nullptr || fallback == nullptr || out == nullptr || fe < fb)
+        return arg_fail("learned_chroma: bad arguments");
+    if (fe == fb) return 0;
+    if (const int rc = ensure_partial(2 * (fe - fb)); rc != 0) return rc;
+    tpal::T3Params P{};
+    t3_params(P, fields, stride, 0, nfields, fb, fe, partial_);
+    tpal::T3Learn L{};
+    L.p = p;
+    L.fallback = fallback;
+    L.z0 = fb - 2;
+    if (tpal::tp3_learned_launch(P, L, 1, s) != 0) return cuda_fail("learned apply", cudaGetLastError());
+    const long long n = (long long)(fe - fb) * 2 * rows_ * cols_;
+    sum_classes_kernel<<<1024, 256, 0, s>>>(partial_, n, n, out);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? 0 : cuda_fail("sum", e);
+}
+
+int Engine::learned_stats(long long *tiles, long long *fallback_tiles)
+{
+    unsigned long long h[2] = {0, 0};
+    if (lcount_ != nullptr) {
+        cudaError_t e = cudaMemcpy(h, lcount_, sizeof(h), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail("learned stats", e);
+    }
+    if (tiles) *tiles = (long long)h[0];
+    if (fallback_tiles) *fallback_tiles = (long long)h[1];
+    return 0;
+}
+
 int Engine::set_tc_form(int variant)
 {
     if (variant < -1 || variant > 1) return arg_fail("set_tc_form: variant must be -1, 0 or 1");
-    if (variant >= 0 && (c_.kind != 8 || thr_dev_ != nullptr || static_))
+    if (variant >= 0 && (c_.kind != 8 || thr_dev_ != nullptr || static_ || net_ != nullptr))
         return arg_fail("set_tc_form: the tensor-core form is Transform 3D with a uniform threshold");
     tc_variant_ = variant;
     return 0;
@@ -507,7 +642,8 @@ int Engine::decode(const uint16_t *fields, long long stride, int field_base, int
 {
     if (fields == nullptr || out == nullptr || fe < fb || stride < (long long)g_.field_width * g_.field_height)
         return arg_fail("decode: bad arguments");
-    const int maxb = max_batch_frames_;
+    // the learned form keeps per-Z-tile buffers: batches of at most 64 frames
+    const int maxb = net_ != nullptr ? std::min(max_batch_frames_, 64) : max_batch_frames_;
     char *o = (char *)out;
     for (int b = fb; b < fe; b += maxb) {
         const int be = std::min(fe, b + maxb);
@@ -529,7 +665,9 @@ int Engine::decode(const uint16_t *fields, long long stride, int field_base, int
         }
         // transform (+ resolve and apply when deferred) and demodulator;
         // PALcolour runs the demodulator alone
-        launches_ += (c_.kind == 6) ? 1 : (c_.kind == 8) ? (tc_variant_ >= 0 ? tpal::tc3_launches_per_frames(be - b) + 1 : 4) : 2;
+        launches_ += (c_.kind == 6) ? 1
+                     : (c_.kind == 8) ? (tc_variant_ >= 0 ? tpal::tc3_launches_per_frames(be - b) + 1 : net_ ? 5 : 4)
+                                      : 2;
         o += frame_bytes() * (size_t)(be - b);
     }
     return 0;
@@ -800,6 +938,40 @@ int chdg_engine_set_tc_form(chdg_engine *e, int32_t variant)
 {
     if (!e) return chdg::arg_fail("chdg_engine_set_tc_form: null engine");
     return e->eng.set_tc_form(variant);
+}
+
+int chdg_engine_set_masknet(chdg_engine *e, chdg_masknet *net)
+{
+    if (!e) return chdg::arg_fail("chdg_engine_set_masknet: null engine");
+    return e->eng.set_masknet(net != nullptr ? chdg::masknet_of(net) : nullptr);
+}
+
+int chdg_engine_learned_stats(chdg_engine *e, int64_t *tiles, int64_t *fallback_tiles)
+{
+    if (!e) return chdg::arg_fail("chdg_engine_learned_stats: null engine");
+    long long t = 0, f = 0;
+    const int rc = e->eng.learned_stats(&t, &f);
+    if (tiles) *tiles = t;
+    if (fallback_tiles) *fallback_tiles = f;
+    return rc;
+}
+
+int chdg_learned_features(chdg_engine *e, const uint16_t *d_fields, int64_t field_stride, int32_t nfields,
+                          int32_t frame_begin, int32_t frame_end, uint16_t *d_feat, float *d_spec,
+                          float *d_threshold_p, void *stream)
+{
+    if (!e) return chdg::arg_fail("chdg_learned_features: null engine");
+    return e->eng.learned_features(d_fields, field_stride, nfields, frame_begin, frame_end, d_feat,
+                                   reinterpret_cast<float2 *>(d_spec), d_threshold_p, (cudaStream_t)stream);
+}
+
+int chdg_learned_chroma(chdg_engine *e, const uint16_t *d_fields, int64_t field_stride, int32_t nfields,
+                        int32_t frame_begin, int32_t frame_end, const float *d_p, const uint8_t *d_fallback,
+                        float *d_chroma, void *stream)
+{
+    if (!e) return chdg::arg_fail("chdg_learned_chroma: null engine");
+    return e->eng.learned_chroma(d_fields, field_stride, nfields, frame_begin, frame_end, d_p, d_fallback, d_chroma,
+                                 (cudaStream_t)stream);
 }
 
 int chdg_engine_stats(chdg_engine *e, uint64_t *exact_decisions, uint64_t *fp32_flips)

@@ -8,6 +8,8 @@
 #include <cuda_runtime.h>
 
 #include "../../include/chromadec_gb300.h"
+#include "masknet.h"
+#include "tpal_kernels.h"
 
 namespace chdg {
 
@@ -80,6 +82,14 @@ public:
     // 0: 3xTF32; 1: BF16x3). Transform 3D, uniform threshold only.
     int set_tc_form(int variant);
     int tc_form() const { return tc_variant_; }
+    // Learned form (borrowed network; null restores the plain form).
+    int set_masknet(MaskNet *net);
+    // The learned form's passes with caller buffers (chdg_learned_*).
+    int learned_features(const uint16_t *fields, long long stride, int nfields, int fb, int fe, uint16_t *feat,
+                         float2 *spec, float *thr_p, cudaStream_t s);
+    int learned_chroma(const uint16_t *fields, long long stride, int nfields, int fb, int fe, const float *p,
+                       const uint8_t *fallback, float *out, cudaStream_t s);
+    int learned_stats(long long *tiles, long long *fallback_tiles);
     // Batches of captures in one frame index space: every field's first
     // sample (null for the black gap fields between captures), every frame's
     // squared threshold (f, hi, lo) and output pointer (null for gap frames).
@@ -103,6 +113,9 @@ private:
                       float *partial, cudaStream_t s);
     int run_demod(const uint16_t *fields, long long stride, int field_base, int fb, int fe, const float *partial,
                   void *out, cudaStream_t s);
+    // the 3D transform's parameters for frames [fb, fe)
+    void t3_params(tpal::T3Params &P, const uint16_t *fields, long long stride, int field_base, int nfields, int fb,
+                   int fe, float *partial) const;
     int ensure_host_pipeline(size_t field_bytes, size_t out_bytes);
     void record_pending();
     int fill_border(void *out, int nframes, cudaStream_t s);
@@ -125,6 +138,15 @@ private:
     int chunk_frames_ = 48;
     int max_blocks3_ = 0;
     int tc_variant_ = -1;
+    // learned form: the network (borrowed), per-Z-tile buffers, counters
+    MaskNet *net_ = nullptr;
+    uint16_t *lfeat_ = nullptr;
+    float *lp_ = nullptr;
+    uint8_t *lfb_ = nullptr;
+    long long lcap_ = 0;
+    unsigned long long *lcount_ = nullptr;   // [0] tiles, [1] fallback tiles
+    int ensure_learned(long long ntiles);
+    int run_learned(const tpal::T3Params &P, cudaStream_t s);
     const uint16_t *const *field_ptrs_ = nullptr;
     const float *frame_t2_ = nullptr;
     void *const *frame_out_ = nullptr;

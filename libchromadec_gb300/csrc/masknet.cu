@@ -1,0 +1,691 @@
+// masknet.cu -- the learned chroma mask of the Transform-PAL 3D learned form:
+// a small 3D convolutional network over one tile's spectrum that predicts,
+// for each bin the filter can keep, the fraction of it that is chroma, in
+// place of the fixed mirror threshold of TransformPal3D::applyFilter
+// (src/decoders/palcolour/transform_pal_3d.cpp:249-333). The reference has no
+// learned PAL path; its NTSC nnTransform3D decoder is the precedent for a
+// per-bin mask on a 3D tile spectrum (src/decoders/nntransform3d/
+// nntransform3d_pipeline_cuda.cu:160-244, 544-567).
+//
+// Domain of one tile: the 1,280 bins kz 0..7, ky 0..31 (periodic axes of the
+// DFT) and q = kx - 2 in 0..4 (zero outside), voxel v = (q * 8 + kz) * 32 + ky.
+// Network: input channels f(b) = ln(1 + |X_b|) / 16 and f at b's mirror about
+// the carrier, ((10 - kz) mod 8, (40 - ky) mod 32, 4 - q); three 3x3x3
+// convolutions of 16 channels with bias and ReLU; a 1x1x1 sigmoid head giving
+// p(b). BF16 weights, features and activations, FP32 accumulation. A tile
+// whose mean |p - 1/2| is below the confidence limit falls back to the
+// threshold decisions.
+//
+// Kernels (one CTA of 256 threads per tile, persistent over tiles; thread t
+// owns the (kz, ky) column t and computes its 5 q x 16 channels):
+//  * mn_forward_kernel<TRAIN>: features -> p (+ fallback flags); the
+//    training variant also keeps each layer's activations for the backward
+//    pass.
+//  * mn_loss_kernel: dL/dz of the head for L = sum |p X - C|^2 / sum |X|^2.
+//  * mn_backward_kernel: the head, then per layer the weight gradient (thread
+//    (ci, co) sums over the tile's voxels for all 27 taps) and the input
+//    gradient (the transposed convolution), each CTA adding into its own
+//    slice of a partial-gradient buffer; mn_adam_kernel reduces the slices
+//    and takes one Adam step on the FP32 master weights.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "../../include/chromadec_gb300.h"
+#include "error_state.h"
+#include "masknet.h"
+
+namespace chdg {
+namespace mn {
+
+constexpr int kThreads = 256;
+constexpr int NQ = 5, NZY = 256, NV = 1280, NC = 16, NCIN = 2;
+constexpr int CS = 1282;   // channel stride of shared activations (bf16), bank-skewed
+constexpr int OFF_W1 = 0, OFF_B1 = OFF_W1 + 27 * NCIN * NC, OFF_W2 = OFF_B1 + NC, OFF_B2 = OFF_W2 + 27 * NC * NC,
+              OFF_W3 = OFF_B2 + NC, OFF_B3 = OFF_W3 + 27 * NC * NC, OFF_WH = OFF_B3 + NC, OFF_BH = OFF_WH + NC;
+constexpr int NPARAM = OFF_BH + 1;
+constexpr int NPARAM_PAD = (NPARAM + 3) & ~3;
+static_assert(NPARAM == CHDG_MASKNET_PARAMS, "parameter count");
+static_assert(OFF_W2 % 4 == 0 && OFF_W3 % 4 == 0, "float4 weight rows");
+
+__device__ __forceinline__ float bfr(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+
+// Accumulate a 3x3x3 convolution of CI input channels into acc[q][co] for
+// the thread's column (z, y). in(ci, v) reads input channel ci at voxel v;
+// wrow(t, ci) points at the 16 output-channel weights of tap t, input ci
+// (stride `wstride` floats between them).
+template <int CI, typename In, typename WRow>
+__device__ __forceinline__ void conv_acc(const In &in, const WRow &wrow, int z, int y, float (&acc)[NQ][NC])
+{
+#pragma unroll 1
+    for (int dz = -1; dz <= 1; dz++) {
+#pragma unroll 1
+        for (int dy = -1; dy <= 1; dy++) {
+            const int zy = (((z + dz) & 7) << 5) | ((y + dy) & 31);
+            const int tb = (dz + 1) * 9 + (dy + 1) * 3;
+#pragma unroll 2
+            for (int ci = 0; ci < CI; ci++) {
+                float xin[NQ + 2];
+                xin[0] = 0.f;
+                xin[NQ + 1] = 0.f;
+#pragma unroll
+                for (int q = 0; q < NQ; q++) xin[q + 1] = in(ci, q * NZY + zy);
+#pragma unroll
+                for (int j = 0; j < 3; j++) {
+                    float w[NC];
+                    wrow(tb + j, ci, w);
+#pragma unroll
+                    for (int q = 0; q < NQ; q++) {
+                        const float xv = xin[q + j];
+#pragma unroll
+                        for (int co = 0; co < NC; co++) acc[q][co] = __fmaf_rn(xv, w[co], acc[q][co]);
+                    }
+                }
+            }
+        }
+    }
+}
+
+// Weight rows of a layer's W[27][CI][16] in shared memory (forward)
+template <int CI>
+struct WFwd {
+    const float *W;
+    __device__ __forceinline__ void operator()(int t, int ci, float (&w)[NC]) const
+    {
+        const float4 *p = reinterpret_cast<const float4 *>(W + (t * CI + ci) * NC);
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const float4 v = p[k];
+            w[4 * k] = v.x, w[4 * k + 1] = v.y, w[4 * k + 2] = v.z, w[4 * k + 3] = v.w;
+        }
+    }
+};
+
+// Transposed, flipped rows for the input gradient: input channel = the
+// layer's output channel co, outputs = its input channels ci:
+// w[ci] = W[26 - t][ci][co]
+struct WTrans {
+    const float *W;
+    __device__ __forceinline__ void operator()(int t, int co, float (&w)[NC]) const
+    {
+        const float *p = W + (26 - t) * NC * NC + co;
+#pragma unroll
+        for (int ci = 0; ci < NC; ci++) w[ci] = p[ci * NC];
+    }
+};
+
+struct InBf16 {
+    const __nv_bfloat16 *a;   // [16][CS]
+    __device__ __forceinline__ float operator()(int c, int v) const { return __bfloat162float(a[c * CS + v]); }
+};
+
+struct InF32 {
+    const float *a;   // [CI][NV]
+    __device__ __forceinline__ float operator()(int c, int v) const { return a[c * NV + v]; }
+};
+
+__device__ __forceinline__ void acc_init(float (&acc)[NQ][NC], const float *bias)
+{
+#pragma unroll
+    for (int q = 0; q < NQ; q++)
+#pragma unroll
+        for (int co = 0; co < NC; co++) acc[q][co] = bias ? bias[co] : 0.f;
+}
+
+// ReLU, round to bf16 and store channel co of the thread's voxels
+__device__ __forceinline__ void acc_store_relu(const float (&acc)[NQ][NC], __nv_bfloat16 *out, int zy)
+{
+#pragma unroll
+    for (int q = 0; q < NQ; q++)
+#pragma unroll
+        for (int co = 0; co < NC; co++) out[co * CS + q * NZY + zy] = __float2bfloat16_rn(fmaxf(acc[q][co], 0.f));
+}
+
+// Inputs: the tile's features and their mirror, as two FP32 channels
+__device__ __forceinline__ void load_input(const uint16_t *feat_tile, float *x0, int zy)
+{
+    const int z = zy >> 5, y = zy & 31;
+    const int mzy = (((10 - z) & 7) << 5) | ((40 - y) & 31);
+    const __nv_bfloat16 *f = reinterpret_cast<const __nv_bfloat16 *>(feat_tile);
+#pragma unroll
+    for (int q = 0; q < NQ; q++) {
+        x0[q * NZY + zy] = __bfloat162float(f[q * NZY + zy]);
+        x0[NV + q * NZY + zy] = __bfloat162float(f[(4 - q) * NZY + mzy]);
+    }
+}
+
+__device__ __forceinline__ void copy_act_out(const __nv_bfloat16 *s, __nv_bfloat16 *g, int zy)
+{
+    // [16][CS] shared -> [16][NV] global, the thread's column
+#pragma unroll
+    for (int c = 0; c < NC; c++)
+#pragma unroll
+        for (int q = 0; q < NQ; q++) g[c * NV + q * NZY + zy] = s[c * CS + q * NZY + zy];
+}
+
+__device__ __forceinline__ float block_sum(float v, float *red)
+{
+#pragma unroll
+    for (int h = 16; h >= 1; h >>= 1) v += __shfl_xor_sync(0xffffffffu, v, h);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    float s = 0.f;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; w++) s += red[w];
+    return s;
+}
+
+constexpr size_t kFwdSmem = sizeof(float) * (NPARAM_PAD + 2 * NV) + 2 * sizeof(__nv_bfloat16) * NC * CS;
+
+// params: the network's weights as used (weights bf16-rounded, biases FP32).
+// TRAIN: also write A1, A2, A3 ([tile][16][NV] bf16 each) for the backward pass.
+template <bool TRAIN>
+__global__ void __launch_bounds__(kThreads, 1)
+    mn_forward_kernel(const float *params, const uint16_t *feat, long long ntiles, float conf_limit, float *p_out,
+                      uint8_t *fallback, __nv_bfloat16 *a1g, __nv_bfloat16 *a2g, __nv_bfloat16 *a3g)
+{
+    extern __shared__ float4 smem4[];
+    float *wsm = reinterpret_cast<float *>(smem4);
+    float *x0 = wsm + NPARAM_PAD;
+    __nv_bfloat16 *act0 = reinterpret_cast<__nv_bfloat16 *>(x0 + 2 * NV);
+    __nv_bfloat16 *act1 = act0 + NC * CS;
+    __shared__ float red[kThreads / 32];
+    for (int i = threadIdx.x; i < NPARAM; i += kThreads) wsm[i] = params[i];
+    const int zy = threadIdx.x, z = zy >> 5, y = zy & 31;
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        __syncthreads();   // the previous tile is done with x0 and the activations
+        load_input(feat + tile * NV, x0, zy);
+        __syncthreads();
+        float acc[NQ][NC];
+        acc_init(acc, wsm + OFF_B1);
+        conv_acc<NCIN>(InF32{x0}, WFwd<NCIN>{wsm + OFF_W1}, z, y, acc);
+        acc_store_relu(acc, act0, zy);
+        __syncthreads();
+        acc_init(acc, wsm + OFF_B2);
+        conv_acc<NC>(InBf16{act0}, WFwd<NC>{wsm + OFF_W2}, z, y, acc);
+        acc_store_relu(acc, act1, zy);
+        __syncthreads();
+        acc_init(acc, wsm + OFF_B3);
+        conv_acc<NC>(InBf16{act1}, WFwd<NC>{wsm + OFF_W3}, z, y, acc);
+        if (TRAIN) {
+            copy_act_out(act0, a1g + tile * NC * NV, zy);
+            copy_act_out(act1, a2g + tile * NC * NV, zy);
+        }
+        float conf = 0.f;
+#pragma unroll
+        for (int q = 0; q < NQ; q++) {
+            float zh = wsm[OFF_BH];
+#pragma unroll
+            for (int co = 0; co < NC; co++) {
+                const float a = bfr(fmaxf(acc[q][co], 0.f));
+                if (TRAIN) a3g[tile * NC * NV + co * NV + q * NZY + zy] = __float2bfloat16_rn(a);
+                zh = __fmaf_rn(a, wsm[OFF_WH + co], zh);
+            }
+            const float p = 1.0f / (1.0f + expf(-zh));
+            p_out[tile * NV + q * NZY + zy] = p;
+            conf += fabsf(p - 0.5f);
+        }
+        const float s = block_sum(conf, red);
+        if (threadIdx.x == 0 && fallback != nullptr) fallback[tile] = (s * (1.0f / NV) < conf_limit) ? 1 : 0;
+    }
+}
+
+// sum of a = |X|^2 over the batch (ac: [tile][NV] of (a, c))
+__global__ void mn_sum_kernel(const float2 *ac, long long n, double *out)
+{
+    double s = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        s += (double)ac[i].x;
+#pragma unroll
+    for (int h = 16; h >= 1; h >>= 1) s += __shfl_xor_sync(0xffffffffu, s, h);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
+}
+
+// dz = dL/dz_head = 2 (p a - c) / S * p (1 - p); loss partial sums
+__global__ void mn_loss_kernel(const float *p, const float2 *ac, long long n, const double *S, float *dz, double *loss)
+{
+    const float inv = (float)(1.0 / *S);
+    double l = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float pv = p[i];
+        const float2 v = ac[i];
+        const float dp = 2.0f * (pv * v.x - v.y) * inv;
+        dz[i] = dp * pv * (1.0f - pv);
+        l += (double)((pv * pv * v.x - 2.0f * pv * v.y) * inv);
+    }
+#pragma unroll
+    for (int h = 16; h >= 1; h >>= 1) l += __shfl_xor_sync(0xffffffffu, l, h);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, l);
+}
+
+// Weight gradient of one layer for the thread's (ci, co):
+// g[t] += sum_v in[ci][v + t] * d[co][v]
+template <typename In, typename D>
+__device__ __forceinline__ void wgrad(const In &in, const D &d, int ci, int co, float (&g)[27])
+{
+#pragma unroll 1
+    for (int zy = 0; zy < NZY; zy++) {
+        const int z = zy >> 5, y = zy & 31;
+        float dv[NQ];
+#pragma unroll
+        for (int q = 0; q < NQ; q++) dv[q] = d(co, q * NZY + zy);
+#pragma unroll
+        for (int dz = -1; dz <= 1; dz++) {
+#pragma unroll
+            for (int dy = -1; dy <= 1; dy++) {
+                const int zy2 = (((z + dz) & 7) << 5) | ((y + dy) & 31);
+                float xin[NQ + 2];
+                xin[0] = 0.f;
+                xin[NQ + 1] = 0.f;
+#pragma unroll
+                for (int q = 0; q < NQ; q++) xin[q + 1] = in(ci, q * NZY + zy2);
+                const int tb = (dz + 1) * 9 + (dy + 1) * 3;
+#pragma unroll
+                for (int j = 0; j < 3; j++)
+#pragma unroll
+                    for (int q = 0; q < NQ; q++) g[tb + j] = __fmaf_rn(xin[q + j], dv[q], g[tb + j]);
+            }
+        }
+    }
+}
+
+constexpr size_t kBwdSmem =
+    sizeof(float) * (NPARAM_PAD + 2 * NV + NV) + 2 * sizeof(__nv_bfloat16) * NC * CS;
+
+__device__ __forceinline__ void load_act(const __nv_bfloat16 *g, __nv_bfloat16 *s, int zy)
+{
+#pragma unroll
+    for (int c = 0; c < NC; c++)
+#pragma unroll
+        for (int q = 0; q < NQ; q++) s[c * CS + q * NZY + zy] = g[c * NV + q * NZY + zy];
+}
+
+// The backward pass of the tiles given; each CTA accumulates into
+// gpart[blockIdx.x][NPARAM] (zeroed by the caller).
+__global__ void __launch_bounds__(kThreads, 1)
+    mn_backward_kernel(const float *params, const uint16_t *feat, const __nv_bfloat16 *a1g,
+                       const __nv_bfloat16 *a2g, const __nv_bfloat16 *a3g, const float *dzg, long long ntiles,
+                       float *gpart)
+{
+    extern __shared__ float4 smem4[];
+    float *wsm = reinterpret_cast<float *>(smem4);
+    float *x0 = wsm + NPARAM_PAD;   // [2][NV]
+    float *dzs = x0 + 2 * NV;       // [NV]
+    __nv_bfloat16 *bufA = reinterpret_cast<__nv_bfloat16 *>(dzs + NV);
+    __nv_bfloat16 *bufB = bufA + NC * CS;
+    for (int i = threadIdx.x; i < NPARAM; i += kThreads) wsm[i] = params[i];
+    const int t = threadIdx.x, zy = t, z = zy >> 5, y = zy & 31;
+    const int ci = t >> 4, co = t & 15;   // the thread's weight-gradient pair
+    float *gp = gpart + (size_t)blockIdx.x * NPARAM;
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        __syncthreads();
+        // head: dz, A3
+        for (int q = 0; q < NQ; q++) dzs[q * NZY + zy] = dzg[tile * NV + q * NZY + zy];
+        load_act(a3g + tile * NC * NV, bufA, zy);
+        __syncthreads();
+        {
+            // d wh[co] = sum_v dz[v] A3[co][v]; d bh = sum_v dz[v] (threads split the voxels)
+            const int part = t >> 4;   // 16 parts of 80 voxels
+            float s = 0.f, sb = 0.f;
+            for (int v = part * 80; v < part * 80 + 80; v++) {
+                s = __fmaf_rn(dzs[v], __bfloat162float(bufA[co * CS + v]), s);
+                if (co == 0) sb += dzs[v];
+            }
+            atomicAdd(gp + OFF_WH + co, s);
+            if (co == 0) atomicAdd(gp + OFF_BH, sb);
+        }
+        __syncthreads();
+        // dZ3 = bf16(dz * wh[c] * (A3 > 0)), in place
+#pragma unroll
+        for (int c = 0; c < NC; c++)
+#pragma unroll
+            for (int q = 0; q < NQ; q++) {
+                const int e = c * CS + q * NZY + zy;
+                const float a = __bfloat162float(bufA[e]);
+                bufA[e] = __float2bfloat16_rn(a > 0.f ? dzs[q * NZY + zy] * wsm[OFF_WH + c] : 0.f);
+            }
+        load_act(a2g + tile * NC * NV, bufB, zy);
+        __syncthreads();
+        // layer 3: weight and bias gradients, then dA2 -> dZ2 in place of A2
+        {
+            float g[27];
+#pragma unroll
+            for (int k = 0; k < 27; k++) g[k] = 0.f;
+            wgrad(InBf16{bufB}, InBf16{bufA}, ci, co, g);
+#pragma unroll
+            for (int k = 0; k < 27; k++) gp[OFF_W3 + (k * NC + ci) * NC + co] += g[k];
+            if (ci == 0) {
+                float b = 0.f;
+                for (int v = 0; v < NV; v++) b += __bfloat162float(bufA[co * CS + v]);
+                gp[OFF_B3 + co] += b;
+            }
+        }
+        float acc[NQ][NC];
+        acc_init(acc, nullptr);
+        conv_acc<NC>(InBf16{bufA}, WTrans{wsm + OFF_W3}, z, y, acc);
+        __syncthreads();   // every thread has read A2 for the weight gradient
+#pragma unroll
+        for (int c = 0; c < NC; c++)
+#pragma unroll
+            for (int q = 0; q < NQ; q++) {
+                const int e = c * CS + q * NZY + zy;
+                bufB[e] = __float2bfloat16_rn(__bfloat162float(bufB[e]) > 0.f ? acc[q][c] : 0.f);
+            }
+        load_act(a1g + tile * NC * NV, bufA, zy);   // dZ3 is no longer needed
+        __syncthreads();
+        // layer 2
+        {
+            float g[27];
+#pragma unroll
+            for (int k = 0; k < 27; k++) g[k] = 0.f;
+            wgrad(InBf16{bufA}, InBf16{bufB}, ci, co, g);
+#pragma unroll
+            for (int k = 0; k < 27; k++) gp[OFF_W2 + (k * NC + ci) * NC + co] += g[k];
+            if (ci == 0) {
+                float b = 0.f;
+                for (int v = 0; v < NV; v++) b += __bfloat162float(bufB[co * CS + v]);
+                gp[OFF_B2 + co] += b;
+            }
+        }
+        acc_init(acc, nullptr);
+        conv_acc<NC>(InBf16{bufB}, WTrans{wsm + OFF_W2}, z, y, acc);
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < NC; c++)
+#pragma unroll
+            for (int q = 0; q < NQ; q++) {
+                const int e = c * CS + q * NZY + zy;
+                bufA[e] = __float2bfloat16_rn(__bfloat162float(bufA[e]) > 0.f ? acc[q][c] : 0.f);
+            }
+        load_input(feat + tile * NV, x0, zy);
+        __syncthreads();
+        // layer 1 (two input channels)
+        if (ci < NCIN) {
+            float g[27];
+#pragma unroll
+            for (int k = 0; k < 27; k++) g[k] = 0.f;
+            wgrad(InF32{x0}, InBf16{bufA}, ci, co, g);
+#pragma unroll
+            for (int k = 0; k < 27; k++) gp[OFF_W1 + (k * NCIN + ci) * NC + co] += g[k];
+        } else if (ci == NCIN) {
+            float b = 0.f;
+            for (int v = 0; v < NV; v++) b += __bfloat162float(bufA[co * CS + v]);
+            gp[OFF_B1 + co] += b;
+        }
+    }
+}
+
+// One Adam step: g = sum over the partial slices (then zeroed); the FP32
+// master weights move, and `used` gets the values the kernels compute with
+// (weights rounded to bf16, biases as they are).
+__global__ void mn_adam_kernel(float *master, float *used, float *m, float *v, float *gpart, int nslices, float lr,
+                               float b1, float b2, float eps, float c1, float c2, float *grad_out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= NPARAM) return;
+    float g = 0.f;
+    for (int s = 0; s < nslices; s++) {
+        g += gpart[(size_t)s * NPARAM + i];
+        gpart[(size_t)s * NPARAM + i] = 0.f;
+    }
+    if (grad_out) grad_out[i] = g;
+    if (lr == 0.f) return;
+    const float mi = b1 * m[i] + (1.f - b1) * g;
+    const float vi = b2 * v[i] + (1.f - b2) * g * g;
+    m[i] = mi;
+    v[i] = vi;
+    const float w = master[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+    master[i] = w;
+    const bool bias = (i >= OFF_B1 && i < OFF_W2) || (i >= OFF_B2 && i < OFF_W3) || (i >= OFF_B3 && i < OFF_WH) ||
+                      i == OFF_BH;
+    used[i] = bias ? w : bfr(w);
+}
+
+// Training pairs per bin: (|X|^2, Re(C conj X)) from the composite's and the
+// true chroma's spectra
+__global__ void mn_pairs_kernel(const float2 *x, const float2 *c, long long n, float2 *ac)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float2 a = x[i], b = c[i];
+        ac[i] = make_float2(a.x * a.x + a.y * a.y, b.x * a.x + b.y * a.y);
+    }
+}
+
+__global__ void mn_round_kernel(const float *master, float *used)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= NPARAM) return;
+    const bool bias = (i >= OFF_B1 && i < OFF_W2) || (i >= OFF_B2 && i < OFF_W3) || (i >= OFF_B3 && i < OFF_WH) ||
+                      i == OFF_BH;
+    used[i] = bias ? master[i] : bfr(master[i]);
+}
+
+}  // namespace mn
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+static int mn_fail(const std::string &what, int code = CHDG_E_INVALID_ARG)
+{
+    chd::detail::set_last_error("chdg_masknet: " + what);
+    return code;
+}
+
+static int mn_cuda(const char *what, cudaError_t e)
+{
+    return mn_fail(std::string(what) + ": " + cudaGetErrorString(e), CHDG_E_CUDA);
+}
+
+MaskNet::~MaskNet()
+{
+    for (void *p : {(void *)master_, (void *)used_, (void *)m_, (void *)v_, (void *)gpart_, (void *)a1_, (void *)a2_,
+                    (void *)a3_, (void *)p_, (void *)dz_, (void *)scal_, (void *)grad_})
+        if (p) cudaFree(p);
+}
+
+int MaskNet::init()
+{
+    cudaError_t e;
+    const size_t pb = sizeof(float) * mn::NPARAM;
+    for (float **p : {&master_, &used_, &m_, &v_, &grad_})
+        if ((e = cudaMalloc(p, pb)) != cudaSuccess) return mn_cuda("cudaMalloc", e);
+    cudaMemset(m_, 0, pb);
+    cudaMemset(v_, 0, pb);
+    if ((e = cudaMalloc(&scal_, 2 * sizeof(double))) != cudaSuccess) return mn_cuda("cudaMalloc", e);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    grid_ = sms > 0 ? sms : 1;
+    if ((e = cudaMalloc(&gpart_, sizeof(float) * mn::NPARAM * (size_t)grid_)) != cudaSuccess)
+        return mn_cuda("cudaMalloc", e);
+    cudaMemset(gpart_, 0, sizeof(float) * mn::NPARAM * (size_t)grid_);
+    static bool attr[64] = {};
+    if (dev >= 0 && dev < 64 && !attr[dev]) {
+        const auto a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+        if (cudaFuncSetAttribute(mn::mn_forward_kernel<false>, a, (int)mn::kFwdSmem) != cudaSuccess ||
+            cudaFuncSetAttribute(mn::mn_forward_kernel<true>, a, (int)mn::kFwdSmem) != cudaSuccess ||
+            cudaFuncSetAttribute(mn::mn_backward_kernel, a, (int)mn::kBwdSmem) != cudaSuccess)
+            return mn_cuda("cudaFuncSetAttribute", cudaGetLastError());
+        attr[dev] = true;
+    }
+    return 0;
+}
+
+int MaskNet::set_weights(const float *host, size_t n)
+{
+    if (n != (size_t)mn::NPARAM) return mn_fail("expected " + std::to_string(mn::NPARAM) + " parameters");
+    cudaError_t e = cudaMemcpy(master_, host, sizeof(float) * n, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return mn_cuda("cudaMemcpy", e);
+    cudaMemset(m_, 0, sizeof(float) * n);
+    cudaMemset(v_, 0, sizeof(float) * n);
+    step_ = 0;
+    mn::mn_round_kernel<<<(mn::NPARAM + 255) / 256, 256>>>(master_, used_);
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return mn_cuda("round", e);
+    return 0;
+}
+
+int MaskNet::get_weights(float *host, size_t n) const
+{
+    if (n != (size_t)mn::NPARAM) return mn_fail("expected " + std::to_string(mn::NPARAM) + " parameters");
+    cudaError_t e = cudaMemcpy(host, master_, sizeof(float) * n, cudaMemcpyDeviceToHost);
+    return e == cudaSuccess ? 0 : mn_cuda("cudaMemcpy", e);
+}
+
+int MaskNet::forward(const uint16_t *d_feat, long long ntiles, float *d_p, uint8_t *d_fallback, cudaStream_t s) const
+{
+    if (ntiles <= 0) return 0;
+    if (d_feat == nullptr || d_p == nullptr) return mn_fail("forward: null buffer");
+    const unsigned blocks = (unsigned)std::min<long long>(ntiles, (long long)grid_ * 1);
+    mn::mn_forward_kernel<false><<<blocks, mn::kThreads, mn::kFwdSmem, s>>>(used_, d_feat, ntiles, conf_limit_, d_p,
+                                                                            d_fallback, nullptr, nullptr, nullptr);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? 0 : mn_cuda("forward launch", e);
+}
+
+int MaskNet::ensure_batch(long long ntiles)
+{
+    if (ntiles <= cap_) return 0;
+    for (void *p : {(void *)a1_, (void *)a2_, (void *)a3_, (void *)p_, (void *)dz_})
+        if (p) cudaFree(p);
+    a1_ = a2_ = a3_ = nullptr;
+    p_ = dz_ = nullptr;
+    cap_ = 0;
+    cudaError_t e;
+    const size_t act = sizeof(uint16_t) * mn::NC * mn::NV * (size_t)ntiles;
+    if ((e = cudaMalloc(&a1_, act)) != cudaSuccess || (e = cudaMalloc(&a2_, act)) != cudaSuccess ||
+        (e = cudaMalloc(&a3_, act)) != cudaSuccess ||
+        (e = cudaMalloc(&p_, sizeof(float) * mn::NV * (size_t)ntiles)) != cudaSuccess ||
+        (e = cudaMalloc(&dz_, sizeof(float) * mn::NV * (size_t)ntiles)) != cudaSuccess)
+        return mn_cuda("training buffers", e);
+    cap_ = ntiles;
+    return 0;
+}
+
+// Loss and gradients of a batch; with lr > 0 one Adam step follows.
+int MaskNet::train_step(const uint16_t *d_feat, const float2 *d_ac, long long ntiles, float lr, double *loss,
+                        float *host_grad, cudaStream_t s)
+{
+    if (ntiles <= 0 || d_feat == nullptr || d_ac == nullptr) return mn_fail("train_step: empty batch or null buffer");
+    if (const int rc = ensure_batch(ntiles); rc != 0) return rc;
+    const unsigned blocks = (unsigned)std::min<long long>(ntiles, grid_);
+    cudaMemsetAsync(scal_, 0, 2 * sizeof(double), s);
+    mn::mn_forward_kernel<true><<<blocks, mn::kThreads, mn::kFwdSmem, s>>>(
+        used_, d_feat, ntiles, conf_limit_, p_, nullptr, (__nv_bfloat16 *)a1_, (__nv_bfloat16 *)a2_,
+        (__nv_bfloat16 *)a3_);
+    const long long n = ntiles * mn::NV;
+    mn::mn_sum_kernel<<<256, 256, 0, s>>>(d_ac, n, scal_);
+    mn::mn_loss_kernel<<<256, 256, 0, s>>>(p_, d_ac, n, scal_, dz_, scal_ + 1);
+    mn::mn_backward_kernel<<<blocks, mn::kThreads, mn::kBwdSmem, s>>>(
+        used_, d_feat, (const __nv_bfloat16 *)a1_, (const __nv_bfloat16 *)a2_, (const __nv_bfloat16 *)a3_, dz_,
+        ntiles, gpart_);
+    float c1 = 1.f, c2 = 1.f;
+    if (lr > 0.f) {
+        step_++;
+        c1 = (float)(1.0 / (1.0 - std::pow(0.9, (double)step_)));
+        c2 = (float)(1.0 / (1.0 - std::pow(0.999, (double)step_)));
+    }
+    mn::mn_adam_kernel<<<(mn::NPARAM + 255) / 256, 256, 0, s>>>(master_, used_, m_, v_, gpart_, (int)blocks, lr, 0.9f,
+                                                               0.999f, 1e-8f, c1, c2, grad_);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return mn_cuda("train launch", e);
+    if (loss != nullptr || host_grad != nullptr) {
+        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return mn_cuda("train sync", e);
+        if (loss != nullptr) {
+            double h[2];
+            cudaMemcpy(h, scal_, sizeof(h), cudaMemcpyDeviceToHost);
+            *loss = h[1];
+        }
+        if (host_grad != nullptr)
+            if ((e = cudaMemcpy(host_grad, grad_, sizeof(float) * mn::NPARAM, cudaMemcpyDeviceToHost)) != cudaSuccess)
+                return mn_cuda("gradient copy", e);
+    }
+    return 0;
+}
+
+}  // namespace chdg
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+struct chdg_masknet {
+    chdg::MaskNet net;
+};
+
+namespace chdg {
+MaskNet *masknet_of(chdg_masknet *n) { return &n->net; }
+}  // namespace chdg
+
+#pragma GCC visibility push(default)
+extern "C" {
+
+int chdg_masknet_create(chdg_masknet **out)
+{
+    if (out == nullptr) return chdg::mn_fail("create: null argument");
+    *out = nullptr;
+    auto n = new (std::nothrow) chdg_masknet;
+    if (n == nullptr) return chdg::mn_fail("create: out of memory", CHDG_E_OOM);
+    if (const int rc = n->net.init(); rc != 0) {
+        delete n;
+        return rc;
+    }
+    *out = n;
+    return 0;
+}
+
+void chdg_masknet_free(chdg_masknet *n) { delete n; }
+
+int chdg_masknet_set_weights(chdg_masknet *n, const float *w, int64_t count)
+{
+    if (n == nullptr || w == nullptr) return chdg::mn_fail("set_weights: null argument");
+    return n->net.set_weights(w, (size_t)count);
+}
+
+int chdg_masknet_get_weights(const chdg_masknet *n, float *w, int64_t count)
+{
+    if (n == nullptr || w == nullptr) return chdg::mn_fail("get_weights: null argument");
+    return n->net.get_weights(w, (size_t)count);
+}
+
+int chdg_masknet_set_confidence(chdg_masknet *n, float limit)
+{
+    if (n == nullptr || !(limit >= 0.f && limit <= 0.5f)) return chdg::mn_fail("set_confidence: limit must be in [0, 0.5]");
+    n->net.set_confidence(limit);
+    return 0;
+}
+
+int chdg_masknet_forward(const chdg_masknet *n, const uint16_t *d_feat, int64_t ntiles, float *d_p,
+                         uint8_t *d_fallback, void *stream)
+{
+    if (n == nullptr) return chdg::mn_fail("forward: null network");
+    return n->net.forward(d_feat, ntiles, d_p, d_fallback, (cudaStream_t)stream);
+}
+
+int chdg_masknet_train_step(chdg_masknet *n, const uint16_t *d_feat, const float *d_ac, int64_t ntiles,
+                            float learning_rate, double *loss, float *grad, void *stream)
+{
+    if (n == nullptr) return chdg::mn_fail("train_step: null network");
+    if (!(learning_rate >= 0.f)) return chdg::mn_fail("train_step: learning rate must be >= 0");
+    return n->net.train_step(d_feat, reinterpret_cast<const float2 *>(d_ac), ntiles, learning_rate, loss, grad,
+                             (cudaStream_t)stream);
+}
+
+int chdg_masknet_pairs(const float *d_spec_x, const float *d_spec_c, int64_t nbins, float *d_ac, void *stream)
+{
+    if (d_spec_x == nullptr || d_spec_c == nullptr || d_ac == nullptr || nbins < 0)
+        return chdg::mn_fail("pairs: bad arguments");
+    if (nbins == 0) return 0;
+    chdg::mn::mn_pairs_kernel<<<1024, 256, 0, (cudaStream_t)stream>>>(reinterpret_cast<const float2 *>(d_spec_x),
+                                                                       reinterpret_cast<const float2 *>(d_spec_c),
+                                                                       nbins, reinterpret_cast<float2 *>(d_ac));
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? 0 : chdg::mn_cuda("pairs launch", e);
+}
+
+}  // extern "C"
+#pragma GCC visibility pop

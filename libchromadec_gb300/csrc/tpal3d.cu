@@ -36,6 +36,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "tpal_common.cuh"
@@ -511,6 +512,71 @@ __device__ __forceinline__ unsigned resolve_uncertain(const T3Params &P, int m, 
     return keep;
 }
 
+// Output stage of step m: inverse Y then X of output fields 2m (RA) and
+// 2m + 1 (RB), and the store of each lane's row into its overlap class.
+__device__ __forceinline__ void walk_store(const T3Params &P, const LaneConst &LC, const float2 *RA, const float2 *RB,
+                                           int m, int tileX, int tileY, int cls)
+{
+    // Inverse Y then X, one kx at a time: lane (j, i) folds ky = kk and
+    // kk+16 of output field 2m+j for its row parity, runs a 16-point
+    // inverse DFT over the half-warp, and accumulates row i's cosine and
+    // sine sums of the inverse X transform.
+    float2 CS[8];   // (cosine sum, sine sum) of row i
+#pragma unroll
+    for (int x = 0; x < 8; x++) CS[x] = make_float2(0.f, 0.f);
+    const float2 *Rj = LC.j ? RB : RA;
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const float2 lo_v = Rj[k * 32 + LC.i];        // R[kk]   (lane kappa^-1(kk) = i)
+        const float2 hi_v = Rj[k * 32 + LC.i + 16];   // R[kk+16]
+        float2 G = LC.y0 ? sub2(lo_v, hi_v) : add2(lo_v, hi_v);
+        G = cmul(G, make_float2(LC.ptw.x, -LC.ptw.y));   // exp(+i pi kk y0 / 16)
+        // 16-point inverse DFT, bit-reversed input -> natural order (DIT)
+        int st = 3;
+#pragma unroll
+        for (int h = 1; h <= 8; h <<= 1, st--) {
+            const bool upper = (LC.i & h) != 0;
+            const float2 w = make_float2(LC.ftw[st].x, -LC.ftw[st].y);   // exp(+2 pi i r/(2h))
+            const float2 o = shfl_xor2(G, h);
+            const float2 t = cmul(upper ? G : o, w);
+            G = upper ? sub2(o, t) : add2(G, t);
+        }
+#pragma unroll
+        for (int x = 0; x < 8; x++) CS[x] = __ffma2_rn(G, c3_xi[k][x], CS[x]);
+    }
+    // Store row i of field 2m + j.
+    const int L = tileY + LC.y0 + 2 * LC.i;
+    if (L >= P.fafl && L <= P.lafl) {
+        const int ofield = 2 * (m - P.frame_begin) + LC.j;
+        float *dst = P.partial + (long long)cls * P.part_class_stride + (long long)ofield * P.part_field_stride +
+                     (long long)((L >> 1) - P.fl_lo) * P.part_row_stride - P.avs;
+        // tileX - avs is a multiple of 8, so an interior tile's row starts
+        // on a 32-byte boundary whenever the planes' strides are multiples
+        // of 4 floats and their base is 16-byte aligned: four vector stores
+        const bool vec = ((P.part_row_stride | P.part_field_stride | P.part_class_stride) & 3) == 0 &&
+                         (reinterpret_cast<uintptr_t>(P.partial) & 15) == 0 && tileX >= P.avs &&
+                         tileX + 16 <= P.ave;
+        if (vec) {
+            float o[16];
+#pragma unroll
+            for (int x = 0; x < 8; x++) {
+                o[x] = CS[x].x - CS[x].y;
+                o[15 - x] = CS[x].x + CS[x].y;
+            }
+            float4 *d4 = reinterpret_cast<float4 *>(dst + tileX);
+#pragma unroll
+            for (int q = 0; q < 4; q++) d4[q] = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
+        } else {
+#pragma unroll
+            for (int x = 0; x < 8; x++) {
+                const int X0 = tileX + x, X1 = tileX + 15 - x;
+                if (X0 >= P.avs && X0 < P.ave) dst[X0] = CS[x].x - CS[x].y;
+                if (X1 >= P.avs && X1 < P.ave) dst[X1] = CS[x].x + CS[x].y;
+            }
+        }
+    }
+}
+
 // TMODE: 0 = one uniform threshold, 1 = per-bin table, 2 = per-frame
 // thresholds (batches of captures). EXACT = false: the walk over every work
 // item, guard-band decisions taken in FP32 and recorded for
@@ -677,67 +743,178 @@ __global__ void __launch_bounds__(32 * kWarps3, 3) tpal3d_kernel(T3Params P)
         __syncwarp();
         if (m < m0) continue;   // warm-up step: only the carries are needed
 
-        // Inverse Y then X, one kx at a time: lane (j, i) folds ky = kk and
-        // kk+16 of output field 2m+j for its row parity, runs a 16-point
-        // inverse DFT over the half-warp, and accumulates row i's cosine and
-        // sine sums of the inverse X transform.
-        float2 CS[8];   // (cosine sum, sine sum) of row i
-#pragma unroll
-        for (int x = 0; x < 8; x++) CS[x] = make_float2(0.f, 0.f);
-        const float2 *Rj = LC.j ? RB : RA;
-#pragma unroll
-        for (int k = 0; k < 5; k++) {
-            const float2 lo_v = Rj[k * 32 + LC.i];        // R[kk]   (lane kappa^-1(kk) = i)
-            const float2 hi_v = Rj[k * 32 + LC.i + 16];   // R[kk+16]
-            float2 G = LC.y0 ? sub2(lo_v, hi_v) : add2(lo_v, hi_v);
-            G = cmul(G, make_float2(LC.ptw.x, -LC.ptw.y));   // exp(+i pi kk y0 / 16)
-            // 16-point inverse DFT, bit-reversed input -> natural order (DIT)
-            int st = 3;
-#pragma unroll
-            for (int h = 1; h <= 8; h <<= 1, st--) {
-                const bool upper = (LC.i & h) != 0;
-                const float2 w = make_float2(LC.ftw[st].x, -LC.ftw[st].y);   // exp(+2 pi i r/(2h))
-                const float2 o = shfl_xor2(G, h);
-                const float2 t = cmul(upper ? G : o, w);
-                G = upper ? sub2(o, t) : add2(G, t);
-            }
-#pragma unroll
-            for (int x = 0; x < 8; x++) CS[x] = __ffma2_rn(G, c3_xi[k][x], CS[x]);
-        }
-        // Store row i of field 2m + j.
-        const int L = tileY + LC.y0 + 2 * LC.i;
-        if (L >= P.fafl && L <= P.lafl) {
-            const int ofield = 2 * (m - P.frame_begin) + LC.j;
-            float *dst = P.partial + (long long)cls * P.part_class_stride + (long long)ofield * P.part_field_stride +
-                         (long long)((L >> 1) - P.fl_lo) * P.part_row_stride - P.avs;
-            // tileX - avs is a multiple of 8, so an interior tile's row starts
-            // on a 32-byte boundary whenever the planes' strides are multiples
-            // of 4 floats and their base is 16-byte aligned: four vector stores
-            const bool vec = ((P.part_row_stride | P.part_field_stride | P.part_class_stride) & 3) == 0 &&
-                             (reinterpret_cast<uintptr_t>(P.partial) & 15) == 0 && tileX >= P.avs &&
-                             tileX + 16 <= P.ave;
-            if (vec) {
-                float o[16];
-#pragma unroll
-                for (int x = 0; x < 8; x++) {
-                    o[x] = CS[x].x - CS[x].y;
-                    o[15 - x] = CS[x].x + CS[x].y;
-                }
-                float4 *d4 = reinterpret_cast<float4 *>(dst + tileX);
-#pragma unroll
-                for (int q = 0; q < 4; q++) d4[q] = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
-            } else {
-#pragma unroll
-                for (int x = 0; x < 8; x++) {
-                    const int X0 = tileX + x, X1 = tileX + 15 - x;
-                    if (X0 >= P.avs && X0 < P.ave) dst[X0] = CS[x].x - CS[x].y;
-                    if (X1 >= P.avs && X1 < P.ave) dst[X1] = CS[x].x + CS[x].y;
-                }
-            }
-        }
+        walk_store(P, LC, RA, RB, m, tileX, tileY, cls);
     }
     __syncwarp();   // the next item reuses this warp's shared window
     }
+}
+
+// ---------------------------------------------------------------------------
+// Learned-mask form: feature pass and apply pass
+// ---------------------------------------------------------------------------
+// FP32 threshold decisions of kx group g (the walk's rule without the exact
+// resolution): bits kz of column A kept; the caller derives column B's.
+__device__ __forceinline__ unsigned fp32_keep(const Col &A, const float (&rmag)[8], int g, int my_ky, int kyr, float t)
+{
+    unsigned keep = 0;
+#pragma unroll
+    for (int kz = 0; kz < 8; kz++) {
+        const int kzr = (10 - kz) & 7;
+        const bool self = (g == 2) && (kz == kzr) && (my_ky == kyr);
+        if (fsim(A.mag[kz], rmag[kzr], t) || self) keep |= 1u << kz;
+    }
+    return keep;
+}
+
+__device__ __forceinline__ unsigned mirror_keep(unsigned keep, int mirror_lane)
+{
+    const unsigned mk = __shfl_sync(0xffffffffu, keep, mirror_lane);
+    unsigned keepB = 0;
+#pragma unroll
+    for (int kz = 0; kz < 8; kz++) keepB |= ((mk >> ((10 - kz) & 7)) & 1u) << kz;
+    return keepB;
+}
+
+__device__ __forceinline__ uint16_t bf16_bits(float x)
+{
+    const __nv_bfloat16 h = __float2bfloat16_rn(x);
+    return *reinterpret_cast<const uint16_t *>(&h);
+}
+
+// PASS 0: features (+ spectrum, + threshold decisions) of every Z tile the
+// walk computes; PASS 1: the same walk with each bin scaled by its fraction
+// (or, on fallback tiles, masked by the FP32 threshold decisions), then the
+// inverse and overlap-add of the plain walk.
+template <int PASS>
+__global__ void __launch_bounds__(32 * kWarps3, 3) tpal3d_learned_kernel(T3Params P, T3Learn L)
+{
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int ntiles = P.ntx * P.nty;
+    const unsigned nitems = (unsigned)(ntiles * P.nchunks);
+    for (unsigned w = blockIdx.x * kWarps3 + warp; w < nitems; w += gridDim.x * kWarps3) {
+    const int item = (int)w;
+    const int tile = item % ntiles;
+    const int chunk = item / ntiles;
+    const int tx = tile % P.ntx, ty = tile / P.ntx;
+    const int tileX = P.tileX0 + 8 * tx;
+    const int tileY = P.tileY0 + 16 * ty;
+    const int m0 = P.frame_begin + chunk * P.chunk_frames;
+    const int m1 = min(m0 + P.chunk_frames, P.frame_end);
+    const int cls = ((ty & 1) << 1) | (tx & 1);
+
+    extern __shared__ float4 s_dyn[];
+    float2 *wbase = reinterpret_cast<float2 *>(s_dyn) + (size_t)warp * kWarpSmemF2;
+    float2 *win = wbase;
+    float2 *carry_base = wbase + 8 * 5 * 32;
+    float *bnd = reinterpret_cast<float *>(carry_base + 2 * 2 * 5 * 32);
+
+    const LaneConst LC = lane_const(lane, tileY, P.swap);
+    const int my_ky = kappa(lane);
+    const int kyr = (40 - my_ky) & 31;
+    const int mirror_lane = kappa(kyr);
+
+    for (int m = m0 - 5; m < m1; m++) {
+        __syncwarp();
+        forward_pair(P, m + 3, tileX, tileY, LC, lane, win, bnd);
+        __syncwarp();
+        if (m < m0 - 2) continue;
+        const long long base = ((long long)(m - L.z0) * ntiles + tile) * 1280;
+        float2 *carry = carry_base + (m & 1) * (2 * 5 * 32);
+        float2 *RA = win + ((2 * m) & 7) * 5 * 32;
+        float2 *RB = win + ((2 * m + 1) & 7) * 5 * 32;
+        const bool fb = (PASS == 1) ? (L.fallback[(long long)(m - L.z0) * ntiles + tile] != 0) : false;
+#pragma unroll 1
+        for (int g = 0; g < 3; g++) {
+            const int ka = g, kb = 4 - g;
+            float rmag[8];
+            Col B;
+            if (g < 2) {
+                z_column(win, m, kb, lane, 0.f, B);
+#pragma unroll
+                for (int kz = 0; kz < 8; kz++) rmag[kz] = __shfl_sync(0xffffffffu, B.mag[kz], mirror_lane);
+            }
+            Col A;
+            z_column(win, m, ka, lane, 0.f, A);
+            if (g == 2) {
+#pragma unroll
+                for (int kz = 0; kz < 8; kz++) rmag[kz] = __shfl_sync(0xffffffffu, A.mag[kz], mirror_lane);
+            }
+            if (PASS == 0) {
+#pragma unroll
+                for (int kz = 0; kz < 8; kz++) {
+                    const long long va = base + (ka * 8 + kz) * 32 + my_ky;
+                    L.feat[va] = bf16_bits(log1pf(sqrtf(A.mag[kz])) * 0.0625f);
+                    if (L.spec != nullptr) L.spec[va] = A.Y[kz];
+                    if (g < 2) {
+                        const long long vb = base + (kb * 8 + kz) * 32 + my_ky;
+                        L.feat[vb] = bf16_bits(log1pf(sqrtf(B.mag[kz])) * 0.0625f);
+                        if (L.spec != nullptr) L.spec[vb] = B.Y[kz];
+                    }
+                }
+                if (L.plain_p != nullptr) {
+                    const unsigned keep = fp32_keep(A, rmag, g, my_ky, kyr, P.t2f);
+                    const unsigned keepB = mirror_keep(keep, mirror_lane);
+#pragma unroll
+                    for (int kz = 0; kz < 8; kz++) {
+                        L.plain_p[base + (ka * 8 + kz) * 32 + my_ky] = (float)((keep >> kz) & 1u);
+                        if (g < 2) L.plain_p[base + (kb * 8 + kz) * 32 + my_ky] = (float)((keepB >> kz) & 1u);
+                    }
+                }
+            } else {
+                if (fb) {
+                    const unsigned keep = fp32_keep(A, rmag, g, my_ky, kyr, P.t2f);
+                    const unsigned keepB = mirror_keep(keep, mirror_lane);
+                    z_inverse(A.Y, keep, carry, RA, RB, ka, lane);
+                    if (g < 2) z_inverse(B.Y, keepB, carry, RA, RB, kb, lane);
+                } else {
+#pragma unroll
+                    for (int kz = 0; kz < 8; kz++) {
+                        const float pa = __ldg(L.p + base + (ka * 8 + kz) * 32 + my_ky);
+                        A.Y[kz] = __fmul2_rn(A.Y[kz], make_float2(pa, pa));
+                        if (g < 2) {
+                            const float pb = __ldg(L.p + base + (kb * 8 + kz) * 32 + my_ky);
+                            B.Y[kz] = __fmul2_rn(B.Y[kz], make_float2(pb, pb));
+                        }
+                    }
+                    z_inverse(A.Y, 0xFFu, carry, RA, RB, ka, lane);
+                    if (g < 2) z_inverse(B.Y, 0xFFu, carry, RA, RB, kb, lane);
+                }
+            }
+        }
+        __syncwarp();
+        if (PASS == 0 || m < m0) continue;
+        walk_store(P, LC, RA, RB, m, tileX, tileY, cls);
+    }
+    __syncwarp();
+    }
+}
+
+int tp3_learned_launch(const T3Params &P, const T3Learn &L, int pass, cudaStream_t stream)
+{
+    const long long items = (long long)P.ntx * P.nty * P.nchunks;
+    if (items <= 0) return 0;
+    const unsigned blocks = (unsigned)((items + kWarps3 - 1) / kWarps3);
+    const size_t smem = sizeof(float2) * (size_t)kWarpSmemF2 * kWarps3;
+    static bool attr_set[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return -1;
+    if (!attr_set[dev]) {
+        const auto a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+        if (cudaFuncSetAttribute(tpal3d_learned_kernel<0>, a, (int)smem) != cudaSuccess ||
+            cudaFuncSetAttribute(tpal3d_learned_kernel<1>, a, (int)smem) != cudaSuccess)
+            return -1;
+        attr_set[dev] = true;
+    }
+    if (pass == 0) {
+        if (L.feat == nullptr) return -1;
+        tpal3d_learned_kernel<0><<<blocks, 32 * kWarps3, smem, stream>>>(P, L);
+    } else {
+        if (L.p == nullptr || L.fallback == nullptr || P.partial == nullptr) return -1;
+        tpal3d_learned_kernel<1><<<blocks, 32 * kWarps3, smem, stream>>>(P, L);
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 // ---------------------------------------------------------------------------

@@ -108,10 +108,27 @@ struct DemodParams {
     long long out_frame_stride;  // elements per frame
     int out_w, out_h, left_pad, top_pad;
     float ey_scale, ecb_scale, ecr_scale;   // 1/range, ecbFromU/range, ecrFromV/range
+    // the integer formats' code scales, each split hi + lo from double:
+    // 219*256/range (Y, gray16), 224*256*ecbFromU/range, 224*256*ecrFromV/range
+    float qy_hi, qy_lo, qcb_hi, qcb_lo, qcr_hi, qcr_lo;
     float y_lo, y_hi, c_lo, c_hi;           // Y'CbCr clamp bounds (code units for p16/gray16, E' for ps/grays)
     float rgb_y_scale, rgb_uv_scale;        // rgb48: 65535/range; rgbs: 1/range
     float r_from_v, g_from_u, g_from_v, b_from_u;
     float r_lo, r_hi, g_lo, g_hi, b_lo, b_hi;   // R'G'B' clamp bounds
+};
+
+// Learned-mask form of the 3D transform: the walk's two extra passes.
+// Per Z tile T(2m) (zi = m - z0) and spatial tile, the 1,280 bins the filter
+// can keep are indexed v = (q * 8 + kz) * 32 + ky with q = kx - 2 in 0..4.
+struct T3Learn {
+    // feature pass (learned_pass 0): outputs, each [nz][ntiles][1280]
+    uint16_t *feat;              // bf16 bits of ln(1 + |X|) / 16
+    float2 *spec;                // the complex spectrum X (optional)
+    float *plain_p;              // the FP32 threshold decisions as 0 / 1 (optional)
+    // apply pass (learned_pass 1): inputs
+    const float *p;              // kept fraction of each bin [nz][ntiles][1280]
+    const uint8_t *fallback;     // [nz][ntiles]: 1 = the tile takes the threshold decisions instead
+    int z0;                      // Z tile index of step m: m - z0
 };
 
 int tp3_init_constants(int device);
@@ -120,6 +137,11 @@ int tp3_launch(const T3Params &p, cudaStream_t stream, int max_blocks = 0);
 // The resolve pass and the exact walk of the listed items (after
 // tp3_launch; the counters are zeroed before it).
 int tp3_resolve_launch(const T3Params &p, cudaStream_t stream);
+// Learned form: pass 0 writes the features (and optionally the spectrum and
+// the FP32 threshold decisions) of every Z tile of frames
+// [frame_begin, frame_end)'s walk; pass 1 walks again applying the fractions
+// and writes the overlap-class planes. Uniform threshold only.
+int tp3_learned_launch(const T3Params &p, const T3Learn &l, int pass, cudaStream_t stream);
 // Records one launch can write at most: every kx group of every step.
 constexpr unsigned long long tp3_unc_capacity(int ntiles, int frames, int nchunks)
 {

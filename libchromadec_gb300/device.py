@@ -89,6 +89,21 @@ def lib(build: bool = True):
         L.chdg_tc3d_sync.argtypes = [C.c_void_p]
         L.chdg_engine_set_tc_form.argtypes = [C.c_void_p, C.c_int32]
         L.chdg_tc3d_operand.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_size_t]
+        L.chdg_masknet_create.argtypes = [C.POINTER(C.c_void_p)]
+        L.chdg_masknet_free.argtypes = [C.c_void_p]
+        L.chdg_masknet_set_weights.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.c_int64]
+        L.chdg_masknet_get_weights.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.c_int64]
+        L.chdg_masknet_set_confidence.argtypes = [C.c_void_p, C.c_float]
+        L.chdg_masknet_forward.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.chdg_masknet_train_step.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float,
+                                              C.POINTER(C.c_double), C.POINTER(C.c_float), C.c_void_p]
+        L.chdg_masknet_pairs.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
+        L.chdg_learned_features.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
+                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.chdg_learned_chroma.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
+                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.chdg_engine_set_masknet.argtypes = [C.c_void_p, C.c_void_p]
+        L.chdg_engine_learned_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         L.chd_last_error.restype = C.c_char_p
         _lib = L
     return _lib
@@ -181,6 +196,47 @@ class Engine:
         lib().chdg_engine_stats(self._h, C.byref(a), C.byref(b))
         return a.value, b.value
 
+    def set_masknet(self, net: Optional["MaskNet"]):
+        """The learned form with `net`, or the plain form (None)."""
+        rc = lib().chdg_engine_set_masknet(self._h, net._h if net is not None else None)
+        if rc != 0:
+            raise RuntimeError(f"chdg_engine_set_masknet failed ({rc}): {last_error()}")
+        self._net = net   # borrowed by the engine: keep it alive
+
+    def learned_stats(self):
+        t, f = C.c_int64(), C.c_int64()
+        rc = lib().chdg_engine_learned_stats(self._h, C.byref(t), C.byref(f))
+        if rc != 0:
+            raise RuntimeError(f"chdg_engine_learned_stats failed ({rc}): {last_error()}")
+        return t.value, f.value
+
+    def ntiles(self) -> int:
+        """Spatial tiles of the 3D transform (chdg_tc3d_spectra's order)."""
+        g = self.geometry
+        ntx = (g.active_end - g.active_start + 8 + 7) // 8
+        nty = (g.last_active_frame_line - g.first_active_frame_line + 16) // 16 + 1
+        return ntx * nty
+
+    def learned_features(self, fields, frame_begin: int, frame_end: int, feat, spec=None, threshold_p=None,
+                         stream=None):
+        """Features (bf16 bits as int16/uint16 tensor) of the Z tiles of
+        frames [frame_begin, frame_end): (frame_end - frame_begin + 2) x ntiles x 1280."""
+        rc = lib().chdg_learned_features(self._h, C.c_void_p(fields.data_ptr()), fields[0].numel(), fields.shape[0],
+                                         frame_begin, frame_end, C.c_void_p(feat.data_ptr()),
+                                         C.c_void_p(spec.data_ptr()) if spec is not None else None,
+                                         C.c_void_p(threshold_p.data_ptr()) if threshold_p is not None else None,
+                                         self._stream_ptr(stream))
+        if rc != 0:
+            raise RuntimeError(f"chdg_learned_features failed ({rc}): {last_error()}")
+
+    def learned_chroma(self, fields, frame_begin: int, frame_end: int, p, fallback, out, stream=None):
+        rc = lib().chdg_learned_chroma(self._h, C.c_void_p(fields.data_ptr()), fields[0].numel(), fields.shape[0],
+                                       frame_begin, frame_end, C.c_void_p(p.data_ptr()),
+                                       C.c_void_p(fallback.data_ptr()), C.c_void_p(out.data_ptr()),
+                                       self._stream_ptr(stream))
+        if rc != 0:
+            raise RuntimeError(f"chdg_learned_chroma failed ({rc}): {last_error()}")
+
 
 class Batch:
     """chdg_batch: many captures (mixed Transform 2D/3D, one threshold each)
@@ -264,3 +320,81 @@ def tc3d_operand(variant: int, stage: int, y0: int = 0, split: int = 0) -> bytes
     if n < 0:
         raise RuntimeError(f"chdg_tc3d_operand failed ({n}): {last_error()}")
     return bytes(buf[:n])
+
+
+MASKNET_PARAMS = 14753
+MASKNET_BINS = 1280
+
+
+class MaskNet:
+    """chdg_masknet: the learned form's per-bin chroma-fraction network."""
+
+    def __init__(self, weights=None):
+        h = C.c_void_p()
+        rc = lib().chdg_masknet_create(C.byref(h))
+        if rc != 0:
+            raise RuntimeError(f"chdg_masknet_create failed ({rc}): {last_error()}")
+        self._h = h
+        if weights is not None:
+            self.set_weights(weights)
+
+    def set_weights(self, w):
+        import numpy as np
+        a = np.ascontiguousarray(w, dtype=np.float32)
+        if a.size != MASKNET_PARAMS:
+            raise ValueError(f"expected {MASKNET_PARAMS} parameters, got {a.size}")
+        rc = lib().chdg_masknet_set_weights(self._h, a.ctypes.data_as(C.POINTER(C.c_float)), a.size)
+        if rc != 0:
+            raise RuntimeError(f"chdg_masknet_set_weights failed ({rc}): {last_error()}")
+
+    def weights(self):
+        import numpy as np
+        a = np.empty(MASKNET_PARAMS, dtype=np.float32)
+        rc = lib().chdg_masknet_get_weights(self._h, a.ctypes.data_as(C.POINTER(C.c_float)), a.size)
+        if rc != 0:
+            raise RuntimeError(f"chdg_masknet_get_weights failed ({rc}): {last_error()}")
+        return a
+
+    def set_confidence(self, limit: float):
+        rc = lib().chdg_masknet_set_confidence(self._h, limit)
+        if rc != 0:
+            raise RuntimeError(f"chdg_masknet_set_confidence failed ({rc}): {last_error()}")
+
+    def forward(self, feat, ntiles: int, p, fallback=None, stream=None):
+        rc = lib().chdg_masknet_forward(self._h, C.c_void_p(feat.data_ptr()), ntiles, C.c_void_p(p.data_ptr()),
+                                        C.c_void_p(fallback.data_ptr()) if fallback is not None else None,
+                                        Engine._stream_ptr(stream))
+        if rc != 0:
+            raise RuntimeError(f"chdg_masknet_forward failed ({rc}): {last_error()}")
+
+    def train_step(self, feat, ac, ntiles: int, lr: float, want_loss: bool = True, want_grad: bool = False,
+                   stream=None):
+        """One step (lr = 0: gradient only). Returns (loss or None, grad or None)."""
+        import numpy as np
+        loss = C.c_double()
+        grad = np.empty(MASKNET_PARAMS, dtype=np.float32) if want_grad else None
+        rc = lib().chdg_masknet_train_step(self._h, C.c_void_p(feat.data_ptr()), C.c_void_p(ac.data_ptr()), ntiles,
+                                           lr, C.byref(loss) if want_loss else None,
+                                           grad.ctypes.data_as(C.POINTER(C.c_float)) if want_grad else None,
+                                           Engine._stream_ptr(stream))
+        if rc != 0:
+            raise RuntimeError(f"chdg_masknet_train_step failed ({rc}): {last_error()}")
+        return (loss.value if want_loss else None), grad
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().chdg_masknet_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def masknet_pairs(spec_x, spec_c, nbins: int, ac, stream=None):
+    rc = lib().chdg_masknet_pairs(C.c_void_p(spec_x.data_ptr()), C.c_void_p(spec_c.data_ptr()), nbins,
+                                  C.c_void_p(ac.data_ptr()), Engine._stream_ptr(stream))
+    if rc != 0:
+        raise RuntimeError(f"chdg_masknet_pairs failed ({rc}): {last_error()}")
