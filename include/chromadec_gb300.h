@@ -246,8 +246,10 @@ int chdg_masknet_pairs(const float *d_spec_x, const float *d_spec_c, int64_t nbi
  * conventions): Z tiles T(2m) for m = frame_begin - 2 .. frame_end - 1, in
  * that order, each over the engine's spatial tiles (chdg_tc3d_spectra's
  * order). chdg_learned_features writes every Z tile's 1,280 features (and,
- * when not NULL, its complex spectrum X as FP32 pairs and its FP32 threshold
- * decisions as 0 / 1); chdg_learned_chroma decodes the separated chroma, as
+ * when not NULL, its complex spectrum X as FP32 pairs -- with the horizontal
+ * origin at the tile centre, i.e. the reference's r2c bin times
+ * exp(i pi kx 15 / 16), which leaves |X| and products C conj X of two such
+ * spectra unchanged -- and its FP32 threshold decisions as 0 / 1); chdg_learned_chroma decodes the separated chroma, as
  * chdg_chroma_device does, with the given fractions (and fallback flags)
  * applied in place of the threshold. */
 int chdg_learned_features(chdg_engine *e, const uint16_t *d_fields, int64_t field_stride, int32_t nfields,

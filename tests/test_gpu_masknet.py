@@ -95,6 +95,9 @@ def test_feature_pass_matches_fp64_tile_spectra(cuda):
     for zi in range(nz):
         m = fb - 2 + zi
         ref = T.fp64_spectra(cap.fields, m, tiles, g)             # [t, kz, q, ky]
+        # the walk's horizontal origin is the tile centre (x = 7.5): its
+        # spectrum is the reference's times exp(i pi kx 15 / 16)
+        ref = ref * np.exp(1j * np.pi * (2 + np.arange(5)) * 15.0 / 16.0)[None, None, :, None]
         ref = ref.transpose(0, 2, 1, 3).reshape(len(tiles), R.NV)   # v = (q * 8 + kz) * 32 + ky
         got = S[zi, tiles]
         scale = np.abs(ref).max()
@@ -145,3 +148,16 @@ def test_short_training_lowers_the_loss(cuda):
     curve = rec["loss_curve"]
     assert np.all(np.isfinite(w))
     assert curve[-1][1] < curve[0][1] - 0.1 * abs(curve[0][1]), curve
+
+
+def test_trained_network_beats_the_threshold_on_held_out_fields(cuda):
+    """The committed network (trained on seeds >= 1001) against the plain
+    0.4 threshold on a held-out capture: higher chroma PSNR, and less
+    cross-colour and cross-luma energy."""
+    from libchromadec_gb300 import masknet_train as MT
+    from tests import learned_eval as E
+    res = E.evaluate(MT.load_weights(), nfields=60, seed=1, chunk_frames=30)
+    pl, le = res["plain"], res["learned"]
+    assert le["chroma_psnr_db"] > pl["chroma_psnr_db"] + 0.3, res
+    assert le["cross_colour_rel_energy"] < pl["cross_colour_rel_energy"], res
+    assert le["cross_luma_rel_energy"] < pl["cross_luma_rel_energy"], res
