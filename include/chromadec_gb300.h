@@ -227,6 +227,12 @@ void chdg_masknet_free(chdg_masknet *n);
 int chdg_masknet_set_weights(chdg_masknet *n, const float *weights, int64_t count);
 int chdg_masknet_get_weights(const chdg_masknet *n, float *weights, int64_t count);
 int chdg_masknet_set_confidence(chdg_masknet *n, float limit);
+/* The network's convolutions run on the tensor cores (tcgen05 implicit
+ * GEMMs, the default; on = 1) or on the CUDA cores (on = 0, the cross-check).
+ * chdg_masknet_sync waits for `stream` and reports a tensor-core completion
+ * wait that ran out (none is expected). */
+int chdg_masknet_set_tensor_cores(chdg_masknet *n, int32_t on);
+int chdg_masknet_sync(const chdg_masknet *n, void *stream);
 /* d_feat: ntiles x 1280 bf16 features (device); d_p: ntiles x 1280 FP32;
  * d_fallback: ntiles bytes (1 = the tile takes the threshold) or NULL. */
 int chdg_masknet_forward(const chdg_masknet *n, const uint16_t *d_feat, int64_t ntiles, float *d_p,

@@ -39,6 +39,7 @@
 #include "../../include/chromadec_gb300.h"
 #include "error_state.h"
 #include "masknet.h"
+#include "tcgen05_ptx.cuh"
 
 namespace chdg {
 namespace mn {
@@ -466,6 +467,196 @@ __global__ void mn_round_kernel(const float *master, float *used)
     used[i] = bias ? master[i] : bfr(master[i]);
 }
 
+// ---------------------------------------------------------------------------
+// Tensor-core forward pass (tcgen05): each convolution as implicit GEMMs
+// ---------------------------------------------------------------------------
+// Rows m = ky * 8 + kz (kz fastest: each ky is one 8-row core-matrix group),
+// N = 80 columns (q, co), K = (q', ci): the five kx positions fold into N and
+// K, so the kx taps become a banded weight matrix -- block (q, q') holds
+// W[dz][dy][q' - q] for |q' - q| <= 1 and zeros otherwise. A ky tap is an
+// offset of whole groups into the A operand (a one-group periodic halo on
+// both sides); the three kz taps use three copies of the activations with kz
+// rotated inside each group. One layer of one tile: for dz in -1..1, build
+// the rotated copy (34 groups x K) from the compact activations and copy the
+// dz's three weight images, then 3 (ky taps) x 2 (M blocks of 128 rows) x
+// K/16 MMAs of 128 x 80 x 16 accumulate in tensor memory; the epilogue adds
+// the bias, applies ReLU and rounds to bf16 (or runs the sigmoid head).
+constexpr int kTcThreads = 256;
+constexpr int kActStride = 176;                       // bytes per compact activation row (80 bf16 + pad)
+constexpr int kGroupsA = 34;                          // 32 ky groups + one halo group on each side
+constexpr int SM_ACT = 0;                             // [256 rows][kActStride]
+constexpr int SM_A = 256 * kActStride;                // [34 groups][8 rows][K] canonical
+constexpr int SM_B = SM_A + kGroupsA * 8 * 160;       // [3 ky taps][80 rows][K] canonical
+constexpr int SM_BAR = SM_B + 3 * 80 * 160;
+constexpr int kTcSmem = SM_BAR + 64;
+// weight images in global memory: layer 1 (K = 16), layers 2 and 3 (K = 80),
+// each [dz][dy][80 rows][K] in the canonical layout
+constexpr int IMG_L1 = 0;
+constexpr int IMG_L2 = IMG_L1 + 9 * 80 * 32;
+constexpr int IMG_L3 = IMG_L2 + 9 * 80 * 160;
+constexpr int IMG_BYTES = IMG_L3 + 9 * 80 * 160;
+static_assert(SM_A % 16 == 0 && SM_B % 16 == 0 && SM_BAR % 16 == 0, "operand alignment");
+
+__global__ void mn_build_images_kernel(const float *used, uint8_t *img)
+{
+    const int n1 = 9 * 80 * 16, n2 = 9 * 80 * 80;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n1 + 2 * n2; idx += gridDim.x * blockDim.x) {
+        int layer, r = idx;
+        if (r < n1) layer = 0;
+        else if (r < n1 + n2) layer = 1, r -= n1;
+        else layer = 2, r -= n1 + n2;
+        const int K = layer == 0 ? 16 : 80, Ci = layer == 0 ? NCIN : NC;
+        const int k = r % K, n = (r / K) % 80, tap = r / (K * 80);   // tap = dz * 3 + dy
+        const int q = n >> 4, co = n & 15;
+        float v = 0.f;
+        if (k < 5 * Ci) {
+            const int qp = k / Ci, ci = k % Ci, dq = qp - q;
+            if (dq >= -1 && dq <= 1) {
+                const int woff = layer == 0 ? OFF_W1 : (layer == 1 ? OFF_W2 : OFF_W3);
+                v = used[woff + ((tap * 3 + dq + 1) * Ci + ci) * NC + co];
+            }
+        }
+        const int base = layer == 0 ? IMG_L1 : (layer == 1 ? IMG_L2 : IMG_L3);
+        *reinterpret_cast<__nv_bfloat16 *>(img + base + tap * 80 * 2 * K + tpal::tc::elem_off(n, k, 2, 2 * K)) =
+            __float2bfloat16_rn(v);
+    }
+}
+
+template <bool TRAIN>
+__global__ void __launch_bounds__(kTcThreads, 1)
+    mn_tc_forward_kernel(const uint8_t *img, const float *params, const uint16_t *feat, long long ntiles,
+                         float conf_limit, float *p_out, uint8_t *fallback, __nv_bfloat16 *a1g, __nv_bfloat16 *a2g,
+                         __nv_bfloat16 *a3g, int *err)
+{
+    using namespace tpal::tc;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t *act = smem + SM_ACT;
+    uint8_t *A = smem + SM_A;
+    uint8_t *B = smem + SM_B;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + SM_BAR);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + SM_BAR + 8);
+    __shared__ float s_par[4 * NC + 1];   // b1, b2, b3, wh, bh
+    __shared__ float red[kTcThreads / 32];
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    for (int i = t; i < 4 * NC + 1; i += kTcThreads) {
+        const int off[5] = {OFF_B1, OFF_B2, OFF_B3, OFF_WH, OFF_BH};
+        s_par[i] = params[off[i / NC] + i % NC];
+    }
+    if (t == 0) bar_init(bar);
+    if (warp == 0) tmem_alloc(tslot, 256);
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tslot;
+    uint32_t phase = 0;
+    bool ok = true;
+    const int eb = warp >> 2;                          // the epilogue's M block
+    const int erow = eb * 128 + (warp & 3) * 32 + lane;   // its row: ky = erow >> 3, kz = erow & 7
+    const int eky = erow >> 3, ekz = erow & 7;
+    for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        // inputs: row m = t, k = 2 q + c (c = 0: the bin, 1: its mirror), zero-padded to 16
+        {
+            const int ky = t >> 3, kz = t & 7;
+            const __nv_bfloat16 *f = reinterpret_cast<const __nv_bfloat16 *>(feat) + tile * NV;
+            __align__(16) __nv_bfloat16 v[16];
+#pragma unroll
+            for (int q = 0; q < NQ; q++) {
+                v[2 * q] = f[(q * 8 + kz) * 32 + ky];
+                v[2 * q + 1] = f[((4 - q) * 8 + ((10 - kz) & 7)) * 32 + ((40 - ky) & 31)];
+            }
+#pragma unroll
+            for (int k = 10; k < 16; k++) v[k] = __float2bfloat16_rn(0.f);
+            uint4 *d = reinterpret_cast<uint4 *>(act + t * kActStride);
+            d[0] = reinterpret_cast<const uint4 *>(v)[0];
+            d[1] = reinterpret_cast<const uint4 *>(v)[1];
+        }
+        __syncthreads();
+        float conf = 0.f;
+        for (int L = 0; L < 3 && ok; L++) {
+            const int K = L == 0 ? 16 : 80, KB = 2 * K, chunks = K / 8, grp = 8 * KB;
+            const uint8_t *imgL = img + (L == 0 ? IMG_L1 : (L == 1 ? IMG_L2 : IMG_L3));
+            for (int dz = 0; dz < 3 && ok; dz++) {
+                // A: group g holds ky = g - 1 (periodic), row i holds kz = (i + dz - 1) mod 8
+                const int nitems = kGroupsA * chunks * 8;
+                for (int it = t; it < nitems; it += kTcThreads) {
+                    const int i = it & 7, rest = it >> 3, c = rest % chunks, g = rest / chunks;
+                    const int src = (((g + 31) & 31) << 3) | ((i + dz + 7) & 7);
+                    *reinterpret_cast<uint4 *>(A + g * grp + c * 128 + i * 16) =
+                        *reinterpret_cast<const uint4 *>(act + src * kActStride + c * 16);
+                }
+                // B: this dz's three ky-tap images
+                const uint4 *bs = reinterpret_cast<const uint4 *>(imgL + dz * 3 * 80 * KB);
+                uint4 *bd = reinterpret_cast<uint4 *>(B);
+                for (int o = t; o < 3 * 80 * KB / 16; o += kTcThreads) bd[o] = __ldg(bs + o);
+                fence_async_smem();
+                fence_before();
+                __syncthreads();
+                if (t == 0) {
+                    fence_after();
+                    const uint32_t id = idesc(1, 128, 80);
+                    for (int dy = 0; dy < 3; dy++)
+                        for (int b = 0; b < 2; b++)
+                            for (int ks = 0; ks < K / 16; ks++) {
+                                const uint32_t a = smem_addr(A + (b * 16 + dy) * grp + ks * 256);
+                                const uint32_t bb = smem_addr(B + dy * 80 * KB + ks * 256);
+                                mma<1>(tmem + b * 128, sdesc(a, grp), sdesc(bb, grp), id,
+                                       (dz > 0 || dy > 0 || ks > 0) ? 1u : 0u);
+                            }
+                    mma_commit(bar);
+                }
+                const bool done = bar_wait(bar, phase);
+                phase ^= 1;
+                if (__syncthreads_or(!done)) ok = false;
+                fence_after();
+            }
+            if (!ok) break;
+            // epilogue: the warp's 32 rows of its M block, 80 columns (q, co)
+            const uint32_t tb = tmem + ((uint32_t)((warp & 3) * 32) << 16) + eb * 128;
+#pragma unroll 1
+            for (int q = 0; q < NQ; q++) {
+                float v[16];
+                tmem_ld16(tb + 16 * q, v);
+                const int vox = (q * 8 + ekz) * 32 + eky;
+                if (L < 2) {
+                    __align__(16) __nv_bfloat16 o[16];
+#pragma unroll
+                    for (int co = 0; co < NC; co++) o[co] = __float2bfloat16_rn(fmaxf(v[co] + s_par[L * NC + co], 0.f));
+                    uint4 *d = reinterpret_cast<uint4 *>(act + erow * kActStride + q * 32);
+                    d[0] = reinterpret_cast<const uint4 *>(o)[0];
+                    d[1] = reinterpret_cast<const uint4 *>(o)[1];
+                    if (TRAIN) {
+                        __nv_bfloat16 *ag = (L == 0 ? a1g : a2g) + tile * NC * NV;
+#pragma unroll
+                        for (int co = 0; co < NC; co++) ag[co * NV + vox] = o[co];
+                    }
+                } else {
+                    float zh = s_par[4 * NC];
+#pragma unroll
+                    for (int co = 0; co < NC; co++) {
+                        const float a = bfr(fmaxf(v[co] + s_par[2 * NC + co], 0.f));
+                        if (TRAIN) a3g[tile * NC * NV + co * NV + vox] = __float2bfloat16_rn(a);
+                        zh = __fmaf_rn(a, s_par[3 * NC + co], zh);
+                    }
+                    const float p = 1.0f / (1.0f + expf(-zh));
+                    p_out[tile * NV + vox] = p;
+                    conf += fabsf(p - 0.5f);
+                }
+            }
+            fence_before();
+            __syncthreads();
+        }
+        if (!ok) break;
+        const float s = block_sum(conf, red);
+        if (t == 0 && fallback != nullptr) fallback[tile] = (s * (1.0f / NV) < conf_limit) ? 1 : 0;
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 0) tmem_dealloc(tmem, 256);
+    if (!ok && t == 0) atomicExch(err, 1);
+}
+
 }  // namespace mn
 
 // ---------------------------------------------------------------------------
@@ -485,7 +676,7 @@ static int mn_cuda(const char *what, cudaError_t e)
 MaskNet::~MaskNet()
 {
     for (void *p : {(void *)master_, (void *)used_, (void *)m_, (void *)v_, (void *)gpart_, (void *)a1_, (void *)a2_,
-                    (void *)a3_, (void *)p_, (void *)dz_, (void *)scal_, (void *)grad_})
+                    (void *)a3_, (void *)p_, (void *)dz_, (void *)scal_, (void *)grad_, (void *)img_, (void *)err_})
         if (p) cudaFree(p);
 }
 
@@ -498,6 +689,9 @@ int MaskNet::init()
     cudaMemset(m_, 0, pb);
     cudaMemset(v_, 0, pb);
     if ((e = cudaMalloc(&scal_, 2 * sizeof(double))) != cudaSuccess) return mn_cuda("cudaMalloc", e);
+    if ((e = cudaMalloc(&img_, mn::IMG_BYTES)) != cudaSuccess) return mn_cuda("cudaMalloc", e);
+    if ((e = cudaMalloc(&err_, sizeof(int))) != cudaSuccess) return mn_cuda("cudaMalloc", e);
+    cudaMemset(err_, 0, sizeof(int));
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -510,7 +704,9 @@ int MaskNet::init()
         const auto a = cudaFuncAttributeMaxDynamicSharedMemorySize;
         if (cudaFuncSetAttribute(mn::mn_forward_kernel<false>, a, (int)mn::kFwdSmem) != cudaSuccess ||
             cudaFuncSetAttribute(mn::mn_forward_kernel<true>, a, (int)mn::kFwdSmem) != cudaSuccess ||
-            cudaFuncSetAttribute(mn::mn_backward_kernel, a, (int)mn::kBwdSmem) != cudaSuccess)
+            cudaFuncSetAttribute(mn::mn_backward_kernel, a, (int)mn::kBwdSmem) != cudaSuccess ||
+            cudaFuncSetAttribute(mn::mn_tc_forward_kernel<false>, a, mn::kTcSmem) != cudaSuccess ||
+            cudaFuncSetAttribute(mn::mn_tc_forward_kernel<true>, a, mn::kTcSmem) != cudaSuccess)
             return mn_cuda("cudaFuncSetAttribute", cudaGetLastError());
         attr[dev] = true;
     }
@@ -526,7 +722,25 @@ int MaskNet::set_weights(const float *host, size_t n)
     cudaMemset(v_, 0, sizeof(float) * n);
     step_ = 0;
     mn::mn_round_kernel<<<(mn::NPARAM + 255) / 256, 256>>>(master_, used_);
+    if (const int rc = build_images(nullptr); rc != 0) return rc;
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return mn_cuda("round", e);
+    return 0;
+}
+
+int MaskNet::build_images(cudaStream_t s)
+{
+    mn::mn_build_images_kernel<<<256, 256, 0, s>>>(used_, img_);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? 0 : mn_cuda("weight images", e);
+}
+
+int MaskNet::sync(cudaStream_t s) const
+{
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return mn_cuda("sync", e);
+    int h = 0;
+    if ((e = cudaMemcpy(&h, err_, sizeof(int), cudaMemcpyDeviceToHost)) != cudaSuccess) return mn_cuda("sync", e);
+    if (h != 0) return mn_fail("a tensor-core completion wait ran out", CHDG_E_CUDA);
     return 0;
 }
 
@@ -542,8 +756,13 @@ int MaskNet::forward(const uint16_t *d_feat, long long ntiles, float *d_p, uint8
     if (ntiles <= 0) return 0;
     if (d_feat == nullptr || d_p == nullptr) return mn_fail("forward: null buffer");
     const unsigned blocks = (unsigned)std::min<long long>(ntiles, (long long)grid_ * 1);
-    mn::mn_forward_kernel<false><<<blocks, mn::kThreads, mn::kFwdSmem, s>>>(used_, d_feat, ntiles, conf_limit_, d_p,
-                                                                            d_fallback, nullptr, nullptr, nullptr);
+    if (tc_)
+        mn::mn_tc_forward_kernel<false><<<blocks, mn::kTcThreads, mn::kTcSmem, s>>>(
+            img_, used_, d_feat, ntiles, conf_limit_, d_p, d_fallback, nullptr, nullptr, nullptr, err_);
+    else
+        mn::mn_forward_kernel<false><<<blocks, mn::kThreads, mn::kFwdSmem, s>>>(used_, d_feat, ntiles, conf_limit_,
+                                                                                d_p, d_fallback, nullptr, nullptr,
+                                                                                nullptr);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? 0 : mn_cuda("forward launch", e);
 }
@@ -575,9 +794,14 @@ int MaskNet::train_step(const uint16_t *d_feat, const float2 *d_ac, long long nt
     if (const int rc = ensure_batch(ntiles); rc != 0) return rc;
     const unsigned blocks = (unsigned)std::min<long long>(ntiles, grid_);
     cudaMemsetAsync(scal_, 0, 2 * sizeof(double), s);
-    mn::mn_forward_kernel<true><<<blocks, mn::kThreads, mn::kFwdSmem, s>>>(
-        used_, d_feat, ntiles, conf_limit_, p_, nullptr, (__nv_bfloat16 *)a1_, (__nv_bfloat16 *)a2_,
-        (__nv_bfloat16 *)a3_);
+    if (tc_)
+        mn::mn_tc_forward_kernel<true><<<blocks, mn::kTcThreads, mn::kTcSmem, s>>>(
+            img_, used_, d_feat, ntiles, conf_limit_, p_, nullptr, (__nv_bfloat16 *)a1_, (__nv_bfloat16 *)a2_,
+            (__nv_bfloat16 *)a3_, err_);
+    else
+        mn::mn_forward_kernel<true><<<blocks, mn::kThreads, mn::kFwdSmem, s>>>(
+            used_, d_feat, ntiles, conf_limit_, p_, nullptr, (__nv_bfloat16 *)a1_, (__nv_bfloat16 *)a2_,
+            (__nv_bfloat16 *)a3_);
     const long long n = ntiles * mn::NV;
     mn::mn_sum_kernel<<<256, 256, 0, s>>>(d_ac, n, scal_);
     mn::mn_loss_kernel<<<256, 256, 0, s>>>(p_, d_ac, n, scal_, dz_, scal_ + 1);
@@ -592,10 +816,12 @@ int MaskNet::train_step(const uint16_t *d_feat, const float2 *d_ac, long long nt
     }
     mn::mn_adam_kernel<<<(mn::NPARAM + 255) / 256, 256, 0, s>>>(master_, used_, m_, v_, gpart_, (int)blocks, lr, 0.9f,
                                                                0.999f, 1e-8f, c1, c2, grad_);
+    if (lr > 0.f)
+        if (const int rc = build_images(s); rc != 0) return rc;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return mn_cuda("train launch", e);
     if (loss != nullptr || host_grad != nullptr) {
-        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return mn_cuda("train sync", e);
+        if (const int rc = sync(s); rc != 0) return rc;
         if (loss != nullptr) {
             double h[2];
             cudaMemcpy(h, scal_, sizeof(h), cudaMemcpyDeviceToHost);
@@ -657,6 +883,19 @@ int chdg_masknet_set_confidence(chdg_masknet *n, float limit)
     if (n == nullptr || !(limit >= 0.f && limit <= 0.5f)) return chdg::mn_fail("set_confidence: limit must be in [0, 0.5]");
     n->net.set_confidence(limit);
     return 0;
+}
+
+int chdg_masknet_set_tensor_cores(chdg_masknet *n, int32_t on)
+{
+    if (n == nullptr) return chdg::mn_fail("set_tensor_cores: null network");
+    n->net.set_tensor_cores(on != 0);
+    return 0;
+}
+
+int chdg_masknet_sync(const chdg_masknet *n, void *stream)
+{
+    if (n == nullptr) return chdg::mn_fail("sync: null network");
+    return n->net.sync((cudaStream_t)stream);
 }
 
 int chdg_masknet_forward(const chdg_masknet *n, const uint16_t *d_feat, int64_t ntiles, float *d_p,

@@ -20,6 +20,11 @@ public:
     int set_weights(const float *host, size_t n);
     int get_weights(float *host, size_t n) const;
     void set_confidence(float limit) { conf_limit_ = limit; }
+    // forward passes on the tensor cores (tcgen05, the default) or on the
+    // CUDA cores (the SIMT kernel, kept as the cross-check)
+    void set_tensor_cores(bool on) { tc_ = on; }
+    // wait for `s` and report a tensor-core completion wait that ran out
+    int sync(cudaStream_t s) const;
     float confidence() const { return conf_limit_; }
     // p (and fallback flags) of ntiles tiles of features, [tile][1280]
     int forward(const uint16_t *d_feat, long long ntiles, float *d_p, uint8_t *d_fallback, cudaStream_t s) const;
@@ -31,6 +36,7 @@ public:
 
 private:
     int ensure_batch(long long ntiles);
+    int build_images(cudaStream_t s);
     float *master_ = nullptr, *used_ = nullptr, *m_ = nullptr, *v_ = nullptr, *grad_ = nullptr;
     float *gpart_ = nullptr;
     double *scal_ = nullptr;
@@ -40,6 +46,9 @@ private:
     int grid_ = 1;
     long long step_ = 0;
     float conf_limit_ = 0.1f;
+    bool tc_ = true;
+    uint8_t *img_ = nullptr;   // bf16 weight images of the tensor-core kernel
+    int *err_ = nullptr;
 };
 
 }  // namespace chdg

@@ -97,6 +97,8 @@ def lib(build: bool = True):
         L.chdg_masknet_forward.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
         L.chdg_masknet_train_step.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float,
                                               C.POINTER(C.c_double), C.POINTER(C.c_float), C.c_void_p]
+        L.chdg_masknet_set_tensor_cores.argtypes = [C.c_void_p, C.c_int32]
+        L.chdg_masknet_sync.argtypes = [C.c_void_p, C.c_void_p]
         L.chdg_masknet_pairs.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
         L.chdg_learned_features.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int32, C.c_int32, C.c_int32,
                                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -359,6 +361,16 @@ class MaskNet:
         rc = lib().chdg_masknet_set_confidence(self._h, limit)
         if rc != 0:
             raise RuntimeError(f"chdg_masknet_set_confidence failed ({rc}): {last_error()}")
+
+    def set_tensor_cores(self, on: bool):
+        rc = lib().chdg_masknet_set_tensor_cores(self._h, 1 if on else 0)
+        if rc != 0:
+            raise RuntimeError(f"chdg_masknet_set_tensor_cores failed ({rc}): {last_error()}")
+
+    def sync(self, stream=None):
+        rc = lib().chdg_masknet_sync(self._h, Engine._stream_ptr(stream))
+        if rc != 0:
+            raise RuntimeError(f"chdg_masknet_sync failed ({rc}): {last_error()}")
 
     def forward(self, feat, ntiles: int, p, fallback=None, stream=None):
         rc = lib().chdg_masknet_forward(self._h, C.c_void_p(feat.data_ptr()), ntiles, C.c_void_p(p.data_ptr()),

@@ -28,16 +28,18 @@ def _problem(seed, b):
     return params, feat, a, c
 
 
-def test_forward_matches_restatement(cuda):
+@pytest.mark.parametrize("tensor_cores", [True, False])
+def test_forward_matches_restatement(cuda, tensor_cores):
     torch = cuda
     from libchromadec_gb300 import device as D
     params, feat, _, _ = _problem(3, 6)
     net = D.MaskNet(params)
+    net.set_tensor_cores(tensor_cores)
     f = _bf16_bits(feat.reshape(6, -1)).cuda()
     p = torch.empty((6, R.NV), dtype=torch.float32, device="cuda")
     fb = torch.empty(6, dtype=torch.uint8, device="cuda")
     net.forward(f, 6, p, fb)
-    torch.cuda.synchronize()
+    net.sync()
     ref, _ = R.forward(params.astype(np.float64), feat)
     got = p.cpu().numpy().reshape(ref.shape)
     assert np.abs(got - ref).max() < 3e-3, np.abs(got - ref).max()
@@ -48,12 +50,14 @@ def test_forward_matches_restatement(cuda):
     net.close()
 
 
-def test_gradient_of_every_layer_matches_restatement(cuda):
+@pytest.mark.parametrize("tensor_cores", [True, False])
+def test_gradient_of_every_layer_matches_restatement(cuda, tensor_cores):
     torch = cuda
     from libchromadec_gb300 import device as D
     b = 5
     params, feat, a, c = _problem(4, b)
     net = D.MaskNet(params)
+    net.set_tensor_cores(tensor_cores)
     f = _bf16_bits(feat.reshape(b, -1)).cuda()
     ac = torch.from_numpy(np.stack([a, c], axis=-1).reshape(b, R.NV, 2).astype(np.float32)).cuda()
     loss, grad = net.train_step(f, ac, b, 0.0, want_loss=True, want_grad=True)
@@ -167,3 +171,29 @@ def test_trained_network_beats_the_threshold_on_held_out_fields(cuda):
     assert le["cross_colour_rel_energy"] < 0.5 * pl["cross_colour_rel_energy"], res
     assert le["cross_colour_rel_energy"] + le["cross_luma_rel_energy"] < \
         pl["cross_colour_rel_energy"] + pl["cross_luma_rel_energy"], res
+
+
+def test_tensor_core_and_cuda_core_forward_agree_on_trained_weights(cuda):
+    """The trained network over real tile features: both forward kernels give
+    the same fractions up to FP32 accumulation order (and the rare bf16
+    activation that rounds the other way)."""
+    torch = cuda
+    from libchromadec_gb300 import device as D, masknet_train as MT
+    cap = capture(16, 63)
+    fields = torch.from_numpy(cap.fields.reshape(16, -1).view(np.int16)).cuda()
+    eng = D.Engine(D.default_geometry(), D.default_config(kind=D.KIND_TRANSFORM_3D))
+    nt = eng.ntiles()
+    feat = torch.empty((5 * nt, R.NV), dtype=torch.int16, device="cuda")
+    eng.learned_features(fields, 2, 5, feat)
+    net = D.MaskNet(MT.load_weights())
+    out = []
+    for tc in (True, False):
+        net.set_tensor_cores(tc)
+        p = torch.empty((5 * nt, R.NV), dtype=torch.float32, device="cuda")
+        fb = torch.empty(5 * nt, dtype=torch.uint8, device="cuda")
+        net.forward(feat, 5 * nt, p, fb)
+        net.sync()
+        out.append((p, fb))
+    d = (out[0][0] - out[1][0]).abs()
+    assert float(d.max()) < 2e-2 and float(d.mean()) < 1e-5
+    assert float((out[0][1] != out[1][1]).float().mean()) < 1e-3
