@@ -62,8 +62,8 @@ def parse():
     ap.add_argument("--no-forms", action="store_true", help="skip the tensor-core forms and chroma PSNR report")
     ap.add_argument("--kind", default="3d", choices=["3d", "2d"],
                     help="Transform-PAL 3D (the metric) or 2D (for profiling the 2D kernel)")
-    ap.add_argument("--form", default="plain", choices=["plain", "tc_3xtf32", "tc_bf16x3"],
-                    help="transform form of the timed decode (the tensor-core forms for profiling them)")
+    ap.add_argument("--form", default="plain", choices=["plain", "tc_3xtf32", "tc_bf16x3", "learned"],
+                    help="transform form of the timed decode (the tensor-core and learned forms for profiling them)")
     ap.add_argument("--workload", default="stream", choices=["stream", "batched"],
                     help="stream: the 500-field 3D capture (the headline line); batched: 48 captures of "
                          "6-300 fields, 40%% 2D / 60%% 3D, one threshold each, through chdg_batch_*")
@@ -599,10 +599,15 @@ def main():
         a.no_e2e = a.no_cpu = a.no_forms = True
     eng = D.Engine(D.default_geometry(),
                    D.default_config(kind=D.KIND_TRANSFORM_2D if two else D.KIND_TRANSFORM_3D, fmt=fmt))
-    tc_form = {"plain": -1, "tc_3xtf32": D.TC_3XTF32, "tc_bf16x3": D.TC_BF16X3}[a.form]
-    if two and tc_form >= 0:
-        raise SystemExit("the tensor-core form is Transform 3D only")
+    tc_form = {"plain": -1, "tc_3xtf32": D.TC_3XTF32, "tc_bf16x3": D.TC_BF16X3, "learned": -1}[a.form]
+    if two and (tc_form >= 0 or a.form == "learned"):
+        raise SystemExit("the tensor-core and learned forms are Transform 3D only")
     eng.set_tc_form(tc_form)
+    if a.form == "learned":
+        from libchromadec_gb300 import masknet_train as MT
+        learned_net = D.MaskNet(MT.load_weights())
+        eng.set_masknet(learned_net)
+        a.no_forms = True
     lib = D.lib()
     dfields = torch.from_numpy(fields_np.reshape(nfields, -1).view(np.int16)).cuda()
     out_dtype = torch.int16 if fmt == D.FMT_P16 else torch.float32
@@ -639,7 +644,8 @@ def main():
     # roofline of the dominant kernel (the transform): launches per step
     # one engine batch = 4 launches: the transform walk, the resolve pass,
     # the exact re-walk of the items it lists, the demodulator
-    launches_transform = (nl.value // 2 if two else nl.value // 4) if tc_form < 0 else a.steps * ((nframes + 255) // 256)
+    launches_transform = (nl.value // 2 if two else nl.value // (5 if a.form == "learned" else 4)) if tc_form < 0 \
+        else a.steps * ((nframes + 255) // 256)
     per_launch_ms = mt.value / max(1, launches_transform)
     fields_per_launch = nfields * a.steps / max(1, launches_transform)
     bytes_per_field = FIELD_BYTES_IN + OUT_BYTES[a.format]

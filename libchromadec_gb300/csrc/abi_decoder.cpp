@@ -503,9 +503,6 @@ CHD_API chd_status_t chd_decoder_commit(chd_decoder_t *d)
         log_returned(CHD_LOG_ERROR, "This decoder is for PAL video sources only");
         return fail(CHD_E_DECODER_INCOMPATIBLE, "chd_decoder_commit: This decoder is for PAL video sources only");
     }
-    // what the GPU path covers: the 625-line 4fsc raster
-    if (src.system != SYS_PAL)
-        return fail(CHD_E_UNSUPPORTED, "chd_decoder_commit: the GPU path decodes 625-line PAL only");
     c.threshold = find_or(o.f64, CHD_OPT_TRANSFORM_THRESHOLD, c.threshold);
     c.chroma_gain = find_or(o.f64, CHD_OPT_CHROMA_GAIN, c.chroma_gain);
     c.chroma_phase_deg = find_or(o.f64, CHD_OPT_CHROMA_PHASE_DEG, c.chroma_phase_deg);

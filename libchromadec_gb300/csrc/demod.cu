@@ -39,8 +39,6 @@
 
 namespace tpal {
 
-__constant__ float cd_cfilt[8][4];   // PALcolour chroma 2D FIR taps (filterSize = 7)
-__constant__ float cd_yfilt[8][2];   // PALcolour luma-extraction taps
 __constant__ float cd_nrpal[25];     // doYNR high-pass (c_nrpal_b)
 static bool g_demod_ready[64];
 
@@ -62,9 +60,14 @@ __device__ __forceinline__ float carrier_cos(int x) { return (x & 1) ? 0.f : ((x
 
 // The 2D FIR of one work item: PU, QU, PV, QV (and PY, QY from the luma
 // taps when WITH_Y) for 8 samples from the 4 vertical combinations v.
+// Taps b = 0..7 of the launch's filter (a filter of size 6, at PAL-M's
+// sample rate, has zero taps at b = 7). swap: the reference's PAL-M tables
+// (sine and cosine exchanged at fieldHeight 263, palcolour.cpp:158-173) make
+// each P sum the other table's Q sum and vice versa: (PU, QU, PV, QV)
+// become (QV, PV, QU, PU); the luma resynthesis is unchanged.
 template <bool WITH_Y>
-__device__ __forceinline__ void item_fir(const float (&v)[4][22], float (&PU)[8], float (&QU)[8], float (&PV)[8],
-                                         float (&QV)[8], float (&PY)[8], float (&QY)[8])
+__device__ __forceinline__ void item_fir(const DemodParams &P, const float (&v)[4][22], float (&PU)[8], float (&QU)[8],
+                                         float (&PV)[8], float (&QV)[8], float (&PY)[8], float (&QY)[8])
 {
 #pragma unroll
     for (int s = 0; s < 8; s++) {
@@ -75,10 +78,10 @@ __device__ __forceinline__ void item_fir(const float (&v)[4][22], float (&PU)[8]
             float sg[4];
 #pragma unroll
             for (int k = 0; k < 4; k++) sg[k] = (b & 1) ? v[k][r] - v[k][l] : v[k][r] + v[k][l];
-            const float A = __fmaf_rn(cd_cfilt[b][1], sg[1], cd_cfilt[b][0] * sg[0]);
-            const float B = __fmaf_rn(cd_cfilt[b][3], sg[3], cd_cfilt[b][2] * sg[2]);
+            const float A = __fmaf_rn(P.cfilt[b][1], sg[1], P.cfilt[b][0] * sg[0]);
+            const float B = __fmaf_rn(P.cfilt[b][3], sg[3], P.cfilt[b][2] * sg[2]);
             float AY = 0.f;
-            if (WITH_Y) AY = __fmaf_rn(cd_yfilt[b][1], sg[1], cd_yfilt[b][0] * sg[0]);
+            if (WITH_Y) AY = __fmaf_rn(P.yfilt[b][1], sg[1], P.yfilt[b][0] * sg[0]);
             switch ((s + b) & 3) {
             case 1: PA += A; PB += B; if (WITH_Y) PYs += AY; break;
             case 3: PA -= A; PB -= B; if (WITH_Y) PYs -= AY; break;
@@ -86,10 +89,17 @@ __device__ __forceinline__ void item_fir(const float (&v)[4][22], float (&PU)[8]
             default: QA -= A; QB -= B; if (WITH_Y) QYs -= AY; break;
             }
         }
-        PU[s] = PA + QB;
-        PV[s] = PA - QB;
-        QU[s] = QA - PB;
-        QV[s] = QA + PB;
+        if (P.swap_carrier) {
+            PU[s] = QA + PB;
+            PV[s] = QA - PB;
+            QU[s] = PA - QB;
+            QV[s] = PA + QB;
+        } else {
+            PU[s] = PA + QB;
+            PV[s] = PA - QB;
+            QU[s] = QA - PB;
+            QV[s] = QA + PB;
+        }
         PY[s] = PYs;
         QY[s] = QYs;
     }
@@ -259,7 +269,7 @@ __device__ __forceinline__ df df_div_f(float a, df d)
 __device__ __forceinline__ float df_round(df v) { return __fadd_rn(v.hi, v.lo); }
 
 template <bool COMPOSITE, bool YNR>
-__global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
+__global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(const __grid_constant__ DemodParams P)
 {
     constexpr int kDemodLines = demod_lines(YNR);
     constexpr int kRows = kDemodLines + 6;   // input lines fl0-3 .. fl0+L+2
@@ -374,6 +384,13 @@ __global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
             POs += __shfl_xor_sync(0xffffffffu, POs, h);
             QOs += __shfl_xor_sync(0xffffffffu, QOs, h);
         }
+        if (P.swap_carrier) {   // the PAL-M tables: the sine sums are the cosine sums and vice versa
+            const long long t0 = Ps, t1 = POs;
+            Ps = Qs;
+            Qs = t0;
+            POs = QOs;
+            QOs = t1;
+        }
         if (lane == 0) {
             // bp = P/(4 len), bpo = PO/(2 len): the V-switch test scaled by (4 len)^2
             const long long a = Ps - 2 * POs, b = Qs - 2 * QOs;
@@ -408,7 +425,7 @@ __global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
                 float v[4][22];
                 item_window(ch + t * SW + kPad + xl0 - 7, SW, v);
                 float PU[8], QU[8], PV[8], QV[8], PY[8], QY[8];
-                item_fir<true>(v, PU, QU, PV, QV, PY, QY);
+                item_fir<true>(P, v, PU, QU, PV, QV, PY, QY);
 #pragma unroll
                 for (int s = 0; s < 8; s++) {
                     const int x = base4 + xl0 + s;
@@ -466,7 +483,7 @@ __global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
             float v[4][22];
             item_window(ch + t * SW + kPad + xl0 - 7, SW, v);
             float PU[8], QU[8], PV[8], QV[8], PY[8], QY[8];
-            item_fir<COMPOSITE && !YNR>(v, PU, QU, PV, QV, PY, QY);
+            item_fir<COMPOSITE && !YNR>(P, v, PU, QU, PV, QV, PY, QY);
 
             const float bp = s_bp[t], bq = s_bq[t], vsw = s_vsw[t];
             const int orow = P.top_pad + 2 * fl + off - P.fafl;
@@ -534,15 +551,15 @@ __global__ void __launch_bounds__(kDemodThreads, 2) demod_kernel(DemodParams P)
     }
 }
 
-// PalColour::buildLookUpTables chroma taps (palcolour.cpp:197-276), in double.
-int demod_init_constants(int device, double sample_rate, int /*field_width*/)
+// PalColour::buildLookUpTables chroma taps (palcolour.cpp:197-276), in double,
+// for the sample rate; -2 when the filter is longer than the kernel's 8 taps.
+int demod_taps(double sample_rate, float (&cfilt)[8][4], float (&yfilt)[8][2])
 {
-    if (device >= 0 && device < 64 && g_demod_ready[device]) return 0;
     const double chromaBandwidthHz = 1100000.0 / 0.93;
     const double ca = 0.5 * sample_rate / chromaBandwidthHz;
     int fs = 1;
     if ((int)ca > fs) fs = (int)ca;
-    if (fs != 7) return -2;   // the kernel's tap count is fixed for 4fsc PAL
+    if (fs > 7) return -2;
     double cf[8][4] = {}, yf[8][2] = {};
     double cdiv = 0, ydiv = 0;
     for (int f = 0; f <= fs; f++) {
@@ -563,11 +580,17 @@ int demod_init_constants(int device, double sample_rate, int /*field_width*/)
         yf[f][1] = 0.2 * (1 + cos(M_PI * fffy / ca)) / d;
         ydiv += 2 * (1 * yf[f][0] + 2 * yf[f][1]);
     }
-    float cff[8][4], yff[8][2];
     for (int f = 0; f < 8; f++) {
-        for (int i = 0; i < 4; i++) cff[f][i] = (float)(cf[f][i] / cdiv);
-        for (int i = 0; i < 2; i++) yff[f][i] = (float)(yf[f][i] / ydiv);
+        for (int i = 0; i < 4; i++) cfilt[f][i] = (float)(cf[f][i] / cdiv);
+        for (int i = 0; i < 2; i++) yfilt[f][i] = (float)(yf[f][i] / ydiv);
     }
+    return 0;
+}
+
+// The doYNR high-pass, once per device.
+int demod_init_constants(int device)
+{
+    if (device >= 0 && device < 64 && g_demod_ready[device]) return 0;
     // c_nrpal_b, src/decoders/filter/deemp.h:620-628
     static const double nrpal[25] = {
         1.141291975113614e-04, -1.857019211291029e-03, -4.499636864042073e-03, -5.577680979937061e-03,
@@ -579,8 +602,6 @@ int demod_init_constants(int device, double sample_rate, int /*field_width*/)
         1.141291975113614e-04};
     float nrf[25];
     for (int i = 0; i < 25; i++) nrf[i] = (float)nrpal[i];
-    if (cudaMemcpyToSymbol(cd_cfilt, cff, sizeof(cff)) != cudaSuccess) return -1;
-    if (cudaMemcpyToSymbol(cd_yfilt, yff, sizeof(yff)) != cudaSuccess) return -1;
     if (cudaMemcpyToSymbol(cd_nrpal, nrf, sizeof(nrf)) != cudaSuccess) return -1;
     if (device >= 0 && device < 64) g_demod_ready[device] = true;
     return 0;

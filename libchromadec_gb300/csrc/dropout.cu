@@ -6,8 +6,10 @@
 // src/dropout/dropout_corrector.cpp:117-157, 469-530): a later operation may
 // read a line an earlier one rewrote, so one block owns a frame and runs its
 // operations one after another, the block's threads splitting each line.
-// The low/high-frequency blend uses the reference's 5-tap PAL luma FIR
-// (src/dropout/luma_filters.cpp:27-30) evaluated the way FIRFilter::apply
+// The low/high-frequency blend uses the reference's 5-tap luma FIR -- the PAL
+// taps, or the NTSC taps the reference also uses for PAL-M
+// (src/dropout/luma_filters.cpp:27-38, dropout_corrector.cpp:498-506) --
+// evaluated the way FIRFilter::apply
 // does (src/decoders/filter/firfilter.h:52-99): FP64 accumulation in tap
 // order with zero outside the line, each product and sum rounded separately,
 // then truncation to uint16; the final update is modular uint16 arithmetic.
@@ -18,15 +20,16 @@
 
 namespace chdg {
 
-__constant__ double c_luma_fir[5] = {0.03283437, 0.23959832, 0.45513461, 0.23959832, 0.03283437};
+__constant__ double c_luma_fir[2][5] = {{0.03283437, 0.23959832, 0.45513461, 0.23959832, 0.03283437},
+                                         {0.03275786, 0.23955702, 0.45537024, 0.23955702, 0.03275786}};
 
-__device__ __forceinline__ uint16_t luma_fir(const uint16_t *line, int fw, int x)
+__device__ __forceinline__ uint16_t luma_fir(const uint16_t *line, int fw, int x, int taps)
 {
     double v = 0.0;
 #pragma unroll
     for (int j = 0; j < 5; j++) {
         const int k = x - 2 + j;
-        if (k >= 0 && k < fw) v = __dadd_rn(v, __dmul_rn(c_luma_fir[j], (double)line[k]));
+        if (k >= 0 && k < fw) v = __dadd_rn(v, __dmul_rn(c_luma_fir[taps][j], (double)line[k]));
     }
     return (uint16_t)__double2uint_rz(v);
 }
@@ -36,7 +39,7 @@ __device__ __forceinline__ uint16_t luma_fir(const uint16_t *line, int fw, int x
 // extras: the batch's extra-capture fields (same stride), which ops with
 // srcExtra / chrExtra >= 0 read their replacement lines from.
 __global__ void dropout_apply_kernel(uint16_t *fields, long long field_stride, int fw, const int *frames,
-                                     const DropOp *ops, const int *op_begin, const uint16_t *extras)
+                                     const DropOp *ops, const int *op_begin, const uint16_t *extras, int taps)
 {
     const int b = blockIdx.x;
     uint16_t *base = fields + (long long)frames[b] * field_stride;
@@ -54,8 +57,8 @@ __global__ void dropout_apply_kernel(uint16_t *fields, long long field_stride, i
                                                     : base + (long long)op.chrField * field_stride) +
                                   (long long)op.chrLine * fw;
             for (int x = x0 + (int)threadIdx.x; x < x1; x += blockDim.x) {
-                const uint16_t lf = luma_fir(src, fw, x);
-                const uint16_t lfc = luma_fir(chr, fw, x);
+                const uint16_t lf = luma_fir(src, fw, x, taps);
+                const uint16_t lfc = luma_fir(chr, fw, x, taps);
                 target[x] = (uint16_t)((int)lf + ((int)chr[x] - (int)lfc));
             }
         }
@@ -63,11 +66,13 @@ __global__ void dropout_apply_kernel(uint16_t *fields, long long field_stride, i
     }
 }
 
+// ntsc_taps: the NTSC / PAL-M luma filter instead of PAL's
 int dropout_apply(uint16_t *fields, long long field_stride, int fw, const int *d_frames, const DropOp *d_ops,
-                  const int *d_op_begin, int nframes, const uint16_t *extras, cudaStream_t s)
+                  const int *d_op_begin, int nframes, const uint16_t *extras, bool ntsc_taps, cudaStream_t s)
 {
     if (nframes <= 0) return 0;
-    dropout_apply_kernel<<<nframes, 256, 0, s>>>(fields, field_stride, fw, d_frames, d_ops, d_op_begin, extras);
+    dropout_apply_kernel<<<nframes, 256, 0, s>>>(fields, field_stride, fw, d_frames, d_ops, d_op_begin, extras,
+                                                 ntsc_taps ? 1 : 0);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

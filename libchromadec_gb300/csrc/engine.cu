@@ -27,6 +27,10 @@ static int cuda_fail(const char *what, cudaError_t e)
     return CHDG_E_CUDA;
 }
 
+// PalColour::MAX_WIDTH (src/decoders/palcolour/palcolour.h:93): the widest
+// line the reference decodes
+constexpr int kMaxWidth = 1135;
+
 static int arg_fail(const std::string &what)
 {
     chd::detail::set_last_error("chromadec_gb300: " + what);
@@ -94,7 +98,7 @@ int Engine::init(const chdg_geometry &g, const chdg_config &c)
         return arg_fail("invalid geometry");
     if (std::fabs(g.fsc / g.sample_rate - 0.25) > 1e-9)
         return chd::detail::set_last_error("chromadec_gb300: only 4fsc sampling is supported"), CHDG_E_UNSUPPORTED;
-    if (g.active_start - 7 < 0 || g.active_end + 8 > 1135 || g.field_width > 1135)
+    if (g.active_start - 7 < 0 || g.active_end + 8 > kMaxWidth || g.field_width > kMaxWidth)
         return chd::detail::set_last_error("chromadec_gb300: active window too close to the line ends"),
                CHDG_E_UNSUPPORTED;
     if (c.output_format < 0 || c.output_format > 5) return arg_fail("output_format must be 0..5");
@@ -113,10 +117,9 @@ int Engine::init(const chdg_geometry &g, const chdg_config &c)
     } else if (c.kind == 7) {
         if (tpal::tp2_init_constants(device_) != 0) return cuda_fail("2D constants", cudaGetLastError());
     }
-    if (const int rc = tpal::demod_init_constants(device_, g.sample_rate, g.field_width); rc != 0)
-        return rc == -2 ? (chd::detail::set_last_error("chromadec_gb300: unsupported chroma filter size"),
-                           CHDG_E_UNSUPPORTED)
-                        : cuda_fail("demod constants", cudaGetLastError());
+    if (tpal::demod_init_constants(device_) != 0) return cuda_fail("demod constants", cudaGetLastError());
+    if (tpal::demod_taps(g.sample_rate, cfilt_, yfilt_) != 0)
+        return chd::detail::set_last_error("chromadec_gb300: unsupported chroma filter size"), CHDG_E_UNSUPPORTED;
 
     // Squared thresholds (TransformPal::updateConfiguration, transform_pal.cpp:53-78)
     const double t2 = c.threshold * c.threshold;
@@ -158,7 +161,7 @@ int Engine::init_static(const chdg_geometry &g, const chdg_config &c, float *thr
         return arg_fail("invalid geometry");
     if (std::fabs(g.fsc / g.sample_rate - 0.25) > 1e-9)
         return chd::detail::set_last_error("chromadec_gb300: only 4fsc sampling is supported"), CHDG_E_UNSUPPORTED;
-    if (g.active_start - 7 < 0 || g.active_end + 8 > 1135 || g.field_width > 1135)
+    if (g.active_start - 7 < 0 || g.active_end + 8 > kMaxWidth || g.field_width > kMaxWidth)
         return chd::detail::set_last_error("chromadec_gb300: active window too close to the line ends"),
                CHDG_E_UNSUPPORTED;
     if (c.output_format < 0 || c.output_format > 5) return arg_fail("output_format must be 0..5");
@@ -169,10 +172,9 @@ int Engine::init_static(const chdg_geometry &g, const chdg_config &c, float *thr
     cudaError_t e = cudaGetDevice(&device_);
     if (e != cudaSuccess) return cuda_fail("cudaGetDevice", e);
     if (tpal::tp3_init_constants(device_) != 0) return cuda_fail("3D constants", cudaGetLastError());
-    if (const int rc = tpal::demod_init_constants(device_, g.sample_rate, g.field_width); rc != 0)
-        return rc == -2 ? (chd::detail::set_last_error("chromadec_gb300: unsupported chroma filter size"),
-                           CHDG_E_UNSUPPORTED)
-                        : cuda_fail("demod constants", cudaGetLastError());
+    if (tpal::demod_init_constants(device_) != 0) return cuda_fail("demod constants", cudaGetLastError());
+    if (tpal::demod_taps(g.sample_rate, cfilt_, yfilt_) != 0)
+        return chd::detail::set_last_error("chromadec_gb300: unsupported chroma filter size"), CHDG_E_UNSUPPORTED;
     const double t2 = c.threshold * c.threshold;
     t2f_ = (float)t2;
     t2hi_ = (float)t2;
@@ -474,6 +476,9 @@ int Engine::run_demod(const uint16_t *fields, long long stride, int field_base, 
         }
         D.r_lo = b[0], D.r_hi = b[1], D.g_lo = b[2], D.g_hi = b[3], D.b_lo = b[4], D.b_hi = b[5];
     }
+    std::memcpy(D.cfilt, cfilt_, sizeof(cfilt_));
+    std::memcpy(D.yfilt, yfilt_, sizeof(yfilt_));
+    D.swap_carrier = g_.field_height == 263 ? 1 : 0;   // palcolour.cpp:158-173 keys on fieldHeight
     if (padded() && frame_out_ == nullptr) {
         // black border: Y 16*256 / Cb,Cr 128*256 (p16), zeros (ps)
         const int rc = fill_border(out, fe - fb, s);

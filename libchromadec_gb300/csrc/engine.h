@@ -124,6 +124,7 @@ private:
     chdg_config c_{};
     int device_ = 0;
     float t2f_ = 0.f, t2hi_ = 0.f, t2lo_ = 0.f;
+    float cfilt_[8][4] = {}, yfilt_[8][2] = {};   // the demodulator's taps for this sample rate
     float *thr_dev_ = nullptr;
     unsigned *stats_dev_ = nullptr;
     float *partial_ = nullptr;

@@ -12,7 +12,7 @@
 namespace chdg {
 
 int dropout_apply(uint16_t *fields, long long field_stride, int fw, const int *d_frames, const DropOp *d_ops,
-                  const int *d_op_begin, int nframes, const uint16_t *extras, cudaStream_t s);
+                  const int *d_op_begin, int nframes, const uint16_t *extras, bool ntsc_taps, cudaStream_t s);
 int fill_fields(uint16_t *fields, long long field_stride, long long field_len, int nfields, uint16_t value,
                 cudaStream_t s);
 int fill_samples(uint16_t *p, long long n, uint16_t value, cudaStream_t s);
@@ -333,7 +333,7 @@ int FramePipeline::conceal_frame(int64_t frame, uint16_t *host_out)
     int nplan = 0;
     if (const int rc = upload_batch(0, frame, frame + 1, nplan); rc != CHD_OK) return rc;
     if (nplan > 0 && dropout_apply(dwin_[0], dstride_, cap_->vp().fieldWidth, d_idx_[0], d_ops_[0], d_idx_[0] + nplan,
-                                   nplan, dext_[0], copy_) != 0)
+                                   nplan, dext_[0], ntsc_luma_taps(), copy_) != 0)
         return cuda_status("dropout kernel", cudaGetLastError());
     if ((e = cudaMemcpy2DAsync(host_out, flen_ * 2, dwin_[0], (size_t)dstride_ * 2, flen_ * 2, 2,
                                cudaMemcpyDeviceToHost, copy_)) != cudaSuccess)
@@ -413,7 +413,7 @@ int FramePipeline::decode(int64_t a, int64_t b, const Deliver &deliver, const st
         if (bi >= 2) cudaStreamWaitEvent(comp_, ev_d2h_[slot], 0);   // output slot drained
         if (nplan > 0 &&
             dropout_apply(dwin_[slot], dstride_, cap_->vp().fieldWidth, d_idx_[slot], d_ops_[slot],
-                          d_idx_[slot] + nplan, nplan, dext_[slot], comp_) != 0)
+                          d_idx_[slot] + nplan, nplan, dext_[slot], ntsc_luma_taps(), comp_) != 0)
             return cuda_status("dropout kernel", cudaGetLastError());
         if (const int rc = eng_.decode(dwin_[slot], dstride_, (int)(2 * w0), 2 * nframes_, (int)c, (int)ce,
                                        dout_[slot], comp_);

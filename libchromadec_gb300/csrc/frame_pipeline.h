@@ -83,6 +83,9 @@ private:
     // fields they read; nplan = frames with a plan.
     int upload_batch(int slot, int64_t w0, int64_t w1, int &nplan);
     const FramePlan &plan_for(int64_t frame);   // cached, window frame (0-based)
+    // the concealment's luma filter: PAL's, or the NTSC taps that NTSC and
+    // PAL-M use (dropout_corrector.cpp:498-506)
+    bool ntsc_luma_taps() const { return cap_->vp().system == SYS_NTSC || cap_->vp().system == SYS_PAL_M; }
     // A pinned chunk of at least `bytes`, reused once every frame borrowing
     // from it has been freed.
     std::shared_ptr<HostChunk> take_chunk(size_t bytes);

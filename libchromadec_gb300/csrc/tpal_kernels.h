@@ -115,6 +115,9 @@ struct DemodParams {
     float rgb_y_scale, rgb_uv_scale;        // rgb48: 65535/range; rgbs: 1/range
     float r_from_v, g_from_u, g_from_v, b_from_u;
     float r_lo, r_hi, g_lo, g_hi, b_lo, b_hi;   // R'G'B' clamp bounds
+    float cfilt[8][4];           // chroma FIR taps of the sample rate (PalColour::buildLookUpTables)
+    float yfilt[8][2];           // luma-extraction taps
+    int swap_carrier;            // 1 at fieldHeight 263: the reference's PAL-M sine/cosine exchange
 };
 
 // Learned-mask form of the 3D transform: the walk's two extra passes.
@@ -155,7 +158,8 @@ int tp2_launch(const T2Params &p, cudaStream_t stream);
 // spectra. Uniform threshold, one capture buffer.
 int tc3_transform(const T3Params &p, int field_height, int variant, cudaStream_t stream);
 int tc3_launches_per_frames(int frames);
-int demod_init_constants(int device, double sample_rate, int field_width);
+int demod_init_constants(int device);
+int demod_taps(double sample_rate, float (&cfilt)[8][4], float (&yfilt)[8][2]);
 int demod_launch(const DemodParams &p, cudaStream_t stream);
 
 }  // namespace tpal

@@ -1,4 +1,5 @@
-"""Seeded synthetic PAL 4fsc composite generator (line-locked, 1135x313 fields).
+"""Seeded synthetic PAL / PAL-M 4fsc composite generator (line-locked fields:
+1135x313 for 625-line PAL, 909x263 for 525-line PAL-M).
 
 The modulation follows the PAL maths the reference's own test encoder uses
 (src/legacy/ld-chroma-decoder/encoder/palencoder.cpp:173-324): chroma is
@@ -11,7 +12,11 @@ phased by integer sample index; the per-line remainder comes from prevCycles.
 Levels are the reference's PAL preset (src/format/video_standards.cpp:18-26):
 black 0x4000, white 0xD300, sync tip 0x0100. Geometry is the line-locked
 preset (sync-start rows): burst [98, 138), active samples [177, 1125), active
-frame lines 44..619.
+frame lines 44..619. PAL-M (SynthConfig.standard = "PAL_M") follows the
+reference's PAL_M preset (video_standards.cpp:28-40, 44-52, 85-100,
+116-207): 909 samples x 263 lines per field at 4 fSC with fSC = 227.25 fH,
+SMPTE ST 244 levels (black 282 x 64, white 800 x 64, sync tip 16 x 64),
+burst [75, 95), active samples [124, 892), active frame lines 39..524.
 
 Content (all seeded):
   * 75% colour bars in the top third of the picture (static);
@@ -49,6 +54,38 @@ LAST_ACTIVE_FRAME_LINE = 619
 SAMPLE_RATE = 4.0 * 625.0 * 25.0 * (1135.0 / 4.0 + 1.0 / 625.0)
 FSC = 283.75 * 15625.0 + 25.0
 
+@dataclass(frozen=True)
+class Standard:
+    name: str                 # the sidecar's "system"
+    field_width: int
+    field_height: int
+    lines_per_frame: int
+    sample_rate: float
+    fsc: float
+    cycles_per_line: float    # subcarrier cycles per line (the encoder's phase step)
+    black: int
+    white: int
+    blanking: int
+    sync_tip: int
+    active_start: int
+    active_end: int
+    burst_start: int
+    burst_end: int
+    first_active_frame_line: int
+    last_active_frame_line: int
+    sync_width: int           # samples of sync tip at the start of each line
+    sync_level: float         # sync tip relative to black, in units of white - black
+    zone_plate_y: float       # the zone plate's centre (frame line)
+
+
+PAL = Standard("PAL", FIELD_WIDTH, FIELD_HEIGHT, 625, SAMPLE_RATE, FSC, 283.7516, BLACK, WHITE, BLANKING, SYNC_TIP,
+               ACTIVE_START, ACTIVE_END, BURST_START, BURST_END, FIRST_ACTIVE_FRAME_LINE, LAST_ACTIVE_FRAME_LINE, 83,
+               -0.3 / 0.7, 420.0)
+PAL_M = Standard("PAL_M", 909, 263, 525, 4.0 * 525.0 * (30000.0 / 1001.0) * (909.0 / 4.0),
+                 5.0e6 * (63.0 / 88.0) * (909.0 / 910.0), 909.0 / 4.0, 282 * 64, 800 * 64, 240 * 64, 16 * 64,
+                 124, 892, 75, 95, 39, 524, 67, -(282.0 - 16.0) / (800.0 - 282.0), 356.0)
+STANDARDS = {"PAL": PAL, "PAL_M": PAL_M}
+
 # Composite U/V reduction factors at the "scientific" precision
 # (src/common/color_conversion.cpp:25-27).
 U_REDUCTION = 0.49211104112248356308804691718185
@@ -74,16 +111,18 @@ class SynthConfig:
     # `seed`) with its own noise and dropouts.
     noise_seed: Optional[int] = None
     dropout_seed: Optional[int] = None
+    standard: str = "PAL"
 
 
 @dataclass
 class SynthCapture:
-    fields: np.ndarray                       # (nfields, 313, 1135) uint16
+    fields: np.ndarray                       # (nfields, field_height, field_width) uint16
     dropouts: List[List[Tuple[int, int, int]]]  # per field: (startx, endx, fieldLine)
-    y: Optional[np.ndarray] = None           # ground truth, (nfields, 313, 1135) float32
+    y: Optional[np.ndarray] = None           # ground truth, same shape, float32
     u: Optional[np.ndarray] = None
     v: Optional[np.ndarray] = None
     chroma: Optional[np.ndarray] = None      # chroma-only composite, sample units
+    standard: str = "PAL"
 
 
 def _gaussian_kernel(sigma: float) -> np.ndarray:
@@ -133,6 +172,7 @@ class PalEncoder:
 
     def __init__(self, cfg: SynthConfig):
         self.cfg = cfg
+        self.std = std = STANDARDS[cfg.standard]
         rng = np.random.default_rng(cfg.seed)
         self.rng = rng
         # Patch canvas, larger than the frame so panning never runs out.
@@ -150,32 +190,33 @@ class PalEncoder:
         else:
             self.canvas_u = np.zeros((ch, cw))
             self.canvas_v = np.zeros((ch, cw))
-        self.zp_cx = 0.5 * (ACTIVE_START + ACTIVE_END) + rng.uniform(-40, 40)
-        self.zp_cy = 420.0 + rng.uniform(-20, 20)
-        self.zp_r = 240.0
+        self.zp_cx = 0.5 * (std.active_start + std.active_end) + rng.uniform(-40, 40)
+        self.zp_cy = std.zone_plate_y + rng.uniform(-20, 20)
+        self.zp_r = 240.0 * (std.active_end - std.active_start) / 948.0
         self.noise_rng = np.random.default_rng(cfg.seed + 7919 if cfg.noise_seed is None else cfg.noise_seed)
-        x = np.arange(FIELD_WIDTH, dtype=np.float64)
+        x = np.arange(std.field_width, dtype=np.float64)
         # Raised-cosine gate for the active region (4-sample edges).
-        self.active_gate = np.clip(np.minimum(x - (ACTIVE_START - 4), (ACTIVE_END + 3) - x) / 4.0, 0.0, 1.0)
+        self.active_gate = np.clip(np.minimum(x - (std.active_start - 4), (std.active_end + 3) - x) / 4.0, 0.0, 1.0)
         self.active_gate = 0.5 - 0.5 * np.cos(np.pi * self.active_gate)
-        bg = np.clip(np.minimum(x - (BURST_START - 2), (BURST_END + 1) - x) / 3.0, 0.0, 1.0)
+        bg = np.clip(np.minimum(x - (std.burst_start - 2), (std.burst_end + 1) - x) / 3.0, 0.0, 1.0)
         self.burst_gate = 0.5 - 0.5 * np.cos(np.pi * bg)
-        self.sync_gate = (x < 83).astype(np.float64)
+        self.sync_gate = (x < std.sync_width).astype(np.float64)
         # Bars are static: build one band-limited row of Y, U, V.
-        bar_w = (ACTIVE_END - ACTIVE_START) / 8.0
-        idx = np.clip(np.floor((x - ACTIVE_START) / bar_w), 0, 7).astype(np.int64)
+        bar_w = (std.active_end - std.active_start) / 8.0
+        idx = np.clip(np.floor((x - std.active_start) / bar_w), 0, 7).astype(np.int64)
         by, bu, bv = _rgb_to_yuv(_bars_rgb()[idx])
         # chroma band-limited like the encoder's 1.3 MHz Gaussian low-pass
         self.bar_row = (by, _blur_axis(bu[None, :], 1.5, 1)[0], _blur_axis(bv[None, :], 1.5, 1)[0])
 
     def components(self, field_index: int):
-        """Y (0=black, 1=white), U, V planes for one field, (313, 1135)."""
+        """Y (0=black, 1=white), U, V planes for one field, (field_height, field_width)."""
         cfg = self.cfg
+        std = self.std
         parity = field_index % 2
-        fl = np.arange(FIELD_HEIGHT, dtype=np.float64)
+        fl = np.arange(std.field_height, dtype=np.float64)
         frame_y = 2.0 * fl + parity                      # frame line of each field line
-        x = np.arange(FIELD_WIDTH, dtype=np.float64)
-        Y = np.full((FIELD_HEIGHT, FIELD_WIDTH), 0.45)
+        x = np.arange(std.field_width, dtype=np.float64)
+        Y = np.full((std.field_height, std.field_width), 0.45)
         U = np.zeros_like(Y)
         V = np.zeros_like(Y)
         # Panned coordinates.
@@ -186,14 +227,14 @@ class PalEncoder:
             cxp = self.zp_cx + cfg.pan_x * field_index
             cyp = self.zp_cy + cfg.pan_y * field_index
             x0 = max(0, int(cxp - self.zp_r) - 1)
-            x1 = min(FIELD_WIDTH, int(cxp + self.zp_r) + 2)
+            x1 = min(std.field_width, int(cxp + self.zp_r) + 2)
             l0 = max(0, int((cyp - self.zp_r / 1.23 - parity) / 2) - 1)
-            l1 = min(FIELD_HEIGHT, int((cyp + self.zp_r / 1.23 - parity) / 2) + 2)
+            l1 = min(std.field_height, int((cyp + self.zp_r / 1.23 - parity) / 2) + 2)
             if x1 > x0 and l1 > l0:
                 dx = px[:, x0:x1] - self.zp_cx
                 dy = (py[l0:l1, :] - self.zp_cy) * 1.23
                 r2 = dx * dx + dy * dy
-                kmax = (5.0e6 / SAMPLE_RATE) / self.zp_r   # cycles/sample per sample of radius
+                kmax = (5.0e6 / std.sample_rate) / self.zp_r   # cycles/sample per sample of radius
                 zp = 0.25 * np.cos(np.pi * kmax * r2)
                 Y[l0:l1, x0:x1] += np.where(r2 <= self.zp_r ** 2, zp, 0.0)
         if cfg.patches:
@@ -221,8 +262,8 @@ class PalEncoder:
             U = _blur_axis(U, 1.5, 1)
             V = _blur_axis(V, 1.5, 1)
         if cfg.bars:
-            top = FIRST_ACTIVE_FRAME_LINE
-            bottom = FIRST_ACTIVE_FRAME_LINE + (LAST_ACTIVE_FRAME_LINE - FIRST_ACTIVE_FRAME_LINE + 1) // 3
+            top = std.first_active_frame_line
+            bottom = top + (std.last_active_frame_line - top + 1) // 3
             rows = (frame_y >= top) & (frame_y < bottom)
             by, bu, bv = self.bar_row
             Y[rows, :] = by[None, :]
@@ -232,13 +273,14 @@ class PalEncoder:
 
     def encode_field(self, field_index: int):
         """Composite uint16 field plus its ground truth (Y, U, V, chroma)."""
+        std = self.std
         Y, U, V = self.components(field_index)
-        fl = np.arange(FIELD_HEIGHT)
+        fl = np.arange(std.field_height)
         field_id = field_index % 8
-        prev_lines = (field_id // 2) * 625 + (field_id % 2) * 313 + fl
+        prev_lines = (field_id // 2) * std.lines_per_frame + (field_id % 2) * std.field_height + fl
         vsw = np.where(prev_lines % 2 == 0, 1.0, -1.0)
-        line_phase = np.mod(prev_lines * 283.7516, 1.0)        # cycles at 0H
-        x = np.arange(FIELD_WIDTH)
+        line_phase = np.mod(prev_lines * std.cycles_per_line, 1.0)        # cycles at 0H
+        x = np.arange(std.field_width)
         # a = 2*pi*(x/4 + phase): sin/cos repeat every 4 samples, so build them
         # from each line's sin/cos of the 0H phase.
         th = 2.0 * np.pi * line_phase
@@ -247,30 +289,31 @@ class PalEncoder:
         c4 = np.stack([ct, -st, -ct, st], axis=1)            # cos(th + k*pi/2)
         s = s4[:, x % 4]
         c = c4[:, x % 4]
-        active_rows = ((2 * fl + field_index % 2) >= FIRST_ACTIVE_FRAME_LINE) & \
-                      ((2 * fl + field_index % 2) <= LAST_ACTIVE_FRAME_LINE)
+        active_rows = ((2 * fl + field_index % 2) >= std.first_active_frame_line) & \
+                      ((2 * fl + field_index % 2) <= std.last_active_frame_line)
         gate = self.active_gate[None, :] * active_rows[:, None]
         chroma = (U * s + V * c * vsw[:, None]) * gate
         luma = Y * gate
-        burst_rows = (fl >= 6) & (fl <= 309)
+        burst_rows = (fl >= 6) & (fl <= std.field_height - 4)
         off = vsw[:, None] * (135.0 * np.pi / 180.0)
         burst = (s * np.cos(off) + c * np.sin(off)) * (3.0 / 7.0) / 2.0
         burst = burst * self.burst_gate[None, :] * burst_rows[:, None]
-        sync = (-0.3 / 0.7) * self.sync_gate[None, :]
+        sync = std.sync_level * self.sync_gate[None, :]
         sig = luma + chroma + burst + sync
         if self.cfg.noise > 0:
             sig = sig + self.noise_rng.standard_normal(sig.shape) * self.cfg.noise
-        samples = np.rint(BLACK + (WHITE - BLACK) * sig)
-        samples = np.clip(samples, 0x0100, 0xFEFF).astype(np.uint16)
-        return samples, (Y * gate, U * gate, V * gate, chroma * (WHITE - BLACK))
+        samples = np.rint(std.black + (std.white - std.black) * sig)
+        samples = np.clip(samples, std.sync_tip, 0xFEFF).astype(np.uint16)
+        return samples, (Y * gate, U * gate, V * gate, chroma * (std.white - std.black))
 
 
 def make_capture(nfields: int, cfg: SynthConfig, truth: bool = False) -> SynthCapture:
     enc = PalEncoder(cfg)
-    fields = np.empty((nfields, FIELD_HEIGHT, FIELD_WIDTH), dtype=np.uint16)
+    std = enc.std
+    fields = np.empty((nfields, std.field_height, std.field_width), dtype=np.uint16)
     ys = us = vs = cs = None
     if truth:
-        ys = np.empty((nfields, FIELD_HEIGHT, FIELD_WIDTH), dtype=np.float32)
+        ys = np.empty((nfields, std.field_height, std.field_width), dtype=np.float32)
         us = np.empty_like(ys)
         vs = np.empty_like(ys)
         cs = np.empty_like(ys)
@@ -283,29 +326,30 @@ def make_capture(nfields: int, cfg: SynthConfig, truth: bool = False) -> SynthCa
     if cfg.dropout_line_fraction > 0:
         drng = np.random.default_rng(cfg.seed + 104729 if cfg.dropout_seed is None else cfg.dropout_seed)
         for f in range(nfields):
-            for line in range(FIELD_HEIGHT):
+            for line in range(std.field_height):
                 if drng.random() >= cfg.dropout_line_fraction:
                     continue
                 length = int(drng.integers(cfg.dropout_min_len, cfg.dropout_max_len + 1))
-                start = int(drng.integers(0, FIELD_WIDTH - length))
-                fields[f, line, start:start + length] = SYNC_TIP
+                start = int(drng.integers(0, std.field_width - length))
+                fields[f, line, start:start + length] = std.sync_tip
                 dropouts[f].append((start, start + length, line + 1))
-    return SynthCapture(fields=fields, dropouts=dropouts, y=ys, u=us, v=vs, chroma=cs)
+    return SynthCapture(fields=fields, dropouts=dropouts, y=ys, u=us, v=vs, chroma=cs, standard=cfg.standard)
 
 
-def video_parameters_json(nfields: int) -> dict:
+def video_parameters_json(nfields: int, standard: str = "PAL") -> dict:
+    std = STANDARDS[standard]
     return {
-        "system": "PAL",
-        "fieldWidth": FIELD_WIDTH,
-        "fieldHeight": FIELD_HEIGHT,
-        "sampleRate": SAMPLE_RATE,
-        "activeVideoStart": ACTIVE_START,
-        "activeVideoEnd": ACTIVE_END,
-        "colourBurstStart": BURST_START,
-        "colourBurstEnd": BURST_END,
-        "white16bIre": WHITE,
-        "black16bIre": BLACK,
-        "blanking16bIre": BLANKING,
+        "system": std.name,
+        "fieldWidth": std.field_width,
+        "fieldHeight": std.field_height,
+        "sampleRate": std.sample_rate,
+        "activeVideoStart": std.active_start,
+        "activeVideoEnd": std.active_end,
+        "colourBurstStart": std.burst_start,
+        "colourBurstEnd": std.burst_end,
+        "white16bIre": std.white,
+        "black16bIre": std.black,
+        "blanking16bIre": std.blanking,
         "isSubcarrierLocked": False,
         "isWidescreen": False,
         "isMapped": False,
@@ -347,7 +391,7 @@ def write_tbc(path: str, cap: SynthCapture, vbi=None, bpsnr=None) -> str:
     with open(path, "wb") as fp:
         fp.write(np.ascontiguousarray(cap.fields).tobytes())
     meta = {
-        "videoParameters": video_parameters_json(nfields),
+        "videoParameters": video_parameters_json(nfields, cap.standard),
         "fields": [],
     }
     for i in range(nfields):

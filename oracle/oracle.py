@@ -136,6 +136,21 @@ def params(kind: int = 3, fmt: int = FMT_P16, threshold: float = 0.4,
     return p
 
 
+def pal_m(p: Params) -> Params:
+    """PAL-M geometry and levels: the reference's PAL_M preset
+    (src/format/video_standards.cpp:28-52, 85-100, 116-207; active frame
+    lines src/metadata/core.cpp:52-70)."""
+    p.field_width, p.field_height = 909, 263
+    p.active_start, p.active_end = 124, 892
+    p.first_active_frame_line, p.last_active_frame_line = 39, 524
+    p.burst_start, p.burst_end = 75, 95
+    p.black, p.white = 282 * 64, 800 * 64
+    p.sample_rate = 4.0 * 525.0 * (30000.0 / 1001.0) * (909.0 / 4.0)
+    p.fsc = 5.0e6 * (63.0 / 88.0) * (909.0 / 910.0)
+    p.is_pal_m = 1
+    return p
+
+
 def frame_dtype(p: Params):
     return np.float32 if p.output_format in (FMT_PS, FMT_RGBS, FMT_GRAYS) else np.uint16
 

@@ -28,7 +28,9 @@
 //   (src/dropout/multi_source_alignment.cpp:54-71), skipped when the extra
 //   does not hold it (src/abi/c_api_decoder.cpp:252-262)
 //   bpsnr=<file>: lines "source field bPSNR" (source 0 = primary)
-// The field file holds N fields of 1135x313 uint16, first field first.
+//   std=pal|palm: the video standard (default pal)
+// The field file holds N fields of 1135x313 (PAL-M 909x263) uint16, first
+// field first.
 // The dropout file holds lines "field_index startx endx fieldLine".
 
 #include <cstdint>
@@ -78,6 +80,33 @@ LdDecodeMetaData::VideoParameters palParams()
     vp.tileReadStart = vp.activeVideoStart;
     vp.tileReadEnd = vp.activeVideoEnd;
     vp.isValid = true;
+    return vp;
+}
+
+// PAL-M: the reference's PAL_M preset (src/format/video_standards.cpp:28-52,
+// 85-100, 116-207, sync-start rows) and its active frame lines
+// (src/metadata/core.cpp:52-70): 909 x 263 fields at 4 fSC, ST 244 levels.
+LdDecodeMetaData::VideoParameters palMParams()
+{
+    LdDecodeMetaData::VideoParameters vp = palParams();
+    vp.system = chd::metadata::PAL_M;
+    vp.fieldWidth = 909;
+    vp.fieldHeight = 263;
+    vp.sampleRate = 4.0 * 525.0 * (30000.0 / 1001.0) * (909.0 / 4.0);
+    vp.fSC = 5.0e6 * (63.0 / 88.0) * (909.0 / 910.0);
+    vp.colourBurstStart = 75;
+    vp.colourBurstEnd = 95;
+    vp.activeVideoStart = 124;
+    vp.activeVideoEnd = 892;
+    vp.black16bIre = 282 * 64;
+    vp.white16bIre = 800 * 64;
+    vp.blanking16bIre = 240 * 64;
+    vp.firstActiveFrameLine = 39;
+    vp.lastActiveFrameLine = 524;
+    vp.pictureStart = vp.activeVideoStart;
+    vp.pictureEnd = vp.activeVideoEnd;
+    vp.tileReadStart = vp.activeVideoStart;
+    vp.tileReadEnd = vp.activeVideoEnd;
     return vp;
 }
 
@@ -171,7 +200,7 @@ int main(int argc, char **argv)
     const bool overcorrect = a.count("overcorrect") && a["overcorrect"] == "1";
     const bool intra = a.count("intra") && a["intra"] == "1";
 
-    auto vp = palParams();
+    auto vp = (a.count("std") && a["std"] == "palm") ? palMParams() : palParams();
     if (a.count("avs")) vp.activeVideoStart = vp.pictureStart = vp.tileReadStart = std::atoi(a["avs"].c_str());
     if (a.count("ave")) vp.activeVideoEnd = vp.pictureEnd = vp.tileReadEnd = std::atoi(a["ave"].c_str());
     if (a.count("fafl")) vp.firstActiveFrameLine = std::atoi(a["fafl"].c_str());

@@ -959,12 +959,16 @@ static replacement find_replacement(const tpo_params *p, const do_list *thisD, c
     return rep;
 }
 
-/* Filters::palLumaFirFilter, src/dropout/luma_filters.cpp:27-30,60-68 and
- * FIRFilter::apply, src/decoders/filter/firfilter.h:52-99 (zero outside,
- * double accumulation in tap order, truncating store to uint16). */
-static void pal_luma_fir(uint16_t *data, int32_t n, uint16_t *tmp)
+/* Filters::palLumaFirFilter and palMLumaFirFilter (= ntscLumaFirFilter),
+ * src/dropout/luma_filters.cpp:27-38,60-93, with FIRFilter::apply,
+ * src/decoders/filter/firfilter.h:52-99 (zero outside, double accumulation
+ * in tap order, truncating store to uint16); the PAL-M taps for system
+ * PAL_M (dropout_corrector.cpp:498-506). */
+static void pal_luma_fir(uint16_t *data, int32_t n, uint16_t *tmp, int32_t pal_m)
 {
-    static const double coeffs[5] = {0.03283437, 0.23959832, 0.45513461, 0.23959832, 0.03283437};
+    static const double pal[5] = {0.03283437, 0.23959832, 0.45513461, 0.23959832, 0.03283437};
+    static const double palm[5] = {0.03275786, 0.23955702, 0.45537024, 0.23955702, 0.03275786};
+    const double *coeffs = pal_m ? palm : pal;
     for (int32_t i = 0; i < n; i++) {
         double v = 0;
         for (int32_t j = 0, k = i - 2; j < 5; j++, k++) {
@@ -990,12 +994,12 @@ static void correct_dropout(const tpo_params *p, const do_loc *d, const replacem
         for (int32_t px = d->startx; px < d->endx; px++) targetLine[px] = sourceLine[px];
     } else {
         memcpy(lineBuf, sourceLine, sizeof(uint16_t) * (size_t)fw);
-        pal_luma_fir(lineBuf, fw, tmp);
+        pal_luma_fir(lineBuf, fw, tmp, p->is_pal_m);
         for (int32_t px = d->startx; px < d->endx; px++) targetLine[px] = lineBuf[px];
         const uint16_t *chromaLine = (crep->isSameField ? thisData[crep->sourceNumber] : otherData[crep->sourceNumber]) +
                                      ((crep->fieldLine - 1) * fw);
         memcpy(lineBuf, chromaLine, sizeof(uint16_t) * (size_t)fw);
-        pal_luma_fir(lineBuf, fw, tmp);
+        pal_luma_fir(lineBuf, fw, tmp, p->is_pal_m);
         for (int32_t px = d->startx; px < d->endx; px++)
             targetLine[px] = (uint16_t)(targetLine[px] + (chromaLine[px] - lineBuf[px]));
     }

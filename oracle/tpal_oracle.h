@@ -45,7 +45,8 @@ typedef struct tpo_params {
     int32_t burst_start, burst_end;
     int32_t black, white;
     double sample_rate, fsc;
-    int32_t is_pal_m;           /* system PAL_M (only changes the PAL-M LUT swap at fieldHeight 263) */
+    int32_t is_pal_m;           /* system PAL_M: the PAL-M luma filter of the dropout corrector (the
+                                   demodulator's table swap follows field_height 263, as the reference's) */
     /* decoder */
     int32_t kind;               /* 2 = Transform 2D, 3 = Transform 3D */
     double threshold;

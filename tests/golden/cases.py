@@ -84,28 +84,40 @@ CASES = {
                                                dict(noise_seed=66, dropout_seed=76, dropouts=0.02, offset=1, trim=1)]),
     "t2d_drop_multi_rev_ps": dict(mode="decode", kind=2, fmt="ps", nfields=9, seed=35, first=0, count=4, sff=1,
                                   dropouts=0.03, extras=[dict(noise_seed=67, dropout_seed=77, dropouts=0.03)]),
+    # PAL-M (525 lines, 909 samples, ST 244 levels): the same decoders on the other raster
+    "palm_t3d_p16": dict(mode="decode", kind=3, fmt="p16", nfields=12, seed=37, first=0, count=6, std="palm"),
+    "palm_t3d_ps": dict(mode="decode", kind=3, fmt="ps", nfields=12, seed=37, first=1, count=3, std="palm"),
+    "palm_t2d_p16": dict(mode="decode", kind=2, fmt="p16", nfields=8, seed=38, first=0, count=4, std="palm"),
+    "palm_pal2d_ps": dict(mode="decode", kind=1, fmt="ps", nfields=8, seed=38, first=0, count=4, std="palm"),
+    "palm_chroma3d": dict(mode="chroma", kind=3, nfields=12, seed=37, first=0, count=4, std="palm"),
+    "palm_t3d_drop": dict(mode="decode", kind=3, fmt="p16", nfields=12, seed=39, first=0, count=6, dropouts=0.02,
+                          std="palm"),
+    "palm_conceal": dict(mode="dropout", kind=3, fmt="p16", nfields=12, seed=39, first=0, count=6, dropouts=0.02,
+                         overcorrect=1, std="palm"),
 }
 
 # harness argument of each optional case key
 HARNESS_ARGS = {"chroma_gain": "gain", "chroma_phase_deg": "phase", "clamp_mode": "clamp",
                 "padding_multiple": "padding", "active_start": "avs", "active_end": "ave",
                 "first_active_frame_line": "fafl", "last_active_frame_line": "lafl", "y_nr_level": "ynr",
-                "sff": "sff", "sc_locked": "sclocked", "cdp": "cdp", "bsp": "bsp"}
+                "sff": "sff", "sc_locked": "sclocked", "cdp": "cdp", "bsp": "bsp", "std": "std"}
+
+SYNTH_STANDARD = {"pal": "PAL", "palm": "PAL_M"}
 
 
 @functools.lru_cache(maxsize=8)
-def _capture(nfields: int, seed: int, dropouts: float):
-    cfg = synth.SynthConfig(seed=seed, pan_x=1.5, pan_y=0.5, dropout_line_fraction=dropouts)
+def _capture(nfields: int, seed: int, dropouts: float, standard: str = "PAL"):
+    cfg = synth.SynthConfig(seed=seed, pan_x=1.5, pan_y=0.5, dropout_line_fraction=dropouts, standard=standard)
     return synth.make_capture(nfields, cfg)
 
 
 def case_inputs(case: dict):
-    """(fields uint16 (n, 313, 1135), flat dropouts [(field, startx, endx, fieldLine)] or None).
+    """(fields uint16 (n, field_height, field_width), flat dropouts [(field, startx, endx, fieldLine)] or None).
 
     For the reversed pairing (sff) the capture's first field is dropped, so
     the array starts with a second field and frame k is fields 2k, 2k+1 of
     the array, slot 0 being a second field."""
-    cap = _capture(case["nfields"], case["seed"], case.get("dropouts", 0.0))
+    cap = _capture(case["nfields"], case["seed"], case.get("dropouts", 0.0), SYNTH_STANDARD[case.get("std", "pal")])
     skip = 1 if case.get("sff") else 0
     flat = None
     if case.get("dropouts", 0.0) > 0:

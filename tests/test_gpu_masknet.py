@@ -141,10 +141,12 @@ def test_apply_pass_with_threshold_decisions(cuda):
     eng.chroma(fields, fb, fe, plain)
     torch.cuda.synchronize()
     assert torch.equal(a, b)
-    # FP32 decisions equal the exact ones except on a few guard-band bins,
-    # each of which moves its tile's chroma by a few sample units
-    off = (a - plain).abs() > 2e-2
-    assert float(off.float().mean()) < 2e-3
+    # FP32 decisions equal the exact ones except on the guard-band bins the
+    # plain form corrected; each such flip changes one tile's output (at most
+    # 4 fields x 16 rows x 16 samples)
+    _, flips = eng.stats()
+    off = int(((a - plain).abs() > 2e-2).sum())
+    assert off <= 1024 * flips, (off, flips)
 
 
 def test_short_training_lowers_the_loss(cuda):

@@ -27,6 +27,8 @@ FMTS = {"p16": O.FMT_P16, "ps": O.FMT_PS, "rgb48": O.FMT_RGB48, "rgbs": O.FMT_RG
 def _params(case):
     p = O.params(case["kind"], FMTS[case.get("fmt", "p16")], threshold=case.get("threshold", 0.4),
                  thresholds=thresholds_for(case))
+    if case.get("std") == "palm":
+        O.pal_m(p)
     for k in ("chroma_gain", "chroma_phase_deg", "clamp_mode", "padding_multiple", "active_start", "active_end",
               "first_active_frame_line", "last_active_frame_line", "y_nr_level"):
         if k in case:
