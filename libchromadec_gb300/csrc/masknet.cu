@@ -533,7 +533,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     uint8_t *act = smem + SM_ACT;
     uint8_t *A = smem + SM_A;
     uint8_t *B = smem + SM_B;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + SM_BAR);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + SM_BAR);        // MMA completion
+    uint64_t *bbar = reinterpret_cast<uint64_t *>(smem + SM_BAR + 16);  // weight-image copy
     uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + SM_BAR + 8);
     __shared__ float s_par[4 * NC + 1];   // b1, b2, b3, wh, bh
     __shared__ float red[kTcThreads / 32];
@@ -542,14 +543,17 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const int off[5] = {OFF_B1, OFF_B2, OFF_B3, OFF_WH, OFF_BH};
         s_par[i] = params[off[i / NC] + i % NC];
     }
-    if (t == 0) bar_init(bar);
+    if (t == 0) {
+        bar_init(bar);
+        bar_init(bbar);
+    }
     if (warp == 0) tmem_alloc(tslot, 256);
     fence_async_smem();
     fence_before();
     __syncthreads();
     fence_after();
     const uint32_t tmem = *tslot;
-    uint32_t phase = 0;
+    uint32_t phase = 0, bphase = 0;
     bool ok = true;
     const int eb = warp >> 2;                          // the epilogue's M block
     const int erow = eb * 128 + (warp & 3) * 32 + lane;   // its row: ky = erow >> 3, kz = erow & 7
@@ -577,6 +581,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             const int K = L == 0 ? 16 : 80, KB = 2 * K, chunks = K / 8, grp = 8 * KB;
             const uint8_t *imgL = img + (L == 0 ? IMG_L1 : (L == 1 ? IMG_L2 : IMG_L3));
             for (int dz = 0; dz < 3 && ok; dz++) {
+                // B: the previous MMAs (which read it) are complete
+                if (t == 0) {
+                    const uint32_t bytes = 3 * 80 * KB;
+                    bar_arrive_expect_tx(bbar, bytes);
+                    bulk_g2s(B, imgL + dz * 3 * 80 * KB, bytes, bbar);
+                }
                 // A: group g holds ky = g - 1 (periodic), row i holds kz = (i + dz - 1) mod 8
                 const int nitems = kGroupsA * chunks * 8;
                 for (int it = t; it < nitems; it += kTcThreads) {
@@ -585,17 +595,17 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     *reinterpret_cast<uint4 *>(A + g * grp + c * 128 + i * 16) =
                         *reinterpret_cast<const uint4 *>(act + src * kActStride + c * 16);
                 }
-                // B: this dz's three ky-tap images
-                const uint4 *bs = reinterpret_cast<const uint4 *>(imgL + dz * 3 * 80 * KB);
-                uint4 *bd = reinterpret_cast<uint4 *>(B);
-                for (int o = t; o < 3 * 80 * KB / 16; o += kTcThreads) bd[o] = __ldg(bs + o);
                 fence_async_smem();
                 fence_before();
                 __syncthreads();
+                bool bok = true;
                 if (t == 0) {
                     fence_after();
+                    // this dz's three ky-tap weight images, copied by the TMA engine
+                    // while the threads built A
+                    bok = bar_wait(bbar, bphase);
                     const uint32_t id = idesc(1, 128, 80);
-                    for (int dy = 0; dy < 3; dy++)
+                    for (int dy = 0; dy < 3 && bok; dy++)
                         for (int b = 0; b < 2; b++)
                             for (int ks = 0; ks < K / 16; ks++) {
                                 const uint32_t a = smem_addr(A + (b * 16 + dy) * grp + ks * 256);
@@ -607,7 +617,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 }
                 const bool done = bar_wait(bar, phase);
                 phase ^= 1;
-                if (__syncthreads_or(!done)) ok = false;
+                bphase ^= 1;
+                if (__syncthreads_or(!done || !bok)) ok = false;
                 fence_after();
             }
             if (!ok) break;

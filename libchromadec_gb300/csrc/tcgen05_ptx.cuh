@@ -123,6 +123,23 @@ __host__ __device__ __forceinline__ uint32_t elem_off(int r, int k, int eb, int 
 }
 
 
+// Expect `bytes` of asynchronous copies on the barrier and arrive once.
+__device__ __forceinline__ void bar_arrive_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// Bulk copy global -> shared by the TMA engine (both addresses 16-byte
+// aligned, bytes a multiple of 16), completing `bytes` on the barrier.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
 // 8 consecutive 32-bit columns of this thread's lane, then wait for the load
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8])
 {
