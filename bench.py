@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the tensor-core forms and chroma PSNR report")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-captures measurement")
     ap.add_argument("--kind", default="3d", choices=["3d", "2d"],
                     help="Transform-PAL 3D (the metric) or 2D (for profiling the 2D kernel)")
     ap.add_argument("--form", default="plain", choices=["plain", "tc_3xtf32", "tc_bf16x3", "learned"],
@@ -359,86 +360,125 @@ def e2e_abi(a, fields_np, rank, barrier, dist):
                     "per-frame callback frees the chd_frame_t"}
 
 
-def batched_workload(a):
-    """48 captures, 6-300 fields each, 40 % Transform 2D / 60 % 3D, thresholds
-    uniform in [0.3, 0.6] (seeded). Their fields are windows of the
-    synthetic stream at seeded offsets: the batch's cost depends on the
-    captures' lengths, modes and thresholds, not on which pictures they hold,
-    so the content is shared to keep generation to one stream."""
+BATCH_CAPTURES = 48
+
+
+def batched_specs(seed: int):
+    """The batched workload: 48 captures of uniform 6-300 fields, 40 % Transform
+    2D / 60 % 3D, threshold U[0.3, 0.6], horizontal pan U[0, 3] px/field and
+    vertical U[0, 1] line/field, each its own seeded content, 1 % of lines
+    with dropouts (runs of 20-400 samples at the sync tip, with sidecar spans)."""
     import numpy as np
-    rng = np.random.default_rng(a.seed + 100)
-    fields = make_capture(a)
-    caps = []
-    for _ in range(48):
+    rng = np.random.default_rng(seed + 100)
+    specs = []
+    for i in range(BATCH_CAPTURES):
         n = int(rng.integers(6, 301))
-        n = min(n, fields.shape[0])
-        start = int(rng.integers(0, fields.shape[0] - n + 1))
         kind = 7 if rng.random() < 0.4 else 8
-        caps.append((start, n, kind, float(rng.uniform(0.3, 0.6))))
-    return fields, caps
+        specs.append(dict(nfields=n, kind=kind, threshold=float(rng.uniform(0.3, 0.6)),
+                          pan_x=float(rng.uniform(0.0, 3.0)), pan_y=float(rng.uniform(0.0, 1.0)),
+                          seed=seed * 1000 + 17 * i + 5))
+    return specs
 
 
-def run_batched(a):
-    import ctypes as C
+def _gen_capture(args):
+    """Worker: encode one capture into its slice of the shared field file."""
+    import numpy as np
+    from libchromadec_gb300 import synth
+    path, offset, spec = args
+    cap = synth.make_capture(spec["nfields"], synth.SynthConfig(seed=spec["seed"], pan_x=spec["pan_x"],
+                                                                pan_y=spec["pan_y"], dropout_line_fraction=0.01))
+    mm = np.memmap(path, dtype=np.uint16, mode="r+", offset=offset * 2, shape=cap.fields.shape)
+    mm[:] = cap.fields
+    mm.flush()
+    del mm
+    return [(f, s[0], s[1], s[2]) for f, spans in enumerate(cap.dropouts) for s in spans]
+
+
+def batched_workload(a):
+    """Every capture's fields in one file (generated once per host in
+    parallel worker processes, started with spawn) and their dropouts."""
+    import multiprocessing as mp
+    import pickle
+    import numpy as np
+    from libchromadec_gb300 import synth
+    specs = batched_specs(a.seed)
+    flen = synth.FIELD_WIDTH * synth.FIELD_HEIGHT
+    total = sum(s["nfields"] for s in specs)
+    path = f"/tmp/chdg_batch_{a.seed}_{total}.u16"
+    dpath = path + ".drop.pkl"
+    offsets, o = [], 0
+    for sp in specs:
+        offsets.append(o)
+        o += sp["nfields"] * flen
+    if not (os.path.exists(path) and os.path.exists(dpath) and os.path.getsize(path) == 2 * total * flen):
+        np.memmap(path, dtype=np.uint16, mode="w+", shape=(total * flen,)).flush()
+        with mp.get_context("spawn").Pool(max(1, min(cpu_threads(), 32))) as pool:
+            drops = pool.map(_gen_capture, [(path, offsets[i], sp) for i, sp in enumerate(specs)])
+        with open(dpath, "wb") as fp:
+            pickle.dump(drops, fp)
+    with open(dpath, "rb") as fp:
+        drops = pickle.load(fp)
+    fields = np.memmap(path, dtype=np.uint16, mode="r", shape=(total, synth.FIELD_HEIGHT, synth.FIELD_WIDTH))
+    return fields, specs, offsets, drops
+
+
+def batched_measure(a):
+    """Device-resident fields/s of the batched workload through chdg_batch_*:
+    concealment, masks and both Transform modes of all 48 captures per step,
+    replayed from one CUDA graph after autotuning."""
     import numpy as np
     import torch
-    from libchromadec_gb300 import device as D
-    fields, spec = batched_workload(a)
+    from libchromadec_gb300 import device as D, synth
+    fields, specs, offsets, drops = batched_workload(a)
     fmt = D.FMT_P16 if a.format == "p16" else D.FMT_PS
     dtype = torch.int16 if fmt == D.FMT_P16 else torch.float32
-    dfields = torch.from_numpy(fields.reshape(fields.shape[0], -1).view(np.int16)).cuda()
-    items = []
-    for start, n, kind, thr in spec:
+    flen = synth.FIELD_WIDTH * synth.FIELD_HEIGHT
+    dfields = torch.from_numpy(np.ascontiguousarray(fields).reshape(-1, flen).view(np.int16)).cuda()
+    items, total_fields = [], 0
+    for sp, off, dr in zip(specs, offsets, drops):
+        n = sp["nfields"]
+        f0 = off // flen
         out = torch.empty((n // 2, 3, 576, 948), dtype=dtype, device="cuda")
-        items.append((dfields[start:start + n], kind, thr, out))
-    total_fields = sum(2 * (n // 2) for _, n, _, _ in spec)
+        mask = torch.empty((n // 2, 576, 948), dtype=torch.int16, device="cuda")
+        items.append((dfields[f0:f0 + n], sp["kind"], sp["threshold"], out, dr, D.CONCEAL, mask))
+        total_fields += 2 * (n // 2)
     s = torch.cuda.Stream()
     b = D.Batch(D.default_geometry(), D.default_config(kind=8, fmt=fmt))
     arr = D.Batch.captures(items)
     tuning = b.autotune(arr, s)
-    for _ in range(max(3, a.warmup)):
+    warm = max(3, a.warmup)
+    for _ in range(warm):
         b.decode(arr, s)
     s.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    steps = max(3, a.steps // 4)
     with torch.cuda.stream(s):
         e0.record(s)
-        for _ in range(a.steps):
+        for _ in range(steps):
             b.decode(arr, s)
         e1.record(s)
     s.synchronize()
-    ms_batch = e0.elapsed_time(e1) / a.steps
-    # the same captures one engine call each (what a per-capture loop does)
-    engines = {}
-    for _, kind, thr, _ in items:
-        if (kind, thr) not in engines:
-            engines[(kind, thr)] = D.Engine(D.default_geometry(), D.default_config(kind=kind, fmt=fmt, threshold=thr))
-
-    def per_capture():
-        for f, kind, thr, out in items:
-            engines[(kind, thr)].decode(f, 0, f.shape[0] // 2, out, s)
-
-    for _ in range(max(3, a.warmup)):
-        per_capture()
-    s.synchronize()
-    e0.record(s)
-    for _ in range(a.steps):
-        per_capture()
-    e1.record(s)
-    s.synchronize()
-    ms_loop = e0.elapsed_time(e1) / a.steps
-    line = {
-        "metric": "Transform-PAL batched captures fields/s on 1 GB300", "value": total_fields / (ms_batch / 1000.0),
-        "unit": "fields/s", "n_gpus": 1, "steps": a.steps, "warmup": max(3, a.warmup), "ms_per_step": ms_batch,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
-        "config": {"workload": f"48 captures, 6-300 fields each ({total_fields} fields), 40% Transform 2D / 60% 3D, "
-                               f"thresholds U[0.3, 0.6], yuv444{a.format}, device-resident, one CUDA graph per step",
-                   "tuning": {"chunk_frames": tuning.chunk_frames, "max_blocks": tuning.max_blocks,
-                              "ms": tuning.ms}},
-        "per_capture_loop": {"value": total_fields / (ms_loop / 1000.0), "unit": "fields/s", "ms_per_step": ms_loop,
-                             "path": "chdg_decode_device once per capture on one stream"},
-    }
-    print(json.dumps(line), flush=True)
+    ms = e0.elapsed_time(e1) / steps
     b.close()
+    n2d = sum(1 for sp in specs if sp["kind"] == 7)
+    return {"metric": "Transform-PAL batched captures fields/s on 1 GB300", "value": total_fields / (ms / 1000.0),
+            "unit": "fields/s", "ms_per_step": ms, "steps": steps, "warmup": warm,
+            "workload": f"{len(specs)} captures of 6-300 fields ({total_fields} fields decoded), {n2d} Transform 2D / "
+                        f"{len(specs) - n2d} 3D, thresholds U[0.3, 0.6], pans U[0, 3] px/field + U[0, 1] line/field, "
+                        f"each its own seeded content, 1 % of lines with dropouts ({sum(len(d) for d in drops)} "
+                        f"spans) concealed and masked inside the batch, yuv444{a.format}, device-resident, one "
+                        f"CUDA graph per step",
+            "dropout_spans": sum(len(d) for d in drops),
+            "tuning": {"chunk_frames": tuning.chunk_frames, "max_blocks": tuning.max_blocks, "ms": tuning.ms}}
+
+
+def run_batched(a):
+    r = batched_measure(a)
+    line = {"metric": r["metric"], "value": r["value"], "unit": "fields/s", "n_gpus": 1, "steps": r["steps"],
+            "warmup": r["warmup"], "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+            "config": {"workload": r["workload"], "tuning": r["tuning"]}}
+    print(json.dumps(line), flush=True)
 
 
 def learned_report(a, dfields, nfields, stream):
@@ -595,8 +635,8 @@ def main():
     nframes = nfields // 2
     fmt = D.FMT_P16 if a.format == "p16" else D.FMT_PS
     two = a.kind == "2d"
-    if two:   # the end-to-end, CPU and forms legs are the 3D metric's
-        a.no_e2e = a.no_cpu = a.no_forms = True
+    if two:   # the end-to-end, CPU, forms and batched legs are the 3D metric's
+        a.no_e2e = a.no_cpu = a.no_forms = a.no_batched = True
     eng = D.Engine(D.default_geometry(),
                    D.default_config(kind=D.KIND_TRANSFORM_2D if two else D.KIND_TRANSFORM_3D, fmt=fmt))
     tc_form = {"plain": -1, "tc_3xtf32": D.TC_3XTF32, "tc_bf16x3": D.TC_BF16X3, "learned": -1}[a.form]
@@ -739,6 +779,8 @@ def main():
 
     if rank == 0 and not a.no_forms and a.format == "p16" and tc_form < 0 and not two:
         line["forms"] = forms_report(a, dfields, nfields, value, stream)
+    if rank == 0 and not a.no_batched and not two and a.form == "plain":
+        line["batched"] = batched_measure(a)
     if rank == 0 and not a.no_cpu:
         line["cpu_baseline"] = cpu_baseline(a, fields_np)
     if rank == 0:

@@ -141,6 +141,16 @@ int chdg_decode_device_static(const chdg_geometry *g, const chdg_config *c, cons
  * (padding_multiple 1, no per-bin thresholds). Asynchronous on `stream`;
  * graphs need a created stream (on the legacy default stream, NULL, every
  * decode runs eagerly). */
+typedef struct chdg_dropout {
+    int32_t field;                /* 0-based field of the capture */
+    int32_t startx, endx;         /* samples [startx, endx) */
+    int32_t field_line;           /* 1-based field line, as ld-decode's metadata counts */
+} chdg_dropout;
+
+#define CHDG_CONCEAL 1                /* conceal the capture's dropouts before decoding */
+#define CHDG_CONCEAL_OVERCORRECT 2    /* chd_dropout_opts_t.overcorrect */
+#define CHDG_CONCEAL_INTRA 4          /* chd_dropout_opts_t.intra_field */
+
 typedef struct chdg_capture {
     const uint16_t *fields;       /* device: field f at fields + f * field_stride */
     int64_t field_stride;
@@ -148,6 +158,19 @@ typedef struct chdg_capture {
     int32_t kind;                 /* 7 = Transform 2D, 8 = Transform 3D */
     double threshold;             /* transform_threshold of this capture */
     void *out;                    /* device: nfields / 2 output frames */
+    /* The capture's dropouts (host array, ld-decode sidecar spans; read when
+     * the batch's shape changes, so it must not change between decodes of
+     * one batch) and what to do with them: `conceal` = CHDG_CONCEAL (plus
+     * _OVERCORRECT / _INTRA) conceals them as DropoutCorrector does
+     * (src/dropout/dropout_corrector.cpp:50-530) on a device copy of the
+     * capture -- the caller's fields are not modified -- before decoding;
+     * mask_out, when not NULL, receives each frame's dropout mask
+     * (chd_decode_dropout_mask's detected mode, GRAY16 0 / 0xFFFF in the
+     * output geometry: nfields / 2 planes, device memory). */
+    const chdg_dropout *dropouts;
+    int32_t ndropouts;
+    int32_t conceal;
+    uint16_t *mask_out;
 } chdg_capture;
 
 typedef struct chdg_batch chdg_batch;

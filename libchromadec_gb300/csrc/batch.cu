@@ -17,6 +17,17 @@
 // transform launch and one demodulator launch then cover every capture of a
 // mode, so short captures no longer leave the GPU mostly idle.
 //
+// Dropouts. A capture with CHDG_CONCEAL set is copied once per decode into a
+// device pool (the caller's fields stay as they are, so a replayed decode
+// conceals the same samples again) and each of its frames with dropouts is
+// concealed there by the pipeline's own kernel, from the plan the host makes
+// once per batch shape (dropout_plan.cpp, DropoutCorrector::correctFrame);
+// its field-table entries then point into the pool. A frame's plan reads only
+// its own two fields, so concealing every frame once is what the reference's
+// per-window concealment gives each window. Dropout masks (the detected
+// mode's spans in output framing, c_api_dropout_detect.cpp:92-174) are
+// rastered by one launch over every span of the batch.
+//
 // Graphs. The first decode of a batch shape runs eagerly (it sizes every
 // buffer); the copies and launches of a shape are then captured once into a
 // CUDA graph, and later decodes of the same captures replay it with one
@@ -31,8 +42,14 @@
 
 #include <cuda_runtime.h>
 
+#include "dropout_plan.h"
 #include "engine.h"
 #include "error_state.h"
+
+namespace chdg {
+int dropout_apply(uint16_t *fields, long long field_stride, int fw, const int *d_frames, const DropOp *d_ops,
+                  const int *d_op_begin, int nframes, const uint16_t *extras, bool ntsc_taps, cudaStream_t s);
+}
 
 namespace {
 
@@ -61,6 +78,40 @@ struct ModeLayout {
     std::vector<void *> outs;            // per frame
 };
 
+// A mask span of the batch: row `row` (a plane row's first sample) gets
+// 0xFFFF in [x0, x1).
+struct MaskSpan {
+    uint16_t *row;
+    int32_t x0, x1;
+};
+
+__global__ void batch_mask_kernel(const MaskSpan *spans)
+{
+    const MaskSpan m = spans[blockIdx.x];
+    for (int x = m.x0 + (int)threadIdx.x; x < m.x1; x += blockDim.x) m.row[x] = 0xFFFF;
+}
+
+// Concealment of a batch: captures copied into the pool, the frames' plans.
+struct ConcealPlan {
+    struct Copy {
+        const uint16_t *src;
+        int64_t src_stride;
+        int64_t pool_field;   // first pool field
+        int32_t nfields;
+    };
+    std::vector<Copy> copies;
+    std::vector<int> frames;        // per planned frame: its slot-0 pool field
+    std::vector<int> op_begin;      // per planned frame, plus the end
+    std::vector<chdg::DropOp> ops;
+    std::vector<MaskSpan> spans;
+    struct Clear {
+        uint16_t *plane;
+        size_t bytes;
+    };
+    std::vector<Clear> clears;      // mask buffers to zero
+    int64_t pool_fields = 0;
+};
+
 // The device copy of one mode's tables.
 struct ModeTables {
     const uint16_t **fptr = nullptr;
@@ -83,6 +134,15 @@ struct chdg_batch {
     chdg_config c{};
     chdg::Engine eng3, eng2;
     ModeTables tab3, tab2;
+    // concealment and masks of the current shape
+    ConcealPlan cp;
+    uint16_t *pool = nullptr;
+    int64_t pool_cap = 0;     // fields
+    int64_t pool_stride = 0;  // samples per pool field
+    chdg::DropOp *d_ops = nullptr;
+    int *d_idx = nullptr;     // frames, then op_begin
+    MaskSpan *d_spans = nullptr;
+    size_t ops_cap = 0, idx_cap = 0, spans_cap = 0;
     // the shape of the last decode, and its graph
     std::vector<chdg_capture> last;
     cudaGraph_t graph = nullptr;
@@ -93,6 +153,149 @@ struct chdg_batch {
     {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
+        cudaFree(pool);
+        cudaFree(d_ops);
+        cudaFree(d_idx);
+        cudaFree(d_spans);
+    }
+
+    // VideoParameters of the batch's raster for the concealment planner
+    chdg::VideoParams video_params() const
+    {
+        chdg::VideoParams vp;
+        vp.system = g.field_height == 263 ? chdg::SYS_PAL_M : chdg::SYS_PAL;
+        vp.fieldWidth = g.field_width;
+        vp.fieldHeight = g.field_height;
+        vp.sampleRate = g.sample_rate;
+        vp.fSC = g.fsc;
+        vp.activeVideoStart = g.active_start;
+        vp.activeVideoEnd = g.active_end;
+        vp.colourBurstStart = g.burst_start;
+        vp.colourBurstEnd = g.burst_end;
+        vp.black16bIre = g.black;
+        vp.white16bIre = g.white;
+        vp.blanking16bIre = g.black;
+        vp.firstActiveFrameLine = g.first_active_frame_line;
+        vp.lastActiveFrameLine = g.last_active_frame_line;
+        return vp;
+    }
+
+    // Plans, pool placement and mask spans of the captures with dropouts;
+    // `fields_of` gives each capture's field pointers (pool or caller).
+    int plan_dropouts(const chdg_capture *caps, int n, std::vector<int64_t> &pool_first)
+    {
+        cp = ConcealPlan{};
+        pool_first.assign((size_t)n, -1);
+        const chdg::VideoParams vp = video_params();
+        const int aw = g.active_end - g.active_start;
+        const int ah = g.last_active_frame_line - g.first_active_frame_line + 1;
+        const chdg::OutputFraming fr{g.active_start, aw, aw, ah, g.first_active_frame_line, 0, 0, g.field_width};
+        const size_t plane = (size_t)aw * ah;
+        for (int i = 0; i < n; i++) {
+            const chdg_capture &k = caps[i];
+            if (k.ndropouts < 0 || (k.ndropouts > 0 && k.dropouts == nullptr))
+                return bfail("chdg_batch_decode: capture " + std::to_string(i) + " has a bad dropout list");
+            const int nf = k.nfields / 2;
+            std::vector<chdg::FieldMeta> meta((size_t)2 * nf);
+            for (int f = 0; f < 2 * nf; f++) meta[f].isFirstField = (f & 1) == 0;
+            for (int j = 0; j < k.ndropouts; j++) {
+                const chdg_dropout &d = k.dropouts[j];
+                if (d.field >= 0 && d.field < 2 * nf) meta[d.field].dropouts.push_back({d.startx, d.endx, d.field_line});
+            }
+            if (k.mask_out != nullptr) {
+                cp.clears.push_back({k.mask_out, plane * sizeof(uint16_t) * (size_t)nf});
+                for (int f = 0; f < nf; f++) {
+                    if (meta[2 * f].dropouts.empty() && meta[2 * f + 1].dropouts.empty()) continue;
+                    const std::vector<chdg::Span> sp = chdg::frame_spans(fr, meta[2 * f], true, meta[2 * f + 1], false,
+                                                                         false);
+                    for (const chdg::Span &s : sp)
+                        cp.spans.push_back({k.mask_out + plane * (size_t)f + (size_t)s.y * aw, s.x_start, s.x_end});
+                }
+            }
+            if ((k.conceal & CHDG_CONCEAL) == 0 || k.ndropouts == 0 || nf == 0) continue;
+            pool_first[i] = cp.pool_fields;
+            cp.copies.push_back({k.fields, k.field_stride, cp.pool_fields, 2 * nf});
+            const bool oc = (k.conceal & CHDG_CONCEAL_OVERCORRECT) != 0, intra = (k.conceal & CHDG_CONCEAL_INTRA) != 0;
+            for (int f = 0; f < nf; f++) {
+                if (meta[2 * f].dropouts.empty() && meta[2 * f + 1].dropouts.empty()) continue;
+                const chdg::FramePlan pl = chdg::plan_frame(vp, meta[2 * f], meta[2 * f + 1], oc, intra);
+                if (pl.ops.empty()) continue;
+                cp.frames.push_back((int)(cp.pool_fields + 2 * f));
+                cp.op_begin.push_back((int)cp.ops.size());
+                cp.ops.insert(cp.ops.end(), pl.ops.begin(), pl.ops.end());
+            }
+            cp.pool_fields += 2 * nf;
+        }
+        cp.op_begin.push_back((int)cp.ops.size());
+        return 0;
+    }
+
+    int upload_dropouts(cudaStream_t s)
+    {
+        cudaError_t e;
+        pool_stride = ((int64_t)g.field_width * g.field_height + 63) & ~(int64_t)63;
+        if (cp.pool_fields > pool_cap) {
+            cudaFree(pool);
+            pool = nullptr;
+            pool_cap = 0;
+            if ((e = cudaMalloc(&pool, (size_t)cp.pool_fields * pool_stride * sizeof(uint16_t))) != cudaSuccess)
+                return cfail("concealment pool", e);
+            pool_cap = cp.pool_fields;
+        }
+        auto grow = [&](void **p, size_t &cap, size_t need, size_t elem) -> cudaError_t {
+            if (need <= cap) return cudaSuccess;
+            cudaFree(*p);
+            *p = nullptr;
+            cap = 0;
+            const cudaError_t r = cudaMalloc(p, need * elem);
+            if (r == cudaSuccess) cap = need;
+            return r;
+        };
+        const size_t nidx = cp.frames.size() + cp.op_begin.size();
+        if ((e = grow((void **)&d_ops, ops_cap, std::max<size_t>(cp.ops.size(), 1), sizeof(chdg::DropOp))) !=
+                cudaSuccess ||
+            (e = grow((void **)&d_idx, idx_cap, std::max<size_t>(nidx, 1), sizeof(int))) != cudaSuccess ||
+            (e = grow((void **)&d_spans, spans_cap, std::max<size_t>(cp.spans.size(), 1), sizeof(MaskSpan))) !=
+                cudaSuccess)
+            return cfail("concealment tables", e);
+        std::vector<int> idx(cp.frames);
+        idx.insert(idx.end(), cp.op_begin.begin(), cp.op_begin.end());
+        if (!cp.ops.empty() &&
+            (e = cudaMemcpyAsync(d_ops, cp.ops.data(), cp.ops.size() * sizeof(chdg::DropOp), cudaMemcpyHostToDevice,
+                                 s)) != cudaSuccess)
+            return cfail("concealment tables", e);
+        if ((e = cudaMemcpyAsync(d_idx, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice, s)) !=
+            cudaSuccess)
+            return cfail("concealment tables", e);
+        if (!cp.spans.empty() &&
+            (e = cudaMemcpyAsync(d_spans, cp.spans.data(), cp.spans.size() * sizeof(MaskSpan), cudaMemcpyHostToDevice,
+                                 s)) != cudaSuccess)
+            return cfail("mask spans", e);
+        // the host vectors must outlive the copies
+        return (e = cudaStreamSynchronize(s)) == cudaSuccess ? 0 : cfail("sync", e);
+    }
+
+    // Copies, concealment and masks (no allocation, no sync: capturable).
+    int enqueue_dropouts(cudaStream_t s)
+    {
+        cudaError_t e;
+        const size_t flen = (size_t)g.field_width * g.field_height;
+        for (const auto &c : cp.copies)
+            if ((e = cudaMemcpy2DAsync(pool + (size_t)c.pool_field * pool_stride, pool_stride * sizeof(uint16_t),
+                                       c.src, (size_t)c.src_stride * sizeof(uint16_t), flen * sizeof(uint16_t),
+                                       (size_t)c.nfields, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+                return cfail("concealment copy", e);
+        if (!cp.frames.empty() &&
+            chdg::dropout_apply(pool, pool_stride, g.field_width, d_idx, d_ops, d_idx + cp.frames.size(),
+                                (int)cp.frames.size(), nullptr, g.field_height == 263, s) != 0)
+            return cfail("concealment", cudaGetLastError());
+        for (const auto &c : cp.clears)
+            if ((e = cudaMemsetAsync(c.plane, 0, c.bytes, s)) != cudaSuccess) return cfail("mask clear", e);
+        if (!cp.spans.empty()) {
+            batch_mask_kernel<<<(unsigned)cp.spans.size(), 128, 0, s>>>(d_spans);
+            if ((e = cudaGetLastError()) != cudaSuccess) return cfail("mask launch", e);
+        }
+        return 0;
     }
 
     void drop_graph()
@@ -111,8 +314,14 @@ struct chdg_batch {
         return true;
     }
 
-    int layout(const chdg_capture *caps, int n, ModeLayout &m3, ModeLayout &m2)
+    int layout(const chdg_capture *caps, int n, const std::vector<int64_t> &pool_first, ModeLayout &m3,
+               ModeLayout &m2)
     {
+        // a capture's field i: in the concealment pool, or the caller's buffer
+        auto field_ptr = [&](int ci, int64_t i) -> const uint16_t * {
+            if (pool_first[(size_t)ci] >= 0) return pool + (size_t)(pool_first[(size_t)ci] + i) * pool_stride;
+            return caps[ci].fields + i * caps[ci].field_stride;
+        };
         const size_t fb = eng3.frame_bytes();
         for (int i = 0; i < n; i++) {
             const chdg_capture &k = caps[i];
@@ -147,7 +356,7 @@ struct chdg_batch {
             for (int64_t f = a - kGapFrames; f < a + nf; f++) frame_t2(k.threshold, &m3.t2[3 * f]);
             for (int64_t f = 0; f < nf; f++) m3.outs[a + f] = (char *)k.out + fb * (size_t)f;
             // an unpaired last field is outside every frame: black, as in the reference's window
-            for (int64_t i = 0; i < 2 * nf; i++) m3.fptr[2 * a + i] = k.fields + i * k.field_stride;
+            for (int64_t i = 0; i < 2 * nf; i++) m3.fptr[2 * a + i] = field_ptr(m3.caps[j], i);
         }
         int64_t fr2 = 0;
         for (int ci : m2.caps) {
@@ -163,7 +372,7 @@ struct chdg_batch {
             const int64_t a = m2.first_frame[j], nf = k.nfields / 2;
             for (int64_t f = a; f < a + nf; f++) frame_t2(k.threshold, &m2.t2[3 * f]);
             for (int64_t f = 0; f < nf; f++) m2.outs[a + f] = (char *)k.out + fb * (size_t)f;
-            for (int64_t i = 0; i < 2 * nf; i++) m2.fptr[2 * a + i] = k.fields + i * k.field_stride;
+            for (int64_t i = 0; i < 2 * nf; i++) m2.fptr[2 * a + i] = field_ptr(m2.caps[j], i);
         }
         return 0;
     }
@@ -217,8 +426,11 @@ struct chdg_batch {
             const cudaError_t e = cudaGraphLaunch(exec, s);
             return e == cudaSuccess ? 0 : cfail("graph launch", e);
         }
+        std::vector<int64_t> pool_first;
+        if (const int rc = plan_dropouts(caps, n, pool_first); rc != 0) return rc;
+        if (const int rc = upload_dropouts(s); rc != 0) return rc;
         ModeLayout m3, m2;
-        if (const int rc = layout(caps, n, m3, m2); rc != 0) return rc;
+        if (const int rc = layout(caps, n, pool_first, m3, m2); rc != 0) return rc;
         if (const int rc = upload(m3, tab3, s); rc != 0) return rc;
         if (const int rc = upload(m2, tab2, s); rc != 0) return rc;
         cudaError_t e;
@@ -234,13 +446,15 @@ struct chdg_batch {
         if (!allow_graph || eager_runs == 0) {
             // eager: sizes the engines' scratch before any capture
             eager_runs++;
+            if (const int rc = enqueue_dropouts(s); rc != 0) return rc;
             if (const int rc = enqueue(caps, m3, eng3, s); rc != 0) return rc;
             return enqueue(caps, m2, eng2, s);
         }
         // capture this shape once, then replay
         if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
             return cfail("begin capture", e);
-        int rc = enqueue(caps, m3, eng3, s);
+        int rc = enqueue_dropouts(s);
+        if (rc == 0) rc = enqueue(caps, m3, eng3, s);
         if (rc == 0) rc = enqueue(caps, m2, eng2, s);
         cudaGraph_t gph = nullptr;
         e = cudaStreamEndCapture(s, &gph);

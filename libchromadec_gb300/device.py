@@ -42,10 +42,21 @@ class Config(C.Structure):
     ]
 
 
+class Dropout(C.Structure):
+    """chdg_dropout: one dropout span of a capture's field (field 0-based, field_line 1-based)."""
+    _fields_ = [("field", C.c_int32), ("startx", C.c_int32), ("endx", C.c_int32), ("field_line", C.c_int32)]
+
+
+CONCEAL = 1
+CONCEAL_OVERCORRECT = 2
+CONCEAL_INTRA = 4
+
+
 class Capture(C.Structure):
-    """chdg_capture: one capture of a batch (device buffers)."""
+    """chdg_capture: one capture of a batch (device buffers; dropouts on the host)."""
     _fields_ = [("fields", C.c_void_p), ("field_stride", C.c_int64), ("nfields", C.c_int32), ("kind", C.c_int32),
-                ("threshold", C.c_double), ("out", C.c_void_p)]
+                ("threshold", C.c_double), ("out", C.c_void_p), ("dropouts", C.POINTER(Dropout)),
+                ("ndropouts", C.c_int32), ("conceal", C.c_int32), ("mask_out", C.c_void_p)]
 
 
 class BatchTuning(C.Structure):
@@ -255,10 +266,19 @@ class Batch:
 
     @staticmethod
     def captures(items):
-        """items: (fields tensor (n, stride), kind, threshold, out tensor) tuples."""
+        """items: (fields tensor (n, stride), kind, threshold, out tensor) tuples, optionally followed by
+        (dropouts [(field, startx, endx, fieldLine)], conceal flags, mask tensor or None)."""
         arr = (Capture * len(items))()
-        for i, (f, kind, thr, out) in enumerate(items):
-            arr[i] = Capture(f.data_ptr(), f[0].numel(), f.shape[0], kind, thr, out.data_ptr())
+        keep = []
+        for i, it in enumerate(items):
+            f, kind, thr, out = it[:4]
+            drops, conceal, mask = (list(it[4]), int(it[5]), it[6]) if len(it) > 4 else ([], 0, None)
+            d = (Dropout * max(1, len(drops)))(*[Dropout(*x) for x in drops])
+            keep.append(d)
+            arr[i] = Capture(f.data_ptr(), f[0].numel(), f.shape[0], kind, thr, out.data_ptr(),
+                             C.cast(d, C.POINTER(Dropout)), len(drops), conceal,
+                             mask.data_ptr() if mask is not None else None)
+        arr._keep = keep
         return arr
 
     def decode(self, caps, stream=None):

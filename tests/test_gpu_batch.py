@@ -60,3 +60,59 @@ def test_batch_equals_per_capture_decode(cuda):
         d = np.abs(out.cpu().numpy().view(np.uint16).astype(np.int32) - ref.astype(np.int32))
         assert d.max() <= 1
     b.close()
+
+
+def test_batch_conceals_and_masks_dropouts(cuda):
+    """Captures with 2 % dropout lines, concealed inside the batch (single-frame
+    plans, every mode) and masked: each frame equals the engine's decode of
+    the capture concealed by the oracle's DropoutCorrector (itself byte-exact
+    with the reference's), bit for bit; masks equal the oracle's spans
+    rastered; the caller's fields are left as they were; eager, captured and
+    replayed decodes agree."""
+    torch = cuda
+    from libchromadec_gb300 import device as D, synth
+    specs = [(12, 8, D.CONCEAL), (7, 7, D.CONCEAL | D.CONCEAL_OVERCORRECT), (20, 8, D.CONCEAL | D.CONCEAL_INTRA),
+             (6, 7, 0), (9, 8, D.CONCEAL | D.CONCEAL_OVERCORRECT | D.CONCEAL_INTRA)]
+    items, refs, masks_ref, originals = [], [], [], []
+    for i, (n, kind, flags) in enumerate(specs):
+        cap = synth.make_capture(n, synth.SynthConfig(seed=90 + i, pan_x=1.0 + 0.5 * i, pan_y=0.5,
+                                                      dropout_line_fraction=0.02))
+        drops = O.flatten_dropouts(cap.dropouts)
+        assert drops
+        p = O.params(3 if kind == 8 else 2, O.FMT_P16)
+        conc = cap.fields.copy()
+        if flags & D.CONCEAL:
+            for k in range(n // 2):
+                conc[2 * k:2 * k + 2], _ = O.dropout_correct_frame(p, cap.fields, k, drops,
+                                                                   overcorrect=bool(flags & D.CONCEAL_OVERCORRECT),
+                                                                   intra=bool(flags & D.CONCEAL_INTRA))
+        f = torch.from_numpy(cap.fields.reshape(n, -1).view(np.int16)).cuda()
+        fc = torch.from_numpy(conc.reshape(n, -1).view(np.int16)).cuda()
+        eng = D.Engine(D.default_geometry(), D.default_config(kind=kind, fmt=D.FMT_P16))
+        ref = torch.empty((n // 2, 3, 576, 948), dtype=torch.int16, device="cuda")
+        eng.decode(fc, 0, n // 2, ref)
+        refs.append(ref)
+        mref = np.zeros((n // 2, 576, 948), dtype=np.uint16)
+        for k in range(n // 2):
+            for y, x0, x1, _ in O.dropout_spans(p, drops, k, 0):
+                mref[k, y, x0:x1] = 0xFFFF
+        masks_ref.append(mref)
+        out = torch.zeros_like(ref)
+        mask = torch.full((n // 2, 576, 948), 7, dtype=torch.int16, device="cuda")
+        items.append((f, kind, 0.4, out, drops, flags, mask))
+        originals.append(f.clone())
+    s = torch.cuda.Stream()
+    b = D.Batch(D.default_geometry(), D.default_config(kind=8, fmt=D.FMT_P16))
+    arr = D.Batch.captures(items)
+    for rep in range(3):                                   # eager, capture, replay
+        for it in items:
+            it[3].zero_()
+            it[6].fill_(7)
+        torch.cuda.synchronize()
+        b.decode(arr, s)
+        s.synchronize()
+        for i, (it, ref, mref, orig) in enumerate(zip(items, refs, masks_ref, originals)):
+            assert torch.equal(it[3], ref), (rep, i)
+            assert np.array_equal(it[6].cpu().numpy().view(np.uint16), mref), (rep, i)
+            assert torch.equal(it[0], orig), (rep, i)
+    b.close()
