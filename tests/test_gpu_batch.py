@@ -90,7 +90,10 @@ def test_batch_conceals_and_masks_dropouts(cuda):
         fc = torch.from_numpy(conc.reshape(n, -1).view(np.int16)).cuda()
         eng = D.Engine(D.default_geometry(), D.default_config(kind=kind, fmt=D.FMT_P16))
         ref = torch.empty((n // 2, 3, 576, 948), dtype=torch.int16, device="cuda")
-        eng.decode(fc, 0, n // 2, ref)
+        # an unpaired last field belongs to no frame: the batch, like the
+        # reference's window, reads it as black, so the reference decode gets
+        # the whole frames only
+        eng.decode(fc[:2 * (n // 2)], 0, n // 2, ref)
         refs.append(ref)
         mref = np.zeros((n // 2, 576, 948), dtype=np.uint16)
         for k in range(n // 2):
