@@ -475,27 +475,33 @@ __global__ void mn_round_kernel(const float *master, float *used)
 // K, so the kx taps become a banded weight matrix -- block (q, q') holds
 // W[dz][dy][q' - q] for |q' - q| <= 1 and zeros otherwise. A ky tap is an
 // offset of whole groups into the A operand (a one-group periodic halo on
-// both sides); the three kz taps use three copies of the activations with kz
-// rotated inside each group. One layer of one tile: for dz in -1..1, build
-// the rotated copy (34 groups x K) from the compact activations and copy the
-// dz's three weight images, then 3 (ky taps) x 2 (M blocks of 128 rows) x
-// K/16 MMAs of 128 x 80 x 16 accumulate in tensor memory; the epilogue adds
-// the bias, applies ReLU and rounds to bf16 (or runs the sigmoid head).
+// both sides); the three kz taps read three copies of the layer's input with
+// kz rotated inside each group. Those copies are written directly by the
+// previous layer's epilogue (and, for the first layer, by the input load):
+// no separate operand-building phase. Per layer, one thread issues the three
+// kz taps' 3 (ky taps) x 2 (M blocks of 128 rows) x K/16 MMAs of 128 x 80 x
+// 16 back to back, taking each tap's three weight images from one of two
+// shared-memory slots that the TMA bulk engine fills ahead (the next layer's
+// first two taps are copied while this layer's epilogue runs); the epilogue
+// adds the bias, applies ReLU, rounds to bf16 and stores the next layer's
+// three input copies (or runs the sigmoid head).
 constexpr int kTcThreads = 256;
-constexpr int kActStride = 176;                       // bytes per compact activation row (80 bf16 + pad)
 constexpr int kGroupsA = 34;                          // 32 ky groups + one halo group on each side
-constexpr int SM_ACT = 0;                             // [256 rows][kActStride]
-constexpr int SM_A = 256 * kActStride;                // [34 groups][8 rows][K] canonical
-constexpr int SM_B = SM_A + kGroupsA * 8 * 160;       // [3 ky taps][80 rows][K] canonical
-constexpr int SM_BAR = SM_B + 3 * 80 * 160;
+constexpr int A_COPY = kGroupsA * 8 * 160;            // one kz rotation of a layer's input, K up to 80
+constexpr int B_SLOT = 3 * 80 * 160;                  // one kz tap's three ky-tap weight images
+constexpr int SM_A = 0;                               // [3 kz rotations][34 groups][8 rows][K] canonical
+constexpr int SM_B = 3 * A_COPY;                      // [2 slots][3 ky taps][80 rows][K] canonical
+constexpr int SM_BAR = SM_B + 2 * B_SLOT;
 constexpr int kTcSmem = SM_BAR + 64;
+static_assert(kTcSmem <= 227 * 1024, "shared memory of one CTA");
 // weight images in global memory: layer 1 (K = 16), layers 2 and 3 (K = 80),
 // each [dz][dy][80 rows][K] in the canonical layout
 constexpr int IMG_L1 = 0;
 constexpr int IMG_L2 = IMG_L1 + 9 * 80 * 32;
 constexpr int IMG_L3 = IMG_L2 + 9 * 80 * 160;
 constexpr int IMG_BYTES = IMG_L3 + 9 * 80 * 160;
-static_assert(SM_A % 16 == 0 && SM_B % 16 == 0 && SM_BAR % 16 == 0, "operand alignment");
+static_assert(SM_A % 16 == 0 && SM_B % 16 == 0 && SM_BAR % 16 == 0 && A_COPY % 16 == 0 && B_SLOT % 16 == 0,
+              "operand alignment");
 
 __global__ void mn_build_images_kernel(const float *used, uint8_t *img)
 {
@@ -522,6 +528,38 @@ __global__ void mn_build_images_kernel(const float *used, uint8_t *img)
     }
 }
 
+// One 16-byte chunk c of input row (ky, kz) of a layer whose rows hold KB
+// bytes, into the layer's three kz-rotated A copies: copy dz (kz tap dz - 1)
+// holds source kz in row (kz - dz + 1) mod 8 of group ky + 1; groups 0 and
+// 33 repeat ky = 31 and ky = 0 (the periodic halo).
+__device__ __forceinline__ void put_rotated(uint8_t *A, int KB, int ky, int kz, int c, uint4 v)
+{
+    const int grp = 8 * KB;
+#pragma unroll
+    for (int dz = 0; dz < 3; dz++) {
+        uint8_t *base = A + dz * A_COPY + c * 128 + ((kz - dz + 1) & 7) * 16;
+        *reinterpret_cast<uint4 *>(base + (ky + 1) * grp) = v;
+        if (ky == 31) *reinterpret_cast<uint4 *>(base) = v;
+        if (ky == 0) *reinterpret_cast<uint4 *>(base + (kGroupsA - 1) * grp) = v;
+    }
+}
+
+// The MMAs of kz tap dz of a layer: A copy dz, weight slot `slot`.
+__device__ __forceinline__ void issue_tap(uint32_t tmem, const uint8_t *A, const uint8_t *B, int dz, int slot, int K,
+                                          bool first)
+{
+    using namespace tpal::tc;
+    const int KB = 2 * K, grp = 8 * KB;
+    const uint32_t id = idesc(1, 128, 80);
+    for (int dy = 0; dy < 3; dy++)
+        for (int b = 0; b < 2; b++)
+            for (int ks = 0; ks < K / 16; ks++) {
+                const uint32_t a = smem_addr(A + dz * A_COPY + (b * 16 + dy) * grp + ks * 256);
+                const uint32_t bb = smem_addr(B + slot * B_SLOT + dy * 80 * KB + ks * 256);
+                mma<1>(tmem + b * 128, sdesc(a, grp), sdesc(bb, grp), id, (!first || dy > 0 || ks > 0) ? 1u : 0u);
+            }
+}
+
 template <bool TRAIN>
 __global__ void __launch_bounds__(kTcThreads, 1)
     mn_tc_forward_kernel(const uint8_t *img, const float *params, const uint16_t *feat, long long ntiles,
@@ -530,12 +568,16 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 {
     using namespace tpal::tc;
     extern __shared__ __align__(1024) uint8_t smem[];
-    uint8_t *act = smem + SM_ACT;
     uint8_t *A = smem + SM_A;
     uint8_t *B = smem + SM_B;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + SM_BAR);        // MMA completion
-    uint64_t *bbar = reinterpret_cast<uint64_t *>(smem + SM_BAR + 16);  // weight-image copy
+    // one completion per layer each: tap 0's MMAs (waited by the issuing
+    // thread, to refill slot 0), all the layer's MMAs (waited by every
+    // thread); one per weight slot fill (issue and wait alternate)
+    uint64_t *bm0 = reinterpret_cast<uint64_t *>(smem + SM_BAR);
     uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + SM_BAR + 8);
+    uint64_t *bm1 = reinterpret_cast<uint64_t *>(smem + SM_BAR + 16);
+    uint64_t *bb0 = reinterpret_cast<uint64_t *>(smem + SM_BAR + 24);
+    uint64_t *bb1 = reinterpret_cast<uint64_t *>(smem + SM_BAR + 32);
     __shared__ float s_par[4 * NC + 1];   // b1, b2, b3, wh, bh
     __shared__ float red[kTcThreads / 32];
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
@@ -544,8 +586,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         s_par[i] = params[off[i / NC] + i % NC];
     }
     if (t == 0) {
-        bar_init(bar);
-        bar_init(bbar);
+        bar_init(bm0);
+        bar_init(bm1);
+        bar_init(bb0);
+        bar_init(bb1);
     }
     if (warp == 0) tmem_alloc(tslot, 256);
     fence_async_smem();
@@ -553,13 +597,39 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     __syncthreads();
     fence_after();
     const uint32_t tmem = *tslot;
-    uint32_t phase = 0, bphase = 0;
+    // issuing thread's state: barrier parities and fills in flight
+    uint32_t pm0 = 0, pb0 = 0, pb1 = 0;
+    bool out0 = false, out1 = false;
+    uint32_t pm1 = 0;   // every thread
+    bool no_fill = false;   // take() argument for the MMA barrier
     bool ok = true;
-    const int eb = warp >> 2;                          // the epilogue's M block
+    auto layer_img = [&](int L) { return img + (L == 0 ? IMG_L1 : (L == 1 ? IMG_L2 : IMG_L3)); };
+    auto fill = [&](uint64_t *bar, int slot, int L, int dz) {
+        const uint32_t bytes = 3 * 80 * 2 * (L == 0 ? 16 : 80);
+        bar_arrive_expect_tx(bar, bytes);
+        bulk_g2s(B + slot * B_SLOT, layer_img(L) + dz * bytes, bytes, bar);
+    };
+    // a bounded wait; the parity advances (and the fill is no longer in
+    // flight) only when the phase completed
+    auto take = [](uint64_t *bar, uint32_t &par, bool &in_flight) {
+        const bool done = bar_wait(bar, par);
+        if (done) {
+            par ^= 1;
+            in_flight = false;
+        }
+        return done;
+    };
+    // the first tile's first layer: taps 0 and 1
+    if (t == 0 && (long long)blockIdx.x < ntiles) {
+        fill(bb0, 0, 0, 0);
+        fill(bb1, 1, 0, 1);
+        out0 = out1 = true;
+    }
+    const int eb = warp >> 2;                             // the epilogue's M block
     const int erow = eb * 128 + (warp & 3) * 32 + lane;   // its row: ky = erow >> 3, kz = erow & 7
     const int eky = erow >> 3, ekz = erow & 7;
     for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        // inputs: row m = t, k = 2 q + c (c = 0: the bin, 1: its mirror), zero-padded to 16
+        // inputs: row t = (ky, kz), k = 2 q + c (c = 0: the bin, 1: its mirror), zero-padded to 16
         {
             const int ky = t >> 3, kz = t & 7;
             const __nv_bfloat16 *f = reinterpret_cast<const __nv_bfloat16 *>(feat) + tile * NV;
@@ -571,57 +641,48 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
 #pragma unroll
             for (int k = 10; k < 16; k++) v[k] = __float2bfloat16_rn(0.f);
-            uint4 *d = reinterpret_cast<uint4 *>(act + t * kActStride);
-            d[0] = reinterpret_cast<const uint4 *>(v)[0];
-            d[1] = reinterpret_cast<const uint4 *>(v)[1];
+            put_rotated(A, 32, ky, kz, 0, reinterpret_cast<const uint4 *>(v)[0]);
+            put_rotated(A, 32, ky, kz, 1, reinterpret_cast<const uint4 *>(v)[1]);
         }
+        fence_async_smem();
+        fence_before();
         __syncthreads();
         float conf = 0.f;
-        for (int L = 0; L < 3 && ok; L++) {
-            const int K = L == 0 ? 16 : 80, KB = 2 * K, chunks = K / 8, grp = 8 * KB;
-            const uint8_t *imgL = img + (L == 0 ? IMG_L1 : (L == 1 ? IMG_L2 : IMG_L3));
-            for (int dz = 0; dz < 3 && ok; dz++) {
-                // B: the previous MMAs (which read it) are complete
-                if (t == 0) {
-                    const uint32_t bytes = 3 * 80 * KB;
-                    bar_arrive_expect_tx(bbar, bytes);
-                    bulk_g2s(B, imgL + dz * 3 * 80 * KB, bytes, bbar);
-                }
-                // A: group g holds ky = g - 1 (periodic), row i holds kz = (i + dz - 1) mod 8
-                const int nitems = kGroupsA * chunks * 8;
-                for (int it = t; it < nitems; it += kTcThreads) {
-                    const int i = it & 7, rest = it >> 3, c = rest % chunks, g = rest / chunks;
-                    const int src = (((g + 31) & 31) << 3) | ((i + dz + 7) & 7);
-                    *reinterpret_cast<uint4 *>(A + g * grp + c * 128 + i * 16) =
-                        *reinterpret_cast<const uint4 *>(act + src * kActStride + c * 16);
-                }
-                fence_async_smem();
-                fence_before();
-                __syncthreads();
-                bool bok = true;
-                if (t == 0) {
-                    fence_after();
-                    // this dz's three ky-tap weight images, copied by the TMA engine
-                    // while the threads built A
-                    bok = bar_wait(bbar, bphase);
-                    const uint32_t id = idesc(1, 128, 80);
-                    for (int dy = 0; dy < 3 && bok; dy++)
-                        for (int b = 0; b < 2; b++)
-                            for (int ks = 0; ks < K / 16; ks++) {
-                                const uint32_t a = smem_addr(A + (b * 16 + dy) * grp + ks * 256);
-                                const uint32_t bb = smem_addr(B + dy * 80 * KB + ks * 256);
-                                mma<1>(tmem + b * 128, sdesc(a, grp), sdesc(bb, grp), id,
-                                       (dz > 0 || dy > 0 || ks > 0) ? 1u : 0u);
-                            }
-                    mma_commit(bar);
-                }
-                const bool done = bar_wait(bar, phase);
-                phase ^= 1;
-                bphase ^= 1;
-                if (__syncthreads_or(!done || !bok)) ok = false;
+        for (int L = 0; L < 3; L++) {
+            const int K = L == 0 ? 16 : 80;
+            bool bok = true;
+            if (t == 0) {
                 fence_after();
+                bok = take(bb0, pb0, out0);
+                if (bok) issue_tap(tmem, A, B, 0, 0, K, true);
+                mma_commit(bm0);
+                if (bok) bok = take(bb1, pb1, out1);
+                if (bok) issue_tap(tmem, A, B, 1, 1, K, false);
+                // slot 0 is free once tap 0's MMAs are done: tap 2's weights
+                bool free0 = false;
+                if (bok) bok = take(bm0, pm0, free0);
+                if (bok) {
+                    fill(bb0, 0, L, 2);
+                    out0 = true;
+                    bok = take(bb0, pb0, out0);
+                }
+                if (bok) issue_tap(tmem, A, B, 2, 0, K, false);
+                mma_commit(bm1);
             }
-            if (!ok) break;
+            const bool done = take(bm1, pm1, no_fill);
+            if (__syncthreads_or(!done || !bok)) {
+                ok = false;
+                break;
+            }
+            fence_after();
+            // every MMA of this layer is done: both slots take the next layer's
+            // (or the next tile's first layer's) first two taps
+            if (t == 0 && (L < 2 || tile + gridDim.x < ntiles)) {
+                const int nl = L < 2 ? L + 1 : 0;
+                fill(bb0, 0, nl, 0);
+                fill(bb1, 1, nl, 1);
+                out0 = out1 = true;
+            }
             // epilogue: the warp's 32 rows of its M block, 80 columns (q, co)
             const uint32_t tb = tmem + ((uint32_t)((warp & 3) * 32) << 16) + eb * 128;
 #pragma unroll 1
@@ -633,9 +694,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     __align__(16) __nv_bfloat16 o[16];
 #pragma unroll
                     for (int co = 0; co < NC; co++) o[co] = __float2bfloat16_rn(fmaxf(v[co] + s_par[L * NC + co], 0.f));
-                    uint4 *d = reinterpret_cast<uint4 *>(act + erow * kActStride + q * 32);
-                    d[0] = reinterpret_cast<const uint4 *>(o)[0];
-                    d[1] = reinterpret_cast<const uint4 *>(o)[1];
+                    put_rotated(A, 160, eky, ekz, 2 * q, reinterpret_cast<const uint4 *>(o)[0]);
+                    put_rotated(A, 160, eky, ekz, 2 * q + 1, reinterpret_cast<const uint4 *>(o)[1]);
                     if (TRAIN) {
                         __nv_bfloat16 *ag = (L == 0 ? a1g : a2g) + tile * NC * NV;
 #pragma unroll
@@ -654,12 +714,18 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     conf += fabsf(p - 0.5f);
                 }
             }
+            fence_async_smem();
             fence_before();
             __syncthreads();
         }
         if (!ok) break;
         const float s = block_sum(conf, red);
         if (t == 0 && fallback != nullptr) fallback[tile] = (s * (1.0f / NV) < conf_limit) ? 1 : 0;
+    }
+    // no copy may still be writing this CTA's shared memory when it leaves
+    if (t == 0) {
+        if (out0 && !bar_wait(bb0, pb0)) ok = false;
+        if (out1 && !bar_wait(bb1, pb1)) ok = false;
     }
     fence_before();
     __syncthreads();
