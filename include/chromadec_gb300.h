@@ -256,8 +256,10 @@ int chdg_masknet_set_confidence(chdg_masknet *n, float limit);
  * wait that ran out (none is expected). */
 int chdg_masknet_set_tensor_cores(chdg_masknet *n, int32_t on);
 int chdg_masknet_sync(const chdg_masknet *n, void *stream);
-/* d_feat: ntiles x 1280 bf16 features (device); d_p: ntiles x 1280 FP32;
- * d_fallback: ntiles bytes (1 = the tile takes the threshold) or NULL. */
+/* d_feat: ntiles x 1280 bf16 features (device; 16-byte aligned on the
+ * tensor cores, where each tile's features are copied by the TMA bulk
+ * engine); d_p: ntiles x 1280 FP32; d_fallback: ntiles bytes (1 = the tile
+ * takes the threshold) or NULL. */
 int chdg_masknet_forward(const chdg_masknet *n, const uint16_t *d_feat, int64_t ntiles, float *d_p,
                          uint8_t *d_fallback, void *stream);
 /* One training step on a batch: d_ac holds per bin (|X|^2, Re(C conj X)) as

@@ -16,11 +16,17 @@
 // whose mean |p - 1/2| is below the confidence limit falls back to the
 // threshold decisions.
 //
-// Kernels (one CTA of 256 threads per tile, persistent over tiles; thread t
-// owns the (kz, ky) column t and computes its 5 q x 16 channels):
-//  * mn_forward_kernel<TRAIN>: features -> p (+ fallback flags); the
-//    training variant also keeps each layer's activations for the backward
-//    pass.
+// Kernels:
+//  * mn_tc_forward_kernel<TRAIN> (the default forward pass): each
+//    convolution as implicit GEMMs on the tensor cores (tcgen05, BF16
+//    operands, FP32 accumulators in tensor memory), warp-specialised and
+//    persistent over tiles; described where it is defined.
+// The CUDA-core kernels (one CTA of 256 threads per tile, persistent over
+// tiles; thread t owns the (kz, ky) column t and computes its 5 q x 16
+// channels):
+//  * mn_forward_kernel<TRAIN>: features -> p (+ fallback flags), the
+//    cross-check of the tensor-core pass; the training variant also keeps
+//    each layer's activations for the backward pass.
 //  * mn_loss_kernel: dL/dz of the head for L = sum |p X - C|^2 / sum |X|^2.
 //  * mn_backward_kernel: the head, then per layer the weight gradient (thread
 //    (ci, co) sums over the tile's voxels for all 27 taps) and the input
@@ -470,94 +476,327 @@ __global__ void mn_round_kernel(const float *master, float *used)
 // ---------------------------------------------------------------------------
 // Tensor-core forward pass (tcgen05): each convolution as implicit GEMMs
 // ---------------------------------------------------------------------------
-// Rows m = ky * 8 + kz (kz fastest: each ky is one 8-row core-matrix group),
-// N = 80 columns (q, co), K = (q', ci): the five kx positions fold into N and
-// K, so the kx taps become a banded weight matrix -- block (q, q') holds
-// W[dz][dy][q' - q] for |q' - q| <= 1 and zeros otherwise. A ky tap is an
-// offset of whole groups into the A operand (a one-group periodic halo on
-// both sides); the three kz taps read three copies of the layer's input with
-// kz rotated inside each group. Those copies are written directly by the
-// previous layer's epilogue (and, for the first layer, by the input load):
-// no separate operand-building phase. Per layer, one thread issues the three
-// kz taps' 3 (ky taps) x 2 (M blocks of 128 rows) x K/16 MMAs of 128 x 80 x
-// 16 back to back, taking each tap's three weight images from one of two
-// shared-memory slots that the TMA bulk engine fills ahead (the next layer's
-// first two taps are copied while this layer's epilogue runs); the epilogue
-// adds the bias, applies ReLU, rounds to bf16 and stores the next layer's
-// three input copies (or runs the sigmoid head).
-constexpr int kTcThreads = 256;
-constexpr int kGroupsA = 34;                          // 32 ky groups + one halo group on each side
-constexpr int A_COPY = kGroupsA * 8 * 160;            // one kz rotation of a layer's input, K up to 80
-constexpr int B_SLOT = 3 * 80 * 160;                  // one kz tap's three ky-tap weight images
-constexpr int SM_A = 0;                               // [3 kz rotations][34 groups][8 rows][K] canonical
-constexpr int SM_B = 3 * A_COPY;                      // [2 slots][3 ky taps][80 rows][K] canonical
-constexpr int SM_BAR = SM_B + 2 * B_SLOT;
-constexpr int kTcSmem = SM_BAR + 64;
-static_assert(kTcSmem <= 227 * 1024, "shared memory of one CTA");
-// weight images in global memory: layer 1 (K = 16), layers 2 and 3 (K = 80),
-// each [dz][dy][80 rows][K] in the canonical layout
+// Rows m = ky * 8 + kz (kz fastest: each ky is one 8-row core-matrix group;
+// 256 rows, two M blocks of 128), K = (q', ci) of the layer's input, N =
+// (q, dz, co): the kz taps are outputs, D_dz(ky, kz) = sum over (dy, q', ci)
+// of x(ky + dy - 1, kz) W[dz][dy][q' - q], and the epilogue forms
+// y(ky, kz) = sum_dz D_dz(ky, kz + dz - 1) with shuffles inside the 8 lanes
+// of each ky (the kz axis is periodic, as the lanes are). A ky tap is an
+// offset of whole groups into the one A operand (a periodic halo group on
+// both sides). The kx taps fold into N and K: output block q takes input
+// block q' through W[.][.][q' - q] for |q' - q| <= 1, so in layers 2 and 3
+// the MMAs of one K chunk (input q', its 16 channels) write only the 96 or
+// 144 columns of the outputs q = q' - 1 .. q' + 1 (N is ordered q, dz, co).
+// Layer 1 (K = 16: the five q' of the two input channels, zero-padded) takes
+// the full N = 240. One layer's MMAs read 30 A tiles (2 M blocks x 3 ky taps
+// x 5 chunks) instead of 90 with the kz taps in the operand.
+//
+// Roles (one CTA per SM, persistent over tiles):
+//  * warps 0-7, the epilogue: warp w reads tensor-memory lanes 32 (w & 3) ..
+//    of M block w >> 2. A layer's epilogue goes through the output blocks
+//    q = 0..4: it reads the block's 48 accumulator columns, zeroes them for
+//    the next layer (whose MMAs all accumulate), adds the dz partial sums,
+//    the bias and ReLU, rounds to bf16 and writes K chunk q of the next
+//    layer's input. The next layer's chunk q' MMAs write the columns of
+//    blocks q' - 1 .. q' + 1, so chunk q' is released once block q' + 1 is
+//    read. The last layer's epilogue writes the next tile's input, runs the
+//    sigmoid head and then releases the tensor memory to the next tile.
+//  * warp 8, one thread: issues each chunk's MMAs as it is released.
+//  * warp 9, one thread: the TMA bulk copies -- the weight pieces of each
+//    tile, in MMA order, through a ring of slots, and each next tile's
+//    features into one of two stages.
+// All waits are bounded; a wait that runs out raises the error flag and the
+// CTA leaves after its copies and MMAs in flight have completed.
+constexpr int kEpiWarps = 8;
+constexpr int kTcThreads = 32 * (kEpiWarps + 2);
+constexpr int kGroupsA = 34;                       // 32 ky groups + one halo group on each side
+constexpr int A_BYTES = kGroupsA * 8 * 160;        // a layer's input, K up to 80
+constexpr int NCOL = 3 * 80;                       // accumulator columns of one M block: (q, dz, co)
+constexpr int kSlots = 8;                          // weight-piece ring
+constexpr int SLOT_BYTES = 3 * 144 * 32;           // the largest piece: three ky taps x 144 rows x K 16
+constexpr int FEAT_BYTES = NV * 2;
+constexpr int kPieces = 13;                        // weight pieces of one tile
+// shared memory: [34 groups][8 rows][K] canonical, the ring, two feature
+// stages, the barriers
+constexpr int SM_A = 0;
+constexpr int SM_SLOT = A_BYTES;
+constexpr int SM_FEAT = SM_SLOT + kSlots * SLOT_BYTES;
+constexpr int SM_BAR = SM_FEAT + 2 * FEAT_BYTES;
+// barriers: a layer's MMAs done; K chunk q of the next input released (5);
+// slot full (kSlots); slot free (kSlots); feature stage full (2) and free
+// (2); the final drain of the MMAs
+constexpr int B_FULL = 0, B_READY = 1, B_SFULL = B_READY + 5, B_SFREE = B_SFULL + kSlots, B_FFULL = B_SFREE + kSlots,
+              B_FFREE = B_FFULL + 2, B_DRAIN = B_FFREE + 2, NBAR = B_DRAIN + 1;
+constexpr int SM_TSLOT = SM_BAR + 8 * NBAR;
+constexpr int SM_FLAG = SM_TSLOT + 4;
+constexpr int kTcSmem = SM_FLAG + 12;
+static_assert(kTcSmem + 1024 <= 227 * 1024, "shared memory of one CTA");
+static_assert(SM_SLOT % 16 == 0 && SLOT_BYTES % 16 == 0 && SM_FEAT % 16 == 0 && SM_BAR % 8 == 0, "copy alignment");
+
+// the band of output blocks of input block (K chunk) ks in layers 2 and 3
+__host__ __device__ constexpr int band_lo(int ks) { return ks > 0 ? ks - 1 : 0; }
+__host__ __device__ constexpr int band_q(int ks) { return (ks < 4 ? ks + 1 : 4) - band_lo(ks) + 1; }
+__host__ __device__ constexpr int band_off(int ks)
+{
+    int o = 0;
+    for (int k = 0; k < ks; k++) o += 3 * 48 * band_q(k) * 32;
+    return o;
+}
+// weight images in global memory, in the order the MMAs take them: layer 1
+// [dy][240 rows (q, dz, co)][K 16]; layers 2 and 3 [chunk ks][dy][48 x
+// band_q(ks) rows][K 16]; each ky tap's image canonical (8-row groups 256
+// bytes apart)
 constexpr int IMG_L1 = 0;
-constexpr int IMG_L2 = IMG_L1 + 9 * 80 * 32;
-constexpr int IMG_L3 = IMG_L2 + 9 * 80 * 160;
-constexpr int IMG_BYTES = IMG_L3 + 9 * 80 * 160;
-static_assert(SM_A % 16 == 0 && SM_B % 16 == 0 && SM_BAR % 16 == 0 && A_COPY % 16 == 0 && B_SLOT % 16 == 0,
-              "operand alignment");
+constexpr int IMG_L2 = IMG_L1 + 3 * NCOL * 32;
+constexpr int IMG_L3 = IMG_L2 + band_off(5);
+constexpr int IMG_BYTES = IMG_L3 + band_off(5);
+static_assert(band_off(5) == 3 * 48 * 13 * 32, "band sizes");
+static_assert(NCOL * 32 <= SLOT_BYTES, "pieces fit a slot");
+
+// Piece p of a tile's weights: source offset and bytes. Pieces 0-2: layer
+// 1's ky taps; 3-7: layer 2's chunks; 8-12: layer 3's.
+__device__ __forceinline__ void weight_piece(int p, int &off, int &bytes)
+{
+    if (p < 3) {
+        off = IMG_L1 + p * NCOL * 32;
+        bytes = NCOL * 32;
+    } else {
+        const int ks = (p - 3) % 5;
+        off = (p < 8 ? IMG_L2 : IMG_L3) + band_off(ks);
+        bytes = 3 * 48 * band_q(ks) * 32;
+    }
+}
 
 __global__ void mn_build_images_kernel(const float *used, uint8_t *img)
 {
-    const int n1 = 9 * 80 * 16, n2 = 9 * 80 * 80;
+    const int n1 = 3 * NCOL * 16, n2 = 3 * 48 * 13 * 16;
     for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n1 + 2 * n2; idx += gridDim.x * blockDim.x) {
-        int layer, r = idx;
-        if (r < n1) layer = 0;
-        else if (r < n1 + n2) layer = 1, r -= n1;
-        else layer = 2, r -= n1 + n2;
-        const int K = layer == 0 ? 16 : 80, Ci = layer == 0 ? NCIN : NC;
-        const int k = r % K, n = (r / K) % 80, tap = r / (K * 80);   // tap = dz * 3 + dy
-        const int q = n >> 4, co = n & 15;
+        const int k = idx & 15;
         float v = 0.f;
-        if (k < 5 * Ci) {
-            const int qp = k / Ci, ci = k % Ci, dq = qp - q;
-            if (dq >= -1 && dq <= 1) {
-                const int woff = layer == 0 ? OFF_W1 : (layer == 1 ? OFF_W2 : OFF_W3);
-                v = used[woff + ((tap * 3 + dq + 1) * Ci + ci) * NC + co];
+        uint32_t off;
+        if (idx < n1) {
+            const int n = (idx >> 4) % NCOL, dy = (idx >> 4) / NCOL;
+            const int q = n / 48, dz = (n % 48) >> 4, co = n & 15;
+            if (k < 5 * NCIN) {
+                const int dq = k / NCIN - q, ci = k % NCIN;
+                if (dq >= -1 && dq <= 1) v = used[OFF_W1 + (((dz * 3 + dy) * 3 + dq + 1) * NCIN + ci) * NC + co];
             }
+            off = IMG_L1 + dy * NCOL * 32 + tpal::tc::elem_off(n, k, 2, 32);
+        } else {
+            const int r = idx - n1, layer = r < n2 ? 1 : 2, rr = (r % n2) >> 4;
+            int ks = 0;
+            while (rr >= band_off(ks + 1) / 32) ks++;
+            const int nb = 48 * band_q(ks), within = rr - band_off(ks) / 32, dy = within / nb, n = within % nb;
+            const int q = band_lo(ks) + n / 48, dz = (n % 48) >> 4, co = n & 15, dq = ks - q;   // |dq| <= 1
+            v = used[(layer == 1 ? OFF_W2 : OFF_W3) + (((dz * 3 + dy) * 3 + dq + 1) * NC + k) * NC + co];
+            off = (layer == 1 ? IMG_L2 : IMG_L3) + band_off(ks) + dy * nb * 32 + tpal::tc::elem_off(n, k, 2, 32);
         }
-        const int base = layer == 0 ? IMG_L1 : (layer == 1 ? IMG_L2 : IMG_L3);
-        *reinterpret_cast<__nv_bfloat16 *>(img + base + tap * 80 * 2 * K + tpal::tc::elem_off(n, k, 2, 2 * K)) =
-            __float2bfloat16_rn(v);
+        *reinterpret_cast<__nv_bfloat16 *>(img + off) = __float2bfloat16_rn(v);
     }
 }
 
 // One 16-byte chunk c of input row (ky, kz) of a layer whose rows hold KB
-// bytes, into the layer's three kz-rotated A copies: copy dz (kz tap dz - 1)
-// holds source kz in row (kz - dz + 1) mod 8 of group ky + 1; groups 0 and
-// 33 repeat ky = 31 and ky = 0 (the periodic halo).
-__device__ __forceinline__ void put_rotated(uint8_t *A, int KB, int ky, int kz, int c, uint4 v)
+// bytes: row kz of group ky + 1; groups 0 and 33 repeat ky = 31 and ky = 0
+// (the periodic halo).
+__device__ __forceinline__ void put_row(uint8_t *A, int KB, int ky, int kz, int c, uint4 v)
 {
     const int grp = 8 * KB;
-#pragma unroll
-    for (int dz = 0; dz < 3; dz++) {
-        uint8_t *base = A + dz * A_COPY + c * 128 + ((kz - dz + 1) & 7) * 16;
-        *reinterpret_cast<uint4 *>(base + (ky + 1) * grp) = v;
-        if (ky == 31) *reinterpret_cast<uint4 *>(base) = v;
-        if (ky == 0) *reinterpret_cast<uint4 *>(base + (kGroupsA - 1) * grp) = v;
-    }
+    uint8_t *base = A + c * 128 + kz * 16;
+    *reinterpret_cast<uint4 *>(base + (ky + 1) * grp) = v;
+    if (ky == 31) *reinterpret_cast<uint4 *>(base) = v;
+    if (ky == 0) *reinterpret_cast<uint4 *>(base + (kGroupsA - 1) * grp) = v;
 }
 
-// The MMAs of kz tap dz of a layer: A copy dz, weight slot `slot`.
-__device__ __forceinline__ void issue_tap(uint32_t tmem, const uint8_t *A, const uint8_t *B, int dz, int slot, int K,
-                                          bool first)
+// OR of a predicate over the epilogue's 256 threads (named barrier 1).
+__device__ __forceinline__ bool epi_or(bool v)
+{
+    uint32_t r;
+    asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.b32 q, %1, 0;\n\tbar.red.or.pred p, 1, %2, q;\n\t"
+                 "selp.b32 %0, 1, 0, p;\n\t}\n"
+                 : "=r"(r)
+                 : "r"((uint32_t)v), "r"(32 * kEpiWarps)
+                 : "memory");
+    return r != 0;
+}
+
+struct TcShared {
+    uint8_t *A, *slots, *stage;
+    uint64_t *bars;
+    volatile int *abort_flag;
+};
+
+// Descriptor arithmetic: the start address is bits 0-13 of a shared-memory
+// descriptor in 16-byte units, so moving an operand by a byte offset that
+// keeps it inside shared memory (below 256 KB) adds offset / 16.
+__device__ __forceinline__ uint64_t desc_at(uint64_t d, uint32_t bytes) { return d + (bytes >> 4); }
+
+// Layer 1, ky tap DY from its weight piece: K = 16, N = 240; tap 0 starts
+// each M block's sum.
+template <int DY>
+__device__ __forceinline__ void mma_layer1(uint32_t tmem, uint64_t a1, uint64_t bslot)
+{
+    constexpr uint32_t id = tpal::tc::idesc(1, 128, NCOL);
+#pragma unroll
+    for (int b = 0; b < 2; b++)
+        tpal::tc::mma<1>(tmem + b * 256, desc_at(a1, (b * 16 + DY) * 256), bslot, id, DY > 0 ? 1u : 0u);
+}
+
+// Layers 2 and 3, K chunk KS (input block q' = KS): three ky taps x two M
+// blocks into the band's 96 or 144 columns; every MMA accumulates.
+template <int KS>
+__device__ __forceinline__ void mma_band(uint32_t tmem, uint64_t a2, uint64_t bslot)
+{
+    constexpr int nb = 48 * band_q(KS);
+    constexpr uint32_t id = tpal::tc::idesc(1, 128, nb);
+    const uint32_t d = tmem + 48 * band_lo(KS);
+#pragma unroll
+    for (int dy = 0; dy < 3; dy++)
+#pragma unroll
+        for (int b = 0; b < 2; b++)
+            tpal::tc::mma<1>(d + b * 256, desc_at(a2, (b * 16 + dy) * 1280 + KS * 256), desc_at(bslot, dy * nb * 32),
+                             id, 1u);
+}
+
+// The MMA warp's thread: every tile's three layers, chunk by chunk.
+__device__ bool tc_mma_role(const TcShared &S, uint32_t tmem, long long first, long long step, long long ntiles)
 {
     using namespace tpal::tc;
-    const int KB = 2 * K, grp = 8 * KB;
-    const uint32_t id = idesc(1, 128, 80);
-    for (int dy = 0; dy < 3; dy++)
-        for (int b = 0; b < 2; b++)
-            for (int ks = 0; ks < K / 16; ks++) {
-                const uint32_t a = smem_addr(A + dz * A_COPY + (b * 16 + dy) * grp + ks * 256);
-                const uint32_t bb = smem_addr(B + slot * B_SLOT + dy * 80 * KB + ks * 256);
-                mma<1>(tmem + b * 128, sdesc(a, grp), sdesc(bb, grp), id, (!first || dy > 0 || ks > 0) ? 1u : 0u);
+    uint64_t *full = S.bars + B_FULL, *ready = S.bars + B_READY, *sfull = S.bars + B_SFULL,
+             *sfree = S.bars + B_SFREE;
+    // operand descriptors at the bases: A with 8-row groups 256 bytes apart
+    // (layer 1) or 1280 (layers 2 and 3), the weight slots 256
+    const uint64_t a1 = sdesc(smem_addr(S.A), 256), a2 = sdesc(smem_addr(S.A), 1280),
+                   b0 = sdesc(smem_addr(S.slots), 256);
+    uint32_t rbits = 0;   // parity of each ready barrier's next phase
+    long long sc = 0;     // weight pieces consumed
+    bool ok = true;
+    auto take_ready = [&](int q) {
+        if (!bar_wait(ready + q, (rbits >> q) & 1)) return false;
+        rbits ^= 1u << q;
+        return true;
+    };
+    // the next weight piece's slot, once its copy has landed (-1: the wait ran out)
+    auto take_slot = [&]() {
+        const int slot = (int)(sc % kSlots);
+        if (!bar_wait(sfull + slot, (uint32_t)((sc / kSlots) & 1))) return -1;
+        fence_after();
+        return slot;
+    };
+    for (long long tile = first; tile < ntiles && ok && !*S.abort_flag; tile += step) {
+        for (int L = 0; L < 3 && ok; L++) {
+            if (L == 0) {
+                // the tile's input is written and the previous tile's head has
+                // read the accumulator
+                ok = take_ready(0);
+                for (int dy = 0; dy < 3 && ok; dy++, sc++) {
+                    const int slot = take_slot();
+                    if (slot < 0) {
+                        ok = false;
+                        break;
+                    }
+                    const uint64_t bs = desc_at(b0, slot * SLOT_BYTES);
+                    if (dy == 0) mma_layer1<0>(tmem, a1, bs);
+                    else if (dy == 1) mma_layer1<1>(tmem, a1, bs);
+                    else mma_layer1<2>(tmem, a1, bs);
+                    mma_commit(sfree + slot);
+                }
+            } else {
+                for (int ks = 0; ks < 5 && ok; ks++, sc++) {
+                    ok = take_ready(ks);
+                    const int slot = ok ? take_slot() : -1;
+                    if (slot < 0) {
+                        ok = false;
+                        break;
+                    }
+                    const uint64_t bs = desc_at(b0, slot * SLOT_BYTES);
+                    switch (ks) {
+                    case 0: mma_band<0>(tmem, a2, bs); break;
+                    case 1: mma_band<1>(tmem, a2, bs); break;
+                    case 2: mma_band<2>(tmem, a2, bs); break;
+                    case 3: mma_band<3>(tmem, a2, bs); break;
+                    default: mma_band<4>(tmem, a2, bs); break;
+                    }
+                    mma_commit(sfree + slot);
+                }
             }
+            mma_commit(full);
+        }
+    }
+    if (!ok) *S.abort_flag = 1;
+    // every MMA issued has completed before the tensor memory is released
+    mma_commit(S.bars + B_DRAIN);
+    return bar_wait(S.bars + B_DRAIN, 0) && ok;
+}
+
+// The copy warp's thread: weight pieces through the ring, features of the
+// next tile into the other stage.
+__device__ bool tc_copy_role(const TcShared &S, const uint8_t *img, const uint16_t *feat, long long first,
+                             long long step, long long ntiles)
+{
+    using namespace tpal::tc;
+    uint64_t *sfull = S.bars + B_SFULL, *sfree = S.bars + B_SFREE, *ffull = S.bars + B_FFULL,
+             *ffree = S.bars + B_FFREE;
+    long long sc = 0;   // pieces issued
+    long long js = 0;   // tiles whose features were issued
+    bool ok = true;
+    auto stage_features = [&](long long tile) {
+        const int b = (int)(js & 1);
+        const long long use = js >> 1;   // earlier fills of this stage
+        if (use >= 1 && !bar_wait(ffree + b, (uint32_t)((use - 1) & 1))) return false;
+        bar_arrive_expect_tx(ffull + b, FEAT_BYTES);
+        bulk_g2s(S.stage + b * FEAT_BYTES, feat + tile * NV, FEAT_BYTES, ffull + b);
+        js++;
+        return true;
+    };
+    if (first < ntiles) ok = stage_features(first);
+    for (long long tile = first; tile < ntiles && ok && !*S.abort_flag; tile += step) {
+        if (tile + step < ntiles) ok = stage_features(tile + step);
+        for (int pc = 0; pc < kPieces && ok; pc++) {
+            const int slot = (int)(sc % kSlots);
+            const long long use = sc / kSlots;
+            if (use >= 1 && !bar_wait(sfree + slot, (uint32_t)((use - 1) & 1))) {
+                ok = false;
+                break;
+            }
+            int off, bytes;
+            weight_piece(pc, off, bytes);
+            bar_arrive_expect_tx(sfull + slot, (uint32_t)bytes);
+            bulk_g2s(S.slots + slot * SLOT_BYTES, img + off, (uint32_t)bytes, sfull + slot);
+            sc++;
+        }
+    }
+    if (!ok) *S.abort_flag = 1;
+    // no copy may still be writing shared memory when the CTA leaves: wait
+    // for the last fill of every slot and stage (already complete unless a
+    // wait ran out)
+    for (int slot = 0; slot < kSlots; slot++)
+        if (sc > slot && !bar_wait(sfull + slot, (uint32_t)(((sc - 1 - slot) / kSlots) & 1))) ok = false;
+    for (int b = 0; b < 2; b++)
+        if (js > b && !bar_wait(ffull + b, (uint32_t)(((js - 1 - b) >> 1) & 1))) ok = false;
+    return ok;
+}
+
+// The 48 accumulator columns of output block q (q * 48 + dz * 16 + co) of
+// the thread's lane: loads issued, not waited for.
+__device__ __forceinline__ void load_block(uint32_t tl, int q, uint32_t (&d)[48])
+{
+    uint32_t(&d0)[16] = *reinterpret_cast<uint32_t(*)[16]>(&d[0]);
+    uint32_t(&d1)[16] = *reinterpret_cast<uint32_t(*)[16]>(&d[16]);
+    uint32_t(&d2)[16] = *reinterpret_cast<uint32_t(*)[16]>(&d[32]);
+    tpal::tc::tmem_ld16_async(tl + q * 48, d0);
+    tpal::tc::tmem_ld16_async(tl + q * 48 + 16, d1);
+    tpal::tc::tmem_ld16_async(tl + q * 48 + 32, d2);
+}
+
+// The block's outputs: the three dz partial sums of each channel added with
+// the kz neighbours' (lanes of the same ky holding kz - 1 and kz + 1).
+__device__ __forceinline__ void combine_block(const uint32_t (&d)[48], int lane, float (&y)[16])
+{
+    const int lm = (lane & ~7) | ((lane - 1) & 7), lp = (lane & ~7) | ((lane + 1) & 7);
+#pragma unroll
+    for (int co = 0; co < 16; co++)
+        y[co] = __shfl_sync(0xffffffffu, __uint_as_float(d[co]), lm) + __uint_as_float(d[16 + co]) +
+                __shfl_sync(0xffffffffu, __uint_as_float(d[32 + co]), lp);
 }
 
 template <bool TRAIN>
@@ -568,71 +807,58 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 {
     using namespace tpal::tc;
     extern __shared__ __align__(1024) uint8_t smem[];
-    uint8_t *A = smem + SM_A;
-    uint8_t *B = smem + SM_B;
-    // one completion per layer each: tap 0's MMAs (waited by the issuing
-    // thread, to refill slot 0), all the layer's MMAs (waited by every
-    // thread); one per weight slot fill (issue and wait alternate)
-    uint64_t *bm0 = reinterpret_cast<uint64_t *>(smem + SM_BAR);
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + SM_BAR + 8);
-    uint64_t *bm1 = reinterpret_cast<uint64_t *>(smem + SM_BAR + 16);
-    uint64_t *bb0 = reinterpret_cast<uint64_t *>(smem + SM_BAR + 24);
-    uint64_t *bb1 = reinterpret_cast<uint64_t *>(smem + SM_BAR + 32);
+    TcShared S;
+    S.A = smem + SM_A;
+    S.slots = smem + SM_SLOT;
+    S.stage = smem + SM_FEAT;
+    S.bars = reinterpret_cast<uint64_t *>(smem + SM_BAR);
+    S.abort_flag = reinterpret_cast<volatile int *>(smem + SM_FLAG);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + SM_TSLOT);
     __shared__ float s_par[4 * NC + 1];   // b1, b2, b3, wh, bh
-    __shared__ float red[kTcThreads / 32];
+    __shared__ float red[2][kEpiWarps];
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     for (int i = t; i < 4 * NC + 1; i += kTcThreads) {
         const int off[5] = {OFF_B1, OFF_B2, OFF_B3, OFF_WH, OFF_BH};
         s_par[i] = params[off[i / NC] + i % NC];
     }
     if (t == 0) {
-        bar_init(bm0);
-        bar_init(bm1);
-        bar_init(bb0);
-        bar_init(bb1);
+        for (int i = 0; i < NBAR; i++) {
+            const bool per_warp = (i >= B_READY && i < B_READY + 5) || i == B_FFREE || i == B_FFREE + 1;
+            bar_init(S.bars + i, per_warp ? kEpiWarps : 1);
+        }
+        *S.abort_flag = 0;
     }
-    if (warp == 0) tmem_alloc(tslot, 256);
-    fence_async_smem();
+    if (warp == 0) tmem_alloc(tslot, 512);
     fence_before();
     __syncthreads();
     fence_after();
     const uint32_t tmem = *tslot;
-    // issuing thread's state: barrier parities and fills in flight
-    uint32_t pm0 = 0, pb0 = 0, pb1 = 0;
-    bool out0 = false, out1 = false;
-    uint32_t pm1 = 0;   // every thread
-    bool no_fill = false;   // take() argument for the MMA barrier
+    const long long first = blockIdx.x, step = gridDim.x;
     bool ok = true;
-    auto layer_img = [&](int L) { return img + (L == 0 ? IMG_L1 : (L == 1 ? IMG_L2 : IMG_L3)); };
-    auto fill = [&](uint64_t *bar, int slot, int L, int dz) {
-        const uint32_t bytes = 3 * 80 * 2 * (L == 0 ? 16 : 80);
-        bar_arrive_expect_tx(bar, bytes);
-        bulk_g2s(B + slot * B_SLOT, layer_img(L) + dz * bytes, bytes, bar);
-    };
-    // a bounded wait; the parity advances (and the fill is no longer in
-    // flight) only when the phase completed
-    auto take = [](uint64_t *bar, uint32_t &par, bool &in_flight) {
-        const bool done = bar_wait(bar, par);
-        if (done) {
-            par ^= 1;
-            in_flight = false;
-        }
-        return done;
-    };
-    // the first tile's first layer: taps 0 and 1
-    if (t == 0 && (long long)blockIdx.x < ntiles) {
-        fill(bb0, 0, 0, 0);
-        fill(bb1, 1, 0, 1);
-        out0 = out1 = true;
-    }
-    const int eb = warp >> 2;                             // the epilogue's M block
-    const int erow = eb * 128 + (warp & 3) * 32 + lane;   // its row: ky = erow >> 3, kz = erow & 7
-    const int eky = erow >> 3, ekz = erow & 7;
-    for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        // inputs: row t = (ky, kz), k = 2 q + c (c = 0: the bin, 1: its mirror), zero-padded to 16
-        {
+    if (warp == kEpiWarps) {
+        if (lane == 0) ok = tc_mma_role(S, tmem, first, step, ntiles);
+        __syncwarp();
+    } else if (warp == kEpiWarps + 1) {
+        if (lane == 0) ok = tc_copy_role(S, img, feat, first, step, ntiles);
+        __syncwarp();
+    } else {
+        uint64_t *full = S.bars + B_FULL, *ready = S.bars + B_READY, *ffull = S.bars + B_FFULL,
+                 *ffree = S.bars + B_FFREE;
+        const int eb = warp >> 2;                             // the epilogue's M block
+        const int erow = eb * 128 + (warp & 3) * 32 + lane;   // its row: ky = erow >> 3, kz = erow & 7
+        const int eky = erow >> 3, ekz = erow & 7;
+        const uint32_t tl = tmem + ((uint32_t)((warp & 3) * 32) << 16) + eb * 256;
+        uint32_t fbits = 0, pfull = 0;
+        long long js = 0;   // tiles whose input was written
+        bool bad = false;
+        // the input of a tile from its feature stage: row t = (ky, kz),
+        // k = 2 q + c (c = 0: the bin, 1: its mirror), zero-padded to 16
+        auto write_input = [&]() {
+            const int b = (int)(js & 1);
+            if (!bar_wait(ffull + b, (fbits >> b) & 1)) return false;
+            fbits ^= 1u << b;
+            const __nv_bfloat16 *f = reinterpret_cast<const __nv_bfloat16 *>(S.stage + b * FEAT_BYTES);
             const int ky = t >> 3, kz = t & 7;
-            const __nv_bfloat16 *f = reinterpret_cast<const __nv_bfloat16 *>(feat) + tile * NV;
             __align__(16) __nv_bfloat16 v[16];
 #pragma unroll
             for (int q = 0; q < NQ; q++) {
@@ -641,97 +867,133 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
 #pragma unroll
             for (int k = 10; k < 16; k++) v[k] = __float2bfloat16_rn(0.f);
-            put_rotated(A, 32, ky, kz, 0, reinterpret_cast<const uint4 *>(v)[0]);
-            put_rotated(A, 32, ky, kz, 1, reinterpret_cast<const uint4 *>(v)[1]);
+            put_row(S.A, 32, ky, kz, 0, reinterpret_cast<const uint4 *>(v)[0]);
+            put_row(S.A, 32, ky, kz, 1, reinterpret_cast<const uint4 *>(v)[1]);
+            fence_async_smem();
+            __syncwarp();
+            if (lane == 0) bar_arrive(ffree + b);
+            js++;
+            return true;
+        };
+        if (first < ntiles) {
+            bad = !write_input();
+            __syncwarp();
+            if (lane == 0) bar_arrive(ready + 0);
         }
-        fence_async_smem();
-        fence_before();
-        __syncthreads();
-        float conf = 0.f;
-        for (int L = 0; L < 3; L++) {
-            const int K = L == 0 ? 16 : 80;
-            bool bok = true;
-            if (t == 0) {
-                fence_after();
-                bok = take(bb0, pb0, out0);
-                if (bok) issue_tap(tmem, A, B, 0, 0, K, true);
-                mma_commit(bm0);
-                if (bok) bok = take(bb1, pb1, out1);
-                if (bok) issue_tap(tmem, A, B, 1, 1, K, false);
-                // slot 0 is free once tap 0's MMAs are done: tap 2's weights
-                bool free0 = false;
-                if (bok) bok = take(bm0, pm0, free0);
-                if (bok) {
-                    fill(bb0, 0, L, 2);
-                    out0 = true;
-                    bok = take(bb0, pb0, out0);
+        long long it = 0;
+        for (long long tile = first; tile < ntiles; tile += step, it++) {
+            float conf = 0.f;
+            for (int L = 0; L < 3 && !bad; L++) {
+                if (!bar_wait(full, pfull)) {
+                    bad = true;
+                    break;
                 }
-                if (bok) issue_tap(tmem, A, B, 2, 0, K, false);
-                mma_commit(bm1);
+                pfull ^= 1;
+                fence_after();
+                if (L < 2) {
+                    // block q's columns in one buffer while block q + 1's
+                    // loads land in the other
+                    auto block = [&](int q, uint32_t(&cur)[48], uint32_t(&nxt)[48]) {
+                        tmem_wait_ld(cur);
+                        // cleared for the next layer, whose MMAs all accumulate
+                        tmem_zero16(tl + q * 48);
+                        tmem_zero16(tl + q * 48 + 16);
+                        tmem_zero16(tl + q * 48 + 32);
+                        if (q + 1 < NQ) load_block(tl, q + 1, nxt);
+                        float y[16];
+                        combine_block(cur, lane, y);
+                        __align__(16) __nv_bfloat16 o[16];
+#pragma unroll
+                        for (int co = 0; co < NC; co++)
+                            o[co] = __float2bfloat16_rn(fmaxf(y[co] + s_par[L * NC + co], 0.f));
+                        put_row(S.A, 160, eky, ekz, 2 * q, reinterpret_cast<const uint4 *>(o)[0]);
+                        put_row(S.A, 160, eky, ekz, 2 * q + 1, reinterpret_cast<const uint4 *>(o)[1]);
+                        if (TRAIN) {
+                            __nv_bfloat16 *ag = (L == 0 ? a1g : a2g) + tile * NC * NV;
+                            const int vox = (q * 8 + ekz) * 32 + eky;
+#pragma unroll
+                            for (int co = 0; co < NC; co++) ag[co * NV + vox] = o[co];
+                        }
+                        // input chunk q is written and blocks 0..q are read and
+                        // zeroed: chunk q - 1 of the next layer may run (all of
+                        // them after the last block)
+                        fence_async_smem();
+                        tmem_wait_st();
+                        fence_before();
+                        __syncwarp();
+                        if (lane == 0) {
+                            if (q > 0) bar_arrive(ready + q - 1);
+                            if (q == NQ - 1) bar_arrive(ready + q);
+                        }
+                    };
+                    uint32_t ba[48], bb[48];
+                    load_block(tl, 0, ba);
+                    block(0, ba, bb);
+                    block(1, bb, ba);
+                    block(2, ba, bb);
+                    block(3, bb, ba);
+                    block(4, ba, bb);
+                } else {
+                    // the next tile's input (this layer's MMAs are done with A)
+                    const bool more = tile + step < ntiles;
+                    if (more && !write_input()) {
+                        bad = true;
+                        break;
+                    }
+                    const float zh0 = s_par[4 * NC];
+                    auto block = [&](int q, uint32_t(&cur)[48], uint32_t(&nxt)[48]) {
+                        tmem_wait_ld(cur);
+                        if (q + 1 < NQ) load_block(tl, q + 1, nxt);
+                        float y[16];
+                        combine_block(cur, lane, y);
+                        const int vox = (q * 8 + ekz) * 32 + eky;
+                        float zh = zh0;
+#pragma unroll
+                        for (int co = 0; co < NC; co++) {
+                            const float a = bfr(fmaxf(y[co] + s_par[2 * NC + co], 0.f));
+                            if (TRAIN) a3g[tile * NC * NV + co * NV + vox] = __float2bfloat16_rn(a);
+                            zh = __fmaf_rn(a, s_par[3 * NC + co], zh);
+                        }
+                        const float p = 1.0f / (1.0f + expf(-zh));
+                        p_out[tile * NV + vox] = p;
+                        conf += fabsf(p - 0.5f);
+                    };
+                    uint32_t ba[48], bb[48];
+                    load_block(tl, 0, ba);
+                    block(0, ba, bb);
+                    block(1, bb, ba);
+                    block(2, ba, bb);
+                    block(3, bb, ba);
+                    block(4, ba, bb);
+                    // the accumulator is read: the next tile's first layer may run
+                    fence_before();
+                    __syncwarp();
+                    if (more && lane == 0) bar_arrive(ready + 0);
+                }
             }
-            const bool done = take(bm1, pm1, no_fill);
-            if (__syncthreads_or(!done || !bok)) {
-                ok = false;
+            // the tile's confidence; a failure anywhere stops every epilogue warp here
+#pragma unroll
+            for (int h = 16; h >= 1; h >>= 1) conf += __shfl_xor_sync(0xffffffffu, conf, h);
+            if (lane == 0) red[it & 1][warp] = conf;
+            if (epi_or(bad || *S.abort_flag != 0)) {
+                bad = true;
                 break;
             }
-            fence_after();
-            // every MMA of this layer is done: both slots take the next layer's
-            // (or the next tile's first layer's) first two taps
-            if (t == 0 && (L < 2 || tile + gridDim.x < ntiles)) {
-                const int nl = L < 2 ? L + 1 : 0;
-                fill(bb0, 0, nl, 0);
-                fill(bb1, 1, nl, 1);
-                out0 = out1 = true;
+            if (t == 0 && fallback != nullptr) {
+                float sum = 0.f;
+#pragma unroll
+                for (int w = 0; w < kEpiWarps; w++) sum += red[it & 1][w];
+                fallback[tile] = (sum * (1.0f / NV) < conf_limit) ? 1 : 0;
             }
-            // epilogue: the warp's 32 rows of its M block, 80 columns (q, co)
-            const uint32_t tb = tmem + ((uint32_t)((warp & 3) * 32) << 16) + eb * 128;
-#pragma unroll 1
-            for (int q = 0; q < NQ; q++) {
-                float v[16];
-                tmem_ld16(tb + 16 * q, v);
-                const int vox = (q * 8 + ekz) * 32 + eky;
-                if (L < 2) {
-                    __align__(16) __nv_bfloat16 o[16];
-#pragma unroll
-                    for (int co = 0; co < NC; co++) o[co] = __float2bfloat16_rn(fmaxf(v[co] + s_par[L * NC + co], 0.f));
-                    put_rotated(A, 160, eky, ekz, 2 * q, reinterpret_cast<const uint4 *>(o)[0]);
-                    put_rotated(A, 160, eky, ekz, 2 * q + 1, reinterpret_cast<const uint4 *>(o)[1]);
-                    if (TRAIN) {
-                        __nv_bfloat16 *ag = (L == 0 ? a1g : a2g) + tile * NC * NV;
-#pragma unroll
-                        for (int co = 0; co < NC; co++) ag[co * NV + vox] = o[co];
-                    }
-                } else {
-                    float zh = s_par[4 * NC];
-#pragma unroll
-                    for (int co = 0; co < NC; co++) {
-                        const float a = bfr(fmaxf(v[co] + s_par[2 * NC + co], 0.f));
-                        if (TRAIN) a3g[tile * NC * NV + co * NV + vox] = __float2bfloat16_rn(a);
-                        zh = __fmaf_rn(a, s_par[3 * NC + co], zh);
-                    }
-                    const float p = 1.0f / (1.0f + expf(-zh));
-                    p_out[tile * NV + vox] = p;
-                    conf += fabsf(p - 0.5f);
-                }
-            }
-            fence_async_smem();
-            fence_before();
-            __syncthreads();
         }
-        if (!ok) break;
-        const float s = block_sum(conf, red);
-        if (t == 0 && fallback != nullptr) fallback[tile] = (s * (1.0f / NV) < conf_limit) ? 1 : 0;
-    }
-    // no copy may still be writing this CTA's shared memory when it leaves
-    if (t == 0) {
-        if (out0 && !bar_wait(bb0, pb0)) ok = false;
-        if (out1 && !bar_wait(bb1, pb1)) ok = false;
+        if (bad) *S.abort_flag = 1;
+        ok = !bad;
     }
     fence_before();
     __syncthreads();
     fence_after();
-    if (warp == 0) tmem_dealloc(tmem, 256);
-    if (!ok && t == 0) atomicExch(err, 1);
+    if (warp == 0) tmem_dealloc(tmem, 512);
+    if (!ok) atomicExch(err, 1);
 }
 
 }  // namespace mn
@@ -832,6 +1094,8 @@ int MaskNet::forward(const uint16_t *d_feat, long long ntiles, float *d_p, uint8
 {
     if (ntiles <= 0) return 0;
     if (d_feat == nullptr || d_p == nullptr) return mn_fail("forward: null buffer");
+    if (tc_ && reinterpret_cast<uintptr_t>(d_feat) % 16 != 0)
+        return mn_fail("forward: the feature buffer must be 16-byte aligned");
     const unsigned blocks = (unsigned)std::min<long long>(ntiles, (long long)grid_ * 1);
     if (tc_)
         mn::mn_tc_forward_kernel<false><<<blocks, mn::kTcThreads, mn::kTcSmem, s>>>(
@@ -868,6 +1132,8 @@ int MaskNet::train_step(const uint16_t *d_feat, const float2 *d_ac, long long nt
                         float *host_grad, cudaStream_t s)
 {
     if (ntiles <= 0 || d_feat == nullptr || d_ac == nullptr) return mn_fail("train_step: empty batch or null buffer");
+    if (tc_ && reinterpret_cast<uintptr_t>(d_feat) % 16 != 0)
+        return mn_fail("train_step: the feature buffer must be 16-byte aligned");
     if (const int rc = ensure_batch(ntiles); rc != 0) return rc;
     const unsigned blocks = (unsigned)std::min<long long>(ntiles, grid_);
     cudaMemsetAsync(scal_, 0, 2 * sizeof(double), s);
@@ -926,7 +1192,6 @@ MaskNet *masknet_of(chdg_masknet *n) { return &n->net; }
 
 #pragma GCC visibility push(default)
 extern "C" {
-
 int chdg_masknet_create(chdg_masknet **out)
 {
     if (out == nullptr) return chdg::mn_fail("create: null argument");

@@ -61,10 +61,17 @@ __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::be
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-__device__ __forceinline__ void bar_init(uint64_t *bar)
+// A barrier whose phase completes after `count` arrivals (and the expected
+// transaction bytes).
+__device__ __forceinline__ void bar_init(uint64_t *bar, uint32_t count = 1)
 {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void bar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
 // Wait for the barrier's phase `parity` to complete; false if the limit ran out.
@@ -139,6 +146,40 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
                  "l"(src), "r"(bytes), "r"(smem_addr(bar))
                  : "memory");
 }
+
+// 16 consecutive 32-bit columns of this thread's lane into r, without
+// waiting: the registers are valid after tmem_wait_ld.
+__device__ __forceinline__ void tmem_ld16_async(uint32_t taddr, uint32_t (&r)[16])
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+                 "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                   "=r"(r[15])
+                 : "r"(taddr));
+}
+
+// Wait for this thread's tensor-memory loads. The "+r" operands tie the
+// registers being loaded to the wait, so no use of them moves above it.
+template <int N>
+__device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[N])
+{
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < N; j++) asm volatile("" : "+r"(r[j]));
+}
+
+// Zero 16 consecutive 32-bit columns of this thread's lane (no wait: the
+// caller issues tmem_wait_st before the columns are used).
+__device__ __forceinline__ void tmem_zero16(uint32_t taddr)
+{
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+                 "{%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1};" ::"r"(taddr),
+                 "r"(0u)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // 8 consecutive 32-bit columns of this thread's lane, then wait for the load
 __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8])
