@@ -488,23 +488,28 @@ __global__ void mn_round_kernel(const float *master, float *used)
 // the MMAs of one K chunk (input q', its 16 channels) write only the 96 or
 // 144 columns of the outputs q = q' - 1 .. q' + 1 (N is ordered q, dz, co).
 // Layer 1 (K = 16: the five q' of the two input channels, zero-padded) takes
-// the full N = 240. One layer's MMAs read 30 A tiles (2 M blocks x 3 ky taps
-// x 5 chunks) instead of 90 with the kz taps in the operand.
+// the full N = 240. Each M block has its own 240 accumulator columns.
+//
+// Schedule: the M blocks take turns. A layer's block-0 MMAs, then its block-1
+// MMAs, which run while the epilogue empties block 0; block 1's epilogue then
+// runs while the next layer's block-0 MMAs go, chunk by chunk as it releases
+// them. Block 0's epilogue writes the next layer's input while block 1's MMAs
+// still read this layer's: the two row groups both touch (ky = 15, and the
+// halo copy of ky = 0) go to a stash that block 1's epilogue moves into place.
 //
 // Roles (one CTA per SM, persistent over tiles):
-//  * warps 0-7, the epilogue: warp w reads tensor-memory lanes 32 (w & 3) ..
-//    of M block w >> 2. A layer's epilogue goes through the output blocks
-//    q = 0..4: it reads the block's 48 accumulator columns, zeroes them for
-//    the next layer (whose MMAs all accumulate), adds the dz partial sums,
-//    the bias and ReLU, rounds to bf16 and writes K chunk q of the next
-//    layer's input. The next layer's chunk q' MMAs write the columns of
-//    blocks q' - 1 .. q' + 1, so chunk q' is released once block q' + 1 is
-//    read. The last layer's epilogue writes the next tile's input, runs the
-//    sigmoid head and then releases the tensor memory to the next tile.
-//  * warp 8, one thread: issues each chunk's MMAs as it is released.
+//  * warps 0-7, the epilogue, all on one M block at a time: warp w reads
+//    tensor-memory lanes 32 (w & 3) .. and the channel half w >> 2 of each
+//    output. Per output block q = 0..4 of a layer: read its columns, zero them
+//    for the next layer (whose banded MMAs all accumulate), add the dz partial
+//    sums, the bias and ReLU, round to bf16 and write K chunk q of the next
+//    layer's input; block 1's step q releases the next layer's chunk q. The
+//    last layer: warps 0-3 run the sigmoid head over all 16 channels, warps
+//    4-7 write the next tile's input (during block 1).
+//  * warp 8, one thread: issues the MMAs.
 //  * warp 9, one thread: the TMA bulk copies -- the weight pieces of each
-//    tile, in MMA order, through a ring of slots, and each next tile's
-//    features into one of two stages.
+//    tile (each used by both M blocks) through a ring of slots, and each next
+//    tile's features into one of two stages.
 // All waits are bounded; a wait that runs out raises the error flag and the
 // CTA leaves after its copies and MMAs in flight have completed.
 constexpr int kEpiWarps = 8;
@@ -512,26 +517,38 @@ constexpr int kTcThreads = 32 * (kEpiWarps + 2);
 constexpr int kGroupsA = 34;                       // 32 ky groups + one halo group on each side
 constexpr int A_BYTES = kGroupsA * 8 * 160;        // a layer's input, K up to 80
 constexpr int NCOL = 3 * 80;                       // accumulator columns of one M block: (q, dz, co)
-constexpr int kSlots = 8;                          // weight-piece ring
+constexpr int kSlots = 8;                          // weight-piece ring (a layer's 5 pieces stay for both blocks)
 constexpr int SLOT_BYTES = 3 * 144 * 32;           // the largest piece: three ky taps x 144 rows x K 16
 constexpr int FEAT_BYTES = NV * 2;
-constexpr int kPieces = 13;                        // weight pieces of one tile
-// shared memory: [34 groups][8 rows][K] canonical, the ring, two feature
-// stages, the barriers
+constexpr int kPieces = 10;                        // streamed weight pieces of one tile (layers 2 and 3)
+constexpr int W1_BYTES = 3 * NCOL * 32;            // layer 1's weights, resident
+constexpr int STASH_BYTES = 2 * 8 * 160;           // row groups 16 and 33 of the next layer's input
+constexpr int IN_BYTES = kGroupsA * 8 * 32;        // layer 1's input, K = 16
+// shared memory: layers 2 and 3's input [34 groups][8 rows][K 80] and layer
+// 1's [34][8][K 16], both canonical (apart, so a tile's input can be written
+// while the previous layers' operands are read), the ring, two feature
+// stages, the stash, the barriers
 constexpr int SM_A = 0;
-constexpr int SM_SLOT = A_BYTES;
+constexpr int SM_IN = A_BYTES;
+constexpr int SM_W1 = SM_IN + IN_BYTES;
+constexpr int SM_SLOT = SM_W1 + W1_BYTES;
 constexpr int SM_FEAT = SM_SLOT + kSlots * SLOT_BYTES;
-constexpr int SM_BAR = SM_FEAT + 2 * FEAT_BYTES;
-// barriers: a layer's MMAs done; K chunk q of the next input released (5);
-// slot full (kSlots); slot free (kSlots); feature stage full (2) and free
-// (2); the final drain of the MMAs
-constexpr int B_FULL = 0, B_READY = 1, B_SFULL = B_READY + 5, B_SFREE = B_SFULL + kSlots, B_FFULL = B_SFREE + kSlots,
-              B_FFREE = B_FFULL + 2, B_DRAIN = B_FFREE + 2, NBAR = B_DRAIN + 1;
+constexpr int SM_STASH = SM_FEAT + 2 * FEAT_BYTES;
+constexpr int SM_BAR = SM_STASH + STASH_BYTES;
+// barriers: an M block's MMAs of a layer done (2); a release of the MMAs (5:
+// chunk q of the next layer's input written, and for layer 1 the input (0)
+// and block 1's columns read (1)); slot full (kSlots); slot free (kSlots);
+// feature stage full (2) and free (2); the final drain of the MMAs; layer
+// 1's weights landed
+constexpr int B_FULL = 0, B_READY = 2, B_SFULL = B_READY + 5, B_SFREE = B_SFULL + kSlots, B_FFULL = B_SFREE + kSlots,
+              B_FFREE = B_FFULL + 2, B_DRAIN = B_FFREE + 2, B_W1 = B_DRAIN + 1, NBAR = B_W1 + 1;
 constexpr int SM_TSLOT = SM_BAR + 8 * NBAR;
 constexpr int SM_FLAG = SM_TSLOT + 4;
 constexpr int kTcSmem = SM_FLAG + 12;
 static_assert(kTcSmem + 1024 <= 227 * 1024, "shared memory of one CTA");
-static_assert(SM_SLOT % 16 == 0 && SLOT_BYTES % 16 == 0 && SM_FEAT % 16 == 0 && SM_BAR % 8 == 0, "copy alignment");
+static_assert(SM_IN % 16 == 0 && SM_W1 % 16 == 0 && SM_SLOT % 16 == 0 && SLOT_BYTES % 16 == 0 && SM_FEAT % 16 == 0 && SM_STASH % 16 == 0 &&
+                  SM_BAR % 8 == 0,
+              "copy alignment");
 
 // the band of output blocks of input block (K chunk) ks in layers 2 and 3
 __host__ __device__ constexpr int band_lo(int ks) { return ks > 0 ? ks - 1 : 0; }
@@ -553,18 +570,14 @@ constexpr int IMG_BYTES = IMG_L3 + band_off(5);
 static_assert(band_off(5) == 3 * 48 * 13 * 32, "band sizes");
 static_assert(NCOL * 32 <= SLOT_BYTES, "pieces fit a slot");
 
-// Piece p of a tile's weights: source offset and bytes. Pieces 0-2: layer
-// 1's ky taps; 3-7: layer 2's chunks; 8-12: layer 3's.
+// Streamed piece p of a tile's weights: source offset and bytes. Pieces
+// 0-4: layer 2's chunks; 5-9: layer 3's. Layer 1's weights stay in shared
+// memory.
 __device__ __forceinline__ void weight_piece(int p, int &off, int &bytes)
 {
-    if (p < 3) {
-        off = IMG_L1 + p * NCOL * 32;
-        bytes = NCOL * 32;
-    } else {
-        const int ks = (p - 3) % 5;
-        off = (p < 8 ? IMG_L2 : IMG_L3) + band_off(ks);
-        bytes = 3 * 48 * band_q(ks) * 32;
-    }
+    const int ks = p % 5;
+    off = (p < 5 ? IMG_L2 : IMG_L3) + band_off(ks);
+    bytes = 3 * 48 * band_q(ks) * 32;
 }
 
 __global__ void mn_build_images_kernel(const float *used, uint8_t *img)
@@ -620,7 +633,7 @@ __device__ __forceinline__ bool epi_or(bool v)
 }
 
 struct TcShared {
-    uint8_t *A, *slots, *stage;
+    uint8_t *A, *in, *w1, *slots, *stage;
     uint64_t *bars;
     volatile int *abort_flag;
 };
@@ -630,96 +643,109 @@ struct TcShared {
 // keeps it inside shared memory (below 256 KB) adds offset / 16.
 __device__ __forceinline__ uint64_t desc_at(uint64_t d, uint32_t bytes) { return d + (bytes >> 4); }
 
-// Layer 1, ky tap DY from its weight piece: K = 16, N = 240; tap 0 starts
-// each M block's sum.
+// Layer 1, ky tap DY of one M block from its weight piece: K = 16, N = 240;
+// tap 0 starts the block's sum. ab: A at the block's first row group.
 template <int DY>
-__device__ __forceinline__ void mma_layer1(uint32_t tmem, uint64_t a1, uint64_t bslot)
+__device__ __forceinline__ void mma_layer1(uint32_t d, uint64_t ab, uint64_t bslot)
 {
-    constexpr uint32_t id = tpal::tc::idesc(1, 128, NCOL);
-#pragma unroll
-    for (int b = 0; b < 2; b++)
-        tpal::tc::mma<1>(tmem + b * 256, desc_at(a1, (b * 16 + DY) * 256), bslot, id, DY > 0 ? 1u : 0u);
+    tpal::tc::mma<1>(d, desc_at(ab, DY * 256), bslot, tpal::tc::idesc(1, 128, NCOL), DY > 0 ? 1u : 0u);
 }
 
-// Layers 2 and 3, K chunk KS (input block q' = KS): three ky taps x two M
-// blocks into the band's 96 or 144 columns; every MMA accumulates.
+// Layers 2 and 3, K chunk KS (input block q' = KS) of one M block: three ky
+// taps into the band's 96 or 144 columns; every MMA accumulates.
 template <int KS>
-__device__ __forceinline__ void mma_band(uint32_t tmem, uint64_t a2, uint64_t bslot)
+__device__ __forceinline__ void mma_band(uint32_t d, uint64_t ab, uint64_t bslot)
 {
     constexpr int nb = 48 * band_q(KS);
     constexpr uint32_t id = tpal::tc::idesc(1, 128, nb);
-    const uint32_t d = tmem + 48 * band_lo(KS);
 #pragma unroll
     for (int dy = 0; dy < 3; dy++)
-#pragma unroll
-        for (int b = 0; b < 2; b++)
-            tpal::tc::mma<1>(d + b * 256, desc_at(a2, (b * 16 + dy) * 1280 + KS * 256), desc_at(bslot, dy * nb * 32),
-                             id, 1u);
+        tpal::tc::mma<1>(d + 48 * band_lo(KS), desc_at(ab, dy * 1280 + KS * 256), desc_at(bslot, dy * nb * 32), id,
+                         1u);
 }
 
-// The MMA warp's thread: every tile's three layers, chunk by chunk.
+__device__ __forceinline__ void mma_band_any(int ks, uint32_t d, uint64_t ab, uint64_t bslot)
+{
+    switch (ks) {
+    case 0: mma_band<0>(d, ab, bslot); break;
+    case 1: mma_band<1>(d, ab, bslot); break;
+    case 2: mma_band<2>(d, ab, bslot); break;
+    case 3: mma_band<3>(d, ab, bslot); break;
+    default: mma_band<4>(d, ab, bslot); break;
+    }
+}
+
+// The MMA warp's thread. Per tile and layer: block 0's MMAs (each chunk once
+// released), then block 1's with the same weight pieces, whose slots are then
+// freed.
 __device__ bool tc_mma_role(const TcShared &S, uint32_t tmem, long long first, long long step, long long ntiles)
 {
     using namespace tpal::tc;
     uint64_t *full = S.bars + B_FULL, *ready = S.bars + B_READY, *sfull = S.bars + B_SFULL,
              *sfree = S.bars + B_SFREE;
     // operand descriptors at the bases: A with 8-row groups 256 bytes apart
-    // (layer 1) or 1280 (layers 2 and 3), the weight slots 256
-    const uint64_t a1 = sdesc(smem_addr(S.A), 256), a2 = sdesc(smem_addr(S.A), 1280),
+    // (layer 1) or 1280 (layers 2 and 3), the weight slots 256; block 1's A
+    // starts 16 row groups in
+    const uint64_t a1 = sdesc(smem_addr(S.in), 256), a2 = sdesc(smem_addr(S.A), 1280),
                    b0 = sdesc(smem_addr(S.slots), 256);
-    uint32_t rbits = 0;   // parity of each ready barrier's next phase
-    long long sc = 0;     // weight pieces consumed
+    const uint64_t a1b[2] = {a1, desc_at(a1, 16 * 256)}, a2b[2] = {a2, desc_at(a2, 16 * 1280)};
+    uint32_t rbits = 0;   // parity of each release barrier's next phase
+    long long sc = 0;     // weight pieces taken
     bool ok = true;
     auto take_ready = [&](int q) {
         if (!bar_wait(ready + q, (rbits >> q) & 1)) return false;
         rbits ^= 1u << q;
+        fence_after();
         return true;
     };
-    // the next weight piece's slot, once its copy has landed (-1: the wait ran out)
-    auto take_slot = [&]() {
-        const int slot = (int)(sc % kSlots);
-        if (!bar_wait(sfull + slot, (uint32_t)((sc / kSlots) & 1))) return -1;
+    // the weight piece p's slot, once its copy has landed
+    auto take_slot = [&](long long p) {
+        if (!bar_wait(sfull + (int)(p % kSlots), (uint32_t)((p / kSlots) & 1))) return false;
         fence_after();
-        return slot;
+        return true;
     };
+    auto slot_desc = [&](long long p) { return desc_at(b0, (int)(p % kSlots) * SLOT_BYTES); };
+    // layer 1's weights, copied once
+    const uint64_t w1 = sdesc(smem_addr(S.w1), 256);
+    if (ntiles > first) {
+        ok = bar_wait(S.bars + B_W1, 0);
+        fence_after();
+    }
     for (long long tile = first; tile < ntiles && ok && !*S.abort_flag; tile += step) {
-        for (int L = 0; L < 3 && ok; L++) {
-            if (L == 0) {
-                // the tile's input is written and the previous tile's head has
-                // read the accumulator
-                ok = take_ready(0);
-                for (int dy = 0; dy < 3 && ok; dy++, sc++) {
-                    const int slot = take_slot();
-                    if (slot < 0) {
-                        ok = false;
-                        break;
-                    }
-                    const uint64_t bs = desc_at(b0, slot * SLOT_BYTES);
-                    if (dy == 0) mma_layer1<0>(tmem, a1, bs);
-                    else if (dy == 1) mma_layer1<1>(tmem, a1, bs);
-                    else mma_layer1<2>(tmem, a1, bs);
-                    mma_commit(sfree + slot);
-                }
-            } else {
-                for (int ks = 0; ks < 5 && ok; ks++, sc++) {
-                    ok = take_ready(ks);
-                    const int slot = ok ? take_slot() : -1;
-                    if (slot < 0) {
-                        ok = false;
-                        break;
-                    }
-                    const uint64_t bs = desc_at(b0, slot * SLOT_BYTES);
-                    switch (ks) {
-                    case 0: mma_band<0>(tmem, a2, bs); break;
-                    case 1: mma_band<1>(tmem, a2, bs); break;
-                    case 2: mma_band<2>(tmem, a2, bs); break;
-                    case 3: mma_band<3>(tmem, a2, bs); break;
-                    default: mma_band<4>(tmem, a2, bs); break;
-                    }
-                    mma_commit(sfree + slot);
+        // layer 1: block 0 once the tile's input is written and the previous
+        // tile's head has read block 0's columns, block 1 once it has read
+        // block 1's
+        ok = take_ready(0);
+        if (ok) {
+            mma_layer1<0>(tmem, a1b[0], w1);
+            mma_layer1<1>(tmem, a1b[0], desc_at(w1, NCOL * 32));
+            mma_layer1<2>(tmem, a1b[0], desc_at(w1, 2 * NCOL * 32));
+        }
+        mma_commit(full + 0);
+        if (ok) ok = take_ready(1);
+        if (ok) {
+            mma_layer1<0>(tmem + 256, a1b[1], w1);
+            mma_layer1<1>(tmem + 256, a1b[1], desc_at(w1, NCOL * 32));
+            mma_layer1<2>(tmem + 256, a1b[1], desc_at(w1, 2 * NCOL * 32));
+        }
+        mma_commit(full + 1);
+        // layers 2 and 3: block 0's chunk ks once block 1's epilogue of the
+        // previous layer released it; block 1's chunks need nothing more
+        for (int L = 1; L < 3 && ok; L++) {
+            const long long p = sc;
+            for (int ks = 0; ks < 5 && ok; ks++) {
+                ok = take_ready(ks) && take_slot(p + ks);
+                if (ok) mma_band_any(ks, tmem, a2b[0], slot_desc(p + ks));
+            }
+            mma_commit(full + 0);
+            if (ok) {
+                for (int ks = 0; ks < 5; ks++) {
+                    mma_band_any(ks, tmem + 256, a2b[1], slot_desc(p + ks));
+                    mma_commit(sfree + (int)((p + ks) % kSlots));
                 }
             }
-            mma_commit(full);
+            mma_commit(full + 1);
+            sc += 5;
         }
     }
     if (!ok) *S.abort_flag = 1;
@@ -748,7 +774,11 @@ __device__ bool tc_copy_role(const TcShared &S, const uint8_t *img, const uint16
         js++;
         return true;
     };
-    if (first < ntiles) ok = stage_features(first);
+    if (first < ntiles) {
+        bar_arrive_expect_tx(S.bars + B_W1, W1_BYTES);
+        bulk_g2s(S.w1, img + IMG_L1, W1_BYTES, S.bars + B_W1);
+        ok = stage_features(first);
+    }
     for (long long tile = first; tile < ntiles && ok && !*S.abort_flag; tile += step) {
         if (tile + step < ntiles) ok = stage_features(tile + step);
         for (int pc = 0; pc < kPieces && ok; pc++) {
@@ -773,11 +803,32 @@ __device__ bool tc_copy_role(const TcShared &S, const uint8_t *img, const uint16
         if (sc > slot && !bar_wait(sfull + slot, (uint32_t)(((sc - 1 - slot) / kSlots) & 1))) ok = false;
     for (int b = 0; b < 2; b++)
         if (js > b && !bar_wait(ffull + b, (uint32_t)(((js - 1 - b) >> 1) & 1))) ok = false;
+    if (first < ntiles && !bar_wait(S.bars + B_W1, 0)) ok = false;
     return ok;
 }
 
-// The 48 accumulator columns of output block q (q * 48 + dz * 16 + co) of
-// the thread's lane: loads issued, not waited for.
+// The 24 accumulator columns of output block q and channel half h of the
+// thread's lane (q * 48 + dz * 16 + 8 h + c; tl already holds 8 h): loads
+// issued, not waited for.
+__device__ __forceinline__ void load_half(uint32_t tl, int q, uint32_t (&d)[24])
+{
+    tpal::tc::tmem_ld8_async(tl + q * 48, &d[0]);
+    tpal::tc::tmem_ld8_async(tl + q * 48 + 16, &d[8]);
+    tpal::tc::tmem_ld8_async(tl + q * 48 + 32, &d[16]);
+}
+
+// The half block's outputs: the three dz partial sums of each channel added
+// with the kz neighbours' (lanes of the same ky holding kz - 1 and kz + 1).
+__device__ __forceinline__ void combine_half(const uint32_t (&d)[24], int lane, float (&y)[8])
+{
+    const int lm = (lane & ~7) | ((lane - 1) & 7), lp = (lane & ~7) | ((lane + 1) & 7);
+#pragma unroll
+    for (int c = 0; c < 8; c++)
+        y[c] = __shfl_sync(0xffffffffu, __uint_as_float(d[c]), lm) + __uint_as_float(d[8 + c]) +
+               __shfl_sync(0xffffffffu, __uint_as_float(d[16 + c]), lp);
+}
+
+// The 48 columns of output block q, all 16 channels (the head).
 __device__ __forceinline__ void load_block(uint32_t tl, int q, uint32_t (&d)[48])
 {
     uint32_t(&d0)[16] = *reinterpret_cast<uint32_t(*)[16]>(&d[0]);
@@ -788,8 +839,6 @@ __device__ __forceinline__ void load_block(uint32_t tl, int q, uint32_t (&d)[48]
     tpal::tc::tmem_ld16_async(tl + q * 48 + 32, d2);
 }
 
-// The block's outputs: the three dz partial sums of each channel added with
-// the kz neighbours' (lanes of the same ky holding kz - 1 and kz + 1).
 __device__ __forceinline__ void combine_block(const uint32_t (&d)[48], int lane, float (&y)[16])
 {
     const int lm = (lane & ~7) | ((lane - 1) & 7), lp = (lane & ~7) | ((lane + 1) & 7);
@@ -809,10 +858,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     extern __shared__ __align__(1024) uint8_t smem[];
     TcShared S;
     S.A = smem + SM_A;
+    S.in = smem + SM_IN;
+    S.w1 = smem + SM_W1;
     S.slots = smem + SM_SLOT;
     S.stage = smem + SM_FEAT;
     S.bars = reinterpret_cast<uint64_t *>(smem + SM_BAR);
     S.abort_flag = reinterpret_cast<volatile int *>(smem + SM_FLAG);
+    uint8_t *stash = smem + SM_STASH;
     uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + SM_TSLOT);
     __shared__ float s_par[4 * NC + 1];   // b1, b2, b3, wh, bh
     __shared__ float red[2][kEpiWarps];
@@ -844,136 +896,192 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     } else {
         uint64_t *full = S.bars + B_FULL, *ready = S.bars + B_READY, *ffull = S.bars + B_FFULL,
                  *ffree = S.bars + B_FFREE;
-        const int eb = warp >> 2;                             // the epilogue's M block
-        const int erow = eb * 128 + (warp & 3) * 32 + lane;   // its row: ky = erow >> 3, kz = erow & 7
-        const int eky = erow >> 3, ekz = erow & 7;
-        const uint32_t tl = tmem + ((uint32_t)((warp & 3) * 32) << 16) + eb * 256;
+        const int qd = warp & 3, h = warp >> 2;       // lane quadrant, channel half
+        const int kz = lane & 7;
+        const uint32_t tq = tmem + ((uint32_t)(qd * 32) << 16);   // the warp's lanes, column 0
         uint32_t fbits = 0, pfull = 0;
         long long js = 0;   // tiles whose input was written
         bool bad = false;
-        // the input of a tile from its feature stage: row t = (ky, kz),
-        // k = 2 q + c (c = 0: the bin, 1: its mirror), zero-padded to 16
+        // A tile's input from its feature stage, by warps 4-7 (two rows a
+        // thread): row r = (ky, kz), k = 2 q + c (c = 0: the bin, 1: its
+        // mirror), zero-padded to 16. Every epilogue warp releases the stage
+        // and the first layer's block-0 MMAs.
         auto write_input = [&]() {
             const int b = (int)(js & 1);
-            if (!bar_wait(ffull + b, (fbits >> b) & 1)) return false;
-            fbits ^= 1u << b;
-            const __nv_bfloat16 *f = reinterpret_cast<const __nv_bfloat16 *>(S.stage + b * FEAT_BYTES);
-            const int ky = t >> 3, kz = t & 7;
-            __align__(16) __nv_bfloat16 v[16];
+            bool done = true;
+            if (h == 1) {
+                done = bar_wait(ffull + b, (fbits >> b) & 1);
+                if (done) {
+                    fbits ^= 1u << b;
+                    const __nv_bfloat16 *f = reinterpret_cast<const __nv_bfloat16 *>(S.stage + b * FEAT_BYTES);
+                    for (int r = t - 128; r < 256; r += 128) {
+                        const int ky = r >> 3, rz = r & 7;
+                        __align__(16) __nv_bfloat16 v[16];
 #pragma unroll
-            for (int q = 0; q < NQ; q++) {
-                v[2 * q] = f[(q * 8 + kz) * 32 + ky];
-                v[2 * q + 1] = f[((4 - q) * 8 + ((10 - kz) & 7)) * 32 + ((40 - ky) & 31)];
+                        for (int q = 0; q < NQ; q++) {
+                            v[2 * q] = f[(q * 8 + rz) * 32 + ky];
+                            v[2 * q + 1] = f[((4 - q) * 8 + ((10 - rz) & 7)) * 32 + ((40 - ky) & 31)];
+                        }
+#pragma unroll
+                        for (int k = 10; k < 16; k++) v[k] = __float2bfloat16_rn(0.f);
+                        put_row(S.in, 32, ky, rz, 0, reinterpret_cast<const uint4 *>(v)[0]);
+                        put_row(S.in, 32, ky, rz, 1, reinterpret_cast<const uint4 *>(v)[1]);
+                    }
+                    fence_async_smem();
+                }
             }
-#pragma unroll
-            for (int k = 10; k < 16; k++) v[k] = __float2bfloat16_rn(0.f);
-            put_row(S.A, 32, ky, kz, 0, reinterpret_cast<const uint4 *>(v)[0]);
-            put_row(S.A, 32, ky, kz, 1, reinterpret_cast<const uint4 *>(v)[1]);
-            fence_async_smem();
             __syncwarp();
-            if (lane == 0) bar_arrive(ffree + b);
+            if (lane == 0) {
+                bar_arrive(ffree + b);
+                bar_arrive(ready + 0);
+            }
             js++;
-            return true;
+            return done;
         };
         if (first < ntiles) {
             bad = !write_input();
-            __syncwarp();
-            if (lane == 0) bar_arrive(ready + 0);
+            // block 1's columns are free for the first tile
+            if (lane == 0) bar_arrive(ready + 1);
         }
         long long it = 0;
         for (long long tile = first; tile < ntiles; tile += step, it++) {
             float conf = 0.f;
-            for (int L = 0; L < 3 && !bad; L++) {
-                if (!bar_wait(full, pfull)) {
-                    bad = true;
-                    break;
-                }
-                pfull ^= 1;
-                fence_after();
-                if (L < 2) {
-                    // block q's columns in one buffer while block q + 1's
-                    // loads land in the other
-                    auto block = [&](int q, uint32_t(&cur)[48], uint32_t(&nxt)[48]) {
-                        tmem_wait_ld(cur);
-                        // cleared for the next layer, whose MMAs all accumulate
-                        tmem_zero16(tl + q * 48);
-                        tmem_zero16(tl + q * 48 + 16);
-                        tmem_zero16(tl + q * 48 + 32);
-                        if (q + 1 < NQ) load_block(tl, q + 1, nxt);
-                        float y[16];
-                        combine_block(cur, lane, y);
-                        __align__(16) __nv_bfloat16 o[16];
-#pragma unroll
-                        for (int co = 0; co < NC; co++)
-                            o[co] = __float2bfloat16_rn(fmaxf(y[co] + s_par[L * NC + co], 0.f));
-                        put_row(S.A, 160, eky, ekz, 2 * q, reinterpret_cast<const uint4 *>(o)[0]);
-                        put_row(S.A, 160, eky, ekz, 2 * q + 1, reinterpret_cast<const uint4 *>(o)[1]);
-                        if (TRAIN) {
-                            __nv_bfloat16 *ag = (L == 0 ? a1g : a2g) + tile * NC * NV;
-                            const int vox = (q * 8 + ekz) * 32 + eky;
-#pragma unroll
-                            for (int co = 0; co < NC; co++) ag[co * NV + vox] = o[co];
-                        }
-                        // input chunk q is written and blocks 0..q are read and
-                        // zeroed: chunk q - 1 of the next layer may run (all of
-                        // them after the last block)
-                        fence_async_smem();
-                        tmem_wait_st();
-                        fence_before();
-                        __syncwarp();
-                        if (lane == 0) {
-                            if (q > 0) bar_arrive(ready + q - 1);
-                            if (q == NQ - 1) bar_arrive(ready + q);
-                        }
-                    };
-                    uint32_t ba[48], bb[48];
-                    load_block(tl, 0, ba);
-                    block(0, ba, bb);
-                    block(1, bb, ba);
-                    block(2, ba, bb);
-                    block(3, bb, ba);
-                    block(4, ba, bb);
-                } else {
-                    // the next tile's input (this layer's MMAs are done with A)
-                    const bool more = tile + step < ntiles;
-                    if (more && !write_input()) {
+            const bool more = tile + step < ntiles;
+            for (int L = 0; L < 3; L++) {
+                for (int b = 0; b < 2; b++) {
+                    if (bad) break;
+                    if (!bar_wait(full + b, (pfull >> b) & 1)) {
                         bad = true;
                         break;
                     }
-                    const float zh0 = s_par[4 * NC];
-                    auto block = [&](int q, uint32_t(&cur)[48], uint32_t(&nxt)[48]) {
-                        tmem_wait_ld(cur);
-                        if (q + 1 < NQ) load_block(tl, q + 1, nxt);
-                        float y[16];
-                        combine_block(cur, lane, y);
-                        const int vox = (q * 8 + ekz) * 32 + eky;
-                        float zh = zh0;
+                    pfull ^= 1u << b;
+                    fence_after();
+                    const int erow = b * 128 + qd * 32 + lane;   // the row: ky = erow >> 3, kz
+                    const int ky = erow >> 3;
+                    if (L < 2) {
+                        const uint32_t tl = tq + b * 256 + h * 8;
+                        float bias[8];
 #pragma unroll
-                        for (int co = 0; co < NC; co++) {
-                            const float a = bfr(fmaxf(y[co] + s_par[2 * NC + co], 0.f));
-                            if (TRAIN) a3g[tile * NC * NV + co * NV + vox] = __float2bfloat16_rn(a);
-                            zh = __fmaf_rn(a, s_par[3 * NC + co], zh);
+                        for (int c = 0; c < 8; c++) bias[c] = s_par[L * NC + h * 8 + c];
+                        auto step_q = [&](int q, uint32_t(&cur)[24], uint32_t(&nxt)[24]) {
+                            tmem_wait_ld(cur);
+                            // cleared for the next layer, whose MMAs all accumulate
+                            tmem_zero8(tl + q * 48);
+                            tmem_zero8(tl + q * 48 + 16);
+                            tmem_zero8(tl + q * 48 + 32);
+                            if (q + 1 < NQ) load_half(tl, q + 1, nxt);
+                            float y[8];
+                            combine_half(cur, lane, y);
+                            __align__(16) __nv_bfloat16 o[8];
+#pragma unroll
+                            for (int c = 0; c < 8; c++)
+                                o[c] = __float2bfloat16_rn(fmaxf(y[c] + bias[c], 0.f));
+                            const uint4 ov = *reinterpret_cast<const uint4 *>(o);
+                            const int ch = 2 * q + h;   // the 16-byte chunk of the input row
+                            if (b == 0) {
+                                // groups 16 (ky = 15) and 33 (the halo copy of
+                                // ky = 0) are still read by block 1's MMAs
+                                if (ky == 15)
+                                    *reinterpret_cast<uint4 *>(stash + (kz * 10 + ch) * 16) = ov;
+                                else
+                                    *reinterpret_cast<uint4 *>(S.A + (ky + 1) * 1280 + ch * 128 + kz * 16) = ov;
+                                if (ky == 0)
+                                    *reinterpret_cast<uint4 *>(stash + ((8 + kz) * 10 + ch) * 16) = ov;
+                            } else {
+                                put_row(S.A, 160, ky, kz, ch, ov);
+                                // the stashed rows of this thread's block-0 twin (same lane)
+                                if (ky == 16)
+                                    *reinterpret_cast<uint4 *>(S.A + (kGroupsA - 1) * 1280 + ch * 128 + kz * 16) =
+                                        *reinterpret_cast<const uint4 *>(stash + ((8 + kz) * 10 + ch) * 16);
+                                if (ky == 31)
+                                    *reinterpret_cast<uint4 *>(S.A + 16 * 1280 + ch * 128 + kz * 16) =
+                                        *reinterpret_cast<const uint4 *>(stash + (kz * 10 + ch) * 16);
+                            }
+                            if (TRAIN) {
+                                __nv_bfloat16 *ag = (L == 0 ? a1g : a2g) + tile * NC * NV;
+                                const int vox = (q * 8 + kz) * 32 + ky;
+#pragma unroll
+                                for (int c = 0; c < 8; c++) ag[(h * 8 + c) * NV + vox] = o[c];
+                            }
+                            if (b == 1) {
+                                // the next layer's input chunk q is complete
+                                // (block 0's rows were written before) and
+                                // block 1's columns 0..q are read; after the
+                                // last step all of them are zeroed
+                                fence_async_smem();
+                                if (q == NQ - 1) tmem_wait_st();
+                                fence_before();
+                                __syncwarp();
+                                if (lane == 0) bar_arrive(ready + q);
+                            }
+                        };
+                        uint32_t ba[24], bb[24];
+                        load_half(tl, 0, ba);
+                        step_q(0, ba, bb);
+                        step_q(1, bb, ba);
+                        step_q(2, ba, bb);
+                        step_q(3, bb, ba);
+                        step_q(4, ba, bb);
+                        if (b == 0) {
+                            // block 0's rows and zeroed columns, before block
+                            // 1's steps release the next layer's chunks
+                            fence_async_smem();
+                            tmem_wait_st();
+                            fence_before();
                         }
-                        const float p = 1.0f / (1.0f + expf(-zh));
-                        p_out[tile * NV + vox] = p;
-                        conf += fabsf(p - 0.5f);
-                    };
-                    uint32_t ba[48], bb[48];
-                    load_block(tl, 0, ba);
-                    block(0, ba, bb);
-                    block(1, bb, ba);
-                    block(2, ba, bb);
-                    block(3, bb, ba);
-                    block(4, ba, bb);
-                    // the accumulator is read: the next tile's first layer may run
-                    fence_before();
-                    __syncwarp();
-                    if (more && lane == 0) bar_arrive(ready + 0);
+                    } else {
+                        // the sigmoid head over the row's 16 channels: warps
+                        // 0-3 take output blocks q = 0..2, warps 4-7 q = 3..4
+                        const uint32_t tl = tq + b * 256;
+                        const float zh0 = s_par[4 * NC];
+                        auto head_q = [&](int q, int qend, uint32_t(&cur)[48], uint32_t(&nxt)[48]) {
+                            tmem_wait_ld(cur);
+                            if (q + 1 < qend) load_block(tl, q + 1, nxt);
+                            float y[16];
+                            combine_block(cur, lane, y);
+                            const int vox = (q * 8 + kz) * 32 + ky;
+                            float zh = zh0;
+#pragma unroll
+                            for (int co = 0; co < NC; co++) {
+                                const float a = bfr(fmaxf(y[co] + s_par[2 * NC + co], 0.f));
+                                if (TRAIN) a3g[tile * NC * NV + co * NV + vox] = __float2bfloat16_rn(a);
+                                zh = __fmaf_rn(a, s_par[3 * NC + co], zh);
+                            }
+                            const float p = 1.0f / (1.0f + expf(-zh));
+                            p_out[tile * NV + vox] = p;
+                            conf += fabsf(p - 0.5f);
+                        };
+                        uint32_t ba[48], bb[48];
+                        if (h == 0) {
+                            load_block(tl, 0, ba);
+                            head_q(0, 3, ba, bb);
+                            head_q(1, 3, bb, ba);
+                            head_q(2, 3, ba, bb);
+                        } else {
+                            load_block(tl, 3, ba);
+                            head_q(3, 5, ba, bb);
+                            head_q(4, 5, bb, ba);
+                        }
+                        // block b's columns are read: the next tile's layer-1
+                        // MMAs of block b may run. During block 0, warps 4-7
+                        // then write the next tile's input (layer 1's operand
+                        // region is free: this tile's layer-1 MMAs are long
+                        // done) and warps 0-3 only release the feature stage.
+                        fence_before();
+                        __syncwarp();
+                        if (more) {
+                            if (b == 0) {
+                                if (!write_input()) bad = true;
+                            } else if (lane == 0) {
+                                bar_arrive(ready + 1);
+                            }
+                        }
+                    }
                 }
             }
             // the tile's confidence; a failure anywhere stops every epilogue warp here
 #pragma unroll
-            for (int h = 16; h >= 1; h >>= 1) conf += __shfl_xor_sync(0xffffffffu, conf, h);
+            for (int hh = 16; hh >= 1; hh >>= 1) conf += __shfl_xor_sync(0xffffffffu, conf, hh);
             if (lane == 0) red[it & 1][warp] = conf;
             if (epi_or(bad || *S.abort_flag != 0)) {
                 bad = true;

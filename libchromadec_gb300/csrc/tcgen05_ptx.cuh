@@ -159,12 +159,22 @@ __device__ __forceinline__ void tmem_ld16_async(uint32_t taddr, uint32_t (&r)[16
                  : "r"(taddr));
 }
 
+// 8 consecutive 32-bit columns of this thread's lane into r, without waiting.
+__device__ __forceinline__ void tmem_ld8_async(uint32_t taddr, uint32_t *r)
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+}
+
 // Wait for this thread's tensor-memory loads. The "+r" operands tie the
-// registers being loaded to the wait, so no use of them moves above it.
+// registers being loaded to the wait, so no use of them moves above it; no
+// memory clobber (it orders no shared or global access), so ordinary loads
+// and stores may be scheduled across it.
 template <int N>
 __device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[N])
 {
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;");
 #pragma unroll
     for (int j = 0; j < N; j++) asm volatile("" : "+r"(r[j]));
 }
@@ -177,6 +187,15 @@ __device__ __forceinline__ void tmem_zero16(uint32_t taddr)
                  "{%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1};" ::"r"(taddr),
                  "r"(0u)
                  : "memory");
+}
+
+// Zero 8 consecutive 32-bit columns of this thread's lane (no wait; tensor
+// memory only, so no memory clobber: the tcgen05 instructions keep their
+// order among themselves).
+__device__ __forceinline__ void tmem_zero8(uint32_t taddr)
+{
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %1, %1, %1, %1, %1, %1, %1};" ::"r"(taddr),
+                 "r"(0u));
 }
 
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
