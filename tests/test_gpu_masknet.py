@@ -28,17 +28,19 @@ def _problem(seed, b):
     return params, feat, a, c
 
 
-@pytest.mark.parametrize("tensor_cores", [True, False])
-def test_forward_matches_restatement(cuda, tensor_cores):
+@pytest.mark.parametrize("tensor_cores,b", [(True, 6), (False, 6), (True, 153)])
+def test_forward_matches_restatement(cuda, tensor_cores, b):
+    """b = 153 with one CTA per SM: one CTA runs two tiles (the next tile's
+    input written during the first one's head), the others one."""
     torch = cuda
     from libchromadec_gb300 import device as D
-    params, feat, _, _ = _problem(3, 6)
+    params, feat, _, _ = _problem(3, b)
     net = D.MaskNet(params)
     net.set_tensor_cores(tensor_cores)
-    f = _bf16_bits(feat.reshape(6, -1)).cuda()
-    p = torch.empty((6, R.NV), dtype=torch.float32, device="cuda")
-    fb = torch.empty(6, dtype=torch.uint8, device="cuda")
-    net.forward(f, 6, p, fb)
+    f = _bf16_bits(feat.reshape(b, -1)).cuda()
+    p = torch.empty((b, R.NV), dtype=torch.float32, device="cuda")
+    fb = torch.empty(b, dtype=torch.uint8, device="cuda")
+    net.forward(f, b, p, fb)
     net.sync()
     ref, _ = R.forward(params.astype(np.float64), feat)
     got = p.cpu().numpy().reshape(ref.shape)
