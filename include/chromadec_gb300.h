@@ -120,7 +120,9 @@ int chdg_chroma_device(chdg_engine *e, const uint16_t *d_fields, int64_t field_s
  * array's device address and uploads constant tables; make that first call
  * before starting any stream capture. Per-bin thresholds, when given, are
  * copied from pageable host memory into a second static array on `stream`
- * at every call, ordered after the decodes already queued on that stream. */
+ * at every call, ordered after the decodes already queued on that stream; a
+ * copy from pageable memory cannot be recorded into a graph, so calls with
+ * per-bin thresholds cannot be stream-captured. */
 int chdg_decode_device_static(const chdg_geometry *g, const chdg_config *c, const uint16_t *d_fields,
                               int64_t field_stride, int32_t nfields, int32_t frame_begin, int32_t frame_end,
                               void *d_out, void *stream);
