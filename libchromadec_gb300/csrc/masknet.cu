@@ -504,8 +504,9 @@ __global__ void mn_round_kernel(const float *master, float *used)
 //    for the next layer (whose banded MMAs all accumulate), add the dz partial
 //    sums, the bias and ReLU, round to bf16 and write K chunk q of the next
 //    layer's input; block 1's step q releases the next layer's chunk q. The
-//    last layer: warps 0-3 run the sigmoid head over all 16 channels, warps
-//    4-7 write the next tile's input (during block 1).
+//    last layer: the sigmoid head over all 16 channels, warps 0-3 taking
+//    output blocks q = 0..2 and warps 4-7 q = 3..4; after block 0's head,
+//    warps 4-7 write the next tile's input.
 //  * warp 8, one thread: issues the MMAs.
 //  * warp 9, one thread: the TMA bulk copies -- the weight pieces of each
 //    tile (each used by both M blocks) through a ring of slots, and each next
@@ -546,8 +547,8 @@ constexpr int SM_TSLOT = SM_BAR + 8 * NBAR;
 constexpr int SM_FLAG = SM_TSLOT + 4;
 constexpr int kTcSmem = SM_FLAG + 12;
 static_assert(kTcSmem + 1024 <= 227 * 1024, "shared memory of one CTA");
-static_assert(SM_IN % 16 == 0 && SM_W1 % 16 == 0 && SM_SLOT % 16 == 0 && SLOT_BYTES % 16 == 0 && SM_FEAT % 16 == 0 && SM_STASH % 16 == 0 &&
-                  SM_BAR % 8 == 0,
+static_assert(SM_IN % 16 == 0 && SM_W1 % 16 == 0 && SM_SLOT % 16 == 0 && SLOT_BYTES % 16 == 0 &&
+                  SM_FEAT % 16 == 0 && SM_STASH % 16 == 0 && SM_BAR % 8 == 0,
               "copy alignment");
 
 // the band of output blocks of input block (K chunk) ks in layers 2 and 3
