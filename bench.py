@@ -314,6 +314,10 @@ def e2e_abi(a, fields_np, rank, barrier, dist):
     path = f"/tmp/chdg_bench_{a.fields}_{a.seed}_r{rank}.tbc"
     if not (os.path.exists(path) and os.path.getsize(path) == fields_np.nbytes):
         synth.write_tbc(path, synth.SynthCapture(fields=fields_np, dropouts=[[] for _ in range(nfields)]))
+    # Write back the page cache's dirty data first (this capture, and whatever
+    # an earlier job on the host wrote): the kernel's background writeback
+    # would otherwise compete with the timed steps for the host's memory.
+    os.sync()
     L = abi.lib()
     v = abi.Video(path)
     d = abi.Decoder(v, abi.DEC_TRANSFORM_3D)
