@@ -201,3 +201,44 @@ def test_tensor_core_and_cuda_core_forward_agree_on_trained_weights(cuda):
     d = (out[0][0] - out[1][0]).abs()
     assert float(d.max()) < 2e-2 and float(d.mean()) < 1e-5
     assert float((out[0][1] != out[1][1]).float().mean()) < 1e-3
+
+
+def test_learned_decode_is_independent_of_the_batch_split(cuda):
+    """The engine runs the learned form in batches of at most 64 frames, and
+    each batch's edge Z tiles read fields outside it. A 72-frame decode (a
+    64-frame batch, then an 8-frame one) gives frames 56-71 bit for bit as a
+    decode of those 16 frames in one batch; and the learned engine's chroma
+    equals the feature pass, network and apply pass run one by one."""
+    torch = cuda
+    from libchromadec_gb300 import device as D, masknet_train as MT
+    n = 144
+    cap = capture(n, 64)
+    fields = torch.from_numpy(cap.fields.reshape(n, -1).view(np.int16)).cuda()
+    net = D.MaskNet(MT.load_weights())
+    eng = D.Engine(D.default_geometry(), D.default_config(kind=D.KIND_TRANSFORM_3D, fmt=D.FMT_PS))
+    eng.set_masknet(net)
+    whole = torch.empty((72, 3, 576, 948), dtype=torch.float32, device="cuda")
+    part = torch.empty((16, 3, 576, 948), dtype=torch.float32, device="cuda")
+    eng.decode(fields, 0, 72, whole)
+    eng.decode(fields, 56, 72, part)
+    torch.cuda.synchronize()
+    assert torch.isfinite(whole).all()
+    assert torch.equal(whole[56:72], part)
+
+    fb, fe = 60, 68
+    nz = fe - fb + 2
+    direct = torch.empty((2 * (fe - fb), 288, 948), dtype=torch.float32, device="cuda")
+    eng.chroma(fields, fb, fe, direct)
+    plain = D.Engine(D.default_geometry(), D.default_config(kind=D.KIND_TRANSFORM_3D, fmt=D.FMT_PS))
+    nt = plain.ntiles()
+    feat = torch.empty((nz * nt, R.NV), dtype=torch.int16, device="cuda")
+    plain.learned_features(fields, fb, fe, feat)
+    p = torch.empty((nz * nt, R.NV), dtype=torch.float32, device="cuda")
+    fbk = torch.empty(nz * nt, dtype=torch.uint8, device="cuda")
+    net.forward(feat, nz * nt, p, fbk)
+    manual = torch.empty_like(direct)
+    plain.learned_chroma(fields, fb, fe, p, fbk, manual)
+    torch.cuda.synchronize()
+    assert torch.equal(direct, manual)
+    eng.set_masknet(None)
+    net.close()
