@@ -731,11 +731,13 @@ __device__ bool tc_mma_role(const TcShared &S, uint32_t tmem, long long first, l
         }
         mma_commit(full + 1);
         // layers 2 and 3: block 0's chunk ks once block 1's epilogue of the
-        // previous layer released it; block 1's chunks need nothing more
+        // previous layer released it (the weight piece is taken first: it
+        // landed long before, so that wait overlaps the epilogue step that
+        // releases the chunk); block 1's chunks need nothing more
         for (int L = 1; L < 3 && ok; L++) {
             const long long p = sc;
             for (int ks = 0; ks < 5 && ok; ks++) {
-                ok = take_ready(ks) && take_slot(p + ks);
+                ok = take_slot(p + ks) && take_ready(ks);
                 if (ok) mma_band_any(ks, tmem, a2b[0], slot_desc(p + ks));
             }
             mma_commit(full + 0);

@@ -15,13 +15,15 @@ test checks the design they rest on, in numpy:
     epilogue cleared, and the lane-shuffle sum of the kz partials;
   * the schedule's hazards: every 16-byte chunk of the operand regions is
     tagged with the layer (and tile) that wrote it and each MMA checks the
-    tags it reads, with each block's epilogue run in the order most likely
-    to break that: block 0's whole epilogue before block 1's MMAs of the same
-    layer (they overlap on the GPU), and block 1's step q just before the
-    next layer's block-0 chunk q that it releases.
+    tags it reads. The MMAs run at the two ends of what the barriers allow:
+    eagerly (a block-0 chunk as soon as block 1's step q releases it; block
+    1's chunks only after block 0's whole epilogue, which overlaps them on the
+    GPU), and lazily (every chunk of an M block just before the block's
+    epilogue, whose barrier is committed after the block's last chunk).
 
-A planted hazard (block 0's epilogue writing its stashed rows in place)
-must trip the tag check.
+Two planted mistakes must be caught: block 0's epilogue writing its stashed
+rows in place (the tag check), and a block's barrier committed before its
+last chunk (the result).
 """
 import numpy as np
 import pytest
@@ -134,7 +136,14 @@ def put_row(reg, row_bytes, ky, kz, c, v8, tag):
         reg.put(base + (GROUPS - 1) * grp, v8, tag)
 
 
-def run(used, img, feats, plant_hazard=False):
+def final_chunk(q):
+    """The chunk after which output block q may be read: an M block's one
+    barrier is committed after its last chunk (4), although chunk ks writes
+    only the output blocks ks - 1 .. ks + 1."""
+    return 4
+
+
+def run(used, img, feats, plant_hazard=False, lazy=False, last_chunk=final_chunk):
     """The kernel's schedule over consecutive tiles of one CTA; fractions per tile."""
     A, IN = Region(A_BYTES), Region(IN_BYTES)
     W1 = Region(3 * NCOL * 32)
@@ -174,6 +183,21 @@ def run(used, img, feats, plant_hazard=False):
             assert not np.isnan(blk).any(), "accumulating into columns nobody cleared"
             tm[b][:, lo:lo + nb] = blk + a @ P.operand(dy * nb * 32, 256, nb).T
 
+    pending = {0: [], 1: []}   # issued chunks not yet executed, in issue order
+
+    def issue(layer, b, ks, tj):
+        if lazy:
+            pending[b].append((layer, ks, tj))
+        else:
+            mma_chunk(layer, b, ks, tj)
+
+    def need(b, q, everything=False):
+        """Output block q's wait: the chunks up to last_chunk(q) have completed
+        (everything: the block's epilogue is over and the rest complete too)."""
+        while pending[b] and (everything or pending[b][0][1] <= last_chunk(q)):
+            layer, ks, tj = pending[b].pop(0)
+            mma_chunk(layer, b, ks, tj)
+
     def combine(b, q):
         D = tm[b]
         y = np.zeros((128, 16))
@@ -184,6 +208,7 @@ def run(used, img, feats, plant_hazard=False):
         return y
 
     def epi_step(layer, b, q, tj):
+        need(b, q)
         y = combine(b, q)
         tm[b][:, q * 48:q * 48 + 48] = 0.0   # cleared after reading: the next layer accumulates
         bias = used[(OFF_B1 if layer == 1 else OFF_B2):][:16]
@@ -209,12 +234,14 @@ def run(used, img, feats, plant_hazard=False):
 
     def head(b, p):
         for q in range(5):
+            need(b, q)
             y = combine(b, q)
             for lr in range(128):
                 ky, kz = (b * 128 + lr) >> 3, lr & 7
                 a = from_bits(bf16_bits(np.maximum(y[lr] + used[OFF_B3:OFF_B3 + 16], 0.0)))
                 zh = used[OFF_BH] + (a * used[OFF_WH:OFF_WH + 16]).sum()
                 p[(q * 8 + kz) * 32 + ky] = 1.0 / (1.0 + np.exp(-zh))
+        need(b, 4, everything=True)
 
     out = []
     write_input(0)
@@ -227,16 +254,22 @@ def run(used, img, feats, plant_hazard=False):
         for layer in (2, 3):
             for q in range(5):
                 epi_step(layer - 1, 1, q, tj)     # block 1's step q releases chunk q
-                mma_chunk(layer, 0, q, tj)
+                issue(layer, 0, q, tj)
+            need(1, 4, everything=True)
+            if lazy:
+                for q in range(5):                # issued right after block 0's
+                    issue(layer, 1, q, tj)
             if layer == 2:
                 for q in range(5):
                     epi_step(2, 0, q, tj)
+                need(0, 4, everything=True)
             else:
                 head(0, p)
                 if tj + 1 < len(feats):
                     write_input(tj + 1)           # during block 0's head
-            for q in range(5):
-                mma_chunk(layer, 1, q, tj)
+            if not lazy:
+                for q in range(5):
+                    issue(layer, 1, q, tj)
         head(1, p)
         out.append(p)
     return out
@@ -252,15 +285,30 @@ def problem():
     return used, img, feat
 
 
-def test_schedule_reproduces_the_fp64_forward(problem):
+@pytest.mark.parametrize("lazy", [False, True])
+def test_schedule_reproduces_the_fp64_forward(problem, lazy):
     used, img, feat = problem
-    got = run(used, img, [bf16_bits(feat[i]) for i in range(3)])
+    got = run(used, img, [bf16_bits(feat[i]) for i in range(3)], lazy=lazy)
     ref, _ = R.forward(used.astype(np.float32), feat)
     for i in range(3):
         assert np.abs(got[i] - ref[i].reshape(-1)).max() < 1e-12
 
 
-def test_planted_hazard_is_caught(problem):
+@pytest.mark.parametrize("lazy", [False, True])
+def test_planted_hazard_is_caught(problem, lazy):
     used, img, feat = problem
     with pytest.raises(AssertionError, match="operand written by"):
-        run(used, img, [bf16_bits(feat[i]) for i in range(2)], plant_hazard=True)
+        run(used, img, [bf16_bits(feat[i]) for i in range(2)], plant_hazard=True, lazy=lazy)
+
+
+def test_block_signalled_early_is_caught(problem):
+    """Chunk 4 then completes after the epilogue has read its columns and
+    rewritten its operand: the tag check or the results must show it."""
+    used, img, feat = problem
+    try:
+        got = run(used, img, [bf16_bits(feat[i]) for i in range(2)], lazy=True, last_chunk=lambda q: 3)
+    except AssertionError as e:
+        assert "operand written by" in str(e)
+        return
+    ref, _ = R.forward(used.astype(np.float32), feat)
+    assert np.abs(got[0] - ref[0].reshape(-1)).max() > 1e-3
