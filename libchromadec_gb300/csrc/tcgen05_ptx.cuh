@@ -78,6 +78,9 @@ __device__ __forceinline__ void bar_arrive(uint64_t *bar)
 __device__ __forceinline__ bool bar_wait(uint64_t *bar, uint32_t parity)
 {
     const uint32_t a = smem_addr(bar);
+    // kept rolled: the wait is inlined at every call site, and unrolled
+    // copies made up a third of the mask network kernel's code
+#pragma unroll 1
     for (unsigned it = 0; it < kWaitLimit; it++) {
         uint32_t done;
         asm volatile("{\n\t.reg .pred P1;\n\tmbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n\t"
