@@ -85,8 +85,10 @@ int chdg_decode_device(chdg_engine *e, const uint16_t *d_fields, int64_t field_s
 /* Decode frames [frame_begin, frame_end) of a capture held in HOST memory
  * (nfields fields, field f at h_fields + f * field_stride samples) into
  * h_out. Field windows are uploaded and frames downloaded in a double-buffered
- * pipeline that overlaps the copies with the kernels; use pinned memory for
- * full-rate copies. Completes asynchronously on `stream`. */
+ * pipeline that overlaps the copies with the kernels (batches of 64 frames, 16
+ * at either end of a longer run); use pinned memory for full-rate copies.
+ * Completes asynchronously on `stream`; a later call on the same engine
+ * reuses its device buffers only after this call's work on them. */
 int chdg_decode_host(chdg_engine *e, const uint16_t *h_fields, int64_t field_stride, int32_t nfields,
                      int32_t frame_begin, int32_t frame_end, void *h_out, void *stream);
 

@@ -751,10 +751,12 @@ int Engine::ensure_host_pipeline(size_t field_bytes, size_t out_bytes)
     return 0;
 }
 
-// Batches of B frames alternate between two device slots: the copy stream
-// uploads batch i+1's field window while the compute stream decodes batch i,
-// and downloads batch i-1's frames. A batch's window is its fields plus the
-// 3D look-behind/ahead halo (frames b-2 .. b+B+3), clipped to the capture.
+// Batches alternate between two device slots: the copy stream uploads batch
+// i+1's field window while the compute stream decodes batch i, and downloads
+// batch i-1's frames. Batches of B frames, with a first and a last batch of
+// at most kHostEdgeFrames (the first upload and the last download are the
+// copies no kernel overlaps). A batch's window is its fields plus the 3D
+// look-behind/ahead halo (frames b-2 .. b+B+3), clipped to the capture.
 int Engine::decode_host(const uint16_t *host_fields, long long host_stride, int nfields, int fb, int fe,
                         void *host_out, cudaStream_t s)
 {
@@ -768,14 +770,17 @@ int Engine::decode_host(const uint16_t *host_fields, long long host_stride, int 
         rc != 0)
         return rc;
     cudaError_t e;
-    int i = 0;
-    for (int b = fb; b < fe; b += B, i++) {
-        const int be = std::min(fe, b + B);
+    const std::vector<std::pair<int64_t, int64_t>> batches = edge_batches(fb, fe, B, kHostEdgeFrames);
+    for (int i = 0; i < (int)batches.size(); i++) {
+        const int b = (int)batches[i].first, be = (int)batches[i].second;
         const int slot = i & 1;
         const int f0 = std::max(0, 2 * (b - look_behind()));
         const int f1 = std::min(nfields, 2 * (be + look_ahead()));
-        // slot reuse: batch i-2's compute must be done before overwriting its fields
-        if (i >= 2) cudaStreamWaitEvent(copy_stream_, ev_comp_[slot], 0);
+        // slot reuse: the slot's previous decode -- batch i-2's, or for the
+        // first two batches the previous call's, which may still be running
+        // -- must be done before its fields are overwritten (an event never
+        // recorded makes the wait a no-op)
+        cudaStreamWaitEvent(copy_stream_, ev_comp_[slot], 0);
         if (f1 > f0) {
             e = cudaMemcpy2DAsync(hp_fields_[slot], dstride * 2, host_fields + (size_t)f0 * host_stride,
                                   host_stride * 2, flen * 2, f1 - f0, cudaMemcpyHostToDevice, copy_stream_);
@@ -783,7 +788,7 @@ int Engine::decode_host(const uint16_t *host_fields, long long host_stride, int 
         }
         cudaEventRecord(ev_h2d_[slot], copy_stream_);
         cudaStreamWaitEvent(s, ev_h2d_[slot], 0);
-        if (i >= 2) cudaStreamWaitEvent(s, ev_d2h_[slot], 0);   // output slot drained
+        cudaStreamWaitEvent(s, ev_d2h_[slot], 0);   // output slot drained (this call's or the previous one's)
         if (const int rc = decode(hp_fields_[slot], dstride, f0, nfields, b, be, hp_out_[slot], s); rc != 0) return rc;
         cudaEventRecord(ev_comp_[slot], s);
         // downloads on their own stream, so the next upload does not queue behind them

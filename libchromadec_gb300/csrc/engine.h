@@ -3,6 +3,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <utility>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -14,6 +15,33 @@
 namespace chdg {
 
 void output_geometry(const chdg_geometry &g, int padding, int &w, int &h, int &lp, int &tp);
+
+// Frames [a, b) as pipeline batches: one batch when the run fits one,
+// otherwise batches of `batch` frames with a first and a last batch of
+// `edge`, so the first upload and the last download -- the copies no kernel
+// overlaps -- stay small.
+inline std::vector<std::pair<int64_t, int64_t>> edge_batches(int64_t a, int64_t b, int64_t batch, int64_t edge)
+{
+    std::vector<std::pair<int64_t, int64_t>> out;
+    edge = edge < batch ? edge : batch;
+    if (b - a <= batch) {
+        if (b > a) out.emplace_back(a, b);
+        return out;
+    }
+    int64_t c = a;
+    out.emplace_back(c, c + edge);
+    c += edge;
+    while (b - c > batch + edge) {
+        out.emplace_back(c, c + batch);
+        c += batch;
+    }
+    if (b - c > edge) {
+        out.emplace_back(c, b - edge);
+        c = b - edge;
+    }
+    out.emplace_back(c, b);
+    return out;
+}
 
 class Engine {
 public:
@@ -152,7 +180,8 @@ private:
     const float *frame_t2_ = nullptr;
     void *const *frame_out_ = nullptr;
     // host pipeline: two slots of device fields + frames, one copy stream
-    int host_batch_frames_ = 32;
+    int host_batch_frames_ = 64;
+    static constexpr int kHostEdgeFrames = 16;   // the first and last batch of a long run
     uint16_t *hp_fields_[2] = {nullptr, nullptr};
     void *hp_out_[2] = {nullptr, nullptr};
     size_t hp_field_bytes_ = 0, hp_out_bytes_ = 0;

@@ -355,29 +355,8 @@ int FramePipeline::decode(int64_t a, int64_t b, const Deliver &deliver, const st
     bool havePrev = false;
     const size_t fb = eng_.frame_bytes();
     cudaError_t e;
-    // Batch boundaries: full batches in the middle, short ones at both ends,
-    // so the first upload and the last download -- the parts no kernel
-    // overlaps -- stay small.
-    std::vector<std::pair<int64_t, int64_t>> batches;
-    {
-        const int64_t edge = std::min<int64_t>(kEdgeFrames, batch_);
-        int64_t c = a;
-        if (b - a <= batch_) {
-            if (b > a) batches.emplace_back(a, b);
-        } else {
-            batches.emplace_back(c, c + edge);
-            c += edge;
-            while (b - c > batch_ + edge) {
-                batches.emplace_back(c, c + batch_);
-                c += batch_;
-            }
-            if (b - c > edge) {
-                batches.emplace_back(c, b - edge);
-                c = b - edge;
-            }
-            batches.emplace_back(c, b);
-        }
-    }
+    // Batch boundaries: full batches in the middle, short ones at both ends.
+    const std::vector<std::pair<int64_t, int64_t>> batches = edge_batches(a, b, batch_, kEdgeFrames);
     // Two stages per batch on two window slots: the upload (window fields,
     // dropout plans, extra-source fields) on copy_, and the kernels plus the
     // download on comp_ / d2h_. The next batch's upload is issued before the

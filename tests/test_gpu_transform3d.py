@@ -62,22 +62,30 @@ def test_decode_matches_oracle(cuda, fmt):
 
 
 def test_host_pipeline_matches_device(cuda):
-    """chdg_decode_host (pinned H2D + decode + D2H in 32-frame windows with
-    the 3D halo) gives the same frames as the device-resident decode."""
+    """chdg_decode_host (pinned H2D + decode + D2H in batches of 16, 64 and
+    16 frames with the 3D halo, on two device slots) gives the same frames as
+    the device-resident decode; a second call issued before the first has
+    finished reuses the slots only after the first call's work on them."""
     import ctypes as C
     torch = cuda
     from libchromadec_gb300 import device as D
-    cap = capture(90, seed=9)
+    cap = capture(200, seed=9)
     n = cap.fields.shape[0]
+    nfr = n // 2
     eng = _engine(fmt=0)
     dfields = torch.from_numpy(cap.fields.reshape(n, -1).view(np.int16)).cuda()
-    dout = torch.empty((n // 2, 3, 576, 948), dtype=torch.int16, device="cuda")
-    eng.decode(dfields, 0, n // 2, dout)
+    dout = torch.empty((nfr, 3, 576, 948), dtype=torch.int16, device="cuda")
+    eng.decode(dfields, 0, nfr, dout)
+    ref = dout.cpu()
     hf = torch.from_numpy(cap.fields.reshape(n, -1).view(np.int16)).pin_memory()
-    hout = torch.zeros((n // 2, 3, 576, 948), dtype=torch.int16).pin_memory()
+    hout = [torch.zeros((nfr, 3, 576, 948), dtype=torch.int16).pin_memory() for _ in range(2)]
     s = torch.cuda.current_stream()
-    rc = D.lib().chdg_decode_host(eng._h, C.c_void_p(hf.data_ptr()), hf[0].numel(), n, 0, n // 2,
-                                  C.c_void_p(hout.data_ptr()), C.c_void_p(s.cuda_stream))
-    assert rc == 0, D.last_error()
+    ranges = [(0, nfr), (3, nfr - 1)]   # back to back, without waiting in between
+    for (fb, fe), ho in zip(ranges, hout):
+        rc = D.lib().chdg_decode_host(eng._h, C.c_void_p(hf.data_ptr()), hf[0].numel(), n, fb, fe,
+                                      C.c_void_p(ho.data_ptr()), C.c_void_p(s.cuda_stream))
+        assert rc == 0, D.last_error()
     torch.cuda.synchronize()
-    assert torch.equal(hout, dout.cpu())
+    assert torch.equal(hout[0], ref)
+    fb, fe = ranges[1]
+    assert torch.equal(hout[1][:fe - fb], ref[fb:fe])
