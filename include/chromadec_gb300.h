@@ -67,7 +67,10 @@ void chdg_default_geometry(chdg_geometry *g);
 void chdg_default_config(chdg_config *c, int32_t kind);
 
 /* Create an engine on the current CUDA device. Constant tables are uploaded
- * once per device; scratch grows on demand. */
+ * once per device; scratch grows on demand. The scratch (chroma planes,
+ * decision records) is shared by all of an engine's calls: issue them on one
+ * stream, or order them with events; decode concurrently with one engine per
+ * stream. */
 int chdg_engine_create(const chdg_geometry *g, const chdg_config *c, chdg_engine **out);
 void chdg_engine_free(chdg_engine *e);
 
