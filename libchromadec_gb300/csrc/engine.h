@@ -18,12 +18,14 @@ void output_geometry(const chdg_geometry &g, int padding, int &w, int &h, int &l
 
 // Frames [a, b) as pipeline batches: one batch when the run fits one,
 // otherwise batches of `batch` frames with a first and a last batch of
-// `edge`, so the first upload and the last download -- the copies no kernel
-// overlaps -- stay small.
+// `edge` (at most half a batch), so the first upload and the last download
+// -- the copies no kernel overlaps -- stay small.
 inline std::vector<std::pair<int64_t, int64_t>> edge_batches(int64_t a, int64_t b, int64_t batch, int64_t edge)
 {
     std::vector<std::pair<int64_t, int64_t>> out;
-    edge = edge < batch ? edge : batch;
+    batch = batch > 1 ? batch : 1;
+    const int64_t half = batch / 2 > 1 ? batch / 2 : 1;
+    edge = edge < half ? (edge > 1 ? edge : 1) : half;
     if (b - a <= batch) {
         if (b > a) out.emplace_back(a, b);
         return out;
