@@ -77,6 +77,13 @@ void chdg_engine_free(chdg_engine *e);
 /* Output frame geometry (after padding) and bytes per output frame. */
 int chdg_output_geometry(const chdg_engine *e, int32_t *width, int32_t *height, size_t *frame_bytes);
 
+/* Frames per GPU batch of chdg_decode_device (default 256, at least 1): a
+ * longer range is decoded in batches of this many frames, with identical
+ * results. It bounds the engine's scratch, which grows with the batch: the
+ * four chroma planes take about 8.7 MB per frame, and the learned form's
+ * tile features, fractions and flags about 34 MB more. */
+int chdg_engine_set_max_batch_frames(chdg_engine *e, int32_t frames);
+
 /* Decode frames [frame_begin, frame_end) of a device-resident capture of
  * nfields fields into d_out (frame_end - frame_begin frames, each in the
  * output format's layout: [Y | Cb | Cr] or [R | G | B] planes, interleaved

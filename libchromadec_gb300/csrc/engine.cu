@@ -647,8 +647,7 @@ int Engine::decode(const uint16_t *fields, long long stride, int field_base, int
 {
     if (fields == nullptr || out == nullptr || fe < fb || stride < (long long)g_.field_width * g_.field_height)
         return arg_fail("decode: bad arguments");
-    // the learned form keeps per-Z-tile buffers: batches of at most 64 frames
-    const int maxb = net_ != nullptr ? std::min(max_batch_frames_, 64) : max_batch_frames_;
+    const int maxb = max_batch_frames_;
     char *o = (char *)out;
     for (int b = fb; b < fe; b += maxb) {
         const int be = std::min(fe, b + maxb);
@@ -942,6 +941,14 @@ int chdg_chroma_device(chdg_engine *e, const uint16_t *d_fields, int64_t field_s
 {
     if (!e) return chdg::arg_fail("chdg_chroma_device: null engine");
     return e->eng.chroma(d_fields, field_stride, nfields, frame_begin, frame_end, d_chroma, (cudaStream_t)stream);
+}
+
+int chdg_engine_set_max_batch_frames(chdg_engine *e, int32_t frames)
+{
+    if (!e) return chdg::arg_fail("chdg_engine_set_max_batch_frames: null engine");
+    if (frames < 1) return chdg::arg_fail("chdg_engine_set_max_batch_frames: frames must be at least 1");
+    e->eng.set_max_batch_frames(frames);
+    return 0;
 }
 
 int chdg_engine_set_tc_form(chdg_engine *e, int32_t variant)

@@ -99,6 +99,7 @@ def lib(build: bool = True):
                                         C.c_int32, C.c_void_p, C.c_void_p]
         L.chdg_tc3d_sync.argtypes = [C.c_void_p]
         L.chdg_engine_set_tc_form.argtypes = [C.c_void_p, C.c_int32]
+        L.chdg_engine_set_max_batch_frames.argtypes = [C.c_void_p, C.c_int32]
         L.chdg_tc3d_operand.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_size_t]
         L.chdg_masknet_create.argtypes = [C.POINTER(C.c_void_p)]
         L.chdg_masknet_free.argtypes = [C.c_void_p]
@@ -197,6 +198,12 @@ class Engine:
                                       C.c_void_p(out.data_ptr()), self._stream_ptr(stream))
         if rc != 0:
             raise RuntimeError(f"chdg_chroma_device failed ({rc}): {last_error()}")
+
+    def set_max_batch_frames(self, frames: int):
+        """Frames per GPU batch of decode() (default 256): bounds the scratch memory."""
+        rc = lib().chdg_engine_set_max_batch_frames(self._h, frames)
+        if rc != 0:
+            raise RuntimeError(f"chdg_engine_set_max_batch_frames failed ({rc}): {last_error()}")
 
     def set_tc_form(self, variant: int):
         """-1: the plain form; TC_3XTF32 / TC_BF16X3: the tensor-core form."""

@@ -204,11 +204,12 @@ def test_tensor_core_and_cuda_core_forward_agree_on_trained_weights(cuda):
 
 
 def test_learned_decode_is_independent_of_the_batch_split(cuda):
-    """The engine runs the learned form in batches of at most 64 frames, and
-    each batch's edge Z tiles read fields outside it. A 72-frame decode (a
-    64-frame batch, then an 8-frame one) gives frames 56-71 bit for bit as a
-    decode of those 16 frames in one batch; and the learned engine's chroma
-    equals the feature pass, network and apply pass run one by one."""
+    """An engine limited to 64-frame batches decodes 72 frames as a 64-frame
+    batch and an 8-frame one, and each batch's edge Z tiles read fields
+    outside it: frames 56-71 come out bit for bit as a decode of those 16
+    frames in one batch, and as the same engine's default 256-frame batch;
+    and the learned engine's chroma equals the feature pass, network and
+    apply pass run one by one."""
     torch = cuda
     from libchromadec_gb300 import device as D, masknet_train as MT
     n = 144
@@ -218,12 +219,18 @@ def test_learned_decode_is_independent_of_the_batch_split(cuda):
     eng = D.Engine(D.default_geometry(), D.default_config(kind=D.KIND_TRANSFORM_3D, fmt=D.FMT_PS))
     eng.set_masknet(net)
     whole = torch.empty((72, 3, 576, 948), dtype=torch.float32, device="cuda")
+    one = torch.empty_like(whole)
     part = torch.empty((16, 3, 576, 948), dtype=torch.float32, device="cuda")
+    eng.decode(fields, 0, 72, one)
+    eng.set_max_batch_frames(64)
     eng.decode(fields, 0, 72, whole)
     eng.decode(fields, 56, 72, part)
     torch.cuda.synchronize()
     assert torch.isfinite(whole).all()
+    assert torch.equal(whole, one)
     assert torch.equal(whole[56:72], part)
+    with pytest.raises(RuntimeError):
+        eng.set_max_batch_frames(0)
 
     fb, fe = 60, 68
     nz = fe - fb + 2
